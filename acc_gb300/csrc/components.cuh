@@ -1,0 +1,230 @@
+// components.cuh -- device restatements of the mcvine/acc components.
+//
+// Each function is written for the two working precisions.  The FP64 forms
+// keep the reference's operation order (they are the "plain" kernels).  The
+// FP32 forms compute the same quantities with float-friendly conditioning:
+// reciprocal square roots instead of divisions, 1 - tanh(x) evaluated as
+// 2 / (1 + e^(2x)), a sample ray re-centred on its closest approach before
+// intersecting, and an FP64 discriminant only near tangency.
+#pragma once
+
+#include "common.cuh"
+
+namespace mcv {
+
+// ===================================================================== source
+// Source_simple.propagate (acc/components/sources/source_simple.py:114-162)
+// with randvec_target_rect (:17-42) for the target on the z axis, where the
+// two normalised perpendiculars are (-1,0,0) and (0,-1,0).
+template <typename R, typename Rng>
+__device__ __forceinline__ void source_simple(Neutron<R>& n, Rng& rng,
+                                              const mcv_component& c) {
+  const R width = prm<R>(c, 0), height = prm<R>(c, 1), radius = prm<R>(c, 2);
+  const R Lambda0 = prm<R>(c, 3), dLambda = prm<R>(c, 4), E0 = prm<R>(c, 5),
+          dE = prm<R>(c, 6);
+  const R xw = prm<R>(c, 7), yh = prm<R>(c, 8), dist = prm<R>(c, 9),
+          pmul = prm<R>(c, 10);
+  R r1 = rng.next(), r2 = rng.next(), r3 = rng.next(), r4 = rng.next(),
+    r5 = rng.next();
+  R x, y;
+  if (c.ip[0]) {
+    x = width * (r1 - R(0.5));
+    y = height * (r2 - R(0.5));
+  } else {
+    R r = m_sqrt(r2) * radius, s, co;
+    m_sincos_2pi(r1, &s, &co);
+    x = r * co;
+    y = r * s;
+  }
+  R tdx = xw * (r3 * 2 - 1) / R(2.0);
+  R tdy = yh * (r4 * 2 - 1) / R(2.0);
+  R dist2 = m_sqrt(tdx * tdx + tdy * tdy + dist * dist);
+  R solidangle = (xw * yh * dist) / (dist2 * dist2 * dist2);
+  R dx = -tdx - x, dy = -tdy - y;
+  R v;
+  if (c.ip[1]) {
+    R L = Lambda0 + dLambda * (r5 * 2 - 1);
+    v = R(kK2V) * (R(2 * kPi) / L);
+  } else {
+    R E = E0 + dE * (r5 * 2 - 1);
+    v = R(kSE2V) * m_sqrt(E);
+  }
+  n.x = x;
+  n.y = y;
+  n.z = R(0);
+  if constexpr (sizeof(R) == 4) {
+    R inv = m_rsqrt(dx * dx + dy * dy + dist * dist);
+    R vs = v * inv;
+    n.vx = vs * dx;
+    n.vy = vs * dy;
+    n.vz = vs * dist;
+  } else {
+    R dist1 = m_sqrt(dx * dx + dy * dy + dist * dist);
+    n.vx = v * dx / dist1;
+    n.vy = v * dy / dist1;
+    n.vz = v * dist / dist1;
+  }
+  n.sx = R(0);
+  n.sy = R(0);
+  n.t.set(R(0));
+  n.p = pmul * solidangle;
+}
+
+// ====================================================================== guide
+// calc_reflectivity (acc/components/optics/_guide_utils.py:6-23)
+__device__ __forceinline__ double reflectivity(double Q, double R0, double Qc,
+                                               double alpha, double m,
+                                               double W) {
+  double R = R0;
+  if (Q > Qc) {
+    double tmp = (Q - m * Qc) / W;
+    if (tmp < 10)
+      R *= (1 - tanh(tmp)) * (1 - alpha * (Q - Qc)) / 2;
+    else
+      R = 0;
+  }
+  return R;
+}
+// (1 - tanh(x)) / 2 == 1 / (1 + e^(2x)), which has no cancellation in float
+__device__ __forceinline__ float reflectivity(float Q, float R0, float Qc,
+                                              float alpha, float m, float W) {
+  float R = R0;
+  if (Q > Qc) {
+    float tmp = (Q - m * Qc) / W;
+    if (tmp < 10.f)
+      R *= (1.f - alpha * (Q - Qc)) / (1.f + __expf(2.f * tmp));
+    else
+      R = 0.f;
+  }
+  return R;
+}
+
+// Guide.propagate (acc/components/optics/guide.py:66-162).  Returns 1 when
+// the bounce loop ran out of its MCV_MAX_BOUNCES iterations.
+template <typename R>
+__device__ __forceinline__ int guide(Neutron<R>& n, const mcv_component& c) {
+  const R ww = prm<R>(c, 0), hh = prm<R>(c, 1), hw1 = prm<R>(c, 2),
+          hh1 = prm<R>(c, 3), l = prm<R>(c, 4);
+  const R R0 = prm<R>(c, 5), Qc = prm<R>(c, 6), alpha = prm<R>(c, 7),
+          m = prm<R>(c, 8), W = prm<R>(c, 9);
+  R x = n.x, y = n.y, z = n.z, vx = n.vx, vy = n.vy, vz = n.vz, prob = n.p;
+  R dt = -z / vz;
+  x += vx * dt;
+  y += vy * dt;
+  z = R(0);
+  if (x <= -hw1 || x >= hw1 || y <= -hh1 || y >= hh1) {
+    // absorb (acc/neutron.py:25-28); the moved position stays local
+    n.p = R(-1);
+    return 0;
+  }
+  n.t.add(dt);
+  // |n| of the vertical and horizontal mirror normals (loop invariants)
+  const R nlen2v = l * l + ww * ww, nlen2h = l * l + hh * hh;
+  int overflow = 1;
+  for (int nb = 0; nb < MCV_MAX_BOUNCES; ++nb) {
+    R av = l * vx, bv = ww * vz, ah = l * vy, bh = hh * vz;
+    R vdotn_v1 = bv + av, vdotn_v2 = bv - av;
+    R vdotn_h1 = bh + ah, vdotn_h2 = bh - ah;
+    R cv1 = -hw1 * l - z * ww, cv2 = x * l;
+    R ch1 = -hh1 * l - z * hh, ch2 = y * l;
+    R t1 = (l - z) / vz, t2;
+    int i = 0;
+    if (vdotn_v1 < 0) {
+      t2 = (cv1 - cv2) / vdotn_v1;
+      if (t2 < t1) { t1 = t2; i = 1; }
+    }
+    if (vdotn_v2 < 0) {
+      t2 = (cv1 + cv2) / vdotn_v2;
+      if (t2 < t1) { t1 = t2; i = 2; }
+    }
+    if (vdotn_h1 < 0) {
+      t2 = (ch1 - ch2) / vdotn_h1;
+      if (t2 < t1) { t1 = t2; i = 3; }
+    }
+    if (vdotn_h2 < 0) {
+      t2 = (ch1 + ch2) / vdotn_h2;
+      if (t2 < t1) { t1 = t2; i = 4; }
+    }
+    if (i == 0) {
+      overflow = 0;
+      break;
+    }
+    x += vx * t1;
+    y += vy * t1;
+    z += vz * t1;
+    n.t.add(t1);
+    R vdn = (i == 1) ? vdotn_v1 : (i == 2) ? vdotn_v2 : (i == 3) ? vdotn_h1
+                                                                 : vdotn_h2;
+    R nlen2 = (i <= 2) ? nlen2v : nlen2h;
+    R q, d;
+    if constexpr (sizeof(R) == 4) {
+      R rn = m_rsqrt(nlen2);
+      q = R(kV2K) * (-2) * vdn * rn;
+      d = 2 * vdn * (rn * rn);
+    } else {
+      q = R(kV2K) * (-2) * vdn / m_sqrt(nlen2);
+      d = 2 * vdn / nlen2;
+    }
+    if (i == 1) {
+      vx = vx - d * l;
+      vz = vz - d * ww;
+    } else if (i == 2) {
+      vx = vx + d * l;
+      vz = vz - d * ww;
+    } else if (i == 3) {
+      vy = vy - d * l;
+      vz = vz - d * hh;
+    } else {
+      vy = vy + d * l;
+      vz = vz - d * hh;
+    }
+    prob *= reflectivity(q, R0, Qc, alpha, m, W);
+    if (prob <= 0) {
+      overflow = 0;
+      break;
+    }
+  }
+  n.x = x;
+  n.y = y;
+  n.z = z;
+  n.vx = vx;
+  n.vy = vy;
+  n.vz = vz;
+  n.p = prob;
+  return overflow;
+}
+
+// Slit / Beamstop (acc/components/optics/slit.py:71-108,
+// beamstop.py:75-112); dp = {xmin, xmax, ymin, ymax, radius^2, cut}
+template <typename R>
+__device__ __forceinline__ void slit_or_beamstop(Neutron<R>& n,
+                                                 const mcv_component& c,
+                                                 bool stop) {
+  R xmin = prm<R>(c, 0), xmax = prm<R>(c, 1), ymin = prm<R>(c, 2),
+    ymax = prm<R>(c, 3), r2 = prm<R>(c, 4), cut = prm<R>(c, 5);
+  R x = n.x, y = n.y, z = n.z, vx = n.vx, vy = n.vy, vz = n.vz;
+  if ((z < 0 && vz <= 0) || (z > 0 && vz >= 0)) return;
+  if (n.p < cut) {
+    n.p = R(-1);
+    return;
+  }
+  R dt = R(0);
+  if (z != 0) {
+    dt = -z / vz;
+    x += vx * dt;
+    y += vy * dt;
+  }
+  bool in;
+  if (r2 != 0) in = x * x + y * y <= r2;
+  else in = xmin <= x && x <= xmax && ymin <= y && y <= ymax;
+  if (stop ? in : !in) {
+    n.p = R(-1);
+    return;
+  }
+  n.x = x;
+  n.y = y;
+  n.z = R(0);
+  if (z != 0) n.t.add(dt);
+}
+
+}  // namespace mcv

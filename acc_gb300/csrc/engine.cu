@@ -1,0 +1,673 @@
+// engine.cu -- propagation kernels and the extern "C" entry points declared
+// in include/acc_gb300.h.
+//
+// One thread carries one neutron at a time through the whole chain; the
+// grid strides over neutron indices.  The chain description is a
+// __grid_constant__ kernel parameter, so component parameters are read from
+// the constant bank and every lane of a warp dispatches on the same opcode.
+
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+#include "common.cuh"
+#include "components.cuh"
+#include "monitors.cuh"
+#include "sample.cuh"
+
+namespace mcv {
+
+enum { kFlagIdentityRot = 1 };
+
+__device__ __forceinline__ uint64_t comp_nbins(const mcv_component& c) {
+  switch (c.opcode) {
+    case MCV_OP_PSD_MONITOR:
+    case MCV_OP_PSD_MONITOR_4PI:
+    case MCV_OP_POSDIV_MONITOR:
+    case MCV_OP_IQE_MONITOR:
+    case MCV_OP_THETA_TOF_4PI:
+    case MCV_OP_CYL_IQE_DETECTOR:
+      return (uint64_t)c.ip[0] * (uint64_t)c.ip[1];
+    case MCV_OP_WAVELENGTH_MONITOR:
+    case MCV_OP_ENERGY_MONITOR:
+      return (uint64_t)c.ip[0];
+    case MCV_OP_BANKED_DETECTOR:
+      return (uint64_t)c.ip[0] * c.ip[1] * c.ip[2] * c.ip[3];
+    default:
+      return 0;
+  }
+}
+
+// r' = rot (r - off), v' = rot v  (acc/vec3.py:148-159, acc/neutron.py:18-23)
+template <typename R>
+__device__ __forceinline__ void apply_transform(Neutron<R>& n,
+                                                const mcv_chain& ch, int k) {
+  const R* o = chain_off<R>(ch, k);
+  R tx = n.x - o[0], ty = n.y - o[1], tz = n.z - o[2];
+  if (ch.comp[k].flags & kFlagIdentityRot) {
+    n.x = tx;
+    n.y = ty;
+    n.z = tz;
+    return;
+  }
+  const R* m = chain_rot<R>(ch, k);
+  n.x = m[0] * tx + m[1] * ty + m[2] * tz;
+  n.y = m[3] * tx + m[4] * ty + m[5] * tz;
+  n.z = m[6] * tx + m[7] * ty + m[8] * tz;
+  R vx = m[0] * n.vx + m[1] * n.vy + m[2] * n.vz;
+  R vy = m[3] * n.vx + m[4] * n.vy + m[5] * n.vz;
+  R vz = m[6] * n.vx + m[7] * n.vy + m[8] * n.vz;
+  n.vx = vx;
+  n.vy = vy;
+  n.vz = vz;
+}
+
+// One component on one neutron; returns 1 when a guide ran out of bounces.
+template <typename R, typename Rng>
+__device__ __forceinline__ int run_component(Neutron<R>& n, Rng& rng,
+                                             const mcv_component& c) {
+  Tally tl{c.tally, comp_nbins(c)};
+  switch (c.opcode) {
+    case MCV_OP_SOURCE_SIMPLE:
+      source_simple<R>(n, rng, c);
+      return 0;
+    case MCV_OP_GUIDE:
+      return guide<R>(n, c);
+    case MCV_OP_HSS:
+      hss(n, rng, c);
+      return 0;
+    case MCV_OP_PSD_MONITOR:
+      psd_monitor<R>(n, c, tl);
+      return 0;
+    case MCV_OP_PSD_MONITOR_4PI:
+      psd_monitor_4pi<R>(n, c, tl);
+      return 0;
+    case MCV_OP_WAVELENGTH_MONITOR:
+      wavelength_monitor<R>(n, c, tl);
+      return 0;
+    case MCV_OP_POSDIV_MONITOR:
+      posdiv_monitor<R>(n, c, tl);
+      return 0;
+    case MCV_OP_IQE_MONITOR:
+      iqe_monitor<R>(n, c, tl);
+      return 0;
+    case MCV_OP_ENERGY_MONITOR:
+      energy_monitor<R>(n, c, tl);
+      return 0;
+    case MCV_OP_THETA_TOF_4PI:
+      theta_tof_4pi<R>(n, c, tl);
+      return 0;
+    case MCV_OP_CYL_IQE_DETECTOR:
+      cyl_iqe<R>(n, c, tl);
+      return 0;
+    case MCV_OP_BANKED_DETECTOR:
+      banked<R>(n, c, tl);
+      return 0;
+    case MCV_OP_SLIT:
+      slit_or_beamstop<R>(n, c, false);
+      return 0;
+    case MCV_OP_BEAMSTOP:
+      slit_or_beamstop<R>(n, c, true);
+      return 0;
+    default:  // MCV_OP_ARM
+      return 0;
+  }
+}
+
+struct Counters {
+  unsigned processed, overflow, nonfinite, overrun;
+};
+
+// Whole chain on one neutron (the body of the generated
+// process_kernel_no_buffer, acc/run_script.py:182-196).  A neutron leaves
+// the chain after a component that leaves its weight not positive.
+template <typename R, typename Rng>
+__device__ __forceinline__ int run_chain_one(Neutron<R>& n, Rng& rng,
+                                             const mcv_chain& ch,
+                                             Counters& k) {
+  int last = -1;
+  const int nc = ch.ncomp;
+  for (int c = 0; c < nc; ++c) {
+    if (c > 0) apply_transform<R>(n, ch, c);
+    last = c;
+    k.overflow += run_component<R>(n, rng, ch.comp[c]);
+    if (!(n.p > 0)) {
+      if (m_isnan(n.p)) k.nonfinite++;
+      break;
+    }
+  }
+  return last;
+}
+
+template <typename R>
+__device__ __forceinline__ void zero_neutron(Neutron<R>& n) {
+  n.x = n.y = n.z = n.vx = n.vy = n.vz = n.sx = n.sy = n.p = R(0);
+  n.t.set(R(0));
+}
+
+template <typename R>
+__device__ __forceinline__ void store_neutron(const Neutron<R>& n,
+                                              double* out) {
+  out[0] = n.x;
+  out[1] = n.y;
+  out[2] = n.z;
+  out[3] = n.vx;
+  out[4] = n.vy;
+  out[5] = n.vz;
+  out[6] = n.sx;
+  out[7] = n.sy;
+  out[8] = n.t.dval();
+  out[9] = n.p;
+}
+
+__device__ __forceinline__ void flush_counters(const Counters& k,
+                                               DevStatus* st) {
+  unsigned p = __reduce_add_sync(0xffffffffu, k.processed);
+  unsigned o = __reduce_add_sync(0xffffffffu, k.overflow);
+  unsigned f = __reduce_add_sync(0xffffffffu, k.nonfinite);
+  unsigned r = __reduce_add_sync(0xffffffffu, k.overrun);
+  if ((threadIdx.x & 31) == 0) {
+    if (p) atomicAdd(&st->processed, (unsigned long long)p);
+    if (o) atomicAdd(&st->bounce_overflow, (unsigned long long)o);
+    if (f) atomicAdd(&st->nonfinite, (unsigned long long)f);
+    if (r) atomicAdd(&st->rng_overrun, (unsigned long long)r);
+  }
+}
+
+constexpr int kMaxThreads = 256;
+
+// MODE 0: Philox; 1: Philox + record; 2: injected uniforms + record
+template <typename R, int MODE>
+__global__ void __launch_bounds__(kMaxThreads)
+    chain_kernel(const __grid_constant__ mcv_chain ch, uint64_t n,
+                 uint64_t first, uint64_t seed, const float* __restrict__ uni,
+                 int stride, double* __restrict__ out_n,
+                 int* __restrict__ out_last, DevStatus* st) {
+  Counters k{0, 0, 0, 0};
+  const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += step) {
+    Neutron<R> nt;
+    zero_neutron(nt);
+    int last;
+    if constexpr (MODE == 2) {
+      InjectedStream rng(uni + i * (uint64_t)stride, stride);
+      last = run_chain_one<R>(nt, rng, ch, k);
+      k.overrun += rng.overrun();
+    } else {
+      PhiloxStream rng(seed, first + i, 0u);
+      last = run_chain_one<R>(nt, rng, ch, k);
+    }
+    k.processed++;
+    if constexpr (MODE != 0) {
+      if (out_n) store_neutron(nt, out_n + i * 10);
+      if (out_last) out_last[i] = last;
+    }
+  }
+  flush_counters(k, st);
+}
+
+// Buffered mode (ComponentBase.process, ComponentBase.py:79-129): the chain
+// applied to a stored neutron array in place; component k draws from
+// Philox stream k+1.
+template <typename R>
+__global__ void __launch_bounds__(kMaxThreads)
+    buffer_kernel(const __grid_constant__ mcv_chain ch, R* __restrict__ buf,
+                  uint64_t n, uint64_t first, uint64_t seed, DevStatus* st) {
+  Counters k{0, 0, 0, 0};
+  const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += step) {
+    R* s = buf + i * 10;
+    Neutron<R> nt;
+    nt.x = s[0];
+    nt.y = s[1];
+    nt.z = s[2];
+    nt.vx = s[3];
+    nt.vy = s[4];
+    nt.vz = s[5];
+    nt.sx = s[6];
+    nt.sy = s[7];
+    nt.t.set(s[8]);
+    nt.p = s[9];
+    for (int c = 0; c < ch.ncomp; ++c) {
+      const mcv_component& cp = ch.comp[c];
+      if (cp.opcode != MCV_OP_SOURCE_SIMPLE && !(nt.p > 0)) break;
+      if (c > 0) apply_transform<R>(nt, ch, c);
+      PhiloxStream rng(seed, first + i, (uint32_t)(c + 1));
+      k.overflow += run_component<R>(nt, rng, cp);
+    }
+    k.processed++;
+    s[0] = nt.x;
+    s[1] = nt.y;
+    s[2] = nt.z;
+    s[3] = nt.vx;
+    s[4] = nt.vy;
+    s[5] = nt.vz;
+    s[6] = nt.sx;
+    s[7] = nt.sy;
+    s[8] = (R)nt.t.dval();
+    s[9] = nt.p;
+  }
+  flush_counters(k, st);
+}
+
+// Geometry probe: sorted hit times of rays with an HSS shape.
+template <typename R>
+__global__ void intersect_kernel(const __grid_constant__ mcv_component c,
+                                 const double* __restrict__ rays, uint64_t n,
+                                 double* __restrict__ out_ts,
+                                 int* __restrict__ out_n) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double* r = rays + i * 6;
+  Hits<R> h = intersect_shape<R>(c, (R)r[0], (R)r[1], (R)r[2], (R)r[3],
+                                 (R)r[4], (R)r[5]);
+  double* o = out_ts + i * MCV_MAX_INTERSECTIONS;
+  for (int k = 0; k < MCV_MAX_INTERSECTIONS; ++k)
+    o[k] = k < h.n ? (double)h.get(k) : __longlong_as_double(0x7ff8000000000000ll);
+  out_n[i] = h.n;
+}
+
+}  // namespace mcv
+
+// =================================================================== host
+using namespace mcv;
+
+struct mcv_ctx {
+  int device;
+  int sm_count;
+  DevStatus* d_status;
+};
+
+namespace {
+
+void set_msg(mcv_status* st, int code, const char* fmt, const char* a = "",
+             long long b = 0) {
+  if (!st) return;
+  st->code = code;
+  snprintf(st->message, sizeof st->message, fmt, a, b);
+}
+
+int cuda_fail(mcv_status* st, cudaError_t e, const char* where) {
+  set_msg(st, MCV_ECUDA, "%s: CUDA error %lld", where, (long long)e);
+  if (st) {
+    size_t l = strlen(st->message);
+    snprintf(st->message + l, sizeof st->message - l, " (%s)",
+             cudaGetErrorString(e));
+  }
+  return MCV_ECUDA;
+}
+
+class DeviceGuard {
+ public:
+  explicit DeviceGuard(int dev) {
+    cudaGetDevice(&prev_);
+    if (prev_ != dev) cudaSetDevice(dev);
+    dev_ = dev;
+  }
+  ~DeviceGuard() {
+    if (prev_ != dev_) cudaSetDevice(prev_);
+  }
+
+ private:
+  int prev_ = 0, dev_ = 0;
+};
+
+int validate_component(const mcv_component& c, int k, mcv_status* st) {
+  if (c.opcode < 0 || c.opcode >= MCV_OP_COUNT) {
+    set_msg(st, MCV_EINVAL, "component %s%lld: unknown opcode", "",
+            (long long)k);
+    return MCV_EINVAL;
+  }
+  switch (c.opcode) {
+    case MCV_OP_PSD_MONITOR:
+    case MCV_OP_PSD_MONITOR_4PI:
+    case MCV_OP_POSDIV_MONITOR:
+    case MCV_OP_IQE_MONITOR:
+    case MCV_OP_THETA_TOF_4PI:
+    case MCV_OP_CYL_IQE_DETECTOR:
+      if (c.ip[0] < 1 || c.ip[1] < 1) {
+        set_msg(st, MCV_EINVAL, "component %s%lld: bin counts must be >= 1",
+                "", (long long)k);
+        return MCV_EINVAL;
+      }
+      break;
+    case MCV_OP_WAVELENGTH_MONITOR:
+    case MCV_OP_ENERGY_MONITOR:
+      if (c.ip[0] < 1) {
+        set_msg(st, MCV_EINVAL, "component %s%lld: bin count must be >= 1", "",
+                (long long)k);
+        return MCV_EINVAL;
+      }
+      break;
+    case MCV_OP_BANKED_DETECTOR:
+      if (c.ip[0] < 1 || c.ip[1] < 1 || c.ip[2] < 1 || c.ip[3] < 1) {
+        set_msg(st, MCV_EINVAL, "component %s%lld: bin counts must be >= 1",
+                "", (long long)k);
+        return MCV_EINVAL;
+      }
+      break;
+    case MCV_OP_HSS: {
+      int op = c.ip[0], ker = c.ip[1];
+      bool shape_ok = c.ip[2] >= MCV_SHAPE_SPHERE && c.ip[2] <= MCV_SHAPE_BOX &&
+                      op >= MCV_CSG_PRIMITIVE && op <= MCV_CSG_INTERSECTION &&
+                      (op == MCV_CSG_PRIMITIVE ||
+                       (c.ip[3] >= MCV_SHAPE_SPHERE && c.ip[3] <= MCV_SHAPE_BOX));
+      if (!shape_ok) {
+        set_msg(st, MCV_EINVAL, "component %s%lld: bad shape description", "",
+                (long long)k);
+        return MCV_EINVAL;
+      }
+      if (ker == MCV_KERNEL_POWDER &&
+          (!c.table || !c.ftable || c.ip[4] < 1 || c.dp[10] <= 0)) {
+        set_msg(st, MCV_EINVAL, "component %s%lld: powder kernel needs peaks",
+                "", (long long)k);
+        return MCV_EINVAL;
+      }
+      if (ker == MCV_KERNEL_SQE_GRID &&
+          (!c.ftable || c.ip[4] < 2 || c.ip[5] < 2)) {
+        set_msg(st, MCV_EINVAL,
+                "component %s%lld: S(Q,E) kernel needs a >= 2x2 table", "",
+                (long long)k);
+        return MCV_EINVAL;
+      }
+      if (ker < MCV_KERNEL_ISOTROPIC || ker > MCV_KERNEL_SQE_GRID) {
+        set_msg(st, MCV_EINVAL, "component %s%lld: unknown scattering kernel",
+                "", (long long)k);
+        return MCV_EINVAL;
+      }
+      break;
+    }
+    default:
+      break;
+  }
+  return MCV_OK;
+}
+
+int validate_chain(const mcv_chain* ch, mcv_status* st) {
+  if (!ch) {
+    set_msg(st, MCV_EINVAL, "chain is NULL%s", "");
+    return MCV_EINVAL;
+  }
+  if (ch->ncomp < 1 || ch->ncomp > MCV_MAX_COMPONENTS) {
+    set_msg(st, MCV_EINVAL, "chain has %s%lld components (1..16 allowed)", "",
+            (long long)ch->ncomp);
+    return MCV_EINVAL;
+  }
+  for (int k = 0; k < ch->ncomp; ++k) {
+    int rc = validate_component(ch->comp[k], k, st);
+    if (rc) return rc;
+  }
+  return MCV_OK;
+}
+
+int precision_ok(int precision, mcv_status* st) {
+  if (precision != MCV_FP32 && precision != MCV_FP64) {
+    set_msg(st, MCV_EINVAL, "precision must be 32 or 64, got %s%lld", "",
+            (long long)precision);
+    return 0;
+  }
+  return 1;
+}
+
+template <typename K>
+void launch_shape(const mcv_ctx* ctx, K kernel, uint64_t n,
+                  const mcv_launch* launch, int* blocks, int* threads) {
+  int t = (launch && launch->threads_per_block > 0) ? launch->threads_per_block
+                                                    : kMaxThreads;
+  if (t > kMaxThreads) t = kMaxThreads;
+  t = (t + 31) / 32 * 32;
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, t, 0);
+  if (per_sm < 1) per_sm = 1;
+  uint64_t want = (n + t - 1) / t;
+  uint64_t full = (uint64_t)ctx->sm_count * per_sm;
+  uint64_t b = (launch && launch->blocks > 0) ? (uint64_t)launch->blocks
+                                              : (want < full ? want : full);
+  if (b < 1) b = 1;
+  if (b > 0x7fffffff) b = 0x7fffffff;
+  *blocks = (int)b;
+  *threads = t;
+}
+
+template <typename R, int MODE>
+int launch_chain(mcv_ctx* ctx, const mcv_chain* chain, uint64_t ncount,
+                 uint64_t first, uint64_t seed, const float* uni, int stride,
+                 double* out_n, int* out_last, const mcv_launch* launch,
+                 cudaStream_t s) {
+  int blocks, threads;
+  launch_shape(ctx, chain_kernel<R, MODE>, ncount, launch, &blocks, &threads);
+  chain_kernel<R, MODE><<<blocks, threads, 0, s>>>(
+      *chain, ncount, first, seed, uni, stride, out_n, out_last,
+      ctx->d_status);
+  return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mcv_abi_version(void) { return MCV_ABI_VERSION; }
+
+int mcv_struct_sizes(uint64_t* component, uint64_t* chain, uint64_t* status,
+                     uint64_t* launch) {
+  if (component) *component = sizeof(mcv_component);
+  if (chain) *chain = sizeof(mcv_chain);
+  if (status) *status = sizeof(mcv_status);
+  if (launch) *launch = sizeof(mcv_launch);
+  return MCV_OK;
+}
+
+int mcv_ctx_create(int device, mcv_ctx** out) {
+  if (!out) return MCV_EINVAL;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+    cudaGetLastError();
+    return MCV_ENODEV;
+  }
+  if (device < 0 || device >= ndev) return MCV_EINVAL;
+  DeviceGuard g(device);
+  mcv_ctx* c = new (std::nothrow) mcv_ctx;
+  if (!c) return MCV_ECAPACITY;
+  c->device = device;
+  cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
+  if (cudaMalloc(&c->d_status, sizeof(DevStatus)) != cudaSuccess) {
+    cudaGetLastError();
+    delete c;
+    return MCV_ECUDA;
+  }
+  if (cudaMemset(c->d_status, 0, sizeof(DevStatus)) != cudaSuccess) {
+    cudaFree(c->d_status);
+    delete c;
+    return MCV_ECUDA;
+  }
+  *out = c;
+  return MCV_OK;
+}
+
+int mcv_ctx_destroy(mcv_ctx* ctx) {
+  if (!ctx) return MCV_OK;
+  {
+    DeviceGuard g(ctx->device);
+    cudaFree(ctx->d_status);
+  }
+  delete ctx;
+  return MCV_OK;
+}
+
+int mcv_ctx_status(mcv_ctx* ctx, void* stream, uint64_t expected,
+                   mcv_status* st) {
+  if (!ctx) return MCV_EINVAL;
+  DeviceGuard g(ctx->device);
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(st, e, "kernel execution");
+  DevStatus h;
+  e = cudaMemcpyAsync(&h, ctx->d_status, sizeof h, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_status, 0, sizeof h, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(st, e, "status read");
+  int code = MCV_OK;
+  if (st) {
+    st->processed = h.processed;
+    st->bounce_overflow = h.bounce_overflow;
+    st->nonfinite = h.nonfinite;
+    st->bin_oob = h.bin_oob;
+    st->code = MCV_OK;
+    st->message[0] = 0;
+  }
+  if (h.rng_overrun) {
+    code = MCV_EINVAL;
+    set_msg(st, code,
+            "%s%lld neutrons drew more uniforms than the replay stride holds",
+            "", (long long)h.rng_overrun);
+  } else if (expected && h.processed != expected) {
+    code = MCV_ECOUNT;
+    set_msg(st, code, "processed neutron count %s%lld does not match request",
+            "", (long long)h.processed);
+  } else if (h.bounce_overflow) {
+    code = MCV_EBOUNCE;
+    set_msg(st, code, "%s%lld neutrons reached the guide bounce limit", "",
+            (long long)h.bounce_overflow);
+  }
+  return code;
+}
+
+int mcv_run_chain(mcv_ctx* ctx, const mcv_chain* chain, uint64_t ncount,
+                  uint64_t first, uint64_t seed, int precision,
+                  const mcv_launch* launch, void* stream, mcv_status* st) {
+  int rc = validate_chain(chain, st);
+  if (rc) return rc;
+  if (!precision_ok(precision, st)) return MCV_EINVAL;
+  if (!ctx) {
+    set_msg(st, MCV_EINVAL, "context is NULL%s", "");
+    return MCV_EINVAL;
+  }
+  if (ncount == 0) return st ? mcv_ctx_status(ctx, stream, 0, st) : MCV_OK;
+  DeviceGuard g(ctx->device);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (precision == MCV_FP32)
+    launch_chain<float, 0>(ctx, chain, ncount, first, seed, nullptr, 0,
+                           nullptr, nullptr, launch, s);
+  else
+    launch_chain<double, 0>(ctx, chain, ncount, first, seed, nullptr, 0,
+                            nullptr, nullptr, launch, s);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(st, e, "mcv_run_chain launch");
+  if (st) return mcv_ctx_status(ctx, stream, ncount, st);
+  return MCV_OK;
+}
+
+int mcv_replay_uniforms(mcv_ctx* ctx, const mcv_chain* chain, uint64_t ncount,
+                        uint64_t first, uint64_t seed, int precision,
+                        const float* uniforms, int32_t stride,
+                        double* out_neutrons, int32_t* out_last,
+                        const mcv_launch* launch, void* stream,
+                        mcv_status* st) {
+  int rc = validate_chain(chain, st);
+  if (rc) return rc;
+  if (!precision_ok(precision, st)) return MCV_EINVAL;
+  if (!ctx) {
+    set_msg(st, MCV_EINVAL, "context is NULL%s", "");
+    return MCV_EINVAL;
+  }
+  if (uniforms && stride < 1) {
+    set_msg(st, MCV_EINVAL, "uniform stride must be >= 1%s", "");
+    return MCV_EINVAL;
+  }
+  if (ncount == 0) return st ? mcv_ctx_status(ctx, stream, 0, st) : MCV_OK;
+  DeviceGuard g(ctx->device);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (precision == MCV_FP32) {
+    if (uniforms)
+      launch_chain<float, 2>(ctx, chain, ncount, first, seed, uniforms, stride,
+                             out_neutrons, out_last, launch, s);
+    else
+      launch_chain<float, 1>(ctx, chain, ncount, first, seed, nullptr, 0,
+                             out_neutrons, out_last, launch, s);
+  } else {
+    if (uniforms)
+      launch_chain<double, 2>(ctx, chain, ncount, first, seed, uniforms,
+                              stride, out_neutrons, out_last, launch, s);
+    else
+      launch_chain<double, 1>(ctx, chain, ncount, first, seed, nullptr, 0,
+                              out_neutrons, out_last, launch, s);
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(st, e, "mcv_replay_uniforms launch");
+  if (st) return mcv_ctx_status(ctx, stream, ncount, st);
+  return MCV_OK;
+}
+
+int mcv_process_buffer(mcv_ctx* ctx, const mcv_chain* chain, void* neutrons,
+                       uint64_t n, uint64_t first, uint64_t seed,
+                       int precision, const mcv_launch* launch, void* stream,
+                       mcv_status* st) {
+  int rc = validate_chain(chain, st);
+  if (rc) return rc;
+  if (!precision_ok(precision, st)) return MCV_EINVAL;
+  if (!ctx) {
+    set_msg(st, MCV_EINVAL, "context is NULL%s", "");
+    return MCV_EINVAL;
+  }
+  if (n == 0) return st ? mcv_ctx_status(ctx, stream, 0, st) : MCV_OK;
+  if (!neutrons) {
+    set_msg(st, MCV_EINVAL, "neutron buffer is NULL%s", "");
+    return MCV_EINVAL;
+  }
+  DeviceGuard g(ctx->device);
+  cudaStream_t s = (cudaStream_t)stream;
+  int blocks, threads;
+  if (precision == MCV_FP32) {
+    launch_shape(ctx, buffer_kernel<float>, n, launch, &blocks, &threads);
+    buffer_kernel<float><<<blocks, threads, 0, s>>>(
+        *chain, (float*)neutrons, n, first, seed, ctx->d_status);
+  } else {
+    launch_shape(ctx, buffer_kernel<double>, n, launch, &blocks, &threads);
+    buffer_kernel<double><<<blocks, threads, 0, s>>>(
+        *chain, (double*)neutrons, n, first, seed, ctx->d_status);
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(st, e, "mcv_process_buffer launch");
+  if (st) return mcv_ctx_status(ctx, stream, n, st);
+  return MCV_OK;
+}
+
+int mcv_intersect(mcv_ctx* ctx, const mcv_component* hss, const double* rays,
+                  uint64_t n, double* out_ts, int32_t* out_n, int precision,
+                  void* stream, mcv_status* st) {
+  if (!ctx || !hss || hss->opcode != MCV_OP_HSS) {
+    set_msg(st, MCV_EINVAL, "mcv_intersect needs an HSS component%s", "");
+    return MCV_EINVAL;
+  }
+  int rc = validate_component(*hss, 0, st);
+  if (rc) return rc;
+  if (!precision_ok(precision, st)) return MCV_EINVAL;
+  if (n == 0) return MCV_OK;
+  if (!rays || !out_ts || !out_n) {
+    set_msg(st, MCV_EINVAL, "mcv_intersect: NULL buffer%s", "");
+    return MCV_EINVAL;
+  }
+  DeviceGuard g(ctx->device);
+  cudaStream_t s = (cudaStream_t)stream;
+  unsigned blocks = (unsigned)((n + 127) / 128);
+  if (precision == MCV_FP32)
+    intersect_kernel<float><<<blocks, 128, 0, s>>>(*hss, rays, n, out_ts,
+                                                   out_n);
+  else
+    intersect_kernel<double><<<blocks, 128, 0, s>>>(*hss, rays, n, out_ts,
+                                                    out_n);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(st, e, "mcv_intersect launch");
+  if (st) {
+    e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(st, e, "mcv_intersect");
+    st->code = MCV_OK;
+    st->message[0] = 0;
+  }
+  return MCV_OK;
+}
+
+}  // extern "C"

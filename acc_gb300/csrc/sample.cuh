@@ -1,0 +1,762 @@
+// sample.cuh -- the homogeneous single scatterer: shape intersection,
+// scattering point and the isotropic / powder / gridded S(Q,E) kernels.
+#pragma once
+
+#include "common.cuh"
+
+namespace mcv {
+
+constexpr double kGeomEps = 1e-10;  // acc/geometry/__init__.py:2
+enum { kOutside = 1, kOnBorder = 0, kInside = -1 };
+
+// ============================================================ intersections
+// cu_device_intersect_sphere (acc/geometry/arrow_intersect.py:154-168).  In
+// FP32 the discriminant v^2 R^2 - |r x v|^2 is recomputed in FP64 when it is
+// within 1e-4 of v^2 R^2 of zero (near tangency).
+template <typename R>
+__device__ __forceinline__ bool isect_sphere(R x, R y, R z, R vx, R vy, R vz,
+                                             R Rad, R& t1, R& t2) {
+  R r0dotv = x * vx + y * vy + z * vz;
+  R cx = y * vz - z * vy, cy = z * vx - x * vz, cz = x * vy - y * vx;
+  R v2 = vx * vx + vy * vy + vz * vz;
+  R r0Xv2 = cx * cx + cy * cy + cz * cz;
+  R vR2 = v2 * Rad * Rad;
+  R disc = vR2 - r0Xv2;
+  if constexpr (sizeof(R) == 4) {
+    if (fabsf(disc) < 1e-4f * vR2) {
+      double X = x, Y = y, Z = z, VX = vx, VY = vy, VZ = vz, RR = Rad;
+      double CX = Y * VZ - Z * VY, CY = Z * VX - X * VZ, CZ = X * VY - Y * VX;
+      double V2 = VX * VX + VY * VY + VZ * VZ;
+      disc = (float)(V2 * RR * RR - (CX * CX + CY * CY + CZ * CZ));
+    }
+  }
+  if (disc < 0) return false;
+  R s = m_sqrt(disc);
+  t1 = -(r0dotv + s) / v2;
+  t2 = -(r0dotv - s) / v2;
+  return true;
+}
+
+// intersectCylinderSide / TopBottom / cu_device_intersect_cylinder
+// (arrow_intersect.py:178-267); cylinder x^2 + y^2 = R^2, |z| < H/2.
+template <typename R>
+__device__ __forceinline__ bool isect_cylinder(R x, R y, R z, R vx, R vy,
+                                               R vz, R Rad, R H, R& o1,
+                                               R& o2) {
+  const R NaN = R(__int_as_float(0x7fc00000));
+  // side
+  R a = vx * vx + vy * vy, b = x * vx + y * vy, c = x * x + y * y - Rad * Rad;
+  R k = b * b - a * c;
+  if constexpr (sizeof(R) == 4) {
+    if (fabsf(k) < 1e-4f * (b * b)) {
+      double A = (double)vx * vx + (double)vy * vy;
+      double B = (double)x * vx + (double)y * vy;
+      double C = (double)x * x + (double)y * y - (double)Rad * Rad;
+      k = (float)(B * B - A * C);
+    }
+  }
+  R hh = H / R(2);
+  int n1 = 0;
+  R t1 = NaN, t2 = NaN;
+  if (!(k < 0 || a == 0)) {
+    bool done = false;
+    if (k == 0) {
+      R t = -b / a;
+      if (m_fabs(z + vz * t) < hh) {
+        n1 = 1;
+        t1 = t;
+        done = true;
+      }
+    }
+    if (!done) {
+      R sk = m_sqrt(k);
+      R ta = (-b + sk) / a, tb = (-b - sk) / a;
+      bool ga = m_fabs(z + vz * ta) < hh, gb = m_fabs(z + vz * tb) < hh;
+      if (ga && gb) { n1 = 2; t1 = tb; t2 = ta; }
+      else if (ga) { n1 = 1; t1 = ta; }
+      else if (gb) { n1 = 1; t1 = tb; }
+    }
+  }
+  // caps
+  int n2 = 0;
+  R t3 = NaN, t4 = NaN;
+  if (vz != 0) {
+    R r2 = Rad * Rad;
+    R ta = (hh - z) / vz;
+    R xa = x + vx * ta, ya = y + vy * ta;
+    bool ga = xa * xa + ya * ya <= r2;
+    R tb = (-hh - z) / vz;
+    R xb = x + vx * tb, yb = y + vy * tb;
+    bool gb = xb * xb + yb * yb <= r2;
+    if (ga && gb) {
+      n2 = 2;
+      if (ta < tb) { t3 = ta; t4 = tb; }
+      else { t3 = tb; t4 = ta; }
+    } else if (ga) { n2 = 1; t3 = ta; }
+    else if (gb) { n2 = 1; t3 = tb; }
+  }
+  int nn = n1 + n2;
+  if (nn == 0) return false;
+  if (nn == 1) {
+    if (n1 == 1) { o1 = t1; o2 = t1; }
+    else { o1 = t3; o2 = t3; }
+  } else if (nn == 2) {
+    if (n1 == 1) {
+      if (t1 > t3) { o1 = t3; o2 = t1; }
+      else { o1 = t1; o2 = t3; }
+    } else if (n1 == 0) { o1 = t3; o2 = t4; }
+    else { o1 = t1; o2 = t2; }
+  } else if (nn == 3) {
+    if (n1 == 1) { o1 = t3 < t1 ? t3 : t1; o2 = t4 > t1 ? t4 : t1; }
+    else { o1 = t1 < t3 ? t1 : t3; o2 = t2 > t3 ? t2 : t3; }
+  } else {
+    o1 = t3 < t1 ? t3 : t1;
+    o2 = t4 > t2 ? t4 : t2;
+  }
+  return true;
+}
+
+// cu_device_intersect_rectangle / update_intersections / intersect_box
+// (acc/geometry/onbox.py:8-56)
+template <typename R>
+__device__ __forceinline__ R rect_hit(R rx, R ry, R rz, R vx, R vy, R vz, R X,
+                                      R Y) {
+  R t = -rz / vz;
+  R r1x = rx + vx * t, r1y = ry + vy * t;
+  if (m_fabs(r1x) > X / 2 || m_fabs(r1y) > Y / 2)
+    t = R(__int_as_float(0x7fc00000));
+  return t;
+}
+template <typename R>
+__device__ __forceinline__ void update_hits(R& t1, R& t2, R t) {
+  if (!isfinite(t)) return;
+  if (!isfinite(t1)) { t1 = t; return; }
+  if (!isfinite(t2)) {
+    if (t > t1) t2 = t;
+    else { t2 = t1; t1 = t; }
+    return;
+  }
+  if (t < t1) t1 = t;
+  else if (t < t2) return;
+  else t2 = t;
+}
+template <typename R>
+__device__ __forceinline__ bool isect_box(R x, R y, R z, R vx, R vy, R vz,
+                                          R X, R Y, R Z, R& t1, R& t2) {
+  t1 = R(__int_as_float(0x7fc00000));
+  t2 = t1;
+  if (vz != 0) {
+    update_hits(t1, t2, rect_hit(x, y, z - Z / 2, vx, vy, vz, X, Y));
+    update_hits(t1, t2, rect_hit(x, y, z + Z / 2, vx, vy, vz, X, Y));
+  }
+  if (vx != 0) {
+    update_hits(t1, t2, rect_hit(y, z, x - X / 2, vy, vz, vx, Y, Z));
+    update_hits(t1, t2, rect_hit(y, z, x + X / 2, vy, vz, vx, Y, Z));
+  }
+  if (vy != 0) {
+    update_hits(t1, t2, rect_hit(z, x, y - Y / 2, vz, vx, vy, Z, X));
+    update_hits(t1, t2, rect_hit(z, x, y + Y / 2, vz, vx, vy, Z, X));
+  }
+  return !m_isnan(t1);
+}
+
+template <typename R>
+__device__ __forceinline__ bool isect_prim(int kind, const mcv_component& c,
+                                           int base, R x, R y, R z, R vx,
+                                           R vy, R vz, R& t1, R& t2) {
+  // the render wrappers (arrow_intersect.py:47-86) report no hit when t1
+  // is NaN
+  bool ok = false;
+  if (kind == MCV_SHAPE_SPHERE)
+    ok = isect_sphere<R>(x, y, z, vx, vy, vz, prm<R>(c, base), t1, t2);
+  else if (kind == MCV_SHAPE_CYLINDER)
+    ok = isect_cylinder<R>(x, y, z, vx, vy, vz, prm<R>(c, base),
+                           prm<R>(c, base + 1), t1, t2);
+  else if (kind == MCV_SHAPE_BOX)
+    ok = isect_box<R>(x, y, z, vx, vy, vz, prm<R>(c, base),
+                      prm<R>(c, base + 1), prm<R>(c, base + 2), t1, t2);
+  return ok && !m_isnan(t1);
+}
+
+// point location (acc/geometry/locate.py:354-421).  FP64 uses the
+// reference's epsilon; FP32 a float-resolvable one, 2e-6 of the shape's
+// largest dimension, because 1e-10 m is below float resolution at these
+// coordinates.
+template <typename R>
+__device__ __forceinline__ int locate_prim(int kind, const mcv_component& c,
+                                           int base, R x, R y, R z) {
+  R e;
+  if constexpr (sizeof(R) == 4) {
+    R s = prm<R>(c, base);
+    if (kind != MCV_SHAPE_SPHERE) s = fmaxf(s, prm<R>(c, base + 1));
+    if (kind == MCV_SHAPE_BOX) s = fmaxf(s, prm<R>(c, base + 2));
+    e = 2e-6f * s;
+  } else {
+    e = R(kGeomEps);
+  }
+  if (kind == MCV_SHAPE_SPHERE) {
+    R Rad = prm<R>(c, base), d2 = x * x + y * y + z * z;
+    if (d2 > (Rad + e) * (Rad + e)) return kOutside;
+    if (d2 < (Rad - e) * (Rad - e)) return kInside;
+    return kOnBorder;
+  }
+  if (kind == MCV_SHAPE_CYLINDER) {
+    R Rad = prm<R>(c, base), H = prm<R>(c, base + 1);
+    if (m_fabs(z) - H / R(2) > e) return kOutside;
+    R r2 = x * x + y * y;
+    if (r2 > (Rad + e) * (Rad + e)) return kOutside;
+    if (H / R(2) - m_fabs(z) > e && r2 < (Rad - e) * (Rad - e)) return kInside;
+    return kOnBorder;
+  }
+  if (kind == MCV_SHAPE_BOX) {
+    R W = prm<R>(c, base), H = prm<R>(c, base + 1), D = prm<R>(c, base + 2);
+    if (m_fabs(x) - R(0.5) * W > e) return kOutside;
+    if (m_fabs(y) - R(0.5) * H > e) return kOutside;
+    if (m_fabs(z) - R(0.5) * D > e) return kOutside;
+    if (-R(0.5) * W < x && x < R(0.5) * W && -R(0.5) * H < y &&
+        y < R(0.5) * H && -R(0.5) * D < z && z < R(0.5) * D)
+      return kInside;
+    return kOnBorder;
+  }
+  return kOutside;
+}
+
+template <typename R>
+__device__ __forceinline__ int locate_shape(const mcv_component& c, R x, R y,
+                                            R z) {
+  int op = c.ip[0];
+  int l1 = locate_prim<R>(c.ip[2], c, 0, x, y, z);
+  if (op == MCV_CSG_PRIMITIVE) return l1;
+  int l2 = locate_prim<R>(c.ip[3], c, 4, x, y, z);
+  if (op == MCV_CSG_DIFFERENCE) {
+    if (l1 == kOutside || l2 == kInside) return kOutside;
+    if (l1 == kOnBorder || l2 == kOnBorder) return kOnBorder;
+    return kInside;
+  }
+  if (op == MCV_CSG_UNION) {
+    if (l1 == kInside || l2 == kInside) return kInside;
+    if (l1 == kOutside && l2 == kOutside) return kOutside;
+    return kOnBorder;
+  }
+  if (l1 == kOutside || l2 == kOutside) return kOutside;
+  if (l1 == kInside && l2 == kInside) return kInside;
+  return kOnBorder;
+}
+
+// Up to four sorted hit times in registers.  A primitive gives two; a
+// binary CSG node keeps the on-border hits of both operands merged in order,
+// which is what intersectComposite (arrow_intersect.py:126-142) builds with
+// insert_into_sorted_list (_utils.py:4-32).
+template <typename R>
+struct Hits {
+  R t0, t1, t2, t3;
+  int n;
+  __device__ __forceinline__ R get(int i) const {
+    return i == 0 ? t0 : i == 1 ? t1 : i == 2 ? t2 : t3;
+  }
+};
+
+template <typename R>
+__device__ __forceinline__ void cswap(R& a, R& b) {
+  R lo = a < b ? a : b, hi = a < b ? b : a;
+  a = lo;
+  b = hi;
+}
+
+template <typename R>
+__device__ __forceinline__ Hits<R> intersect_shape(const mcv_component& c,
+                                                   R x, R y, R z, R vx, R vy,
+                                                   R vz) {
+  Hits<R> h;
+  const R inf = R(__int_as_float(0x7f800000));
+  h.t0 = h.t1 = h.t2 = h.t3 = inf;
+  h.n = 0;
+  R a1, a2;
+  bool ha = isect_prim<R>(c.ip[2], c, 0, x, y, z, vx, vy, vz, a1, a2);
+  if (c.ip[0] == MCV_CSG_PRIMITIVE) {
+    if (ha) {
+      h.t0 = a1;
+      h.t1 = a2;
+      h.n = 2;
+    }
+    return h;
+  }
+  R b1, b2;
+  bool hb = isect_prim<R>(c.ip[3], c, 4, x, y, z, vx, vy, vz, b1, b2);
+  R cand[4] = {a1, a2, b1, b2};
+  bool ok[4] = {ha, ha, hb, hb};
+  R s0 = inf, s1 = inf, s2 = inf, s3 = inf;
+  int n = 0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    if (ok[k]) {
+      R t = cand[k];
+      if (locate_shape<R>(c, x + vx * t, y + vy * t, z + vz * t) ==
+          kOnBorder) {
+        if (n == 0) s0 = t;
+        else if (n == 1) s1 = t;
+        else if (n == 2) s2 = t;
+        else s3 = t;
+        ++n;
+      }
+    }
+  }
+  cswap(s0, s1);
+  cswap(s2, s3);
+  cswap(s0, s2);
+  cswap(s1, s3);
+  cswap(s1, s2);
+  h.t0 = s0;
+  h.t1 = s1;
+  h.t2 = s2;
+  h.t3 = s3;
+  h.n = n;
+  return h;
+}
+
+// =========================================================== HSS helpers
+// _calc_time_to_point_of_scattering_impl
+// (homogeneous_single_scatterer.py:121-159) on hit times measured from
+// "now" (FP64 path).
+template <typename R>
+__device__ __forceinline__ void time_to_scatter_ref(const Hits<R>& h, R rand,
+                                                    R& T, R& ttravel,
+                                                    R& tin) {
+  R tps0 = 0, tps1 = 0, tpg0 = 0, tpg1 = 0;
+  T = 0;
+  int sign = 0, ip = 0;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    if (i < h.n) {
+      R t = h.get(i);
+      if (!(t < 0)) {
+        if (sign == 0) sign = (i % 2 == 0) ? -1 : 1;
+        else sign = -sign;
+        T += sign * t;
+        if (sign > 0) {
+          if (ip == 0) { tps0 = T; tpg0 = t; }
+          else { tps1 = T; tpg1 = t; }
+          ++ip;
+        }
+      }
+    }
+  }
+  tin = rand * T;
+  if (ip == 0) {
+    ttravel = 0;
+  } else if (ip == 1 || tin < tps0) {
+    ttravel = tin - tps0 + tpg0;
+  } else {
+    ttravel = tin - tps1 + tpg1;
+  }
+}
+
+// total_time_in_shape (homogeneous_single_scatterer.py:161-178)
+template <typename R>
+__device__ __forceinline__ R total_time_in_shape(const Hits<R>& h) {
+  R T = 0;
+  int sign = 0;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    if (i < h.n) {
+      R t = h.get(i);
+      if (!(t < 0)) {
+        if (sign == 0) sign = (i % 2 == 0) ? -1 : 1;
+        else sign = -sign;
+        T += sign * t;
+      }
+    }
+  }
+  return T;
+}
+
+// ================================================================ kernels
+// isotropic.S (acc/kernels/isotropic.py:5-21)
+template <typename R, typename Rng>
+__device__ __forceinline__ void isotropic_S(Neutron<R>& n, Rng& rng) {
+  R cos_t = R(rng.next()) * 2 - 1;
+  R u2 = rng.next();
+  if (cos_t > 1) cos_t = 1;
+  R sin_t = m_sqrt(1 - cos_t * cos_t);
+  R sin_p, cos_p;
+  m_sincos_2pi(u2, &sin_p, &cos_p);
+  R vi = m_sqrt(n.vx * n.vx + n.vy * n.vy + n.vz * n.vz);
+  n.vx = vi * sin_t * cos_p;
+  n.vy = vi * sin_t * sin_p;
+  n.vz = vi * cos_t;
+}
+
+// vec3._rotate (acc/vec3.py:77-105)
+template <typename R>
+__device__ __forceinline__ void rotate3(R& vx, R& vy, R& vz, R cx, R cy, R cz,
+                                        R angle, R eps) {
+  R cl = m_sqrt(cx * cx + cy * cy + cz * cz);
+  R ci = R(1.0) / cl;
+  cx *= ci;
+  cy *= ci;
+  cz *= ci;
+  R sf = vx * cx + vy * cy + vz * cz;
+  R px = cx * sf, py = cy * sf, pz = cz * sf;
+  R lpl = m_sqrt(px * px + py * py + pz * pz);
+  R lv = m_sqrt(vx * vx + vy * vy + vz * vz);
+  if (m_fabs(1 - lpl / lv) < eps) return;
+  R qx = vx - px, qy = vy - py, qz = vz - pz;
+  R ql = m_sqrt(qx * qx + qy * qy + qz * qz);
+  R qi = R(1.) / ql;
+  qx *= qi;
+  qy *= qi;
+  qz *= qi;
+  R ex = qy * cz - qz * cy, ey = qz * cx - qx * cz, ez = qx * cy - qy * cx;
+  R ca, sa;
+  if constexpr (sizeof(R) == 4) {
+    sincosf(angle, &sa, &ca);
+  } else {
+    sincos(angle, &sa, &ca);
+  }
+  qx *= ca;
+  qy *= ca;
+  qz *= ca;
+  ex *= sa;
+  ey *= sa;
+  ez *= sa;
+  R rx = qx - ex, ry = qy - ey, rz = qz - ez;
+  rx *= ql;
+  ry *= ql;
+  rz *= ql;
+  vx = rx + px;
+  vy = ry + py;
+  vz = rz + pz;
+}
+
+// powder table rows: {q_v, w_v, my_s_v2, cumulative my_s_v2}
+template <typename R>
+__device__ __forceinline__ const R* powder_table(const mcv_component& c);
+template <>
+__device__ __forceinline__ const float* powder_table<float>(
+    const mcv_component& c) {
+  return c.ftable;
+}
+template <>
+__device__ __forceinline__ const double* powder_table<double>(
+    const mcv_component& c) {
+  return (const double*)c.table;
+}
+
+// number of peaks with q_v/2 <= v (q_v ascending)
+template <typename R>
+__device__ __forceinline__ int powder_reach(const R* pk, int np, R vl) {
+  int lo = 0, hi = np;  // first index with vl < q/2
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (vl < __ldg(&pk[4 * mid]) / 2) hi = mid;
+    else lo = mid + 1;
+  }
+  return lo;
+}
+
+// powderdiffr.scattering_coefficient (acc/kernels/powderdiffr.py:10-25).
+// FP64 sums the peaks in order as the reference does; FP32 reads the
+// prefix sum at the reachable count.
+template <typename R>
+__device__ __forceinline__ R powder_coeff(const Neutron<R>& n,
+                                          const mcv_component& c) {
+  const R* pk = powder_table<R>(c);
+  int np = c.ip[4];
+  R vl = m_sqrt(n.vx * n.vx + n.vy * n.vy + n.vz * n.vz);
+  R xs_v2 = 0;
+  if constexpr (sizeof(R) == 4) {
+    int k = powder_reach(pk, np, vl);
+    xs_v2 = k > 0 ? __ldg(&pk[4 * (k - 1) + 3]) : 0.f;
+  } else {
+    for (int i = 0; i < np; ++i)
+      if (vl >= __ldg(&pk[4 * i]) / 2) xs_v2 += __ldg(&pk[4 * i + 2]);
+  }
+  return xs_v2 / (vl * vl) / prm<R>(c, 10);
+}
+
+// powderdiffr.scatter (acc/kernels/powderdiffr.py:27-109), including the
+// reference's peak count: without a break in `for peakindex in range(1,
+// Npeaks)` the count is Npeaks-1.
+template <typename R, typename Rng>
+__device__ __forceinline__ void powder_scatter(Neutron<R>& n, Rng& rng,
+                                               const mcv_component& c) {
+  const R* pk = powder_table<R>(c);
+  int np = c.ip[4];
+  R ucvol = prm<R>(c, 10), d_phi = prm<R>(c, 11);
+  R vx = n.vx, vy = n.vy, vz = n.vz;
+  R vl = m_sqrt(vx * vx + vy * vy + vz * vz);
+  if (vl < __ldg(&pk[0]) / 2) {
+    n.p = R(-1);
+    return;
+  }
+  int nreach;
+  if (np <= 1) {
+    nreach = 1;
+  } else {
+    int k = powder_reach(pk, np, vl);  // >= 1 here
+    nreach = k < np ? k : np - 1;
+  }
+  int peak = 0;
+  if (nreach > 1) {
+    peak = (int)(R(rng.next()) * nreach);
+    if (peak >= nreach) peak = nreach - 1;
+  }
+  R rt = R(rng.next()) * 2 - 1;
+  R q = __ldg(&pk[4 * peak]), w = __ldg(&pk[4 * peak + 1]),
+    s = __ldg(&pk[4 * peak + 2]);
+  R arg = q * (1 + w * rt) / (R(2.0) * vl);
+  R scatter_xs = s / (vl * vl);
+  scatter_xs *= nreach;
+  R theta = m_asin(arg);
+  R alpha = 0, alpha0;
+  const R DEG2RAD = R(kPi / 180.0);
+  if (d_phi != 0) {
+    R a = sin(d_phi * DEG2RAD / 2) / sin(2 * theta);
+    if (a < -1 || a > 1) d_phi = 0;
+    else alpha = 2 * m_asin(a);
+  }
+  if (d_phi != 0) {
+    alpha = m_fabs(alpha);
+    R r = rng.next();
+    alpha0 = 2 * r * alpha;
+    if (alpha0 > alpha) alpha0 = R(kPi) + (alpha0 - R(1.5) * alpha);
+    else alpha0 = alpha0 - R(0.5) * alpha;
+  } else {
+    R r = R(rng.next()) * 2 - 1;
+    alpha0 = R(kPi) * r;
+  }
+  R nx, ny, nz;
+  if (m_fabs(vx) < m_fabs(vz)) { nx = 1; ny = 0; nz = 0; }
+  else { nx = 0; ny = 0; nz = 1; }
+  // vtmp = v x n
+  R tx = vy * nz - vz * ny, ty = vz * nx - vx * nz, tz = vx * ny - vy * nx;
+  R ox = vx, oy = vy, oz = vz;
+  const R eps = R(1e-7);
+  rotate3<R>(ox, oy, oz, tx, ty, tz, 2 * theta, eps);
+  rotate3<R>(ox, oy, oz, vx, vy, vz, alpha0, eps);
+  n.vx = ox;
+  n.vy = oy;
+  n.vz = oz;
+  if (m_isnan(ox) || m_isnan(oy) || m_isnan(oz)) {
+    n.p = R(-1);
+    return;
+  }
+  n.p *= scatter_xs / ucvol;
+}
+
+// Bilinear lookup of the S(Q,E) grid (node (iq, ie) at Qmin + iq dQ,
+// Emin + ie dE; indices clamp to [0, n-2] as SANS2D_ongrid.py:37-50 does).
+template <typename R>
+__device__ __forceinline__ R sqe_lookup(const mcv_component& c, R Q, R E) {
+  const float* S = c.ftable;
+  int nQ = c.ip[4], nE = c.ip[5];
+  R Qmin = prm<R>(c, 10), Qmax = prm<R>(c, 11), Emin = prm<R>(c, 12),
+    Emax = prm<R>(c, 13);
+  R dQ = (Qmax - Qmin) / (nQ - 1), dE = (Emax - Emin) / (nE - 1);
+  int iq = (int)((Q - Qmin) / dQ), ie = (int)((E - Emin) / dE);
+  iq = iq < 0 ? 0 : (iq > nQ - 2 ? nQ - 2 : iq);
+  ie = ie < 0 ? 0 : (ie > nE - 2 ? nE - 2 : ie);
+  R fx = (Q - Qmin) / dQ - iq, fy = (E - Emin) / dE - ie;
+  R f00 = __ldg(&S[iq * nE + ie]), f10 = __ldg(&S[(iq + 1) * nE + ie]);
+  R f01 = __ldg(&S[iq * nE + ie + 1]), f11 = __ldg(&S[(iq + 1) * nE + ie + 1]);
+  // bilinear_interp (SANS2D_ongrid.py:16-22)
+  R a00 = f00, a10 = f10 - f00, a01 = f01 - f00, a11 = f11 - f10 - f01 + f00;
+  return a00 + a10 * fx + a01 * fy + a11 * fx * fy;
+}
+
+// Gridded S(Q,E) kernel: the kinematics of E_Q._S (acc/kernels/E_Q.py:37-99)
+// with (Q, E) uniform over the table box and S from the grid.
+template <typename R, typename Rng>
+__device__ __forceinline__ void sqe_scatter(Neutron<R>& n, Rng& rng,
+                                            const mcv_component& c) {
+  R Qmin = prm<R>(c, 10), Qmax = prm<R>(c, 11), Emin = prm<R>(c, 12),
+    Emax = prm<R>(c, 13);
+  R vx = n.vx, vy = n.vy, vz = n.vz;
+  R vi = m_sqrt(vx * vx + vy * vy + vz * vz);
+  R Ei = vi * vi * R(kVS2E);
+  R Q = R(rng.next()) * (Qmax - Qmin) + Qmin;
+  R E = R(rng.next()) * (Emax - Emin) + Emin;
+  R u3 = rng.next();
+  R Ef = Ei - E;
+  if (Ef <= 0) {
+    n.p = R(-1);
+    return;
+  }
+  R vf = m_sqrt(Ef) * R(kSE2V);
+  R ki = R(kV2K) * vi, kf = R(kV2K) * vf;
+  R cost = (ki * ki + kf * kf - Q * Q) / (2 * ki * kf);
+  R cost2 = cost * cost;
+  if (cost2 > 1) {
+    n.p = R(-1);
+    return;
+  }
+  R sint = m_sqrt(R(1.0) - cost2);
+  R sp, cp;
+  m_sincos_2pi(u3, &sp, &cp);
+  R v2 = vf * sint * cp, v3 = vf * sint * sp, v1 = vf * cost;
+  R inv = R(1.0) / vi;
+  R e1x = vx * inv, e1y = vy * inv, e1z = vz * inv;
+  R nx, ny, nz;
+  if (m_fabs(e1x) > R(1e-1) || m_fabs(e1y) > R(1e-1)) { nx = 0; ny = 0; nz = 1; }
+  else { nx = 1; ny = 0; nz = 0; }
+  R e2x = ny * e1z - nz * e1y, e2y = nz * e1x - nx * e1z,
+    e2z = nx * e1y - ny * e1x;
+  R l2 = R(1.0) / m_sqrt(e2x * e2x + e2y * e2y + e2z * e2z);
+  e2x *= l2;
+  e2y *= l2;
+  e2z *= l2;
+  R e3x = e1y * e2z - e1z * e2y, e3y = e1z * e2x - e1x * e2z,
+    e3z = e1x * e2y - e1y * e2x;
+  n.vx = e1x * v1 + e2x * v2 + e3x * v3;
+  n.vy = e1y * v1 + e2y * v2 + e3y * v3;
+  n.vz = e1z * v1 + e2z * v2 + e3z * v3;
+  R S = sqe_lookup<R>(c, Q, E);
+  R prob_f = S * (vf / vi) * Q * (Qmax - Qmin) * (Emax - Emin) / (kf * ki) / 2;
+  n.p *= prob_f;
+}
+
+template <typename R>
+__device__ __forceinline__ R hss_sigma(const Neutron<R>& n,
+                                       const mcv_component& c) {
+  if (c.ip[1] == MCV_KERNEL_POWDER) return powder_coeff<R>(n, c);
+  return prm<R>(c, 9);
+}
+
+template <typename R>
+__device__ __forceinline__ R hss_mu(const Neutron<R>& n,
+                                    const mcv_component& c) {
+  // calc_absorption_coeff (acc/kernels/__init__.py:156-161)
+  R v = m_sqrt(n.vx * n.vx + n.vy * n.vy + n.vz * n.vz);
+  return prm<R>(c, 8) / v * 2200;
+}
+
+template <typename R, typename Rng>
+__device__ __forceinline__ void hss_kernel(Neutron<R>& n, Rng& rng,
+                                           const mcv_component& c) {
+  switch (c.ip[1]) {
+    case MCV_KERNEL_ISOTROPIC:
+      n.p *= prm<R>(c, 9);  // kernels/__init__.py:42
+      isotropic_S<R>(n, rng);
+      break;
+    case MCV_KERNEL_POWDER:
+      powder_scatter<R>(n, rng, c);
+      break;
+    case MCV_KERNEL_SQE_GRID:
+      n.p *= prm<R>(c, 9);
+      sqe_scatter<R>(n, rng, c);
+      break;
+    default:
+      break;
+  }
+}
+
+// HomogeneousSingleScatterer.propagate
+// (acc/components/samples/homogeneous_single_scatterer.py:62-100), FP64:
+// the reference's sequence.
+template <typename Rng>
+__device__ __forceinline__ void hss(Neutron<double>& n, Rng& rng,
+                                    const mcv_component& c) {
+  double x = n.x, y = n.y, z = n.z, vx = n.vx, vy = n.vy, vz = n.vz;
+  Hits<double> h = intersect_shape<double>(c, x, y, z, vx, vy, vz);
+  if (h.n < 2) return;
+  if (h.get(h.n - 1) <= 0) return;
+  double rand = rng.next();
+  double T, ttravel, tin;
+  time_to_scatter_ref<double>(h, rand, T, ttravel, tin);
+  double dt = ttravel;
+  if (dt <= 0) return;
+  prop_dt(n, dt);
+  double v = sqrt(vx * vx + vy * vy + vz * vz);
+  double dist = v * tin;
+  double fulllen = v * T;
+  double sigma = hss_sigma<double>(n, c);
+  double mu = hss_mu<double>(n, c);
+  double atten = exp(-(mu + sigma) * dist);
+  n.p *= fulllen * atten;
+  hss_kernel<double>(n, rng, c);
+  if (n.p <= 0) return;
+  h = intersect_shape<double>(c, n.x, n.y, n.z, n.vx, n.vy, n.vz);
+  double dt3 = total_time_in_shape<double>(h);
+  prop_dt(n, dt3);
+  sigma = hss_sigma<double>(n, c);
+  mu = hss_mu<double>(n, c);
+  // the reference uses the incident speed v here (line 98)
+  double atten2 = exp(-(mu + sigma) * v * dt3);
+  n.p *= atten2;
+}
+
+// FP32 form of the same propagate.  The incoming ray is first moved to its
+// closest approach p0 to the shape's origin (tau = 0 there, "now" is at
+// tau_now = -t0), all hit times are measured on that tau axis, and every
+// length that the reference forms as a difference of times measured from
+// "now" is formed as a difference of tau values.  In exact arithmetic this
+// is the reference's sequence; in float it avoids cancelling metre-scale
+// flight times against centimetre-scale chords.
+template <typename Rng>
+__device__ __forceinline__ void hss(Neutron<float>& n, Rng& rng,
+                                    const mcv_component& c) {
+  float vx = n.vx, vy = n.vy, vz = n.vz;
+  float v2 = vx * vx + vy * vy + vz * vz;
+  float t0 = -(n.x * vx + n.y * vy + n.z * vz) / v2;
+  float px = fmaf(vx, t0, n.x), py = fmaf(vy, t0, n.y), pz = fmaf(vz, t0, n.z);
+  float tau_now = -t0;
+  Hits<float> h = intersect_shape<float>(c, px, py, pz, vx, vy, vz);
+  if (h.n < 2) return;
+  if (h.get(h.n - 1) <= tau_now) return;
+  float rand = rng.next();
+  // segments ahead of "now": (enter, exit) pairs of the sorted hits; when
+  // the first hit ahead has odd index the neutron is inside and the first
+  // segment starts at "now".
+  float T = 0.f, seg_a[2] = {0.f, 0.f}, seg_b[2] = {0.f, 0.f};
+  int nseg = 0;
+  int i0 = 0;
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+    if (i < h.n && h.get(i) < tau_now) i0 = i + 1;
+  int j = i0;
+  if (i0 & 1) {
+    seg_a[0] = tau_now;
+    seg_b[0] = h.get(i0);
+    nseg = 1;
+    j = i0 + 1;
+  }
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    if (nseg < 2 && j + 1 < h.n) {
+      float a = h.get(j), b = h.get(j + 1);
+      if (nseg == 0) { seg_a[0] = a; seg_b[0] = b; }
+      else { seg_a[1] = a; seg_b[1] = b; }
+      ++nseg;
+      j += 2;
+    }
+  }
+  float L0 = seg_b[0] - seg_a[0], L1 = nseg > 1 ? seg_b[1] - seg_a[1] : 0.f;
+  T = L0 + L1;
+  float tin = rand * T;
+  // scattering point on the tau axis (reference: the first segment whose
+  // cumulative in-shape time exceeds tin, else the last one)
+  float tau_s = (nseg == 1 || tin < L0) ? seg_b[0] - (L0 - tin)
+                                        : seg_b[1] - (T - tin);
+  float dt = tau_s - tau_now;
+  if (!(dt > 0.f) || nseg == 0) return;
+  n.x = fmaf(vx, tau_s, px);
+  n.y = fmaf(vy, tau_s, py);
+  n.z = fmaf(vz, tau_s, pz);
+  n.t.add(t0);
+  n.t.add(tau_s);
+  float v = sqrtf(v2);
+  float dist = v * tin, fulllen = v * T;
+  float sigma = hss_sigma<float>(n, c);
+  float mu = hss_mu<float>(n, c);
+  n.p *= fulllen * __expf(-(mu + sigma) * dist);
+  hss_kernel<float>(n, rng, c);
+  if (n.p <= 0.f) return;
+  h = intersect_shape<float>(c, n.x, n.y, n.z, n.vx, n.vy, n.vz);
+  float dt3 = total_time_in_shape<float>(h);
+  prop_dt(n, dt3);
+  sigma = hss_sigma<float>(n, c);
+  mu = hss_mu<float>(n, c);
+  n.p *= __expf(-(mu + sigma) * v * dt3);
+}
+
+}  // namespace mcv

@@ -1,0 +1,200 @@
+"""Host side of the engine: assemble an mcv_chain from components and call
+the C ABI (include/acc_gb300.h) through ctypes.
+
+Device memory (tallies, tables, neutron arrays) is allocated with torch;
+only raw pointers cross into the library.
+"""
+
+import ctypes
+
+import numpy as np
+
+from . import _native as nat
+from . import config
+from .instrument import calcTransformations
+
+
+def build_chain(components, offsets=None, rotmats=None, binder=None):
+    """An mcv_chain for `components`, with the frame transforms between
+    consecutive components (identity when offsets/rotmats are None)."""
+    if not 1 <= len(components) <= nat.MCV_MAX_COMPONENTS:
+        raise ValueError(
+            f"a chain holds 1..{nat.MCV_MAX_COMPONENTS} components, "
+            f"got {len(components)}")
+    if binder is None:
+        from .memory import DeviceBinder
+        binder = DeviceBinder()
+    ch = nat.mcv_chain()
+    # the chain holds raw pointers into memory the binder owns
+    ch._binder = binder
+    ch.ncomp = len(components)
+    eye = np.eye(3)
+    for i, comp in enumerate(components):
+        c = ch.comp[i]
+        comp.pack(c, binder)
+        if i == 0:
+            continue
+        if offsets is None:
+            off, rot = np.zeros(3), eye
+        else:
+            off = np.asarray(offsets[i - 1], dtype=float)
+            rot = np.asarray(rotmats[i - 1], dtype=float)
+        for k in range(9):
+            ch.rot[i][k] = float(rot.flat[k])
+            ch.frot[i][k] = float(rot.flat[k])
+        for k in range(3):
+            ch.off[i][k] = float(off[k])
+            ch.foff[i][k] = float(off[k])
+        if np.array_equal(rot, eye):
+            c.flags |= nat.FLAG_IDENTITY_ROT
+    return ch
+
+
+def chain_for_instrument(instrument, binder=None):
+    offsets, rotmats = calcTransformations(instrument)
+    return build_chain(instrument.components, offsets, rotmats, binder)
+
+
+def _launch(threads_per_block=None, blocks=None):
+    if not threads_per_block and not blocks:
+        return None
+    L = nat.mcv_launch()
+    L.threads_per_block = int(threads_per_block or 0)
+    L.blocks = int(blocks or 0)
+    return L
+
+
+def _precision(floattype):
+    return config.precision_bits(floattype)
+
+
+def run_chain(chain, ncount, seed=None, floattype=None, first=0,
+              threads_per_block=None, blocks=None, sync=True, device=None):
+    """mcv_run_chain: ncount neutrons through the fused chain kernel.
+    Returns the mcv_status (sync=True) or None."""
+    ctx = nat.context(device)
+    st = nat.mcv_status() if sync else None
+    L = _launch(threads_per_block, blocks)
+    seed = config.rng_seed if seed is None else seed
+    rc = nat.lib().mcv_run_chain(
+        ctx.handle, ctypes.byref(chain), int(ncount), int(first), int(seed),
+        _precision(floattype), ctypes.byref(L) if L else None,
+        nat.current_stream_handle(), ctypes.byref(st) if st else None)
+    nat.check(rc, st)
+    return st
+
+
+def run_instrument(instrument, ncount, **kw):
+    chain = chain_for_instrument(instrument)
+    return run_chain(chain, ncount, **kw)
+
+
+def run_components(components, ncount, threads_per_block=None, **kw):
+    chain = build_chain(list(components))
+    return run_chain(chain, ncount, threads_per_block=threads_per_block, **kw)
+
+
+def replay(chain, ncount, uniforms=None, seed=None, floattype=None, first=0,
+           record=True, threads_per_block=None, blocks=None, device=None):
+    """mcv_replay_uniforms: returns (neutrons (ncount, 10) float64 on the
+    GPU, last component index (ncount,) int32)."""
+    import torch
+    ctx = nat.context(device)
+    dev = torch.device("cuda", ctx.device)
+    st = nat.mcv_status()
+    out = torch.empty((int(ncount), 10), dtype=torch.float64, device=dev) \
+        if record else None
+    last = torch.empty(int(ncount), dtype=torch.int32, device=dev) \
+        if record else None
+    stride = 0
+    uptr = None
+    if uniforms is not None:
+        u = torch.as_tensor(uniforms, dtype=torch.float32).to(dev).contiguous()
+        if u.ndim != 2 or u.shape[0] != ncount:
+            raise ValueError("uniforms must have shape (ncount, stride)")
+        stride = u.shape[1]
+        uptr = ctypes.c_void_p(u.data_ptr())
+    L = _launch(threads_per_block, blocks)
+    seed = config.rng_seed if seed is None else seed
+    rc = nat.lib().mcv_replay_uniforms(
+        ctx.handle, ctypes.byref(chain), int(ncount), int(first), int(seed),
+        _precision(floattype), uptr, int(stride),
+        ctypes.c_void_p(out.data_ptr()) if record else None,
+        ctypes.c_void_p(last.data_ptr()) if record else None,
+        ctypes.byref(L) if L else None, nat.current_stream_handle(),
+        ctypes.byref(st))
+    nat.check(rc, st)
+    return out, last
+
+
+def process_buffer(components, neutrons, seed=None, first=0, floattype=None,
+                   offsets=None, rotmats=None, device=None):
+    """mcv_process_buffer on a host (N, 10) array; returns the updated host
+    array (float64)."""
+    import torch
+    ctx = nat.context(device)
+    dev = torch.device("cuda", ctx.device)
+    prec = _precision(floattype)
+    dt = torch.float32 if prec == 32 else torch.float64
+    arr = np.ascontiguousarray(neutrons, dtype=np.float64).reshape(-1, 10)
+    buf = torch.from_numpy(arr).to(dev, dtype=dt).contiguous()
+    chain = build_chain(list(components), offsets, rotmats)
+    st = nat.mcv_status()
+    seed = config.rng_seed if seed is None else seed
+    rc = nat.lib().mcv_process_buffer(
+        ctx.handle, ctypes.byref(chain), ctypes.c_void_p(buf.data_ptr()),
+        arr.shape[0], int(first), int(seed), prec, None,
+        nat.current_stream_handle(), ctypes.byref(st))
+    nat.check(rc, st)
+    return buf.to(torch.float64).cpu().numpy()
+
+
+def intersect(hss_component, rays, floattype="float64", device=None):
+    """mcv_intersect: sorted hit times (N, 10; NaN padded) and counts (N,)."""
+    import torch
+    ctx = nat.context(device)
+    dev = torch.device("cuda", ctx.device)
+    from .memory import DeviceBinder
+    c = hss_component.to_struct(DeviceBinder())
+    r = torch.as_tensor(np.asarray(rays, dtype=np.float64).reshape(-1, 6),
+                        device=dev).contiguous()
+    n = r.shape[0]
+    ts = torch.empty((n, nat.MCV_MAX_INTERSECTIONS), dtype=torch.float64,
+                     device=dev)
+    cnt = torch.empty(n, dtype=torch.int32, device=dev)
+    st = nat.mcv_status()
+    rc = nat.lib().mcv_intersect(
+        ctx.handle, ctypes.byref(c), ctypes.c_void_p(r.data_ptr()), n,
+        ctypes.c_void_p(ts.data_ptr()), ctypes.c_void_p(cnt.data_ptr()),
+        _precision(floattype), nat.current_stream_handle(), ctypes.byref(st))
+    nat.check(rc, st)
+    return ts.cpu().numpy(), cnt.cpu().numpy()
+
+
+def read_status(expected=0, device=None):
+    """mcv_ctx_status: synchronise, read and reset the context's counters,
+    check `expected` processed neutrons (0 = no check)."""
+    ctx = nat.context(device)
+    st = nat.mcv_status()
+    rc = nat.lib().mcv_ctx_status(ctx.handle, nat.current_stream_handle(),
+                                  int(expected), ctypes.byref(st))
+    nat.check(rc, st)
+    return st
+
+
+def probe_fma_peak(precision=32, repeats=3, device=None):
+    """Measured FMA-pipe peak of the current GPU in TFLOP/s."""
+    ctx = nat.context(device)
+    out = ctypes.c_double()
+    nat.check(nat.lib().mcv_probe_fma_peak(ctx.device, int(precision),
+                                           int(repeats), ctypes.byref(out)))
+    return out.value
+
+
+def probe_atomic_rate(nbins, repeats=3, device=None):
+    """Measured FP64 atomicAdd rate (ops/s) into `nbins` doubles."""
+    ctx = nat.context(device)
+    out = ctypes.c_double()
+    nat.check(nat.lib().mcv_probe_atomic_rate(ctx.device, int(nbins),
+                                              int(repeats), ctypes.byref(out)))
+    return out.value

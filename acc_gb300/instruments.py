@@ -1,0 +1,160 @@
+"""Example instruments: the workloads the engine is benchmarked and tested on.
+
+sphere_theta_tof   disc source -> isotropic sphere -> 4pi theta x tof shell
+guide_chain        disc source -> 10 m guide -> 5 m tapered guide ->
+                   100x100 PSD + 200-bin energy monitor
+sqe_hollow_cylinder  60 meV beam -> hollow cylinder with a gridded S(Q,E)
+                   -> 3 m cylinder detector binned in I(Q,E)
+powder_banked      guide chain -> powder cylinder -> banked cylinder detector
+
+Numbers that the workload descriptions leave open are fixed here once
+(source distance, gaps between components, detector heights, number
+densities) and documented beside each builder.
+"""
+
+import math
+
+import numpy as np
+
+from .components.monitors.cylinder_detectors import (BankedCylinder_detector,
+                                                     CylinderIQE_detector)
+from .components.monitors.energy_monitor import Energy_monitor
+from .components.monitors.psd_monitor import PSD_monitor
+from .components.monitors.theta_tof_monitor_4pi import ThetaTOF_monitor_4Pi
+from .components.optics.guide import Guide
+from .components.samples.homogeneous_single_scatterer import factory
+from .components.sources.source_simple import Source_simple
+from .geometry import Cylinder, HollowCylinder, Sphere
+from .instrument import instrument
+from .kernels import (IsotropicKernel, Peak, SimplePowderDiffractionKernel,
+                      SQEGridKernel, coefficient_from_cross_section)
+
+COATING = dict(R0=0.99, Qc=0.0219, alpha=3.0, m=3.0, W=0.003)
+
+
+def sphere_theta_tof(ntheta=180, ntof=200):
+    """Disc source (r = 5 cm) aimed at a 1 x 1 cm target 5 m away, E uniform
+    in 50-70 meV; isotropic sphere r = 1 cm at the target with
+    sigma_s = sigma_a = 5 b and n = 0.05 /A^3 (25 /m each, absorption at
+    2200 m/s); 4pi shell of radius 3 m around the sample binned
+    theta 0-180 deg x tof 0-10 ms."""
+    ins = instrument("sphere_theta_tof")
+    src = Source_simple("source", radius=0.05, dist=5.0, xw=0.01, yh=0.01,
+                        E0=60.0, dE=10.0)
+    mu = coefficient_from_cross_section(0.05, 5.0)
+    sigma = coefficient_from_cross_section(0.05, 5.0)
+    HSS = factory(Sphere(0.01), IsotropicKernel(mu, sigma))
+    mon = ThetaTOF_monitor_4Pi("theta_tof", radius=3.0, ntheta=ntheta,
+                               ntof=ntof, tofmin=0.0, tofmax=0.01,
+                               filename="theta_tof.h5")
+    ins.append(src, position=(0, 0, 0))
+    ins.append(HSS("sample"), position=(0, 0, 5.0))
+    ins.append(mon, position=(0, 0, 5.0))
+    return ins
+
+
+def guide_chain(extra=None):
+    """Disc source (r = 5 cm, E uniform 5-100 meV) aimed at the 5 x 5 cm
+    entrance of a 10 m straight guide 1 m away; a 5 m guide tapering
+    5 x 5 cm -> 2 x 2 cm follows after a 1 mm gap (coating m=3, R0=0.99,
+    Qc=0.0219 /A, alpha=3, W=0.003 /A); 1 mm after its exit a 100 x 100
+    PSD over +-3 cm and a 200-bin energy monitor over 0-100 meV (same
+    +-3 cm aperture).  `extra` components are appended at the exit."""
+    ins = instrument("guide_chain")
+    src = Source_simple("source", radius=0.05, dist=1.0, xw=0.05, yh=0.05,
+                        E0=52.5, dE=47.5)
+    g1 = Guide("guide1", w1=0.05, h1=0.05, w2=0.05, h2=0.05, l=10.0,
+               **COATING)
+    g2 = Guide("guide2", w1=0.05, h1=0.05, w2=0.02, h2=0.02, l=5.0, **COATING)
+    psd = PSD_monitor("psd", xmin=-0.03, xmax=0.03, ymin=-0.03, ymax=0.03,
+                      nx=100, ny=100, filename="psd.h5")
+    emon = Energy_monitor("energy", xmin=-0.03, xmax=0.03, ymin=-0.03,
+                          ymax=0.03, Emin=0.0, Emax=100.0, nchan=200,
+                          filename="energy.h5")
+    ins.append(src, position=(0, 0, 0))
+    ins.append(g1, position=(0, 0, 1.0))
+    ins.append(g2, position=(0, 0, 11.001))
+    z = 16.002
+    ins.append(psd, position=(0, 0, z))
+    ins.append(emon, position=(0, 0, z))
+    for c in extra or ():
+        ins.append(c, position=(0, 0, z))
+    return ins
+
+
+def sqe_table(nQ=200, nE=200, Qmin=0.0, Qmax=10.0, Emin=-50.0, Emax=55.0):
+    """Gaussian ridge of width 2 meV at E = 30 |sin(Q/2)| meV times
+    exp(-0.01 Q^2) on nQ x nE nodes spanning the box."""
+    Q = np.linspace(Qmin, Qmax, nQ)[:, None]
+    E = np.linspace(Emin, Emax, nE)[None, :]
+    S = np.exp(-(E - 30 * np.abs(np.sin(Q / 2))) ** 2 / (2 * 2.0 ** 2)) * \
+        np.exp(-0.01 * Q ** 2)
+    return S.astype(np.float32)
+
+
+def sqe_hollow_cylinder(S=None, sigma_abs_barn=2.0, number_density=0.05,
+                        sigma_s_barn=5.0, nQ=100, nE=100):
+    """1 x 1 cm source, monochromatic 60 meV, aimed at a 1 x 1 cm target
+    5 m away; hollow cylinder r 1.0-1.2 cm, height 5 cm, axis vertical,
+    sigma_abs = 2 b, sigma_s = 5 b at 0.05 /A^3; S(Q,E) from `sqe_table`
+    over Q 0-10 /A, E -50..55 meV; a vertical detector cylinder of radius
+    3 m and height 2 m binned 100 x 100 in I(Q, E)."""
+    ins = instrument("sqe_hollow_cylinder")
+    src = Source_simple("source", radius=0, width=0.01, height=0.01, dist=5.0,
+                        xw=0.01, yh=0.01, E0=60.0, dE=0.0)
+    if S is None:
+        S = sqe_table()
+    ker = SQEGridKernel(S, 0.0, 10.0, -50.0, 55.0,
+                        coefficient_from_cross_section(number_density,
+                                                       sigma_abs_barn),
+                        coefficient_from_cross_section(number_density,
+                                                       sigma_s_barn))
+    HSS = factory(HollowCylinder(0.010, 0.012, 0.05), ker)
+    det = CylinderIQE_detector("iqe", radius=3.0, height=2.0, Ei=60.0,
+                               Qmin=0.0, Qmax=10.0, nQ=nQ, Emin=-50.0,
+                               Emax=55.0, nE=nE, filename="iqe.h5")
+    ins.append(src, position=(0, 0, 0))
+    # the cylinder's axis is local z; orientation (90, 0, 0) turns it vertical
+    ins.append(HSS("sample"), position=(0, 0, 5.0), orientation=(90, 0, 0))
+    ins.append(det, position=(0, 0, 5.0))
+    return ins
+
+
+def powder_peaks(npeaks=50, seed=0):
+    """npeaks peaks with d uniform in 0.5-4 A, F^2 lognormal(0, 1),
+    multiplicity from {2,4,6,8,12,24}, Debye-Waller exp(-0.005/d^2)."""
+    rng = np.random.default_rng(seed)
+    d = rng.uniform(0.5, 4.0, npeaks)
+    F2 = rng.lognormal(0.0, 1.0, npeaks)
+    mult = rng.choice([2, 4, 6, 8, 12, 24], npeaks)
+    peaks = [Peak(q=2 * math.pi / di, F_squared=f, multiplicity=int(m),
+                  DebyeWaller_factor=math.exp(-0.005 / di ** 2),
+                  intrinsic_line_width=0.0)
+             for di, f, m in zip(d, F2, mult)]
+    return sorted(peaks, key=lambda p: p.q)
+
+
+def powder_banked(peaks=None, unitcell_volume=66.4, nbanks=8, ntubes=128,
+                  npixels=256, ntof=1000):
+    """The guide chain feeding a powder cylinder (r = 0.5 cm, h = 4 cm,
+    axis vertical) 0.5 m past the guide exit, and a banked vertical
+    cylinder detector of radius 3 m and height 1 m around it: 8 banks of
+    15 deg separated by 5 deg gaps from 10 deg, 128 tubes x 256 pixels,
+    tof 0-20 ms in 1000 bins."""
+    ins = guide_chain()
+    peaks = powder_peaks() if peaks is None else peaks
+    ker = SimplePowderDiffractionKernel(peaks, unitcell_volume,
+                                        absorption_cross_section=0.23,
+                                        incoherent_cross_section=0.0,
+                                        coherent_cross_section=1.5)
+    HSS = factory(Cylinder(0.005, 0.04), ker)
+    det = BankedCylinder_detector("banked", radius=3.0, height=1.0,
+                                  nbanks=nbanks, ntubes=ntubes,
+                                  npixels=npixels, bank_angle0=10.0,
+                                  bank_width=15.0, bank_gap=5.0, tofmin=0.0,
+                                  tofmax=0.02, ntof=ntof,
+                                  filename="banked.h5")
+    z = 16.002 + 0.5
+    ins.append(HSS("sample"), position=(0, 0, z), orientation=(90, 0, 0))
+    ins.append(det, position=(0, 0, z))
+    return ins

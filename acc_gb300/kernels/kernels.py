@@ -1,0 +1,133 @@
+"""Kernel descriptions packed into an HSS component.
+
+mu (absorption) and sigma (scattering) are coefficients in 1/m; mu is the
+value at 2200 m/s and scales as 1/v (acc/kernels/__init__.py:149-161).
+"""
+
+from collections import namedtuple
+from math import pi
+
+import numpy as np
+
+from .. import _native as nat
+from ..conversion import K2V, V2K
+
+
+def coefficient_from_cross_section(number_density, cross_section_barn):
+    """n [1/A^3] x sigma [barn] -> 1/m (1 barn/A^3 = 100 /m)."""
+    return float(number_density) * float(cross_section_barn) * 100.0
+
+
+class IsotropicKernel:
+    """isotropic.S (acc/kernels/isotropic.py:5-21) with p *= sigma
+    (acc/kernels/__init__.py:36-44)."""
+    kind = nat.KERNEL_ISOTROPIC
+
+    def __init__(self, absorption_coefficient, scattering_coefficient):
+        self.absorption_coefficient = float(absorption_coefficient)
+        self.scattering_coefficient = float(scattering_coefficient)
+
+    def pack(self, comp, c, binder, set_param):
+        set_param(c, 8, self.absorption_coefficient)
+        set_param(c, 9, self.scattering_coefficient)
+
+
+Peak = namedtuple("Peak", "q F_squared multiplicity DebyeWaller_factor "
+                  "intrinsic_line_width")
+
+
+class PowderDiffraction:
+    """Peak tables of acc/kernels/powderdiffr.py:112-155: per peak
+    my_s_v2 = 4 pi^3 pack DW / V / V2K^2 * mult F^2 / q * XsectionFactor,
+    q_v = q K2V, w_v = intrinsic line width; peaks sorted by q."""
+
+    def __init__(self, peaks, unitcell_volume, absorption_cross_section,
+                 incoherent_cross_section, coherent_cross_section, pack=1.,
+                 XsectionFactor=100., d_phi=0):
+        n = len(peaks)
+        q_v = np.zeros(n)
+        w_v = np.zeros(n)
+        my_s_v2 = np.zeros(n)
+        for i, pk in enumerate(peaks):
+            dw = pk.DebyeWaller_factor
+            dw = dw if dw > 0 else 1.0
+            my_s_v2[i] = 4 * pi * pi * pi * pack * dw / unitcell_volume / (V2K * V2K)
+            my_s_v2[i] *= (pk.multiplicity * pk.F_squared / pk.q) * XsectionFactor
+            q_v[i] = pk.q * K2V
+            w_v[i] = pk.intrinsic_line_width
+            if i > 0:
+                assert q_v[i - 1] <= q_v[i], "peaks must be sorted by q"
+        self.absorption_cross_section = pack * absorption_cross_section
+        self.absorption_coeff = absorption_cross_section / unitcell_volume * 100
+        self.incoherent_cross_section = incoherent_cross_section
+        self.coherent_cross_section = coherent_cross_section
+        self.Npeaks = n
+        self.q_v, self.w_v, self.my_s_v2 = q_v, w_v, my_s_v2
+        self.d_phi = d_phi
+        self.unitcell_volume = unitcell_volume
+
+    def table(self):
+        """rows {q_v, w_v, my_s_v2, cumulative my_s_v2} (float64)."""
+        return np.stack([self.q_v, self.w_v, self.my_s_v2,
+                         np.cumsum(self.my_s_v2)], axis=1)
+
+
+class SimplePowderDiffractionKernel:
+    """powderdiffr.scatter / scattering_coefficient
+    (acc/kernels/powderdiffr.py:10-109); mu defaults to the kernel's
+    absorption cross section over the unit cell."""
+    kind = nat.KERNEL_POWDER
+
+    def __init__(self, peaks, unitcell_volume, absorption_cross_section=0.,
+                 incoherent_cross_section=0., coherent_cross_section=0.,
+                 d_phi=0, pack=1., absorption_coefficient=None):
+        self.peaks = sorted(peaks, key=lambda p: p.q)
+        self.unitcell_volume = float(unitcell_volume)
+        self.pd = PowderDiffraction(
+            self.peaks, self.unitcell_volume, absorption_cross_section,
+            incoherent_cross_section, coherent_cross_section, pack=pack,
+            d_phi=d_phi)
+        self.absorption_coefficient = (
+            self.pd.absorption_coeff if absorption_coefficient is None
+            else float(absorption_coefficient))
+
+    def pack(self, comp, c, binder, set_param):
+        tab = self.pd.table()
+        set_param(c, 8, self.absorption_coefficient)
+        set_param(c, 9, 0.0)
+        set_param(c, 10, self.unitcell_volume)
+        set_param(c, 11, self.pd.d_phi)
+        c.ip[4] = self.pd.Npeaks
+        c.table = binder.table(comp, "powder", tab, np.float64)
+        c.ftable = binder.table(comp, "powder_f32", tab, np.float32)
+        c.table_len = tab.size
+
+
+class SQEGridKernel:
+    """Gridded S(Q,E) kernel: S sampled on nQ x nE nodes spanning
+    [Qmin, Qmax] x [Emin, Emax], bilinear in between; (Q, E) drawn uniformly
+    over that box with the kinematics of acc/kernels/E_Q.py:37-99.
+    No reference counterpart."""
+    kind = nat.KERNEL_SQE_GRID
+
+    def __init__(self, S, Qmin, Qmax, Emin, Emax, absorption_coefficient,
+                 scattering_coefficient):
+        S = np.ascontiguousarray(S, dtype=np.float32)
+        if S.ndim != 2 or S.shape[0] < 2 or S.shape[1] < 2:
+            raise ValueError("S must be a (nQ >= 2, nE >= 2) array")
+        self.S = S
+        self.Qmin, self.Qmax = float(Qmin), float(Qmax)
+        self.Emin, self.Emax = float(Emin), float(Emax)
+        self.absorption_coefficient = float(absorption_coefficient)
+        self.scattering_coefficient = float(scattering_coefficient)
+
+    def pack(self, comp, c, binder, set_param):
+        set_param(c, 8, self.absorption_coefficient)
+        set_param(c, 9, self.scattering_coefficient)
+        for k, v in enumerate((self.Qmin, self.Qmax, self.Emin, self.Emax)):
+            set_param(c, 10 + k, v)
+        c.ip[4], c.ip[5] = self.S.shape
+        p = binder.table(comp, "sqe", self.S, np.float32)
+        c.table = p
+        c.ftable = p
+        c.table_len = self.S.size

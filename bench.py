@@ -1,0 +1,450 @@
+#!/usr/bin/env python
+"""Benchmark of the fused neutron-propagation kernel on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+A step is one pass of the hot path over one batch: `--ncount` Monte-Carlo
+neutrons (default 1e8) through the guide-chain instrument (disc source ->
+10 m guide -> 5 m tapered guide -> 100x100 PSD + 200-bin energy monitor).
+The headline `value` is FP32-fused neutrons/s over all ranks (each rank
+runs its own neutron index range: weak scaling); the FP64 plain kernel is
+timed the same way beside it, and chi^2/dof between the two histograms
+(independent streams) is reported.  `e2e` repeats the FP32 measurement
+through the public API with host buffers: tallies copied host->device
+before and device->host after every step.
+
+--impl reference times the CPU restatement of the reference algorithm (the
+oracle: the reference itself is Python/Numba and its CPU engine is not
+installable here) on all host cores, on the same workload and metric.
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = ("neutrons/s, FP32 fused vs FP64 plain on 1 GB300 at "
+          "χ²/dof≤1.1; bwd/fwd cost")
+UNIT = "neutrons/s"
+
+WORKLOADS = {
+    "guide_chain": (
+        "guide_chain: disc source r=5cm E 5-100 meV -> 10 m guide 5x5 cm m=3 "
+        "-> 5 m taper 5->2 cm -> PSD 100x100 +-3 cm + energy 200 bins 0-100 "
+        "meV"),
+    "sphere_theta_tof": (
+        "sphere_theta_tof: disc source -> isotropic sphere r=1cm -> 4pi shell "
+        "r=3m theta 180 x tof 200"),
+    "sqe_hollow_cylinder": (
+        "sqe_hollow_cylinder: 60 meV 1x1 cm beam -> hollow cylinder with "
+        "200x200 S(Q,E) -> 3 m cylinder I(Q,E) 100x100"),
+}
+
+# Executed FP32 arithmetic (2*FFMA + FADD + FMUL, thread level) and warp
+# instructions per neutron of the FP32 chain kernel, counted by ncu on the
+# same workload (profiles/chain_kernel_fp32_guide_chain.md).  None until
+# a capture exists.
+KERNEL_COUNTS = {
+    "guide_chain": {"fp32_flops_per_neutron": None,
+                    "warp_inst_per_neutron": None,
+                    "dram_bytes_per_neutron": None},
+}
+
+
+def parse_args(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS),
+                    default="guide_chain")
+    ap.add_argument("--ncount", type=float, default=1e8)
+    ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0,
+                    help="CPU baseline sample length")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    a = ap.parse_args(argv)
+    if a.warmup < 0 or a.steps < 1:
+        ap.error("need --steps >= 1 and --warmup >= 0")
+    return a
+
+
+def build_instrument(name):
+    from acc_gb300 import instruments
+    return getattr(instruments, name)()
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clock/throttle samples taken during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,"
+              "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.dev = device_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.dev}",
+                 f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-f", self.path],
+                stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [],
+                    "note": "nvidia-smi unavailable"}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    smax.append(float(f[2]))
+                    power.append(float(f[3]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, f[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(n)
+        finally:
+            os.unlink(self.path)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [],
+                    "note": "no samples"}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "power_w_max": max(power) if power else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+# --------------------------------------------------------- GPU timing
+def time_chain(chain, ncount, steps, warmup, floattype, seed, first0, world,
+               rank, flush):
+    """Warm up, then time exactly `steps` launches with CUDA events on the
+    launching stream (L2 flushed between launches, outside the events).
+    Returns per-step milliseconds."""
+    import torch
+    import torch.distributed as dist
+    from acc_gb300 import engine
+    stream = torch.cuda.current_stream()
+    for w in range(warmup):
+        engine.run_chain(chain, ncount, seed=seed, floattype=floattype,
+                         first=first0 + (w * world + rank) * ncount,
+                         sync=False)
+    engine.read_status(expected=warmup * ncount if warmup else 0)
+    evs = [(torch.cuda.Event(enable_timing=True),
+            torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    base = first0 + warmup * world * ncount
+    for k in range(steps):
+        flush.zero_()
+        evs[k][0].record(stream)
+        engine.run_chain(chain, ncount, seed=seed, floattype=floattype,
+                         first=base + (k * world + rank) * ncount, sync=False)
+        evs[k][1].record(stream)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    engine.read_status(expected=steps * ncount)
+    return [a.elapsed_time(b) for a, b in evs]
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def e2e_run(ins, ncount, steps, warmup, seed, world, rank):
+    """The FP32 run through the public API with host tallies: per step,
+    pinned host -> device tally copies, the chain call, device -> host
+    copies and the status check (which synchronises)."""
+    import torch
+    from acc_gb300 import engine
+    from acc_gb300.components.monitors.MonitorBase import MonitorBase
+    chain = engine.chain_for_instrument(ins)
+    mons = [c for c in ins.components if isinstance(c, MonitorBase)]
+    dev = [m._device_tally for m in mons]
+    host = [torch.zeros(t.numel(), dtype=torch.float64).pin_memory()
+            for t in dev]
+    h2d = sum(t.numel() * 8 for t in dev) + __import__("ctypes").sizeof(chain)
+    d2h = sum(t.numel() * 8 for t in dev)
+
+    def step(k):
+        for h, d in zip(host, dev):
+            d.copy_(h, non_blocking=True)
+        engine.run_chain(chain, ncount, seed=seed, floattype="float32",
+                         first=(k * world + rank) * ncount, sync=False)
+        for h, d in zip(host, dev):
+            h.copy_(d, non_blocking=True)
+        engine.read_status(expected=ncount)
+
+    for k in range(warmup):
+        step(k)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(steps):
+        step(warmup + k)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    return dt, h2d, d2h
+
+
+# ---------------------------------------------------------- CPU baseline
+def cpu_oracle_rate(workload, seconds, seed, nthreads=0):
+    """Neutrons/s of the CPU oracle on a bounded sample of the workload."""
+    from acc_gb300.engine import build_chain
+    from acc_gb300.instrument import calcTransformations
+    from acc_gb300.memory import HostBinder
+    from oracle import binding as O
+    ins = build_instrument(workload)
+    off, rot = calcTransformations(ins)
+    ch = build_chain(ins.components, off, rot, HostBinder())
+    nthreads = nthreads or os.cpu_count() or 1
+    chunk = 1_000_000
+    O.run_chain(ch, 100_000, seed=seed, nthreads=nthreads)  # warm
+    done, t0 = 0, time.perf_counter()
+    while True:
+        O.run_chain(ch, chunk, seed=seed, first=done, nthreads=nthreads)
+        done += chunk
+        el = time.perf_counter() - t0
+        if el >= seconds:
+            break
+        if el > 0.5 and done / el * (seconds - el) > 4 * chunk:
+            chunk *= 2
+    return done / el, done, nthreads
+
+
+def cpu_model():
+    try:
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu model")):
+                return line.split(":", 1)[1].strip()
+        out = subprocess.run(["lscpu"], capture_output=True, text=True).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name"):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
+# ------------------------------------------------------------- arms
+def reference_arm(a, rank, world):
+    if rank != 0:
+        return 0
+    sample = max(2_000_000, int(a.ncount) // 5)
+    from acc_gb300.engine import build_chain
+    from acc_gb300.instrument import calcTransformations
+    from acc_gb300.memory import HostBinder
+    from oracle import binding as O
+    ins = build_instrument(a.workload)
+    off, rot = calcTransformations(ins)
+    ch = build_chain(ins.components, off, rot, HostBinder())
+    nthreads = os.cpu_count() or 1
+    for w in range(a.warmup):
+        O.run_chain(ch, sample, seed=a.seed, first=w * sample,
+                    nthreads=nthreads)
+    t = []
+    for k in range(a.steps):
+        t0 = time.perf_counter()
+        O.run_chain(ch, sample, seed=a.seed, first=(a.warmup + k) * sample,
+                    nthreads=nthreads)
+        t.append(time.perf_counter() - t0)
+    value = sample * a.steps / sum(t)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": 1e3 * sum(t) / a.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: seeded Philox neutrons, no input data",
+        "config": {"workload": WORKLOADS[a.workload],
+                   "neutrons_per_step": sample},
+        "cpu_baseline": {
+            "value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
+            "sample": f"{sample} neutrons per step of the same workload, "
+                      f"CPU FP64 restatement of the reference chain "
+                      f"(mcvine/acc is Python+Numba; its CPU engine "
+                      f"mcvine-core is not installable offline); "
+                      f"host {cpu_model()}"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def ours_arm(a, rank, world, local_rank):
+    import torch
+    import torch.distributed as dist
+    from acc_gb300 import _build, engine
+    from acc_gb300.components.monitors.MonitorBase import MonitorBase
+    _build.build_engine()
+    torch.cuda.set_device(local_rank)
+    ncount = int(a.ncount)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32,
+                        device="cuda")
+
+    # FP32 fused (headline)
+    ins32 = build_instrument(a.workload)
+    chain32 = engine.chain_for_instrument(ins32)
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    ms32 = time_chain(chain32, ncount, a.steps, a.warmup, "float32", a.seed,
+                      0, world, rank, flush)
+    clk = clocks.stop()
+    t32 = max_over_ranks(sum(ms32) / 1e3, world)
+
+    # FP64 plain
+    ins64 = build_instrument(a.workload)
+    chain64 = engine.chain_for_instrument(ins64)
+    ms64 = time_chain(chain64, ncount, a.steps, a.warmup, "float64",
+                      a.seed + 1, 0, world, rank, flush)
+    t64 = max_over_ranks(sum(ms64) / 1e3, world)
+
+    # all ranks' tallies summed (the one collective of the sharded path)
+    tallies = []
+    for ins in (ins32, ins64):
+        ts = [c._device_tally for c in ins.components
+              if isinstance(c, MonitorBase)]
+        if world > 1:
+            for t in ts:
+                dist.all_reduce(t)
+        tallies.append(ts)
+
+    e2e = None
+    if not a.no_e2e:
+        ins_e = build_instrument(a.workload)
+        engine.chain_for_instrument(ins_e)
+        dt, h2d, d2h = e2e_run(ins_e, ncount, a.steps, a.warmup, a.seed + 2,
+                               world, rank)
+        dt = max_over_ranks(dt, world)
+        e2e = {"value": world * ncount * a.steps / dt, "unit": UNIT,
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+
+    if rank != 0:
+        return 0
+
+    from acc_gb300.stats import chi2_per_dof
+    chi2 = {}
+    names = [c.name for c in ins32.components if isinstance(c, MonitorBase)]
+    for nm, g32, g64 in zip(names, tallies[0], tallies[1]):
+        c2, dof = chi2_per_dof(g32.cpu().numpy().reshape(3, -1),
+                               g64.cpu().numpy().reshape(3, -1))
+        chi2[nm] = {"chi2_per_dof": c2, "bins": dof}
+
+    fp32_peak = engine.probe_fma_peak(32)
+    fp64_peak = engine.probe_fma_peak(64)
+    mean_s = statistics.mean(ms32) / 1e3
+    counts = KERNEL_COUNTS.get(a.workload, {})
+    fpn = counts.get("fp32_flops_per_neutron")
+    achieved = fpn * ncount / mean_s / 1e12 if fpn else None
+    dbn = counts.get("dram_bytes_per_neutron")
+    roofline = {
+        "bound": "compute",
+        "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+        "frac": achieved / fp32_peak if achieved else None,
+        "traffic": dbn * ncount if dbn is not None else None,
+        "kernel": "mcv::chain_kernel<float,0>",
+        "peak_source": "FP32 FMA peak measured in this run "
+                       "(mcv_probe_fma_peak); the measured peak file has "
+                       "HBM and bf16-tensor peaks only",
+        "per_unit": "executed FP32 flops per neutron counted by ncu",
+        "fp64_peak_tflops": fp64_peak,
+    }
+    cpu = None
+    if world == 1 and not a.no_cpu_baseline:
+        rate, n, cores = cpu_oracle_rate(a.workload, a.cpu_seconds, a.seed)
+        cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": f"{n} neutrons of the same workload through the CPU "
+                         f"FP64 oracle (C, OpenMP, {cores} threads), "
+                         f"host {cpu_model()}"}
+    value = world * ncount * a.steps / t32
+    v64 = world * ncount * a.steps / t64
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": 1e3 * t32 / a.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: seeded Philox neutrons, no input data",
+        "config": {"workload": WORKLOADS[a.workload],
+                   "neutrons_per_step_per_gpu": ncount,
+                   "precision": "FP32 fused kernel; tof as a compensated "
+                                "float pair, tallies FP64",
+                   "l2": "512 MiB write between timed launches, outside "
+                         "the CUDA events",
+                   "parallelism": f"{world} replica(s), disjoint neutron "
+                                  "index ranges, one tally all-reduce"},
+        "fp64_plain": {"value": v64, "unit": UNIT,
+                       "ms_per_step": 1e3 * t64 / a.steps, "dtype": "f64"},
+        "fp32_over_fp64": value / v64,
+        "chi2_fp32_vs_fp64": chi2,
+        "bwd_over_fwd": None,
+        "e2e": e2e,
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "clocks": clk,
+        "gpu_launches": a.steps,
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main(argv=None):
+    a = parse_args(argv)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if a.impl == "reference":
+        return reference_arm(a, rank, world)
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    try:
+        return ours_arm(a, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,254 @@
+/*
+ * acc_gb300.h -- C ABI of the GB300-native neutron propagation engine.
+ *
+ * The engine runs an instrument (a linear chain of components: source,
+ * optics, sample, monitors) over N Monte-Carlo neutrons.  One neutron is the
+ * ten-slot state [x, y, z, vx, vy, vz, sx, sy, t, p] (m, m/s, s, weight),
+ * the layout of acc/components/sources/neutronfromstorage.py:80-81 and
+ * acc/neutron.py:44-51 in mcvine/acc.
+ *
+ * Conventions
+ *  - Plain C structs; no C++ or torch types cross this boundary.
+ *  - Device buffers (tallies, tables, neutron arrays, uniforms) are owned by
+ *    the caller and passed as raw device pointers.  The only memory the
+ *    library allocates is a small status/work-queue block per context
+ *    (mcv_ctx_create / mcv_ctx_destroy).
+ *  - Every call is ordered on the caller's stream (NULL = legacy default
+ *    stream).  A call given a non-NULL mcv_status synchronises that stream
+ *    and fills the status; given NULL it stays asynchronous and can be
+ *    captured in a CUDA graph (read the status later with mcv_ctx_status).
+ *  - Every entry point returns 0 on success or an MCV_E* code, never throws,
+ *    and writes a one-line reason into mcv_status.message when given one.
+ *  - A context is used by one host thread at a time.
+ */
+#ifndef ACC_GB300_H
+#define ACC_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MCV_ABI_VERSION 1
+
+#define MCV_MAX_COMPONENTS 16
+#define MCV_NPARAM 40
+#define MCV_NIPARAM 8
+#define MCV_MAX_INTERSECTIONS 10  /* acc/geometry/arrow_intersect.py:16 */
+#define MCV_MAX_BOUNCES 100000    /* acc/components/optics/guide.py:17 */
+
+/* ---- error codes ---------------------------------------------------- */
+enum {
+  MCV_OK = 0,
+  MCV_EINVAL = 1,        /* bad argument or bad chain description        */
+  MCV_ECUDA = 2,         /* a CUDA runtime call failed                    */
+  MCV_ECOUNT = 3,        /* processed neutron count != requested          */
+  MCV_EBOUNCE = 4,       /* a guide hit MCV_MAX_BOUNCES (neutron dropped) */
+  MCV_ENONFINITE = 5,    /* a neutron state went NaN/Inf (dropped)        */
+  MCV_EBIN = 6,          /* a tally bin index fell outside its histogram  */
+  MCV_ENODEV = 7,        /* no CUDA device                                */
+  MCV_ECAPACITY = 8      /* a size exceeds a documented maximum           */
+};
+
+/* ---- component opcodes ---------------------------------------------- */
+enum {
+  MCV_OP_ARM = 0,               /* acc/components/optics/arm.py           */
+  MCV_OP_SOURCE_SIMPLE = 1,     /* acc/components/sources/source_simple.py */
+  MCV_OP_GUIDE = 2,             /* acc/components/optics/guide.py          */
+  MCV_OP_HSS = 3,               /* acc/components/samples/homogeneous_single_scatterer.py */
+  MCV_OP_PSD_MONITOR = 4,       /* acc/components/monitors/psd_monitor.py  */
+  MCV_OP_PSD_MONITOR_4PI = 5,   /* acc/components/monitors/psd_monitor_4pi.py */
+  MCV_OP_WAVELENGTH_MONITOR = 6,/* acc/components/monitors/wavelength_monitor.py */
+  MCV_OP_POSDIV_MONITOR = 7,    /* acc/components/monitors/posdiv_monitor.py */
+  MCV_OP_IQE_MONITOR = 8,       /* acc/components/monitors/iqe_monitor.py  */
+  MCV_OP_ENERGY_MONITOR = 9,    /* no reference counterpart (energy twin of the wavelength monitor) */
+  MCV_OP_THETA_TOF_4PI = 10,    /* no reference counterpart (theta x tof 4pi shell) */
+  MCV_OP_CYL_IQE_DETECTOR = 11, /* no reference counterpart (cylinder, binned I(Q,E)) */
+  MCV_OP_BANKED_DETECTOR = 12,  /* no reference counterpart (banks x tubes x pixels x tof) */
+  MCV_OP_SLIT = 13,             /* acc/components/optics/slit.py            */
+  MCV_OP_BEAMSTOP = 14,         /* acc/components/optics/beamstop.py        */
+  MCV_OP_COUNT = 15
+};
+
+/* ---- shapes of the homogeneous scatterer (acc/geometry/arrow_intersect.py)
+ * A shape is one primitive (A) or a binary CSG node over two primitives. */
+enum {
+  MCV_SHAPE_NONE = 0,
+  MCV_SHAPE_SPHERE = 1,     /* dp: R                 (arrow_intersect.py:47-57)   */
+  MCV_SHAPE_CYLINDER = 2,   /* dp: R, H (axis = z)   (arrow_intersect.py:59-70)   */
+  MCV_SHAPE_BOX = 3         /* dp: W, H, D           (arrow_intersect.py:72-86)   */
+};
+enum {
+  MCV_CSG_PRIMITIVE = 0,
+  MCV_CSG_DIFFERENCE = 1,   /* arrow_intersect.py:88-104  */
+  MCV_CSG_UNION = 2,        /* arrow_intersect.py:28-45   */
+  MCV_CSG_INTERSECTION = 3  /* arrow_intersect.py:106-123 */
+};
+
+/* ---- scattering kernels (acc/kernels) -------------------------------- */
+enum {
+  MCV_KERNEL_ISOTROPIC = 1,   /* acc/kernels/isotropic.py:5-21, __init__.py:36-44 */
+  MCV_KERNEL_POWDER = 2,      /* acc/kernels/powderdiffr.py                        */
+  MCV_KERNEL_SQE_GRID = 3     /* no reference counterpart (gridded S(Q,E) table)   */
+};
+
+/*
+ * Parameter slots.  Doubles go in dp[], a float copy of the same values in
+ * fp[] (the FP32 kernels read fp[], the FP64 kernels dp[]), integers in ip[].
+ *
+ * SOURCE_SIMPLE (source_simple.py:47-112 packs the same values)
+ *   ip[0]=square ip[1]=wl_distr
+ *   dp: 0 width 1 height 2 radius 3 Lambda0 4 dLambda 5 E0 6 dE 7 xw 8 yh
+ *       9 dist 10 pmul
+ * GUIDE (guide.py:44-50)
+ *   dp: 0 ww 1 hh 2 hw1 3 hh1 4 l 5 R0 6 Qc 7 alpha 8 m 9 W
+ * HSS (homogeneous_single_scatterer.py:26-102)
+ *   ip[0]=csg op ip[1]=kernel ip[2]=shape A ip[3]=shape B ip[4]=npeaks / nQ
+ *   ip[5]=nE
+ *   dp: 0-2 shape A params, 4-6 shape B params,
+ *       8 mu (absorption coefficient at 2200 m/s, 1/m), 9 sigma (1/m),
+ *       POWDER: 10 unit-cell volume (A^3), 11 d_phi (deg)
+ *               table: npeaks x {q_v, w_v, my_s_v2, cumulative my_s_v2}
+ *               float64, q_v ascending (powderdiffr.py:112-155)
+ *       SQE_GRID: 10 Qmin 11 Qmax 12 Emin 13 Emax
+ *               table: nQ x nE float32 S(Q,E), row-major in Q
+ * PSD_MONITOR (psd_monitor.py:66-83)          ip: nx ny;  dp: xmin xmax ymin ymax
+ * PSD_MONITOR_4PI (psd_monitor_4pi.py:56-79)  ip: nphi ntheta; dp: radius
+ * WAVELENGTH_MONITOR (wavelength_monitor.py:52-74)
+ *                                ip: nchan; dp: xmin xmax ymin ymax Lmin Lmax
+ * POSDIV_MONITOR (posdiv_monitor.py:67-89)    ip: npos ndiv; dp: xmin xmax ymin ymax maxdiv
+ * IQE_MONITOR (iqe_monitor.py:80-113)          ip: nQ nE;
+ *   dp: Ei Qmin Qmax Emin Emax max_in min_in max_out min_out (degrees)
+ * ENERGY_MONITOR                 ip: nchan; dp: xmin xmax ymin ymax Emin Emax
+ * THETA_TOF_4PI                  ip: ntheta ntof; dp: radius tmin tmax
+ *                                 (theta = polar angle from +z, 0..180 deg)
+ * CYL_IQE_DETECTOR               ip: nQ nE; dp: radius height Ei Qmin Qmax Emin Emax
+ * BANKED_DETECTOR                ip: nbanks ntubes npixels ntof
+ *   dp: radius height bank_angle0 bank_width(rad) bank_gap(rad) tmin tmax
+ * SLIT / BEAMSTOP (slit.py:20-108, beamstop.py:18-112)
+ *                                dp: xmin xmax ymin ymax radius^2 cut
+ *
+ * Every monitor tallies into `tally`: float64 [3][n0][n1] holding
+ * (N, sum p, sum p^2) per bin, the `out` array of psd_monitor.py:61-65.
+ */
+typedef struct mcv_component {
+  int32_t opcode;
+  int32_t flags;
+  int32_t ip[MCV_NIPARAM];
+  double dp[MCV_NPARAM];
+  float fp[MCV_NPARAM];
+  double* tally;          /* device, float64, 3*nbins, or NULL   */
+  const void* table;      /* device lookup table (layout per opcode), or NULL */
+  const float* ftable;    /* float32 copy of `table` for the FP32 kernels     */
+  uint64_t table_len;     /* elements in table                   */
+} mcv_component;
+
+/*
+ * One instrument.  rot[i], off[i] (i >= 1) take a neutron from the frame of
+ * component i-1 into the frame of component i: r' = rot (r - off),
+ * v' = rot v  (acc/neutron.py:18-23 with run_script.py:141-162).
+ */
+typedef struct mcv_chain {
+  int32_t ncomp;
+  int32_t flags;
+  mcv_component comp[MCV_MAX_COMPONENTS];
+  double rot[MCV_MAX_COMPONENTS][9];
+  double off[MCV_MAX_COMPONENTS][3];
+  float frot[MCV_MAX_COMPONENTS][9];
+  float foff[MCV_MAX_COMPONENTS][3];
+} mcv_chain;
+
+/* Launch shape; zeros mean "engine default" (the autotuned value if any). */
+typedef struct mcv_launch {
+  int32_t threads_per_block;
+  int32_t blocks;
+  int32_t chunk;            /* neutrons per work item (batched launch) */
+  int32_t reserved;
+} mcv_launch;
+
+typedef struct mcv_status {
+  int32_t code;
+  int32_t first_bad_component;
+  uint64_t processed;        /* neutrons that entered the chain (run_script.py:195) */
+  uint64_t bounce_overflow;  /* guide loops that reached MCV_MAX_BOUNCES  */
+  uint64_t nonfinite;        /* neutrons dropped for a NaN/Inf state      */
+  uint64_t bin_oob;          /* tally indices out of range (skipped)      */
+  char message[256];
+} mcv_status;
+
+typedef struct mcv_ctx mcv_ctx;
+
+enum { MCV_FP32 = 32, MCV_FP64 = 64 };
+
+/* ---- library ---------------------------------------------------------- */
+int mcv_abi_version(void);
+/* sizeof the ABI structs, so a binding can check its mirror. */
+int mcv_struct_sizes(uint64_t* component, uint64_t* chain, uint64_t* status,
+                     uint64_t* launch);
+
+/* Context: per-device status counters and work-queue words. */
+int mcv_ctx_create(int device, mcv_ctx** out);
+int mcv_ctx_destroy(mcv_ctx* ctx);
+/* Synchronise `stream`, read and reset the counters of the calls since the
+ * last read, validate against `expected` processed neutrons (0 = skip). */
+int mcv_ctx_status(mcv_ctx* ctx, void* stream, uint64_t expected,
+                   mcv_status* st);
+
+/*
+ * Fused run: replaces the generated process_kernel_no_buffer of
+ * acc/run_script.py:165-224 (launched from
+ * acc/components/sources/SourceBase.py:36-52).  Runs neutrons with indices
+ * [first, first+ncount) of the stream keyed by `seed` through the whole chain
+ * in one kernel and adds into the component tallies.  Neutron i draws its
+ * uniforms from Philox4x32-10 with counter (i, draw block), so the result
+ * does not depend on the launch shape, and disjoint index ranges on several
+ * devices sum to the single-device run.
+ */
+int mcv_run_chain(mcv_ctx* ctx, const mcv_chain* chain, uint64_t ncount,
+                  uint64_t first, uint64_t seed, int precision,
+                  const mcv_launch* launch, void* stream, mcv_status* st);
+
+/*
+ * Replay run for parity: as mcv_run_chain, but neutron i takes its uniforms
+ * from uniforms[i*stride ...] (float32, in [0,1), consumed in the draw order
+ * of the reference components) instead of Philox when `uniforms` is non-NULL,
+ * and writes its state when it leaves the chain into out_neutrons[i*10 ...]
+ * (float64) and the index of the last component it reached into
+ * out_last[i] when those are non-NULL.
+ */
+int mcv_replay_uniforms(mcv_ctx* ctx, const mcv_chain* chain, uint64_t ncount,
+                        uint64_t first, uint64_t seed, int precision,
+                        const float* uniforms, int32_t stride,
+                        double* out_neutrons, int32_t* out_last,
+                        const mcv_launch* launch, void* stream,
+                        mcv_status* st);
+
+/*
+ * Buffered (per-component) mode: replaces ComponentBase.process /
+ * call_process (acc/components/ComponentBase.py:79-129) and its stochastic
+ * twin (StochasticComponentBase.py:21-54).  Applies the chain's components
+ * in order to a device array neutrons[n][10] (float64 when precision is
+ * MCV_FP64, float32 when MCV_FP32) in place.  A neutron whose weight is not
+ * positive is left as is by later components.  Component k draws from the
+ * Philox stream (seed, k+1).
+ */
+int mcv_process_buffer(mcv_ctx* ctx, const mcv_chain* chain, void* neutrons,
+                       uint64_t n, uint64_t first, uint64_t seed,
+                       int precision, const mcv_launch* launch, void* stream,
+                       mcv_status* st);
+
+/*
+ * Geometry probe: the intersection times of rays with the shape of an HSS
+ * component (arrow_intersect.py render + intersect).  rays[n][6] float64;
+ * out_ts[n][MCV_MAX_INTERSECTIONS] float64; out_n[n] int32.
+ */
+int mcv_intersect(mcv_ctx* ctx, const mcv_component* hss, const double* rays,
+                  uint64_t n, double* out_ts, int32_t* out_n, int precision,
+                  void* stream, mcv_status* st);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ACC_GB300_H */

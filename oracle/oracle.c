@@ -1,0 +1,1485 @@
+/*
+ * oracle.c -- CPU FP64 restatement of mcvine/acc's per-neutron propagation
+ * chain.  TEST INFRASTRUCTURE ONLY: this file is the checker that the CUDA
+ * engine is compared against (and the timed CPU baseline); no product code
+ * path may call it.
+ *
+ * Each function restates the reference function cited beside it (paths are
+ * relative to the mcvine/acc source tree).  The reference is Python/Numba;
+ * the arithmetic below keeps its operation order so that FP64 results agree
+ * with the reference to rounding.  Compile with -ffp-contract=off so that the
+ * result does not depend on whether the host fuses multiply-adds.
+ *
+ * Components with no reference counterpart (energy monitor, theta x tof
+ * shell, cylinder I(Q,E) detector, banked detector, gridded S(Q,E) kernel)
+ * are restated from the nearest reference template named at each function.
+ *
+ * Uniform random numbers come from Philox4x32-10 (Salmon, Moraes, Dror,
+ * Shaw, "Parallel random numbers: as easy as 1, 2, 3", SC'11), counter
+ * (neutron index lo, hi, draw block, stream), key (seed lo, seed hi); each
+ * 32-bit word w gives the float32-exact uniform (w >> 8) * 2^-24 in [0, 1),
+ * matching the float32 uniforms the reference draws
+ * (xoroshiro128p_uniform_float32, e.g. source_simple.py:128-132).
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "../include/acc_gb300.h"
+
+/* mcni.utils.conversion constants (the reference imports them from mcni;
+ * V2K appears in acc/components/optics/guide_baseline.py:16-17). */
+#define V2K 1.58825361e-3
+#define K2V (1.0 / V2K)
+#define SE2V 437.393377
+#define VS2E 5.22703725e-6
+#define GEOM_EPSILON 1e-10 /* acc/geometry/__init__.py:2 */
+#define LOC_OUTSIDE 1      /* acc/geometry/location.py */
+#define LOC_ONBORDER 0
+#define LOC_INSIDE (-1)
+
+/* ------------------------------------------------------------------ RNG */
+static inline uint32_t mulhilo32(uint32_t a, uint32_t b, uint32_t* hi) {
+  uint64_t p = (uint64_t)a * (uint64_t)b;
+  *hi = (uint32_t)(p >> 32);
+  return (uint32_t)p;
+}
+
+void oracle_philox4x32_10(const uint32_t ctr_in[4], const uint32_t key_in[2],
+                          uint32_t out[4]) {
+  uint32_t c0 = ctr_in[0], c1 = ctr_in[1], c2 = ctr_in[2], c3 = ctr_in[3];
+  uint32_t k0 = key_in[0], k1 = key_in[1];
+  for (int r = 0; r < 10; ++r) {
+    if (r > 0) {
+      k0 += 0x9E3779B9u;
+      k1 += 0xBB67AE85u;
+    }
+    uint32_t hi0, hi1;
+    uint32_t lo0 = mulhilo32(0xD2511F53u, c0, &hi0);
+    uint32_t lo1 = mulhilo32(0xCD9E8D57u, c2, &hi1);
+    uint32_t n0 = hi1 ^ c1 ^ k0;
+    uint32_t n2 = hi0 ^ c3 ^ k1;
+    c0 = n0;
+    c1 = lo1;
+    c2 = n2;
+    c3 = lo0;
+  }
+  out[0] = c0;
+  out[1] = c1;
+  out[2] = c2;
+  out[3] = c3;
+}
+
+typedef struct {
+  uint32_t key[2];
+  uint32_t ctr[4];
+  uint32_t buf[4];
+  int pos;           /* next word in buf; 4 = empty */
+  const float* inj;  /* injected uniforms, or NULL   */
+  int inj_pos, inj_stride;
+  int overrun;
+} rng_t;
+
+static void rng_init(rng_t* r, uint64_t seed, uint64_t index, uint32_t stream,
+                     const float* inj, int stride) {
+  r->key[0] = (uint32_t)seed;
+  r->key[1] = (uint32_t)(seed >> 32);
+  r->ctr[0] = (uint32_t)index;
+  r->ctr[1] = (uint32_t)(index >> 32);
+  r->ctr[2] = 0;
+  r->ctr[3] = stream;
+  r->pos = 4;
+  r->inj = inj;
+  r->inj_pos = 0;
+  r->inj_stride = stride;
+  r->overrun = 0;
+}
+
+static double rng_uniform(rng_t* r) {
+  if (r->inj) {
+    if (r->inj_pos >= r->inj_stride) {
+      r->overrun = 1;
+      return 0.5;
+    }
+    return (double)r->inj[r->inj_pos++];
+  }
+  if (r->pos == 4) {
+    oracle_philox4x32_10(r->ctr, r->key, r->buf);
+    r->ctr[2]++;
+    r->pos = 0;
+  }
+  uint32_t w = r->buf[r->pos++];
+  return (double)(w >> 8) * (1.0 / 16777216.0);
+}
+
+/* ------------------------------------------------------ neutron / vec3 */
+typedef struct {
+  double x, y, z, vx, vy, vz, sx, sy, t, p;
+} neutron_t;
+
+/* vec3.abs2rel + mXv (acc/vec3.py:148-159, acc/neutron.py:18-23) */
+static void apply_transform(neutron_t* n, const double* m, const double* o) {
+  double tx = n->x - o[0], ty = n->y - o[1], tz = n->z - o[2];
+  double rx = m[0] * tx + m[1] * ty + m[2] * tz;
+  double ry = m[3] * tx + m[4] * ty + m[5] * tz;
+  double rz = m[6] * tx + m[7] * ty + m[8] * tz;
+  double vx = m[0] * n->vx + m[1] * n->vy + m[2] * n->vz;
+  double vy = m[3] * n->vx + m[4] * n->vy + m[5] * n->vz;
+  double vz = m[6] * n->vx + m[7] * n->vy + m[8] * n->vz;
+  n->x = rx; n->y = ry; n->z = rz;
+  n->vx = vx; n->vy = vy; n->vz = vz;
+}
+
+/* prop_dt_inplace (acc/neutron.py:44-51) */
+static inline void prop_dt(neutron_t* n, double dt) {
+  n->x = n->x + n->vx * dt;
+  n->y = n->y + n->vy * dt;
+  n->z = n->z + n->vz * dt;
+  n->t = n->t + dt;
+}
+
+static inline double length3(double a, double b, double c) {
+  return sqrt(a * a + b * b + c * c);
+}
+
+static void cross3(const double* a, const double* b, double* o) {
+  o[0] = a[1] * b[2] - a[2] * b[1];
+  o[1] = a[2] * b[0] - a[0] * b[2];
+  o[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+/* vec3.normalize (acc/vec3.py:28-31): scale by 1/length */
+static void normalize3(double* v) {
+  double l = length3(v[0], v[1], v[2]);
+  double s = 1.0 / l;
+  v[0] *= s; v[1] *= s; v[2] *= s;
+}
+
+/* vec3._rotate (acc/vec3.py:77-105) */
+void oracle_rotate(double* v, const double* c, double angle, double epsilon) {
+  double c1[3] = {c[0], c[1], c[2]};
+  normalize3(c1);
+  double sf = v[0] * c1[0] + v[1] * c1[1] + v[2] * c1[2];
+  double vpl[3] = {c1[0] * sf, c1[1] * sf, c1[2] * sf};
+  if (fabs(1 - length3(vpl[0], vpl[1], vpl[2]) / length3(v[0], v[1], v[2])) <
+      epsilon)
+    return;
+  double vpp[3] = {v[0] - vpl[0], v[1] - vpl[1], v[2] - vpl[2]};
+  double vpp_len = length3(vpp[0], vpp[1], vpp[2]);
+  double inv = 1. / vpp_len;
+  vpp[0] *= inv; vpp[1] *= inv; vpp[2] *= inv;
+  double e3[3];
+  cross3(vpp, c1, e3);
+  double ca = cos(angle), sa = sin(angle);
+  vpp[0] *= ca; vpp[1] *= ca; vpp[2] *= ca;
+  e3[0] *= sa; e3[1] *= sa; e3[2] *= sa;
+  double r[3] = {vpp[0] - e3[0], vpp[1] - e3[1], vpp[2] - e3[2]};
+  r[0] *= vpp_len; r[1] *= vpp_len; r[2] *= vpp_len;
+  v[0] = r[0] + vpl[0];
+  v[1] = r[1] + vpl[1];
+  v[2] = r[2] + vpl[2];
+}
+
+/* ------------------------------------------------------------- source */
+/* randvec_target_rect (acc/components/sources/source_simple.py:17-42) */
+static double randvec_target_rect(const double* target, double width,
+                                  double height, double rand1, double rand2,
+                                  double* vecout) {
+  double dx = width * (rand1 * 2 - 1) / 2.0;
+  double dy = height * (rand2 * 2 - 1) / 2.0;
+  double dist = length3(target[0], target[1], target[2]);
+  double vertical[3] = {0.0, 1.0, 0.0};
+  double p1[3], p2[3];
+  cross3(target, vertical, p1);
+  normalize3(p1);
+  cross3(target, p1, p2);
+  normalize3(p2);
+  p1[0] *= dx; p1[1] *= dx; p1[2] *= dx;
+  p2[0] *= dy; p2[1] *= dy; p2[2] *= dy;
+  double tmp[3] = {p1[0] + target[0], p1[1] + target[1], p1[2] + target[2]};
+  vecout[0] = p2[0] + tmp[0];
+  vecout[1] = p2[1] + tmp[1];
+  vecout[2] = p2[2] + tmp[2];
+  double dist2 = sqrt(dx * dx + dy * dy + dist * dist);
+  return (width * height * dist) / (dist2 * dist2 * dist2);
+}
+
+/* Source_simple.propagate (source_simple.py:114-162) */
+static void source_simple(neutron_t* n, rng_t* rng, const mcv_component* c) {
+  const double* d = c->dp;
+  int square = c->ip[0], wl_distr = c->ip[1];
+  double width = d[0], height = d[1], radius = d[2];
+  double Lambda0 = d[3], dLambda = d[4], E0 = d[5], dE = d[6];
+  double xw = d[7], yh = d[8], dist = d[9], pmul = d[10];
+  double r1 = rng_uniform(rng), r2 = rng_uniform(rng), r3 = rng_uniform(rng);
+  double r4 = rng_uniform(rng), r5 = rng_uniform(rng);
+  double x, y;
+  if (square) {
+    x = width * (r1 - 0.5);
+    y = height * (r2 - 0.5);
+  } else {
+    double chi = 2 * M_PI * r1;
+    double r = sqrt(r2) * radius;
+    x = r * cos(chi);
+    y = r * sin(chi);
+  }
+  n->x = x; n->y = y; n->z = 0.;
+  double target[3] = {0.0, 0.0, dist};
+  double vec_f[3];
+  double solidangle = randvec_target_rect(target, xw, yh, r3, r4, vec_f);
+  double dx = vec_f[0] - x, dy = vec_f[1] - y;
+  double dist1 = sqrt(dx * dx + dy * dy + dist * dist);
+  double v;
+  if (wl_distr) {
+    double L = Lambda0 + dLambda * (r5 * 2 - 1);
+    v = K2V * (2 * M_PI / L);
+  } else {
+    double E = E0 + dE * (r5 * 2 - 1);
+    v = SE2V * sqrt(E);
+  }
+  n->vx = v * dx / dist1;
+  n->vy = v * dy / dist1;
+  n->vz = v * dist / dist1;
+  n->sx = 0; n->sy = 0;
+  n->t = 0;
+  n->p = pmul * solidangle;
+}
+
+/* -------------------------------------------------------------- guide */
+/* calc_reflectivity (acc/components/optics/_guide_utils.py:6-23) */
+double oracle_reflectivity(double Q, double R0, double Qc, double alpha,
+                           double m, double W) {
+  double R = R0;
+  if (Q > Qc) {
+    double tmp = (Q - m * Qc) / W;
+    if (tmp < 10)
+      R *= (1 - tanh(tmp)) * (1 - alpha * (Q - Qc)) / 2;
+    else
+      R = 0;
+  }
+  return R;
+}
+
+/* Guide.propagate (acc/components/optics/guide.py:66-162).  Returns 1 if
+ * the bounce loop ran out. */
+static int guide(neutron_t* n, const mcv_component* c) {
+  const double* d = c->dp;
+  double ww = d[0], hh = d[1], hw1 = d[2], hh1 = d[3], l = d[4];
+  double R0 = d[5], Qc = d[6], alpha = d[7], m = d[8], W = d[9];
+  double x = n->x, y = n->y, z = n->z, vx = n->vx, vy = n->vy, vz = n->vz;
+  double t = n->t, prob = n->p;
+  double dt = -z / vz;
+  x += vx * dt;
+  y += vy * dt;
+  z = 0.;
+  t += dt;
+  if (x <= -hw1 || x >= hw1 || y <= -hh1 || y >= hh1) {
+    n->p = -1; /* absorb (acc/neutron.py:25-28) */
+    return 0;
+  }
+  int overflow = 1;
+  for (int nb = 0; nb < MCV_MAX_BOUNCES; ++nb) {
+    double av = l * vx, bv = ww * vz, ah = l * vy, bh = hh * vz;
+    double vdotn_v1 = bv + av, vdotn_v2 = bv - av;
+    double vdotn_h1 = bh + ah, vdotn_h2 = bh - ah;
+    double cv1 = -hw1 * l - z * ww, cv2 = x * l;
+    double ch1 = -hh1 * l - z * hh, ch2 = y * l;
+    double t1 = (l - z) / vz, t2;
+    int i = 0;
+    if (vdotn_v1 < 0) {
+      t2 = (cv1 - cv2) / vdotn_v1;
+      if (t2 < t1) { t1 = t2; i = 1; }
+    }
+    if (vdotn_v2 < 0) {
+      t2 = (cv1 + cv2) / vdotn_v2;
+      if (t2 < t1) { t1 = t2; i = 2; }
+    }
+    if (vdotn_h1 < 0) {
+      t2 = (ch1 - ch2) / vdotn_h1;
+      if (t2 < t1) { t1 = t2; i = 3; }
+    }
+    if (vdotn_h2 < 0) {
+      t2 = (ch1 + ch2) / vdotn_h2;
+      if (t2 < t1) { t1 = t2; i = 4; }
+    }
+    if (i == 0) { overflow = 0; break; }
+    x += vx * t1;
+    y += vy * t1;
+    z += vz * t1;
+    t += t1;
+    double nlen2, q, dd;
+    if (i == 1) {
+      nlen2 = l * l + ww * ww;
+      q = V2K * (-2) * vdotn_v1 / sqrt(nlen2);
+      dd = 2 * vdotn_v1 / nlen2;
+      vx = vx - dd * l;
+      vz = vz - dd * ww;
+    } else if (i == 2) {
+      nlen2 = l * l + ww * ww;
+      q = V2K * (-2) * vdotn_v2 / sqrt(nlen2);
+      dd = 2 * vdotn_v2 / nlen2;
+      vx = vx + dd * l;
+      vz = vz - dd * ww;
+    } else if (i == 3) {
+      nlen2 = l * l + hh * hh;
+      q = V2K * (-2) * vdotn_h1 / sqrt(nlen2);
+      dd = 2 * vdotn_h1 / nlen2;
+      vy = vy - dd * l;
+      vz = vz - dd * hh;
+    } else {
+      nlen2 = l * l + hh * hh;
+      q = V2K * (-2) * vdotn_h2 / sqrt(nlen2);
+      dd = 2 * vdotn_h2 / nlen2;
+      vy = vy + dd * l;
+      vz = vz - dd * hh;
+    }
+    double R = oracle_reflectivity(q, R0, Qc, alpha, m, W);
+    prob *= R;
+    if (prob <= 0) { overflow = 0; break; }
+  }
+  n->x = x; n->y = y; n->z = z;
+  n->vx = vx; n->vy = vy; n->vz = vz;
+  n->t = t;
+  n->p = prob;
+  return overflow;
+}
+
+/* Slit.propagate / Beamstop.propagate (acc/components/optics/slit.py:71-108,
+ * beamstop.py:75-112); dp = {xmin, xmax, ymin, ymax, radius^2, cut} */
+static void slit_or_beamstop(neutron_t* n, const mcv_component* c, int stop) {
+  const double* d = c->dp;
+  double xmin = d[0], xmax = d[1], ymin = d[2], ymax = d[3], r2 = d[4],
+         cut = d[5];
+  double x = n->x, y = n->y, z = n->z, vx = n->vx, vy = n->vy, vz = n->vz;
+  if ((z < 0 && vz <= 0) || (z > 0 && vz >= 0)) return;
+  double t = n->t;
+  if (n->p < cut) { n->p = -1; return; }
+  if (z != 0) {
+    double dt = -z / vz;
+    x += vx * dt;
+    y += vy * dt;
+    t += dt;
+  }
+  int in;
+  if (r2 != 0) in = x * x + y * y <= r2;
+  else in = xmin <= x && x <= xmax && ymin <= y && y <= ymax;
+  if (stop ? in : !in) { n->p = -1; return; }
+  n->x = x;
+  n->y = y;
+  n->z = 0.;
+  n->t = t;
+}
+
+/* ------------------------------------------------------------ geometry */
+/* cu_device_intersect_sphere (acc/geometry/arrow_intersect.py:154-168) */
+void oracle_intersect_sphere(double x, double y, double z, double vx,
+                             double vy, double vz, double R, double* t1,
+                             double* t2) {
+  double r0dotv = x * vx + y * vy + z * vz;
+  double cx = y * vz - z * vy, cy = z * vx - x * vz, cz = x * vy - y * vx;
+  double v2 = vx * vx + vy * vy + vz * vz;
+  double r0Xv2 = cx * cx + cy * cy + cz * cz;
+  double b2m4ac = v2 * R * R - r0Xv2;
+  *t1 = NAN;
+  *t2 = NAN;
+  if (b2m4ac < 0) return;
+  double s = sqrt(b2m4ac);
+  *t1 = -(r0dotv + s) / v2;
+  *t2 = -(r0dotv - s) / v2;
+}
+
+/* intersectCylinderSide (arrow_intersect.py:178-204) */
+static int cyl_side(double x, double y, double z, double vx, double vy,
+                    double vz, double R, double H, double* t1o, double* t2o) {
+  double a = vx * vx + vy * vy;
+  double b = x * vx + y * vy;
+  double c = x * x + y * y - R * R;
+  double k = b * b - a * c;
+  double hh = H / 2.;
+  *t1o = NAN;
+  *t2o = NAN;
+  if (k < 0 || a == 0) return 0;
+  if (k == 0) {
+    double t = -b / a;
+    if (fabs(z + vz * t) < hh) {
+      *t1o = t;
+      return 1;
+    }
+  }
+  k = sqrt(k);
+  double t1 = (-b + k) / a, t2 = (-b - k) / a;
+  int good1 = fabs(z + vz * t1) < hh, good2 = fabs(z + vz * t2) < hh;
+  if (good1) {
+    if (good2) { *t1o = t2; *t2o = t1; return 2; }
+    *t1o = t1;
+    return 1;
+  }
+  if (good2) { *t1o = t2; return 1; }
+  return 0;
+}
+
+/* intersectCylinderTopBottom (arrow_intersect.py:213-239) */
+static int cyl_caps(double x, double y, double z, double vx, double vy,
+                    double vz, double R, double H, double* t1o, double* t2o) {
+  *t1o = NAN;
+  *t2o = NAN;
+  if (vz == 0) return 0;
+  double hh = H / 2, r2 = R * R;
+  double t1 = (hh - z) / vz;
+  double x1 = x + vx * t1, y1 = y + vy * t1;
+  int good1 = x1 * x1 + y1 * y1 <= r2;
+  double t2 = (-hh - z) / vz;
+  x1 = x + vx * t2;
+  y1 = y + vy * t2;
+  int good2 = x1 * x1 + y1 * y1 <= r2;
+  if (good1) {
+    if (good2) {
+      if (t1 < t2) { *t1o = t1; *t2o = t2; }
+      else { *t1o = t2; *t2o = t1; }
+      return 2;
+    }
+    *t1o = t1;
+    return 1;
+  }
+  if (good2) { *t1o = t2; return 1; }
+  return 0;
+}
+
+static inline double pymin(double a, double b) { return b < a ? b : a; }
+static inline double pymax(double a, double b) { return b > a ? b : a; }
+
+/* cu_device_intersect_cylinder (arrow_intersect.py:241-267); the n==0
+ * branch of the reference falls through to NaNs, i.e. no intersection. */
+void oracle_intersect_cylinder(double x, double y, double z, double vx,
+                               double vy, double vz, double R, double H,
+                               double* o1, double* o2) {
+  double t1, t2, t3, t4;
+  int n1 = cyl_side(x, y, z, vx, vy, vz, R, H, &t1, &t2);
+  int n2 = cyl_caps(x, y, z, vx, vy, vz, R, H, &t3, &t4);
+  int n = n1 + n2;
+  if (n == 0) { *o1 = NAN; *o2 = NAN; }
+  else if (n == 1) {
+    if (n1 == 1) { *o1 = t1; *o2 = t1; }
+    else { *o1 = t3; *o2 = t3; }
+  } else if (n == 2) {
+    if (n1 == 1) {
+      if (t1 > t3) { *o1 = t3; *o2 = t1; }
+      else { *o1 = t1; *o2 = t3; }
+    } else if (n1 == 0) { *o1 = t3; *o2 = t4; }
+    else { *o1 = t1; *o2 = t2; }
+  } else if (n == 3) {
+    if (n1 == 1) { *o1 = pymin(t1, t3); *o2 = pymax(t1, t4); }
+    else { *o1 = pymin(t3, t1); *o2 = pymax(t3, t2); }
+  } else {
+    *o1 = pymin(t1, t3);
+    *o2 = pymax(t2, t4);
+  }
+}
+
+/* cu_device_intersect_rectangle (acc/geometry/onbox.py:8-18): the plane
+ * z = 0 of a frame where the rectangle is X x Y.  The reference declares it
+ * float32; restated in float64 like its CUDASIM known-answer tests. */
+static double rect_hit(double rx, double ry, double rz, double vx, double vy,
+                       double vz, double X, double Y) {
+  double t = -rz / vz;
+  double r1x = rx + vx * t, r1y = ry + vy * t;
+  if (fabs(r1x) > X / 2 || fabs(r1y) > Y / 2) t = NAN;
+  return t;
+}
+
+/* cu_device_update_intersections (onbox.py:20-36) */
+static void update_hits(double* t1, double* t2, double t) {
+  if (!isfinite(t)) return;
+  if (!isfinite(*t1)) { *t1 = t; return; }
+  if (!isfinite(*t2)) {
+    if (t > *t1) *t2 = t;
+    else { *t2 = *t1; *t1 = t; }
+    return;
+  }
+  if (t < *t1) *t1 = t;
+  else if (t < *t2) return;
+  else *t2 = t;
+}
+
+/* cu_device_intersect_box (onbox.py:38-56) */
+void oracle_intersect_box(double x, double y, double z, double vx, double vy,
+                          double vz, double X, double Y, double Z, double* o1,
+                          double* o2) {
+  double t1 = NAN, t2 = NAN;
+  if (vz != 0) {
+    update_hits(&t1, &t2, rect_hit(x, y, z - Z / 2, vx, vy, vz, X, Y));
+    update_hits(&t1, &t2, rect_hit(x, y, z + Z / 2, vx, vy, vz, X, Y));
+  }
+  if (vx != 0) {
+    update_hits(&t1, &t2, rect_hit(y, z, x - X / 2, vy, vz, vx, Y, Z));
+    update_hits(&t1, &t2, rect_hit(y, z, x + X / 2, vy, vz, vx, Y, Z));
+  }
+  if (vy != 0) {
+    update_hits(&t1, &t2, rect_hit(z, x, y - Y / 2, vz, vx, vy, Z, X));
+    update_hits(&t1, &t2, rect_hit(z, x, y + Y / 2, vz, vx, vy, Z, X));
+  }
+  *o1 = t1;
+  *o2 = t2;
+}
+
+/* locate functions (acc/geometry/locate.py:354-392) */
+static int locate_prim(int kind, const double* p, double x, double y,
+                       double z) {
+  const double e = GEOM_EPSILON;
+  if (kind == MCV_SHAPE_SPHERE) {
+    double R = p[0], d2 = x * x + y * y + z * z;
+    if (d2 > (R + e) * (R + e)) return LOC_OUTSIDE;
+    if (d2 < (R - e) * (R - e)) return LOC_INSIDE;
+    return LOC_ONBORDER;
+  }
+  if (kind == MCV_SHAPE_CYLINDER) {
+    double R = p[0], H = p[1];
+    if (fabs(z) - H / 2. > e) return LOC_OUTSIDE;
+    double r2 = x * x + y * y;
+    if (r2 > (R + e) * (R + e)) return LOC_OUTSIDE;
+    if (H / 2. - fabs(z) > e && r2 < (R - e) * (R - e)) return LOC_INSIDE;
+    return LOC_ONBORDER;
+  }
+  if (kind == MCV_SHAPE_BOX) {
+    double W = p[0], H = p[1], D = p[2];
+    if (fabs(x) - 0.5 * W > e) return LOC_OUTSIDE;
+    if (fabs(y) - 0.5 * H > e) return LOC_OUTSIDE;
+    if (fabs(z) - 0.5 * D > e) return LOC_OUTSIDE;
+    if (-0.5 * W < x && x < 0.5 * W && -0.5 * H < y && y < 0.5 * H &&
+        -0.5 * D < z && z < 0.5 * D)
+      return LOC_INSIDE;
+    return LOC_ONBORDER;
+  }
+  return LOC_OUTSIDE;
+}
+
+/* locate wrt the HSS shape: primitive, difference (locate.py:395-404),
+ * union (:338-352), intersection (:407-421). */
+int oracle_locate(const mcv_component* c, double x, double y, double z) {
+  int op = c->ip[0];
+  int l1 = locate_prim(c->ip[2], c->dp + 0, x, y, z);
+  if (op == MCV_CSG_PRIMITIVE) return l1;
+  int l2 = locate_prim(c->ip[3], c->dp + 4, x, y, z);
+  if (op == MCV_CSG_DIFFERENCE) {
+    if (l1 == LOC_OUTSIDE || l2 == LOC_INSIDE) return LOC_OUTSIDE;
+    if (l1 == LOC_ONBORDER || l2 == LOC_ONBORDER) return LOC_ONBORDER;
+    return LOC_INSIDE;
+  }
+  if (op == MCV_CSG_UNION) {
+    if (l1 == LOC_INSIDE || l2 == LOC_INSIDE) return LOC_INSIDE;
+    if (l1 == LOC_OUTSIDE && l2 == LOC_OUTSIDE) return LOC_OUTSIDE;
+    return LOC_ONBORDER;
+  }
+  /* intersection */
+  if (l1 == LOC_OUTSIDE || l2 == LOC_OUTSIDE) return LOC_OUTSIDE;
+  if (l1 == LOC_INSIDE && l2 == LOC_INSIDE) return LOC_INSIDE;
+  return LOC_ONBORDER;
+}
+
+/* insert_into_sorted_list (acc/geometry/_utils.py:4-32), capacity len */
+int oracle_insert_sorted(double d, double* l, int N, int len) {
+  if (N >= len) return N;
+  if (N == 0) { l[0] = d; return 1; }
+  int minidx = 0, maxidx = N - 1, idx = minidx;
+  while (minidx < maxidx - 1) {
+    int mididx = (minidx + maxidx) / 2;
+    double mid = l[mididx];
+    if (d > mid) minidx = mididx;
+    else maxidx = mididx;
+  }
+  if (minidx == maxidx) {
+    idx = minidx;
+    if (d > l[idx]) idx = idx + 1;
+  } else {
+    if (d >= l[maxidx]) idx = maxidx + 1;
+    else if (d <= l[minidx]) idx = minidx;
+    else idx = minidx + 1;
+  }
+  for (int i = N; i > idx; --i) l[i] = l[i - 1];
+  l[idx] = d;
+  return N + 1;
+}
+
+/* intersect a primitive: the intersectSphere/Cylinder/Block wrappers of
+ * ArrowIntersectFuncFactory (arrow_intersect.py:47-86) */
+static int intersect_prim(int kind, const double* p, double x, double y,
+                          double z, double vx, double vy, double vz,
+                          double* ts) {
+  double t1, t2;
+  if (kind == MCV_SHAPE_SPHERE)
+    oracle_intersect_sphere(x, y, z, vx, vy, vz, p[0], &t1, &t2);
+  else if (kind == MCV_SHAPE_CYLINDER)
+    oracle_intersect_cylinder(x, y, z, vx, vy, vz, p[0], p[1], &t1, &t2);
+  else if (kind == MCV_SHAPE_BOX)
+    oracle_intersect_box(x, y, z, vx, vy, vz, p[0], p[1], p[2], &t1, &t2);
+  else
+    return 0;
+  if (isnan(t1)) return 0;
+  ts[0] = t1;
+  ts[1] = t2;
+  return 2;
+}
+
+/* intersect the HSS shape; composite per intersectComposite
+ * (arrow_intersect.py:126-142) */
+int oracle_intersect(const mcv_component* c, double x, double y, double z,
+                     double vx, double vy, double vz, double* ts) {
+  int op = c->ip[0];
+  if (op == MCV_CSG_PRIMITIVE)
+    return intersect_prim(c->ip[2], c->dp + 0, x, y, z, vx, vy, vz, ts);
+  double ts1[MCV_MAX_INTERSECTIONS], ts2[MCV_MAX_INTERSECTIONS];
+  int N1 = intersect_prim(c->ip[2], c->dp + 0, x, y, z, vx, vy, vz, ts1);
+  int N2 = intersect_prim(c->ip[3], c->dp + 4, x, y, z, vx, vy, vz, ts2);
+  int N = 0;
+  for (int i = 0; i < N1; ++i) {
+    double t = ts1[i];
+    if (oracle_locate(c, x + vx * t, y + vy * t, z + vz * t) == LOC_ONBORDER) {
+      ts[N] = t;
+      N += 1;
+    }
+  }
+  for (int i = 0; i < N2; ++i) {
+    double t = ts2[i];
+    if (oracle_locate(c, x + vx * t, y + vy * t, z + vz * t) == LOC_ONBORDER) {
+      if (N < MCV_MAX_INTERSECTIONS) ts[N] = t;
+      N = oracle_insert_sorted(t, ts, N, MCV_MAX_INTERSECTIONS);
+    }
+  }
+  return N;
+}
+
+/* ---------------------------------------- propagation helpers (KATs) */
+/* forward_intersect (acc/geometry/propagation.py:11-22) */
+static int forward_intersect(const mcv_component* c, const neutron_t* n,
+                             double* ts) {
+  int N = oracle_intersect(c, n->x, n->y, n->z, n->vx, n->vy, n->vz, ts);
+  int Nm = N;
+  for (int i = 0; i < N; ++i)
+    if (ts[i] >= 0) { Nm = i; break; }
+  int Np = N - Nm;
+  for (int i = 0; i < Np; ++i) ts[i] = ts[i + Nm];
+  return Np;
+}
+
+/* _propagate_out (propagation.py:52-59) */
+void oracle_propagate_out(const mcv_component* c, double* st) {
+  neutron_t* n = (neutron_t*)st;
+  double ts[MCV_MAX_INTERSECTIONS];
+  int N = forward_intersect(c, n, ts);
+  if (N == 0) return;
+  prop_dt(n, ts[N - 1]);
+}
+
+/* _tof_before_first_exit (propagation.py:154-191); returns -1 where the
+ * reference raises (point outside the shape). */
+double oracle_tof_before_first_exit(const mcv_component* c, const double* st) {
+  const neutron_t* n = (const neutron_t*)st;
+  double ts[MCV_MAX_INTERSECTIONS];
+  int loc = oracle_locate(c, n->x, n->y, n->z);
+  if (loc == LOC_OUTSIDE) return -1.0;
+  int N = forward_intersect(c, n, ts);
+  if (N == 0) return 0.;
+  if (loc == LOC_INSIDE) return ts[0];
+  double t = 0.;
+  for (int i = 0; i < N; ++i) {
+    double mx = n->x + ts[i] / 2 * n->vx, my = n->y + ts[i] / 2 * n->vy,
+           mz = n->z + ts[i] / 2 * n->vz;
+    int l1 = oracle_locate(c, mx, my, mz);
+    if (l1 == LOC_OUTSIDE) return 0.;
+    if (l1 == LOC_INSIDE) { t = ts[i]; break; }
+  }
+  return t;
+}
+
+/* _propagate_to_next_incident_surface (propagation.py:61-105); returns 1
+ * where the reference raises (point inside the shape). */
+int oracle_propagate_to_next_incident_surface(const mcv_component* c,
+                                              double* st) {
+  neutron_t* n = (neutron_t*)st;
+  double ts[MCV_MAX_INTERSECTIONS];
+  int loc = oracle_locate(c, n->x, n->y, n->z);
+  if (loc == LOC_INSIDE) return 1;
+  int N = forward_intersect(c, n, ts);
+  if (N == 0) return 0;
+  double t;
+  if (loc == LOC_OUTSIDE) t = ts[0];
+  else {
+    int found = 0;
+    for (int i = 0; i < N; ++i) {
+      double mx = n->x + ts[i] / 2 * n->vx, my = n->y + ts[i] / 2 * n->vy,
+             mz = n->z + ts[i] / 2 * n->vz;
+      int l1 = oracle_locate(c, mx, my, mz);
+      if (l1 == LOC_INSIDE) return 0;
+      if (l1 == LOC_OUTSIDE) { t = ts[i]; found = 1; break; }
+    }
+    if (!found) return 0;
+  }
+  prop_dt(n, t);
+  return 0;
+}
+
+/* _propagate_to_next_exiting_surface (propagation.py:107-152) */
+void oracle_propagate_to_next_exiting_surface(const mcv_component* c,
+                                              double* st) {
+  neutron_t* n = (neutron_t*)st;
+  double ts[MCV_MAX_INTERSECTIONS];
+  int loc = oracle_locate(c, n->x, n->y, n->z);
+  double t;
+  if (loc == LOC_INSIDE) {
+    forward_intersect(c, n, ts);
+    t = ts[0];
+  } else {
+    if (loc == LOC_OUTSIDE) oracle_propagate_to_next_incident_surface(c, st);
+    int N = forward_intersect(c, n, ts);
+    int found = 0;
+    for (int i = 0; i < N; ++i) {
+      double mx = n->x + ts[i] / 2 * n->vx, my = n->y + ts[i] / 2 * n->vy,
+             mz = n->z + ts[i] / 2 * n->vz;
+      int l1 = oracle_locate(c, mx, my, mz);
+      if (l1 == LOC_OUTSIDE) return;
+      if (l1 == LOC_INSIDE) { t = ts[i]; found = 1; break; }
+    }
+    if (!found) return;
+  }
+  prop_dt(n, t);
+}
+
+/* -------------------------------------------------------- HSS helpers */
+/* _calc_time_to_point_of_scattering_impl
+ * (acc/components/samples/homogeneous_single_scatterer.py:121-159).
+ * out = {total_time_in_shape, total_time_travel_to_scattering_point,
+ *        time_travelled_in_shape_to_scattering_point} */
+void oracle_time_to_scatter(const double* ts, int ninter, double rand,
+                            double* out) {
+  double tps[MCV_MAX_INTERSECTIONS], tpg[MCV_MAX_INTERSECTIONS];
+  double T = 0.0;
+  int sign = 0, ip = 0, i = 0;
+  for (i = 0; i < ninter; ++i) {
+    double t = ts[i];
+    if (t < 0) continue;
+    if (sign == 0) sign = (i % 2 == 0) ? -1 : 1;
+    else sign *= -1;
+    T += sign * t;
+    if (sign > 0) {
+      tps[ip] = T;
+      tpg[ip] = t;
+      ip += 1;
+    }
+  }
+  double ttistsp = rand * T;
+  if (ip > 0) {
+    for (i = 0; i < ip; ++i)
+      if (ttistsp < tps[i]) break;
+    if (i == ip) i = ip - 1; /* python for-loop variable keeps its last value */
+  } else {
+    i = -1;
+  }
+  out[0] = T;
+  out[1] = i >= 0 ? ttistsp - tps[i] + tpg[i] : 0.0;
+  out[2] = ttistsp;
+}
+
+/* total_time_in_shape (homogeneous_single_scatterer.py:161-178) */
+double oracle_total_time_in_shape(const double* ts, int ninter) {
+  double T = 0;
+  int sign = 0;
+  for (int i = 0; i < ninter; ++i) {
+    double t = ts[i];
+    if (t < 0) continue;
+    if (sign == 0) sign = (i % 2 == 0) ? -1 : 1;
+    else sign *= -1;
+    T += sign * t;
+  }
+  return T;
+}
+
+/* time_to_enter (homogeneous_single_scatterer.py:180-195) */
+double oracle_time_to_enter(const double* ts, int ninter) {
+  for (int i = 0; i < ninter; ++i) {
+    double t = ts[i];
+    if (t < 0) continue;
+    return (i % 2 == 0) ? t : 0;
+  }
+  return 0;
+}
+
+/* ------------------------------------------------------------ kernels */
+/* calc_absorption_coeff (acc/kernels/__init__.py:156-161) */
+static inline double abs_coeff(const neutron_t* n, double mu) {
+  double v = length3(n->vx, n->vy, n->vz);
+  return mu / v * 2200;
+}
+
+/* isotropic.S (acc/kernels/isotropic.py:5-21) */
+static void isotropic_S(neutron_t* n, rng_t* rng) {
+  double cos_t = rng_uniform(rng) * 2 - 1;
+  double phi = rng_uniform(rng) * (2 * M_PI);
+  if (cos_t > 1) cos_t = 1;
+  double sin_t = sqrt(1 - cos_t * cos_t);
+  double sin_p = sin(phi), cos_p = cos(phi);
+  double vi = length3(n->vx, n->vy, n->vz);
+  n->vx = vi * sin_t * cos_p;
+  n->vy = vi * sin_t * sin_p;
+  n->vz = vi * cos_t;
+}
+
+/* powderdiffr.scattering_xs / scattering_coefficient
+ * (acc/kernels/powderdiffr.py:10-25); peaks = npeaks x {q_v, w_v, my_s_v2,
+ * cumulative my_s_v2} */
+static double powder_coeff(const neutron_t* n, const mcv_component* c) {
+  const double* pk = (const double*)c->table;
+  int Np = c->ip[4];
+  double vl = length3(n->vx, n->vy, n->vz);
+  double xs_v2 = 0.0;
+  for (int i = 0; i < Np; ++i)
+    if (vl >= pk[4 * i + 0] / 2) xs_v2 += pk[4 * i + 2];
+  return xs_v2 / (vl * vl) / c->dp[10];
+}
+
+/* powderdiffr.scatter (acc/kernels/powderdiffr.py:27-109) */
+static void powder_scatter(neutron_t* n, rng_t* rng, const mcv_component* c) {
+  const double* pk = (const double*)c->table;
+  int Npeaks = c->ip[4];
+  double ucvol = c->dp[10], d_phi = c->dp[11];
+  const double eps = 1e-7, DEG2RAD = M_PI / 180.0;
+  double v[3] = {n->vx, n->vy, n->vz};
+  double vl = length3(v[0], v[1], v[2]);
+  if (vl < pk[0] / 2) { n->p = -1; return; }
+  /* `for peakindex in range(1, Npeaks): if vl < q_v[peakindex]/2: break`
+   * then `Npeaks = peakindex`: with a break the reachable count is the
+   * breaking index; without one python leaves the loop variable at
+   * Npeaks-1, so the last peak is never picked (reference quirk).  A single
+   * peak leaves the variable unbound in the reference; it counts as 1. */
+  int Nreach;
+  if (Npeaks <= 1) {
+    Nreach = 1;
+  } else {
+    int j;
+    for (j = 1; j < Npeaks; ++j)
+      if (vl < pk[4 * j] / 2) break;
+    Nreach = j < Npeaks ? j : Npeaks - 1;
+  }
+  int peakindex;
+  if (Nreach > 1) peakindex = (int)(rng_uniform(rng) * Nreach);
+  else peakindex = 0;
+  double rt = rng_uniform(rng) * 2 - 1;
+  double q = pk[4 * peakindex], w = pk[4 * peakindex + 1],
+         s = pk[4 * peakindex + 2];
+  double arg = q * (1 + w * rt) / (2.0 * vl);
+  double scatter_xs = s / (vl * vl);
+  scatter_xs *= Nreach;
+  double theta = asin(arg);
+  double alpha = 0, alpha0;
+  if (d_phi != 0) {
+    double a = sin(d_phi * DEG2RAD / 2) / sin(2 * theta);
+    if (a < -1 || a > 1) d_phi = 0;
+    else alpha = 2 * asin(a);
+  }
+  if (d_phi != 0) {
+    alpha = fabs(alpha);
+    double r = rng_uniform(rng);
+    alpha0 = 2 * r * alpha;
+    if (alpha0 > alpha) alpha0 = M_PI + (alpha0 - 1.5 * alpha);
+    else alpha0 = alpha0 - 0.5 * alpha;
+  } else {
+    double r = rng_uniform(rng) * 2 - 1;
+    alpha0 = M_PI * r;
+  }
+  double nn[3];
+  if (fabs(v[0]) < fabs(v[2])) { nn[0] = 1; nn[1] = 0; nn[2] = 0; }
+  else { nn[0] = 0; nn[1] = 0; nn[2] = 1; }
+  double vtmp[3], vout[3] = {v[0], v[1], v[2]};
+  cross3(v, nn, vtmp);
+  oracle_rotate(vout, vtmp, 2 * theta, eps);
+  oracle_rotate(vout, v, alpha0, eps);
+  n->vx = vout[0]; n->vy = vout[1]; n->vz = vout[2];
+  if (isnan(vout[0]) || isnan(vout[1]) || isnan(vout[2])) { n->p = -1; return; }
+  n->p *= scatter_xs / ucvol;
+}
+
+/* bilinear_interp (acc/kernels/SANS2D_ongrid.py:16-22) */
+static inline double bilinear(double x, double y, double f00, double f01,
+                              double f10, double f11) {
+  double a00 = f00, a10 = f10 - f00, a01 = f01 - f00,
+         a11 = f11 - f10 - f01 + f00;
+  return a00 + a10 * x + a01 * y + a11 * x * y;
+}
+
+/* Bilinear lookup of the S(Q,E) grid: node (iq, ie) sits at
+ * (Qmin + iq dQ, Emin + ie dE), dQ = (Qmax-Qmin)/(nQ-1); indices clamp to
+ * [0, n-2] as SANS2D_ongrid.py:37-50 does. */
+double oracle_sqe_lookup(const mcv_component* c, double Q, double E) {
+  const float* S = (const float*)c->table;
+  int nQ = c->ip[4], nE = c->ip[5];
+  double Qmin = c->dp[10], Qmax = c->dp[11], Emin = c->dp[12], Emax = c->dp[13];
+  double dQ = (Qmax - Qmin) / (nQ - 1), dE = (Emax - Emin) / (nE - 1);
+  int iq = (int)((Q - Qmin) / dQ), ie = (int)((E - Emin) / dE);
+  if (iq < 0) iq = 0;
+  if (ie < 0) ie = 0;
+  if (iq > nQ - 2) iq = nQ - 2;
+  if (ie > nE - 2) ie = nE - 2;
+  double fx = (Q - Qmin) / dQ - iq, fy = (E - Emin) / dE - ie;
+  double f00 = S[iq * nE + ie], f10 = S[(iq + 1) * nE + ie];
+  double f01 = S[iq * nE + ie + 1], f11 = S[(iq + 1) * nE + ie + 1];
+  return bilinear(fx, fy, f00, f01, f10, f11);
+}
+
+/* Gridded S(Q,E) kernel.  No reference counterpart: restated from the
+ * kinematics of E_Q._S (acc/kernels/E_Q.py:37-99) with (Q, E) drawn
+ * uniformly over the table box (one draw each, no rejection loop) and S
+ * from the bilinear grid (SANS2D_ongrid.py:16-56).  Weight
+ * S (vf/vi) Q (Qmax-Qmin)(Emax-Emin) / (2 ki kf); kinematically closed
+ * (Q, E) absorb. */
+static void sqe_scatter(neutron_t* n, rng_t* rng, const mcv_component* c) {
+  double Qmin = c->dp[10], Qmax = c->dp[11], Emin = c->dp[12], Emax = c->dp[13];
+  double v[3] = {n->vx, n->vy, n->vz};
+  double vi = length3(v[0], v[1], v[2]);
+  double Ei = vi * vi * VS2E;
+  double Q = rng_uniform(rng) * (Qmax - Qmin) + Qmin;
+  double E = rng_uniform(rng) * (Emax - Emin) + Emin;
+  double phi = rng_uniform(rng) * 2.0 * M_PI;
+  double Ef = Ei - E;
+  if (Ef <= 0) { n->p = -1; return; }
+  double vf = sqrt(Ef) * SE2V;
+  double ki = V2K * vi, kf = V2K * vf;
+  double cost = (ki * ki + kf * kf - Q * Q) / (2 * ki * kf);
+  double cost2 = cost * cost;
+  if (cost2 > 1) { n->p = -1; return; }
+  double sint = sqrt(1.0 - cost2);
+  double v2 = vf * sint * cos(phi), v3 = vf * sint * sin(phi), v1 = vf * cost;
+  double e1[3] = {v[0], v[1], v[2]}, e2[3], e3[3], nrm[3];
+  normalize3(e1);
+  if (fabs(e1[0]) > 1e-1 || fabs(e1[1]) > 1e-1) { nrm[0] = 0; nrm[1] = 0; nrm[2] = 1; }
+  else { nrm[0] = 1; nrm[1] = 0; nrm[2] = 0; }
+  cross3(nrm, e1, e2);
+  normalize3(e2);
+  cross3(e1, e2, e3);
+  n->vx = e1[0] * v1 + e2[0] * v2 + e3[0] * v3;
+  n->vy = e1[1] * v1 + e2[1] * v2 + e3[1] * v3;
+  n->vz = e1[2] * v1 + e2[2] * v2 + e3[2] * v3;
+  double S = oracle_sqe_lookup(c, Q, E);
+  double prob_f = S * (vf / vi) * Q * (Qmax - Qmin) * (Emax - Emin) / (kf * ki) / 2;
+  n->p *= prob_f;
+}
+
+/* ---------------------------------------------------------------- HSS */
+static double hss_sigma(const neutron_t* n, const mcv_component* c) {
+  if (c->ip[1] == MCV_KERNEL_POWDER) return powder_coeff(n, c);
+  return c->dp[9];
+}
+
+/* HomogeneousSingleScatterer.propagate
+ * (acc/components/samples/homogeneous_single_scatterer.py:62-100) */
+static void hss(neutron_t* n, rng_t* rng, const mcv_component* c) {
+  double x = n->x, y = n->y, z = n->z, vx = n->vx, vy = n->vy, vz = n->vz;
+  double ts[MCV_MAX_INTERSECTIONS];
+  int ninter = oracle_intersect(c, x, y, z, vx, vy, vz, ts);
+  if (ninter < 2) return;
+  if (ts[ninter - 1] <= 0) return;
+  double rand = rng_uniform(rng);
+  double o[3];
+  oracle_time_to_scatter(ts, ninter, rand, o);
+  double dt = o[1];
+  if (dt <= 0) return;
+  prop_dt(n, dt);
+  double v = sqrt(vx * vx + vy * vy + vz * vz);
+  double dist = v * o[2];
+  double fulllen = v * o[0];
+  double sigma = hss_sigma(n, c);
+  double mu = abs_coeff(n, c->dp[8]);
+  double atten = exp(-(mu + sigma) * dist);
+  n->p *= fulllen * atten;
+  switch (c->ip[1]) {
+    case MCV_KERNEL_ISOTROPIC:
+      n->p *= c->dp[9]; /* kernels/__init__.py:42 */
+      isotropic_S(n, rng);
+      break;
+    case MCV_KERNEL_POWDER:
+      powder_scatter(n, rng, c);
+      break;
+    case MCV_KERNEL_SQE_GRID:
+      n->p *= c->dp[9];
+      sqe_scatter(n, rng, c);
+      break;
+    default:
+      break;
+  }
+  if (n->p <= 0) return;
+  ninter = oracle_intersect(c, n->x, n->y, n->z, n->vx, n->vy, n->vz, ts);
+  double dt3 = oracle_total_time_in_shape(ts, ninter);
+  prop_dt(n, dt3);
+  sigma = hss_sigma(n, c);
+  mu = abs_coeff(n, c->dp[8]);
+  /* the reference uses the incident speed v here (line 98) */
+  double atten2 = exp(-(mu + sigma) * v * dt3);
+  n->p *= atten2;
+}
+
+/* ----------------------------------------------------------- monitors */
+typedef struct {
+  double* out; /* [3][nbins] */
+  uint64_t nbins;
+  int atomic;
+} tally_t;
+
+static inline void tally_add(const tally_t* tl, uint64_t bin, double p) {
+  if (!tl || !tl->out) return;
+  double* o = tl->out;
+  if (tl->atomic) {
+#pragma omp atomic
+    o[bin] += 1;
+#pragma omp atomic
+    o[tl->nbins + bin] += p;
+#pragma omp atomic
+    o[2 * tl->nbins + bin] += p * p;
+  } else {
+    o[bin] += 1;
+    o[tl->nbins + bin] += p;
+    o[2 * tl->nbins + bin] += p * p;
+  }
+}
+
+static inline int clampi(int i, int n) { return i < 0 ? 0 : (i >= n ? n - 1 : i); }
+
+/* PSD_monitor.propagate (acc/components/monitors/psd_monitor.py:66-83) */
+static void psd_monitor(const neutron_t* n, const mcv_component* c,
+                        const tally_t* tl) {
+  const double* d = c->dp;
+  double xmin = d[0], xmax = d[1], ymin = d[2], ymax = d[3];
+  int nx = c->ip[0], ny = c->ip[1];
+  double dt = -n->z / n->vz;
+  double x = n->x + n->vx * dt, y = n->y + n->vy * dt, t = n->t + dt;
+  if (n->t > t) return;
+  if (!(x > xmin && x < xmax && y > ymin && y < ymax)) return;
+  int ix = clampi((int)floor((x - xmin) / (xmax - xmin) * nx), nx);
+  int iy = clampi((int)floor((y - ymin) / (ymax - ymin) * ny), ny);
+  tally_add(tl, (uint64_t)ix * ny + iy, n->p);
+}
+
+/* PSD_monitor_4Pi.propagate (psd_monitor_4pi.py:56-79), including the +0.5
+ * in the theta index (line 72).  A neutron that misses the sphere is not
+ * tallied. */
+static void psd_monitor_4pi(neutron_t* n, const mcv_component* c,
+                            const tally_t* tl) {
+  double radius = c->dp[0];
+  int nphi = c->ip[0], ntheta = c->ip[1];
+  double t1, t2;
+  oracle_intersect_sphere(n->x, n->y, n->z, n->vx, n->vy, n->vz, radius, &t1,
+                          &t2);
+  if (isnan(t1)) return;
+  if (t2 < 0) return;
+  if (t1 < 0) t1 = t2;
+  prop_dt(n, t1);
+  double phi = atan2(n->x, n->z);
+  double sy = n->y / radius;
+  if (!(sy == sy)) return;
+  if (sy > 1) sy = 1;
+  if (sy < -1) sy = -1;
+  double theta = asin(sy);
+  int iphi = (int)(nphi * (phi / 2 / M_PI + 0.5));
+  if (iphi >= nphi) iphi = nphi - 1;
+  else if (iphi < 0) iphi = 0;
+  int itheta = (int)(ntheta * (theta + M_PI / 2) / M_PI + 0.5);
+  if (itheta >= ntheta) itheta = ntheta - 1;
+  else if (itheta < 0) itheta = 0;
+  tally_add(tl, (uint64_t)iphi * ntheta + itheta, n->p);
+}
+
+/* Wavelength_monitor.propagate (wavelength_monitor.py:52-74) */
+static void wavelength_monitor(const neutron_t* n, const mcv_component* c,
+                               const tally_t* tl) {
+  const double* d = c->dp;
+  double xmin = d[0], xmax = d[1], ymin = d[2], ymax = d[3], Lmin = d[4],
+         Lmax = d[5];
+  int nchan = c->ip[0];
+  double dt = -n->z / n->vz;
+  double x = n->x + n->vx * dt, y = n->y + n->vy * dt, t = n->t + dt;
+  if (n->t > t) return;
+  if (!(x > xmin && x < xmax && y > ymin && y < ymax)) return;
+  double v = sqrt(n->vx * n->vx + n->vy * n->vy + n->vz * n->vz);
+  double L = 2 * M_PI / (v * V2K);
+  if (!(L > Lmin && L < Lmax)) return;
+  int iL = clampi((int)floor((L - Lmin) / (Lmax - Lmin) * nchan), nchan);
+  tally_add(tl, (uint64_t)iL, n->p);
+}
+
+/* Energy monitor: no reference counterpart; the wavelength monitor
+ * (wavelength_monitor.py:52-74) with E = v^2 VS2E (acc/neutron.py:69-71). */
+static void energy_monitor(const neutron_t* n, const mcv_component* c,
+                           const tally_t* tl) {
+  const double* d = c->dp;
+  double xmin = d[0], xmax = d[1], ymin = d[2], ymax = d[3], Emin = d[4],
+         Emax = d[5];
+  int nchan = c->ip[0];
+  double dt = -n->z / n->vz;
+  double x = n->x + n->vx * dt, y = n->y + n->vy * dt, t = n->t + dt;
+  if (n->t > t) return;
+  if (!(x > xmin && x < xmax && y > ymin && y < ymax)) return;
+  double v2 = n->vx * n->vx + n->vy * n->vy + n->vz * n->vz;
+  double E = v2 * VS2E;
+  if (!(E > Emin && E < Emax)) return;
+  int iE = clampi((int)floor((E - Emin) / (Emax - Emin) * nchan), nchan);
+  tally_add(tl, (uint64_t)iE, n->p);
+}
+
+/* PosDiv_monitor.propagate (posdiv_monitor.py:67-89) */
+static void posdiv_monitor(const neutron_t* n, const mcv_component* c,
+                           const tally_t* tl) {
+  const double* d = c->dp;
+  double xmin = d[0], xmax = d[1], ymin = d[2], ymax = d[3], maxdiv = d[4];
+  int npos = c->ip[0], ndiv = c->ip[1];
+  double dt = -n->z / n->vz;
+  double x = n->x + n->vx * dt, y = n->y + n->vy * dt, t = n->t + dt;
+  if (n->t > t) return;
+  if (!(x > xmin && x < xmax && y > ymin && y < ymax)) return;
+  double div = atan(n->vx / n->vz) * (180. / M_PI);
+  if (!(div < maxdiv && div > -maxdiv)) return;
+  int ix = clampi((int)floor((x - xmin) / (xmax - xmin) * npos), npos);
+  int idiv = clampi((int)floor((div + maxdiv) / (2 * maxdiv) * ndiv), ndiv);
+  tally_add(tl, (uint64_t)ix * ndiv + idiv, n->p);
+}
+
+/* IQE_monitor.propagate (iqe_monitor.py:80-113) */
+static void iqe_monitor(const neutron_t* n, const mcv_component* c,
+                        const tally_t* tl) {
+  const double* d = c->dp;
+  double Ei = d[0], Qmin = d[1], Qmax = d[2], Emin = d[3], Emax = d[4];
+  double max_in = d[5], min_in = d[6], max_out = d[7], min_out = d[8];
+  int nQ = c->ip[0], nE = c->ip[1];
+  double vx = n->vx, vy = n->vy, vz = n->vz;
+  double angle_in = atan2(vx, vz) / M_PI * 180.;
+  double angle_out;
+  if (vy != 0) {
+    double theta = atan(sqrt(vx * vx + vz * vz) / vy) / M_PI * 180.;
+    angle_out = vy > 0 ? 90. - theta : 90. + theta;
+  } else {
+    angle_out = 0.;
+  }
+  if (min_in < angle_in && angle_in < max_in && min_out < angle_out &&
+      angle_out < max_out) {
+    double vi = sqrt(Ei) * SE2V;
+    double Q = sqrt(vx * vx + vy * vy + (vz - vi) * (vz - vi)) * V2K;
+    double E = Ei - (vx * vx + vy * vy + vz * vz) * VS2E;
+    if (Q >= Qmin && Q < Qmax && E >= Emin && E < Emax) {
+      int iQ = clampi((int)floor((Q - Qmin) / (Qmax - Qmin) * nQ), nQ);
+      int iE = clampi((int)floor((E - Emin) / (Emax - Emin) * nE), nE);
+      tally_add(tl, (uint64_t)iQ * nE + iE, n->p);
+    }
+  }
+}
+
+/* theta x tof 4pi shell: no reference counterpart; the sphere crossing of
+ * PSD_monitor_4Pi (psd_monitor_4pi.py:56-66) binned by the polar angle from
+ * +z, atan2(hypot(x, y), z), and the time of flight. */
+static void theta_tof_4pi(neutron_t* n, const mcv_component* c,
+                          const tally_t* tl) {
+  double radius = c->dp[0], tmin = c->dp[1], tmax = c->dp[2];
+  int nth = c->ip[0], nt = c->ip[1];
+  double t1, t2;
+  oracle_intersect_sphere(n->x, n->y, n->z, n->vx, n->vy, n->vz, radius, &t1,
+                          &t2);
+  if (isnan(t1)) return;
+  if (t2 < 0) return;
+  if (t1 < 0) t1 = t2;
+  prop_dt(n, t1);
+  double theta = atan2(sqrt(n->x * n->x + n->y * n->y), n->z);
+  if (!(theta == theta)) return;
+  if (!(n->t >= tmin && n->t < tmax)) return;
+  int ith = clampi((int)floor(theta / M_PI * nth), nth);
+  int it = clampi((int)floor((n->t - tmin) / (tmax - tmin) * nt), nt);
+  tally_add(tl, (uint64_t)ith * nt + it, n->p);
+}
+
+/* Vertical cylinder (axis y) crossing from inside: the exit time of
+ * x^2 + z^2 = R^2 (the side term of intersectCylinderSide,
+ * arrow_intersect.py:178-204, with the axis along y).  Returns NaN if the
+ * neutron leaves through a cap or does not move horizontally. */
+static double vcyl_exit(const neutron_t* n, double R, double H) {
+  double a = n->vx * n->vx + n->vz * n->vz;
+  double b = n->x * n->vx + n->z * n->vz;
+  double c = n->x * n->x + n->z * n->z - R * R;
+  double k = b * b - a * c;
+  if (k < 0 || a == 0) return NAN;
+  double t = (-b + sqrt(k)) / a;
+  if (t < 0) return NAN;
+  double y = n->y + n->vy * t;
+  if (fabs(y) >= H / 2) return NAN;
+  return t;
+}
+
+/* Cylindrical I(Q,E) detector: no reference counterpart; the exit crossing
+ * of a vertical cylinder, then Q and E as IQE_monitor.propagate
+ * (iqe_monitor.py:96-110) computes them. */
+static void cyl_iqe(neutron_t* n, const mcv_component* c, const tally_t* tl) {
+  const double* d = c->dp;
+  double R = d[0], H = d[1], Ei = d[2], Qmin = d[3], Qmax = d[4], Emin = d[5],
+         Emax = d[6];
+  int nQ = c->ip[0], nE = c->ip[1];
+  double t = vcyl_exit(n, R, H);
+  if (isnan(t)) return;
+  prop_dt(n, t);
+  double vx = n->vx, vy = n->vy, vz = n->vz;
+  double vi = sqrt(Ei) * SE2V;
+  double Q = sqrt(vx * vx + vy * vy + (vz - vi) * (vz - vi)) * V2K;
+  double E = Ei - (vx * vx + vy * vy + vz * vz) * VS2E;
+  if (Q >= Qmin && Q < Qmax && E >= Emin && E < Emax) {
+    int iQ = clampi((int)floor((Q - Qmin) / (Qmax - Qmin) * nQ), nQ);
+    int iE = clampi((int)floor((E - Emin) / (Emax - Emin) * nE), nE);
+    tally_add(tl, (uint64_t)iQ * nE + iE, n->p);
+  }
+}
+
+/* Banked cylinder detector: no reference counterpart.  Vertical cylinder
+ * of radius R and height H; banks are azimuthal windows
+ * [a0 + b (w + g), a0 + b (w + g) + w) of phi = atan2(x, z); tubes split a
+ * bank evenly in phi, pixels split the height, then a tof histogram. */
+static void banked(neutron_t* n, const mcv_component* c, const tally_t* tl) {
+  const double* d = c->dp;
+  double R = d[0], H = d[1], a0 = d[2], w = d[3], g = d[4], tmin = d[5],
+         tmax = d[6];
+  int nb = c->ip[0], ntube = c->ip[1], npix = c->ip[2], ntof = c->ip[3];
+  double t = vcyl_exit(n, R, H);
+  if (isnan(t)) return;
+  prop_dt(n, t);
+  double phi = atan2(n->x, n->z);
+  double rel = phi - a0;
+  if (!(rel >= 0)) return;
+  int b = (int)floor(rel / (w + g));
+  if (b >= nb) return;
+  double inb = rel - b * (w + g);
+  if (inb >= w) return;
+  if (!(n->t >= tmin && n->t < tmax)) return;
+  int tube = clampi((int)floor(inb / w * ntube), ntube);
+  int pix = clampi((int)floor((n->y + H / 2) / H * npix), npix);
+  int it = clampi((int)floor((n->t - tmin) / (tmax - tmin) * ntof), ntof);
+  uint64_t bin = (((uint64_t)b * ntube + tube) * npix + pix) * ntof + it;
+  tally_add(tl, bin, n->p);
+}
+
+/* ------------------------------------------------------------ chains */
+static uint64_t comp_nbins(const mcv_component* c) {
+  switch (c->opcode) {
+    case MCV_OP_PSD_MONITOR:
+    case MCV_OP_PSD_MONITOR_4PI:
+    case MCV_OP_POSDIV_MONITOR:
+    case MCV_OP_IQE_MONITOR:
+    case MCV_OP_THETA_TOF_4PI:
+    case MCV_OP_CYL_IQE_DETECTOR:
+      return (uint64_t)c->ip[0] * (uint64_t)c->ip[1];
+    case MCV_OP_WAVELENGTH_MONITOR:
+    case MCV_OP_ENERGY_MONITOR:
+      return (uint64_t)c->ip[0];
+    case MCV_OP_BANKED_DETECTOR:
+      return (uint64_t)c->ip[0] * c->ip[1] * c->ip[2] * c->ip[3];
+    default:
+      return 0;
+  }
+}
+
+typedef struct {
+  uint64_t processed, bounce_overflow, nonfinite, rng_overrun;
+} ostat_t;
+
+/* One component on one neutron. */
+static void run_component(neutron_t* n, rng_t* rng, const mcv_component* c,
+                          const tally_t* tl, ostat_t* st) {
+  switch (c->opcode) {
+    case MCV_OP_ARM: break;
+    case MCV_OP_SOURCE_SIMPLE: source_simple(n, rng, c); break;
+    case MCV_OP_GUIDE: st->bounce_overflow += guide(n, c); break;
+    case MCV_OP_HSS: hss(n, rng, c); break;
+    case MCV_OP_PSD_MONITOR: psd_monitor(n, c, tl); break;
+    case MCV_OP_PSD_MONITOR_4PI: psd_monitor_4pi(n, c, tl); break;
+    case MCV_OP_WAVELENGTH_MONITOR: wavelength_monitor(n, c, tl); break;
+    case MCV_OP_POSDIV_MONITOR: posdiv_monitor(n, c, tl); break;
+    case MCV_OP_IQE_MONITOR: iqe_monitor(n, c, tl); break;
+    case MCV_OP_ENERGY_MONITOR: energy_monitor(n, c, tl); break;
+    case MCV_OP_THETA_TOF_4PI: theta_tof_4pi(n, c, tl); break;
+    case MCV_OP_CYL_IQE_DETECTOR: cyl_iqe(n, c, tl); break;
+    case MCV_OP_BANKED_DETECTOR: banked(n, c, tl); break;
+    case MCV_OP_SLIT: slit_or_beamstop(n, c, 0); break;
+    case MCV_OP_BEAMSTOP: slit_or_beamstop(n, c, 1); break;
+    default: break;
+  }
+}
+
+/*
+ * Run the chain over neutrons [first, first+ncount).  A neutron leaves the
+ * chain after the first component that leaves its weight not positive (the
+ * p > 0 filter of ComponentBase.process, ComponentBase.py:100-102).
+ * Tallies go into comp[k].tally (host memory here).  stats: processed,
+ * bounce_overflow, nonfinite, rng_overrun.
+ */
+int oracle_run_chain(const mcv_chain* chain, uint64_t ncount, uint64_t first,
+                     uint64_t seed, const float* uniforms, int stride,
+                     double* out_neutrons, int32_t* out_last, int nthreads,
+                     uint64_t* stats) {
+  int nc = chain->ncomp;
+  if (nc < 1 || nc > MCV_MAX_COMPONENTS) return MCV_EINVAL;
+  uint64_t total_bins = 0;
+  for (int k = 0; k < nc; ++k) total_bins += comp_nbins(&chain->comp[k]);
+#ifdef _OPENMP
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+#else
+  nthreads = 1;
+#endif
+  /* private tallies per thread when small, atomics when large */
+  int use_private = nthreads > 1 && total_bins * 3 * 8 * (uint64_t)nthreads <
+                                        ((uint64_t)1 << 30);
+  ostat_t gst = {0, 0, 0, 0};
+  double** priv = NULL;
+  if (use_private) {
+    priv = (double**)calloc((size_t)nthreads * nc, sizeof(double*));
+    for (int th = 0; th < nthreads; ++th)
+      for (int k = 0; k < nc; ++k) {
+        uint64_t nb = comp_nbins(&chain->comp[k]);
+        if (nb && chain->comp[k].tally)
+          priv[th * nc + k] = (double*)calloc(3 * nb, sizeof(double));
+      }
+  }
+#pragma omp parallel num_threads(nthreads)
+  {
+    int th = 0;
+#ifdef _OPENMP
+    th = omp_get_thread_num();
+#endif
+    tally_t tl[MCV_MAX_COMPONENTS];
+    for (int k = 0; k < nc; ++k) {
+      tl[k].nbins = comp_nbins(&chain->comp[k]);
+      tl[k].out = use_private ? priv[th * nc + k] : chain->comp[k].tally;
+      tl[k].atomic = !use_private && nthreads > 1;
+    }
+    ostat_t st = {0, 0, 0, 0};
+#pragma omp for schedule(static)
+    for (int64_t ii = 0; ii < (int64_t)ncount; ++ii) {
+      uint64_t idx = first + (uint64_t)ii;
+      rng_t rng;
+      rng_init(&rng, seed, idx, 0, uniforms ? uniforms + (uint64_t)ii * stride : NULL,
+               stride);
+      neutron_t n;
+      memset(&n, 0, sizeof n);
+      int last = -1;
+      st.processed++;
+      for (int k = 0; k < nc; ++k) {
+        const mcv_component* c = &chain->comp[k];
+        if (k > 0) apply_transform(&n, chain->rot[k], chain->off[k]);
+        last = k;
+        run_component(&n, &rng, c, &tl[k], &st);
+        if (!(n.p > 0)) {
+          if (isnan(n.p)) st.nonfinite++;
+          break;
+        }
+      }
+      st.rng_overrun += rng.overrun;
+      if (out_neutrons) memcpy(out_neutrons + (uint64_t)ii * 10, &n, sizeof n);
+      if (out_last) out_last[ii] = last;
+    }
+#pragma omp critical
+    {
+      gst.processed += st.processed;
+      gst.bounce_overflow += st.bounce_overflow;
+      gst.nonfinite += st.nonfinite;
+      gst.rng_overrun += st.rng_overrun;
+    }
+  }
+  if (use_private) {
+    for (int k = 0; k < nc; ++k) {
+      uint64_t nb = comp_nbins(&chain->comp[k]);
+      double* dst = chain->comp[k].tally;
+      if (!nb || !dst) continue;
+      for (int th = 0; th < nthreads; ++th) {
+        double* src = priv[th * nc + k];
+        for (uint64_t b = 0; b < 3 * nb; ++b) dst[b] += src[b];
+        free(src);
+      }
+    }
+    free(priv);
+  }
+  if (stats) {
+    stats[0] = gst.processed;
+    stats[1] = gst.bounce_overflow;
+    stats[2] = gst.nonfinite;
+    stats[3] = gst.rng_overrun;
+  }
+  return gst.rng_overrun ? MCV_EINVAL : MCV_OK;
+}
+
+/*
+ * Buffered mode (ComponentBase.process, ComponentBase.py:79-129): apply the
+ * components to neutrons[n][10] in place; component k draws from stream k+1.
+ * Neutrons whose weight is not positive are skipped by later components.
+ */
+int oracle_process_buffer(const mcv_chain* chain, double* neutrons, uint64_t n,
+                          uint64_t first, uint64_t seed, int nthreads,
+                          uint64_t* stats) {
+  int nc = chain->ncomp;
+  if (nc < 1 || nc > MCV_MAX_COMPONENTS) return MCV_EINVAL;
+#ifdef _OPENMP
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+#else
+  nthreads = 1;
+#endif
+  ostat_t gst = {0, 0, 0, 0};
+#pragma omp parallel num_threads(nthreads)
+  {
+    tally_t tl[MCV_MAX_COMPONENTS];
+    for (int k = 0; k < nc; ++k) {
+      tl[k].nbins = comp_nbins(&chain->comp[k]);
+      tl[k].out = chain->comp[k].tally;
+      tl[k].atomic = nthreads > 1;
+    }
+    ostat_t st = {0, 0, 0, 0};
+#pragma omp for schedule(static)
+    for (int64_t ii = 0; ii < (int64_t)n; ++ii) {
+      neutron_t nt;
+      memcpy(&nt, neutrons + (uint64_t)ii * 10, sizeof nt);
+      st.processed++;
+      for (int k = 0; k < nc; ++k) {
+        const mcv_component* c = &chain->comp[k];
+        if (c->opcode != MCV_OP_SOURCE_SIMPLE && !(nt.p > 0)) break;
+        if (k > 0) apply_transform(&nt, chain->rot[k], chain->off[k]);
+        rng_t rng;
+        rng_init(&rng, seed, first + (uint64_t)ii, (uint32_t)(k + 1), NULL, 0);
+        run_component(&nt, &rng, c, &tl[k], &st);
+      }
+      memcpy(neutrons + (uint64_t)ii * 10, &nt, sizeof nt);
+    }
+#pragma omp critical
+    {
+      gst.processed += st.processed;
+      gst.bounce_overflow += st.bounce_overflow;
+    }
+  }
+  if (stats) {
+    stats[0] = gst.processed;
+    stats[1] = gst.bounce_overflow;
+    stats[2] = gst.nonfinite;
+    stats[3] = 0;
+  }
+  return MCV_OK;
+}
+
+/* single-component probes used by the known-answer tests */
+int oracle_guide_one(const mcv_component* c, double* st) {
+  return guide((neutron_t*)st, c);
+}
+void oracle_source_one(const mcv_component* c, const float* u, double* st) {
+  rng_t rng;
+  rng_init(&rng, 0, 0, 0, u, 5);
+  source_simple((neutron_t*)st, &rng, c);
+}
+void oracle_hss_one(const mcv_component* c, const float* u, int nu,
+                    double* st) {
+  rng_t rng;
+  rng_init(&rng, 0, 0, 0, u, nu);
+  hss((neutron_t*)st, &rng, c);
+}
+void oracle_apply_transform(const double* rot, const double* off, double* st) {
+  apply_transform((neutron_t*)st, rot, off);
+}
+int oracle_sizeof_chain(void) { return (int)sizeof(mcv_chain); }
+int oracle_sizeof_component(void) { return (int)sizeof(mcv_component); }

@@ -1,0 +1,107 @@
+"""The C-ABI library loads, exports every entry point of include/*.h, and
+its struct layout matches the Python mirror and the oracle (no GPU needed)."""
+
+import ctypes
+import glob
+import os
+import re
+
+from acc_gb300 import _native as nat
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = []
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        names += re.findall(r"^\s*(?:int|void|uint64_t)\s+(mcv_\w+)\s*\(",
+                            text, flags=re.M)
+    return sorted(set(names))
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    for n in ("mcv_run_chain", "mcv_replay_uniforms", "mcv_process_buffer",
+              "mcv_ctx_create", "mcv_ctx_destroy", "mcv_ctx_status"):
+        assert n in names
+
+
+def test_library_exports_every_declared_symbol(engine_lib):
+    for name in declared_functions():
+        assert hasattr(engine_lib, name), f"{name} not exported"
+
+
+def test_struct_layout_matches(engine_lib, oracle_lib):
+    nat.check_layout(engine_lib)
+    assert oracle_lib.oracle_sizeof_chain() == ctypes.sizeof(nat.mcv_chain)
+    assert oracle_lib.oracle_sizeof_component() == \
+        ctypes.sizeof(nat.mcv_component)
+    assert engine_lib.mcv_abi_version() == 1
+
+
+def _bad_chain():
+    ch = nat.mcv_chain()
+    ch.ncomp = 1
+    ch.comp[0].opcode = nat.OP_PSD_MONITOR  # zero bins: invalid
+    return ch
+
+
+def test_invalid_chain_rejected_before_any_device_work(engine_lib):
+    st = nat.mcv_status()
+    rc = engine_lib.mcv_run_chain(None, ctypes.byref(_bad_chain()), 10, 0, 1,
+                                  64, None, None, ctypes.byref(st))
+    assert rc == nat.MCV_EINVAL
+    assert b"bin counts" in st.message
+    ch = nat.mcv_chain()
+    ch.ncomp = 0
+    rc = engine_lib.mcv_run_chain(None, ctypes.byref(ch), 10, 0, 1, 64, None,
+                                  None, ctypes.byref(st))
+    assert rc == nat.MCV_EINVAL and b"components" in st.message
+    ch.ncomp = 1
+    ch.comp[0].opcode = 99
+    rc = engine_lib.mcv_process_buffer(None, ctypes.byref(ch), None, 1, 0, 1,
+                                       64, None, None, ctypes.byref(st))
+    assert rc == nat.MCV_EINVAL and b"opcode" in st.message
+
+
+def test_bad_precision_and_null_context(engine_lib):
+    ch = nat.mcv_chain()
+    ch.ncomp = 1  # an Arm
+    st = nat.mcv_status()
+    rc = engine_lib.mcv_run_chain(None, ctypes.byref(ch), 10, 0, 1, 16, None,
+                                  None, ctypes.byref(st))
+    assert rc == nat.MCV_EINVAL and b"precision" in st.message
+    rc = engine_lib.mcv_run_chain(None, ctypes.byref(ch), 10, 0, 1, 32, None,
+                                  None, ctypes.byref(st))
+    assert rc == nat.MCV_EINVAL and b"context" in st.message
+
+
+def test_hss_validation(engine_lib):
+    ch = nat.mcv_chain()
+    ch.ncomp = 1
+    c = ch.comp[0]
+    c.opcode = nat.OP_HSS
+    c.ip[0] = nat.CSG_PRIMITIVE
+    c.ip[1] = nat.KERNEL_POWDER
+    c.ip[2] = nat.SHAPE_SPHERE
+    st = nat.mcv_status()
+    rc = engine_lib.mcv_run_chain(None, ctypes.byref(ch), 1, 0, 1, 32, None,
+                                  None, ctypes.byref(st))
+    assert rc == nat.MCV_EINVAL and b"powder" in st.message
+    c.ip[2] = 7
+    rc = engine_lib.mcv_run_chain(None, ctypes.byref(ch), 1, 0, 1, 32, None,
+                                  None, ctypes.byref(st))
+    assert rc == nat.MCV_EINVAL and b"shape" in st.message
+
+
+def test_context_create(engine_lib):
+    from conftest import HAS_GPU
+    h = ctypes.c_void_p()
+    rc = engine_lib.mcv_ctx_create(0, ctypes.byref(h))
+    if HAS_GPU:
+        assert rc == nat.MCV_OK
+        engine_lib.mcv_ctx_destroy(h)
+    else:
+        assert rc == nat.MCV_ENODEV

@@ -1,0 +1,174 @@
+"""GPU engine versus the CPU oracle (runs through the C ABI).
+
+Tolerances (stated per test):
+ * FP64 kernels, same Philox stream or injected uniforms: every slot of
+   every neutron within 1e-12 relative (denominator floored at the slot's
+   RMS over the batch), identical exit component, identical bin counts.
+ * FP32 kernels against the FP64 oracle on the same stream: 1e-5 relative
+   for all but a 1e-4 fraction of neutrons (neutrons whose path crosses a
+   branch -- a guide wall hit/miss or a bin edge -- within float rounding).
+ * Independent streams: chi^2/dof <= 1.1 between FP32 GPU and FP64 oracle
+   histograms.
+"""
+
+import numpy as np
+import pytest
+import torch
+
+from acc_gb300 import engine, instruments
+from acc_gb300.components.samples.homogeneous_single_scatterer import factory
+from acc_gb300.geometry import Cylinder, Difference, Sphere
+from acc_gb300.kernels import IsotropicKernel
+from helpers import chi2_per_dof, gpu_tallies, oracle_run, rel_err
+
+pytestmark = pytest.mark.gpu
+
+BUILDERS = {
+    "sphere_theta_tof": instruments.sphere_theta_tof,
+    "guide_chain": instruments.guide_chain,
+    "sqe_hollow_cylinder": instruments.sqe_hollow_cylinder,
+}
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _engine(engine_lib):
+    torch.cuda.init()
+    yield
+
+
+def gpu_record(ins, n, seed, floattype, uniforms=None):
+    ch = engine.chain_for_instrument(ins)
+    out, last = engine.replay(ch, n, uniforms=uniforms, seed=seed,
+                              floattype=floattype)
+    return out.cpu().numpy(), last.cpu().numpy()
+
+
+@pytest.mark.parametrize("name", list(BUILDERS))
+def test_fp64_same_stream_matches_oracle(name):
+    n, seed = 20000, 11
+    ins = BUILDERS[name]()
+    g_out, g_last = gpu_record(ins, n, seed, "float64")
+    _, stats, o_out, o_last = oracle_run(BUILDERS[name](), n, seed=seed,
+                                         record=True)
+    assert stats["processed"] == n
+    np.testing.assert_array_equal(g_last, o_last)
+    err = rel_err(g_out, o_out)
+    assert err.max() <= 1e-12, (name, err.max(), np.unravel_index(
+        err.argmax(), err.shape))
+
+
+@pytest.mark.parametrize("name", list(BUILDERS))
+def test_fp64_histograms_match_oracle(name):
+    n, seed = 200000, 5
+    ins = BUILDERS[name]()
+    st = engine.run_instrument(ins, n, seed=seed, floattype="float64")
+    assert st.processed == n
+    gt = gpu_tallies(ins)
+    ot, _, _, _ = oracle_run(BUILDERS[name](), n, seed=seed)
+    assert len(gt) == len(ot) > 0
+    for (gc, g), (oc, o) in zip(gt.items(), ot.items()):
+        assert gc.name == oc.name
+        np.testing.assert_array_equal(g[0], o[0])
+        np.testing.assert_allclose(g[1], o[1], rtol=1e-12, atol=1e-300)
+        np.testing.assert_allclose(g[2], o[2], rtol=1e-12, atol=1e-300)
+        assert g[0].sum() > 0
+
+
+@pytest.mark.parametrize("name", list(BUILDERS))
+def test_fp32_same_stream_within_1e5(name):
+    n, seed = 20000, 13
+    g_out, g_last = gpu_record(BUILDERS[name](), n, seed, "float32")
+    _, _, o_out, o_last = oracle_run(BUILDERS[name](), n, seed=seed,
+                                     record=True)
+    err = rel_err(g_out, o_out).max(axis=1)
+    bad = (err > 1e-5) | (g_last != o_last)
+    assert bad.mean() <= 1e-4, (name, bad.sum(), np.sort(err)[-5:])
+
+
+@pytest.mark.parametrize("name", list(BUILDERS))
+def test_fp32_independent_stream_chi2(name):
+    n = 1_000_000
+    ins = BUILDERS[name]()
+    engine.run_instrument(ins, n, seed=101, floattype="float32")
+    gt = gpu_tallies(ins)
+    ot, _, _, _ = oracle_run(BUILDERS[name](), n, seed=202)
+    for (gc, g), (_, o) in zip(gt.items(), ot.items()):
+        c2, dof = chi2_per_dof(g, o)
+        assert dof > 10, (gc.name, dof)
+        assert c2 <= 1.1, (gc.name, c2, dof)
+
+
+@pytest.mark.parametrize("floattype,tol", [("float64", 1e-12),
+                                           ("float32", 1e-5)])
+def test_injected_uniforms_match_oracle(floattype, tol):
+    n = 5000
+    rng = np.random.default_rng(3)
+    u = (rng.integers(0, 2 ** 24, size=(n, 16)) / 2.0 ** 24).astype(np.float32)
+    g_out, g_last = gpu_record(instruments.sphere_theta_tof(), n, 0, floattype,
+                               uniforms=u)
+    _, _, o_out, o_last = oracle_run(instruments.sphere_theta_tof(), n,
+                                     uniforms=u, record=True)
+    err = rel_err(g_out, o_out).max(axis=1)
+    bad = (err > tol) | (g_last != o_last)
+    assert bad.mean() <= (0 if floattype == "float64" else 1e-3), \
+        (bad.sum(), np.sort(err)[-3:])
+
+
+def _source_only():
+    import acc_gb300
+    ins = acc_gb300.instrument()
+    ins.append(instruments.guide_chain().components[0])
+    return ins
+
+
+def test_buffered_mode_matches_oracle():
+    """Per-component mode (ComponentBase.process): the guide chain's two
+    guides applied to a stored neutron array, FP64, within 1e-12."""
+    from oracle import binding as O
+    from acc_gb300.memory import HostBinder
+    n = 20000
+    _, _, n0, _ = oracle_run(_source_only(), n, seed=3, record=True)
+    n0[:, 2] -= 1.0  # into the first guide's frame
+    comps = instruments.guide_chain().components[1:3]
+    off, rot = [[0, 0, 10.001]], [np.eye(3)]
+    g = engine.process_buffer(comps, n0, seed=9, offsets=off, rotmats=rot,
+                              floattype="float64")
+    o = O.process_buffer(engine.build_chain(comps, off, rot, HostBinder()),
+                         n0, seed=9)
+    assert (o[:, 9] > 0).sum() > 100
+    assert rel_err(g, o).max() <= 1e-12
+
+
+KAT_SHAPES = {
+    "sphere": (lambda: Sphere(1.0),
+               [[0, 0, 0, 0, 0, 1], [0.5, 0, 0, 0, 0, 1]],
+               [[-1, 1], [-0.8660254037844386, 0.8660254037844386]]),
+    "cylinder": (lambda: Cylinder(1.0, 1.0),
+                 [[0, 0, -5, 0, 0, 1], [0.22, 0.35, -5, 0, 0, 1]],
+                 [[4.5, 5.5], [4.5, 5.5]]),
+    "hollow": (lambda: Difference(Cylinder(0.02, 0.10), Cylinder(0.01, 0.11)),
+               [[-1, 0, 0, 1, 0, 0]],
+               [[0.98, 0.99, 1.01, 1.02]]),
+}
+
+
+@pytest.mark.parametrize("shape", list(KAT_SHAPES))
+@pytest.mark.parametrize("floattype,tol", [("float64", 1e-14),
+                                           ("float32", 2e-6)])
+def test_intersections_on_gpu(shape, floattype, tol):
+    make, rays, expected = KAT_SHAPES[shape]
+    H = factory(make(), IsotropicKernel(0, 0))
+    ts, cnt = engine.intersect(H("s"), rays, floattype=floattype)
+    for k, e in enumerate(expected):
+        assert cnt[k] == len(e)
+        np.testing.assert_allclose(ts[k, :cnt[k]], e, rtol=tol, atol=tol)
+
+
+def test_guide_pass_through_on_gpu():
+    from acc_gb300.components.optics.guide import Guide
+    g = Guide("g", 3, 3, 2, 2, 16)
+    n = np.array([[0, 0, 0, 0, 0, 0.5, 0, 0, 0, 1.0]])
+    out = engine.process_buffer([g], n, floattype="float64")[0]
+    dt = (16 - out[2]) / out[5]
+    assert out[2] + out[5] * dt == 16.0
+    assert out[8] + dt == 32.0 and out[9] == 1.0

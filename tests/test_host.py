@@ -1,0 +1,145 @@
+"""Host-side logic: instrument geometry, component packing, the mcvine
+alias and run_script's script loading (no GPU)."""
+
+import json
+import os
+import textwrap
+
+import numpy as np
+import pytest
+
+import acc_gb300
+from acc_gb300 import _native as nat
+from acc_gb300.components.monitors.psd_monitor import PSD_monitor
+from acc_gb300.components.optics.arm import Arm
+from acc_gb300.components.optics.guide import Guide
+from acc_gb300.components.sources.source_simple import Source_simple
+from acc_gb300.engine import build_chain
+from acc_gb300.instrument import applyTransformation, calcTransformations
+from acc_gb300.memory import HostBinder
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+KATS = json.load(open(os.path.join(HERE, "golden", "reference_kats.json")))
+
+
+def test_coordinate_transforms_match_reference_kats():
+    g = KATS["coord_transform"]
+    ins = acc_gb300.instrument()
+    comps = []
+    for i, pl in enumerate(g["placements"]):
+        a = Arm(f"comp{i + 1}")
+        rel = comps[pl["relative"]] if pl["relative"] is not None else None
+        ins.append(a, position=pl["position"], orientation=pl["orientation"],
+                   relativeTo=rel)
+        comps.append(a)
+    offsets, rotmats = calcTransformations(ins)
+    assert len(offsets) == len(rotmats) == len(comps) - 1
+    for hop in g["hops"]:
+        r = np.array(hop["r"], float)
+        v = np.array(hop["v"], float)
+        k = hop["hop"]
+        applyTransformation(r, v, rotmats[k], offsets[k])
+        np.testing.assert_allclose(r, hop["r1"], atol=1e-12)
+        np.testing.assert_allclose(v, hop["v1"], atol=1e-12)
+
+
+def test_source_simple_params_and_checks():
+    s = Source_simple("s", radius=0.05, dist=5, xw=0.01, yh=0.01, E0=60, dE=10)
+    (square, width, height, radius, wl, L0, dL, E0, dE, xw, yh, dist,
+     pmul) = s.propagate_params
+    assert not square and not wl
+    assert pmul == pytest.approx(1e4 * np.pi * 0.05 ** 2)
+    with pytest.raises(RuntimeError):
+        Source_simple("s", radius=0.05, width=0.1, height=0.1)
+    with pytest.raises(RuntimeError):
+        Source_simple("s", radius=0.05, E0=10, dE=20)
+    with pytest.raises(RuntimeError):
+        Source_simple("s", radius=0.05, E0=0, dE=0, Lambda0=1, dLambda=2)
+    sq = Source_simple("s", radius=0, width=0.01, height=0.02, E0=60, dE=1)
+    assert sq.propagate_params[0] is True
+
+
+def test_guide_params():
+    g = Guide("g", w1=0.05, h1=0.05, w2=0.02, h2=0.02, l=5, m=3, alpha=3)
+    assert g.propagate_params == pytest.approx(
+        (-0.015, -0.015, 0.025, 0.025, 5, 0.99, 0.0219, 3, 3, 0.003))
+
+
+def test_build_chain_packs_transforms_and_tallies():
+    ins = acc_gb300.instrument()
+    src = Source_simple("s", radius=0.05, dist=1, xw=0.05, yh=0.05, E0=52.5,
+                        dE=47.5)
+    g = Guide("g", 0.05, 0.05, 0.05, 0.05, 10, m=3, alpha=3)
+    mon = PSD_monitor("m", xwidth=0.06, yheight=0.06, nx=100, ny=100)
+    ins.append(src, position=(0, 0, 0))
+    ins.append(g, position=(0, 0, 1))
+    ins.append(mon, position=(0, 0, 11.001), orientation=(0, 0, 90))
+    b = HostBinder()
+    off, rot = calcTransformations(ins)
+    ch = build_chain(ins.components, off, rot, b)
+    assert ch.ncomp == 3
+    assert ch.comp[1].flags & nat.FLAG_IDENTITY_ROT
+    assert not ch.comp[2].flags & nat.FLAG_IDENTITY_ROT
+    assert ch.off[1][2] == 1.0 and ch.off[2][2] == pytest.approx(10.001)
+    assert ch.comp[2].ip[0] == 100 and ch.comp[2].ip[1] == 100
+    assert ch.comp[2].tally == b.tallies[id(mon)].ctypes.data
+    assert b.out(mon).shape == (3, 100, 100)
+    for k in range(11):
+        assert ch.comp[0].fp[k] == pytest.approx(ch.comp[0].dp[k], rel=1e-7)
+
+
+def test_build_chain_limits():
+    with pytest.raises(ValueError):
+        build_chain([], binder=HostBinder())
+    with pytest.raises(ValueError):
+        build_chain([Arm(f"a{i}") for i in range(17)], binder=HostBinder())
+
+
+def test_mcvine_alias_and_script_loading(tmp_path):
+    from acc_gb300 import compat
+    from acc_gb300.run_script import loadInstrument
+    script = tmp_path / "instr.py"
+    script.write_text(textwrap.dedent('''
+        import mcvine
+        from mcvine.acc.components.sources.source_simple import Source_simple
+        from mcvine.acc.components.optics.guide import Guide
+        from mcvine.acc.components.monitors.psd_monitor import PSD_monitor
+
+        def instrument(z_mon=12., guide_m=3):
+            ins = mcvine.instrument()
+            ins.append(Source_simple('src', radius=0., width=0.03, height=0.03,
+                       dist=1., xw=0.035, yh=0.035, Lambda0=10., dLambda=9.5,
+                       E0=0., dE=0.), position=(0, 0, 0))
+            ins.append(Guide('g', w1=0.035, h1=0.035, w2=0.035, h2=0.035,
+                             l=10, m=guide_m), position=(0, 0, 1.))
+            ins.append(PSD_monitor('m', xwidth=0.08, yheight=0.08),
+                       position=(0, 0, z_mon))
+            return ins
+    '''))
+    assert compat.install_mcvine_alias() in (True, False)
+    with pytest.warns(UserWarning):
+        ins = loadInstrument(str(script), z_mon=13., unknown_kw=1)
+    names = [type(c).__name__ for c in ins.components]
+    assert names == ["Source_simple", "Guide", "PSD_monitor"]
+    off, rot = calcTransformations(ins)
+    np.testing.assert_allclose(off[1], [0, 0, 12.])
+
+
+def test_monitor_axes():
+    m = PSD_monitor("m", xmin=-0.03, xmax=0.03, ymin=-0.03, ymax=0.03, nx=100,
+                    ny=50)
+    assert m.x_centers.size == 100 and m.y_centers.size == 50
+    assert m.x_centers[0] == pytest.approx(-0.03 + 0.0003)
+    h = m.getHistogram(1.0)
+    assert h.data.shape == (100, 50)
+
+
+def test_sharding_ranges_cover_exactly():
+    from acc_gb300.sharding import shard_range
+    for n, w in [(10, 3), (1, 4), (1_000_003, 8), (0, 2)]:
+        parts = [shard_range(n, r, w) for r in range(w)]
+        assert sum(c for _, c in parts) == n
+        pos = 0
+        for f, c in parts:
+            assert f == pos
+            pos += c
