@@ -20,11 +20,13 @@ SOURCES = ["engine.cu", "probe.cu"]
 HEADERS = ["common.cuh", "components.cuh", "sample.cuh", "monitors.cuh"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-# FP32 code paths are written for approximate division/sqrt and flush to
-# zero; none of these flags changes FP64 arithmetic.
-NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--ftz=true",
-              "--prec-div=false", "--prec-sqrt=false", "-Xcompiler", "-fPIC",
-              "-Xcompiler", "-Wall"]
+# FP32 code paths are written for approximate division and square root;
+# neither flag changes FP64 arithmetic.  Denormals are kept (no --ftz): a
+# flush would also zero float32 table entries converted to double and the
+# squares of small float weights.
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--prec-div=false",
+              "--prec-sqrt=false", "-Xcompiler", "-fPIC", "-Xcompiler",
+              "-Wall"]
 
 
 def nvcc():

@@ -261,12 +261,82 @@ __global__ void intersect_kernel(const __grid_constant__ mcv_component c,
   uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double* r = rays + i * 6;
-  Hits<R> h = intersect_shape<R>(c, (R)r[0], (R)r[1], (R)r[2], (R)r[3],
-                                 (R)r[4], (R)r[5]);
+  Hits<R> h = intersect_shape_from<R>(c, (R)r[0], (R)r[1], (R)r[2], (R)r[3],
+                                      (R)r[4], (R)r[5]);
   double* o = out_ts + i * MCV_MAX_INTERSECTIONS;
   for (int k = 0; k < MCV_MAX_INTERSECTIONS; ++k)
     o[k] = k < h.n ? (double)h.get(k) : __longlong_as_double(0x7ff8000000000000ll);
   out_n[i] = h.n;
+}
+
+// Batched persistent launch over many instrument variants.  Blocks take
+// work items of `chunk` neutrons from a device counter (DevStatus::
+// work_next); item k belongs to the variant whose cumulative item range
+// holds k.  The block stages that variant's chain in shared memory once per
+// change of variant.  Neutron i of variant v draws from Philox (seeds[v], i).
+template <typename R>
+__global__ void __launch_bounds__(kMaxThreads)
+    batched_kernel(const mcv_chain* __restrict__ variants, int nvar,
+                   const uint64_t* __restrict__ counts,
+                   const uint64_t* __restrict__ seeds, uint64_t chunk,
+                   DevStatus* st) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  mcv_chain& ch = *reinterpret_cast<mcv_chain*>(smem);
+  uint64_t* item_start = reinterpret_cast<uint64_t*>(
+      smem + (sizeof(mcv_chain) + 15) / 16 * 16);
+  __shared__ uint64_t s_item;
+  __shared__ int s_var;
+  if (threadIdx.x == 0) {
+    uint64_t acc = 0;
+    for (int v = 0; v < nvar; ++v) {
+      item_start[v] = acc;
+      acc += (counts[v] + chunk - 1) / chunk;
+    }
+    item_start[nvar] = acc;
+  }
+  __syncthreads();
+  const uint64_t total = item_start[nvar];
+  int cur = -1;
+  Counters k{0, 0, 0, 0};
+  for (;;) {
+    if (threadIdx.x == 0) {
+      uint64_t it = atomicAdd(&st->work_next, 1ull);
+      int lo = 0, hi = nvar;  // item_start[lo] <= it < item_start[hi]
+      while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (item_start[mid] <= it) lo = mid;
+        else hi = mid;
+      }
+      s_item = it;
+      s_var = lo;
+    }
+    __syncthreads();
+    const uint64_t it = s_item;
+    const int v = s_var;
+    if (it >= total) break;
+    if (v != cur) {
+      const uint2* src = reinterpret_cast<const uint2*>(variants + v);
+      uint2* dst = reinterpret_cast<uint2*>(smem);
+      for (int i = threadIdx.x; i < (int)(sizeof(mcv_chain) / 8);
+           i += blockDim.x)
+        dst[i] = src[i];
+      cur = v;
+      __syncthreads();
+    }
+    const uint64_t a = (it - item_start[v]) * chunk;
+    const uint64_t cnt = counts[v];
+    const uint64_t b = a + chunk < cnt ? a + chunk : cnt;
+    const uint64_t seed = seeds[v];
+    for (uint64_t i = a + threadIdx.x; i < b; i += blockDim.x) {
+      Neutron<R> nt;
+      zero_neutron(nt);
+      PhiloxStream rng(seed, i, 0u);
+      run_chain_one<R>(nt, rng, ch, k);
+      k.processed++;
+    }
+    __syncthreads();
+  }
+  flush_counters(k, st);
 }
 
 }  // namespace mcv
@@ -278,6 +348,15 @@ struct mcv_ctx {
   int device;
   int sm_count;
   DevStatus* d_status;
+  void* d_batch;        // staged variant descriptions (mcv_run_batched)
+  size_t batch_bytes;
+};
+
+struct mcv_graph {
+  mcv_ctx* ctx;
+  void* d_batch;
+  cudaGraph_t graph;
+  cudaGraphExec_t exec;
 };
 
 namespace {
@@ -444,6 +523,82 @@ int launch_chain(mcv_ctx* ctx, const mcv_chain* chain, uint64_t ncount,
   return 0;
 }
 
+constexpr uint64_t kDefaultChunk = 8192;
+
+// Layout of a staged batch: chains, then counts, then seeds.
+size_t batch_bytes(int nvar) {
+  return (size_t)nvar * sizeof(mcv_chain) + 2 * (size_t)nvar * sizeof(uint64_t);
+}
+
+int validate_batch(const mcv_chain* variants, int nvar, const uint64_t* counts,
+                   const uint64_t* seeds, int precision, mcv_status* st) {
+  if (!variants || !counts || !seeds || nvar < 1 || nvar > MCV_MAX_VARIANTS) {
+    set_msg(st, MCV_EINVAL, "batched run needs 1..1024 variants%s", "");
+    return MCV_EINVAL;
+  }
+  for (int v = 0; v < nvar; ++v) {
+    int rc = validate_chain(variants + v, st);
+    if (rc) {
+      if (st) st->first_bad_component = v;
+      return rc;
+    }
+  }
+  if (!precision_ok(precision, st)) return MCV_EINVAL;
+  return MCV_OK;
+}
+
+int stage_batch(void* dst, const mcv_chain* variants, int nvar,
+                const uint64_t* counts, const uint64_t* seeds,
+                cudaStream_t s) {
+  char* d = (char*)dst;
+  size_t nc = (size_t)nvar * sizeof(mcv_chain), nu = nvar * sizeof(uint64_t);
+  cudaError_t e = cudaMemcpyAsync(d, variants, nc, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d + nc, counts, nu, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d + nc + nu, seeds, nu, cudaMemcpyHostToDevice, s);
+  return e == cudaSuccess ? 0 : (int)e;
+}
+
+template <typename R>
+void launch_batched_t(const mcv_ctx* ctx, const void* dbatch, int nvar,
+                      const mcv_launch* launch, cudaStream_t s) {
+  const char* d = (const char*)dbatch;
+  const mcv_chain* chains = (const mcv_chain*)d;
+  const uint64_t* counts = (const uint64_t*)(d + nvar * sizeof(mcv_chain));
+  const uint64_t* seeds = counts + nvar;
+  int t = (launch && launch->threads_per_block > 0) ? launch->threads_per_block
+                                                    : kMaxThreads;
+  if (t > kMaxThreads) t = kMaxThreads;
+  t = (t + 31) / 32 * 32;
+  size_t smem = (sizeof(mcv_chain) + 15) / 16 * 16 + 8 * (size_t)(nvar + 1);
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_kernel<R>, t,
+                                                smem);
+  if (per_sm < 1) per_sm = 1;
+  int blocks = (launch && launch->blocks > 0) ? launch->blocks
+                                              : ctx->sm_count * per_sm;
+  uint64_t chunk = (launch && launch->chunk > 0) ? (uint64_t)launch->chunk
+                                                 : kDefaultChunk;
+  cudaMemsetAsync(&ctx->d_status->work_next, 0, sizeof(unsigned long long), s);
+  batched_kernel<R><<<blocks, t, smem, s>>>(chains, nvar, counts, seeds, chunk,
+                                            ctx->d_status);
+}
+
+void launch_batched(const mcv_ctx* ctx, const void* dbatch, int nvar,
+                    int precision, const mcv_launch* launch, cudaStream_t s) {
+  if (precision == MCV_FP32)
+    launch_batched_t<float>(ctx, dbatch, nvar, launch, s);
+  else
+    launch_batched_t<double>(ctx, dbatch, nvar, launch, s);
+}
+
+uint64_t sum_counts(const uint64_t* counts, int nvar) {
+  uint64_t t = 0;
+  for (int v = 0; v < nvar; ++v) t += counts[v];
+  return t;
+}
+
 }  // namespace
 
 extern "C" {
@@ -472,6 +627,8 @@ int mcv_ctx_create(int device, mcv_ctx** out) {
   mcv_ctx* c = new (std::nothrow) mcv_ctx;
   if (!c) return MCV_ECAPACITY;
   c->device = device;
+  c->d_batch = nullptr;
+  c->batch_bytes = 0;
   cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
   if (cudaMalloc(&c->d_status, sizeof(DevStatus)) != cudaSuccess) {
     cudaGetLastError();
@@ -492,6 +649,7 @@ int mcv_ctx_destroy(mcv_ctx* ctx) {
   {
     DeviceGuard g(ctx->device);
     cudaFree(ctx->d_status);
+    if (ctx->d_batch) cudaFree(ctx->d_batch);
   }
   delete ctx;
   return MCV_OK;
@@ -632,6 +790,103 @@ int mcv_process_buffer(mcv_ctx* ctx, const mcv_chain* chain, void* neutrons,
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(st, e, "mcv_process_buffer launch");
   if (st) return mcv_ctx_status(ctx, stream, n, st);
+  return MCV_OK;
+}
+
+int mcv_run_batched(mcv_ctx* ctx, const mcv_chain* variants,
+                    int32_t nvariants, const uint64_t* counts,
+                    const uint64_t* seeds, int precision,
+                    const mcv_launch* launch, void* stream, mcv_status* st) {
+  int rc = validate_batch(variants, nvariants, counts, seeds, precision, st);
+  if (rc) return rc;
+  if (!ctx) {
+    set_msg(st, MCV_EINVAL, "context is NULL%s", "");
+    return MCV_EINVAL;
+  }
+  DeviceGuard g(ctx->device);
+  cudaStream_t s = (cudaStream_t)stream;
+  size_t need = batch_bytes(nvariants);
+  if (need > ctx->batch_bytes) {
+    // the previous batch may still be read by work queued on the stream
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(st, e, "mcv_run_batched");
+    if (ctx->d_batch) cudaFree(ctx->d_batch);
+    ctx->d_batch = nullptr;
+    ctx->batch_bytes = 0;
+    e = cudaMalloc(&ctx->d_batch, need);
+    if (e != cudaSuccess) return cuda_fail(st, e, "mcv_run_batched staging");
+    ctx->batch_bytes = need;
+  }
+  int e1 = stage_batch(ctx->d_batch, variants, nvariants, counts, seeds, s);
+  if (e1) return cuda_fail(st, (cudaError_t)e1, "mcv_run_batched staging");
+  launch_batched(ctx, ctx->d_batch, nvariants, precision, launch, s);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(st, e, "mcv_run_batched launch");
+  if (st)
+    return mcv_ctx_status(ctx, stream, sum_counts(counts, nvariants), st);
+  return MCV_OK;
+}
+
+int mcv_graph_create_batched(mcv_ctx* ctx, const mcv_chain* variants,
+                             int32_t nvariants, const uint64_t* counts,
+                             const uint64_t* seeds, int precision,
+                             const mcv_launch* launch, mcv_graph** out) {
+  if (!out) return MCV_EINVAL;
+  *out = nullptr;
+  int rc = validate_batch(variants, nvariants, counts, seeds, precision,
+                          nullptr);
+  if (rc) return rc;
+  if (!ctx) return MCV_EINVAL;
+  DeviceGuard g(ctx->device);
+  mcv_graph* gr = new (std::nothrow) mcv_graph;
+  if (!gr) return MCV_ECAPACITY;
+  gr->ctx = ctx;
+  gr->d_batch = nullptr;
+  gr->graph = nullptr;
+  gr->exec = nullptr;
+  cudaStream_t s = nullptr;
+  cudaError_t e = cudaMalloc(&gr->d_batch, batch_bytes(nvariants));
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  if (e == cudaSuccess) {
+    int e1 = stage_batch(gr->d_batch, variants, nvariants, counts, seeds, s);
+    e = e1 ? (cudaError_t)e1 : cudaStreamSynchronize(s);
+  }
+  if (e == cudaSuccess)
+    e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    launch_batched(ctx, gr->d_batch, nvariants, precision, launch, s);
+    cudaError_t le = cudaGetLastError();
+    e = cudaStreamEndCapture(s, &gr->graph);
+    if (le != cudaSuccess) e = le;
+  }
+  if (e == cudaSuccess)
+    e = cudaGraphInstantiate(&gr->exec, gr->graph, 0);
+  if (s) cudaStreamDestroy(s);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    mcv_graph_destroy(gr);
+    return MCV_ECUDA;
+  }
+  *out = gr;
+  return MCV_OK;
+}
+
+int mcv_graph_launch(mcv_graph* graph, void* stream) {
+  if (!graph || !graph->exec) return MCV_EINVAL;
+  DeviceGuard g(graph->ctx->device);
+  cudaError_t e = cudaGraphLaunch(graph->exec, (cudaStream_t)stream);
+  return e == cudaSuccess ? MCV_OK : MCV_ECUDA;
+}
+
+int mcv_graph_destroy(mcv_graph* graph) {
+  if (!graph) return MCV_OK;
+  {
+    DeviceGuard g(graph->ctx->device);
+    if (graph->exec) cudaGraphExecDestroy(graph->exec);
+    if (graph->graph) cudaGraphDestroy(graph->graph);
+    if (graph->d_batch) cudaFree(graph->d_batch);
+  }
+  delete graph;
   return MCV_OK;
 }
 

@@ -25,8 +25,9 @@ __device__ __forceinline__ void tally_add(const Tally& t, uint64_t bin,
                                           float p) {
   if (!t.out) return;
   atomicAdd(t.out + bin, 1.0);
-  atomicAdd(t.out + t.nbins + bin, (double)p);
-  atomicAdd(t.out + 2 * t.nbins + bin, (double)(p * p));
+  const double pd = (double)p;
+  atomicAdd(t.out + t.nbins + bin, pd);
+  atomicAdd(t.out + 2 * t.nbins + bin, pd * pd);
 }
 
 // propagate to z = 0 without moving the neutron (prop_z0, acc/neutron.py:60-66);

@@ -48,7 +48,7 @@ __device__ __forceinline__ bool isect_cylinder(R x, R y, R z, R vx, R vy,
   R a = vx * vx + vy * vy, b = x * vx + y * vy, c = x * x + y * y - Rad * Rad;
   R k = b * b - a * c;
   if constexpr (sizeof(R) == 4) {
-    if (fabsf(k) < 1e-4f * (b * b)) {
+    if (fabsf(k) < 1e-4f * fmaxf(b * b, fabsf(a * c))) {
       double A = (double)vx * vx + (double)vy * vy;
       double B = (double)x * vx + (double)y * vy;
       double C = (double)x * x + (double)y * y - (double)Rad * Rad;
@@ -312,6 +312,27 @@ __device__ __forceinline__ Hits<R> intersect_shape(const mcv_component& c,
   h.t3 = s3;
   h.n = n;
   return h;
+}
+
+// Hit times of a ray with the shape, computed from the ray's closest
+// approach to the shape origin and shifted back by the time to get there
+// (FP32: avoids cancelling a long flight against a short chord).
+template <typename R>
+__device__ __forceinline__ Hits<R> intersect_shape_from(const mcv_component& c,
+                                                        R x, R y, R z, R vx,
+                                                        R vy, R vz) {
+  if constexpr (sizeof(R) == 8) {
+    return intersect_shape<R>(c, x, y, z, vx, vy, vz);
+  } else {
+    float t0 = -(x * vx + y * vy + z * vz) / (vx * vx + vy * vy + vz * vz);
+    Hits<float> h = intersect_shape<float>(c, fmaf(vx, t0, x), fmaf(vy, t0, y),
+                                           fmaf(vz, t0, z), vx, vy, vz);
+    h.t0 += t0;
+    h.t1 += t0;
+    h.t2 += t0;
+    h.t3 += t0;
+    return h;
+  }
 }
 
 // =========================================================== HSS helpers

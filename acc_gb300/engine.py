@@ -198,3 +198,81 @@ def probe_atomic_rate(nbins, repeats=3, device=None):
     nat.check(nat.lib().mcv_probe_atomic_rate(ctx.device, int(nbins),
                                               int(repeats), ctypes.byref(out)))
     return out.value
+
+
+# ------------------------------------------------------------ batched runs
+def _batch_arrays(chains, counts, seeds):
+    n = len(chains)
+    if not 1 <= n <= nat.MCV_MAX_VARIANTS:
+        raise ValueError(f"1..{nat.MCV_MAX_VARIANTS} variants, got {n}")
+    if len(counts) != n or len(seeds) != n:
+        raise ValueError("one count and one seed per variant")
+    arr = (nat.mcv_chain * n)()
+    for v, ch in enumerate(chains):
+        arr[v] = ch
+    cnt = (ctypes.c_uint64 * n)(*[int(c) for c in counts])
+    sd = (ctypes.c_uint64 * n)(*[int(s) for s in seeds])
+    return arr, cnt, sd
+
+
+def _launch3(threads_per_block=None, blocks=None, chunk=None):
+    if not (threads_per_block or blocks or chunk):
+        return None
+    L = nat.mcv_launch()
+    L.threads_per_block = int(threads_per_block or 0)
+    L.blocks = int(blocks or 0)
+    L.chunk = int(chunk or 0)
+    return L
+
+
+def run_batched(instruments, counts, seeds, floattype=None,
+                threads_per_block=None, blocks=None, chunk=None, sync=True,
+                device=None):
+    """mcv_run_batched: every instrument (variant) runs counts[v] neutrons
+    of its own stream seeds[v] in one persistent launch."""
+    ctx = nat.context(device)
+    chains = [chain_for_instrument(ins) for ins in instruments]
+    arr, cnt, sd = _batch_arrays(chains, counts, seeds)
+    L = _launch3(threads_per_block, blocks, chunk)
+    st = nat.mcv_status() if sync else None
+    rc = nat.lib().mcv_run_batched(
+        ctx.handle, arr, len(chains), cnt, sd, _precision(floattype),
+        ctypes.byref(L) if L else None, nat.current_stream_handle(),
+        ctypes.byref(st) if st else None)
+    nat.check(rc, st)
+    return st
+
+
+class BatchedGraph:
+    """The batched launch captured once in a CUDA graph; `launch()` replays
+    it on the current stream (mcv_graph_create_batched / mcv_graph_launch)."""
+
+    def __init__(self, instruments, counts, seeds, floattype=None,
+                 threads_per_block=None, blocks=None, chunk=None,
+                 device=None):
+        self.ctx = nat.context(device)
+        self.instruments = list(instruments)
+        self.total = int(sum(int(c) for c in counts))
+        chains = [chain_for_instrument(ins) for ins in self.instruments]
+        arr, cnt, sd = _batch_arrays(chains, counts, seeds)
+        L = _launch3(threads_per_block, blocks, chunk)
+        self.handle = ctypes.c_void_p()
+        rc = nat.lib().mcv_graph_create_batched(
+            self.ctx.handle, arr, len(chains), cnt, sd, _precision(floattype),
+            ctypes.byref(L) if L else None, ctypes.byref(self.handle))
+        nat.check(rc)
+
+    def launch(self):
+        nat.check(nat.lib().mcv_graph_launch(self.handle,
+                                             nat.current_stream_handle()))
+
+    def close(self):
+        if self.handle:
+            nat.lib().mcv_graph_destroy(self.handle)
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

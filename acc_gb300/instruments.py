@@ -158,3 +158,25 @@ def powder_banked(peaks=None, unitcell_volume=66.4, nbanks=8, ntubes=128,
     ins.append(HSS("sample"), position=(0, 0, z), orientation=(90, 0, 0))
     ins.append(det, position=(0, 0, z))
     return ins
+
+
+def sphere_variants(nvariants=64, seed=0, nmin=1e6, nmax=1e8, emin=20.0,
+                    emax=500.0):
+    """`nvariants` copies of the sphere_theta_tof chain, each with a
+    monochromatic source at Ei log-uniform in [emin, emax] meV, a neutron
+    count log-uniform in [nmin, nmax] and its own seed and histogram.
+    Returns (instruments, counts, seeds)."""
+    rng = np.random.default_rng(seed)
+    Ei = np.exp(rng.uniform(np.log(emin), np.log(emax), nvariants))
+    counts = np.exp(rng.uniform(np.log(nmin), np.log(nmax), nvariants))
+    counts = [int(c) for c in counts]
+    seeds = [int(s) for s in rng.integers(1, 2 ** 62, nvariants)]
+    out = []
+    for e in Ei:
+        ins = sphere_theta_tof()
+        src = ins.components[0]
+        sp = list(src.propagate_params)
+        sp[7], sp[8] = float(e), 0.0  # E0, dE
+        src.propagate_params = tuple(sp)
+        out.append(ins)
+    return out, counts, seeds

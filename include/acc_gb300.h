@@ -239,6 +239,37 @@ int mcv_process_buffer(mcv_ctx* ctx, const mcv_chain* chain, void* neutrons,
                        mcv_status* st);
 
 /*
+ * Batched run: `nvariants` instruments in one persistent launch.  No
+ * counterpart in the reference, which runs one instrument per launch
+ * (acc/run_script.py:210-223).  `variants`, `counts` and `seeds` are host
+ * arrays; variant v runs counts[v] neutrons (indices 0..counts[v]-1 of the
+ * Philox stream seeds[v]) into its own tallies.  Work items of
+ * launch->chunk neutrons (0 = 8192) are handed out from the context's
+ * device work counter, so variants of very different sizes balance across
+ * the SMs.  The descriptions are staged in a context-owned device buffer:
+ * calls sharing a context must be ordered on one stream.
+ */
+#define MCV_MAX_VARIANTS 1024
+int mcv_run_batched(mcv_ctx* ctx, const mcv_chain* variants,
+                    int32_t nvariants, const uint64_t* counts,
+                    const uint64_t* seeds, int precision,
+                    const mcv_launch* launch, void* stream, mcv_status* st);
+
+/*
+ * The batched launch captured once into a CUDA graph (work-counter reset +
+ * kernel), replayed with mcv_graph_launch.  The graph owns device copies of
+ * the variant descriptions; the variants' tallies accumulate over replays.
+ * Read the counters with mcv_ctx_status after the replays.
+ */
+typedef struct mcv_graph mcv_graph;
+int mcv_graph_create_batched(mcv_ctx* ctx, const mcv_chain* variants,
+                             int32_t nvariants, const uint64_t* counts,
+                             const uint64_t* seeds, int precision,
+                             const mcv_launch* launch, mcv_graph** out);
+int mcv_graph_launch(mcv_graph* graph, void* stream);
+int mcv_graph_destroy(mcv_graph* graph);
+
+/*
  * Geometry probe: the intersection times of rays with the shape of an HSS
  * component (arrow_intersect.py render + intersect).  rays[n][6] float64;
  * out_ts[n][MCV_MAX_INTERSECTIONS] float64; out_n[n] int32.
