@@ -16,8 +16,12 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libacc_gb300.so")
 
-SOURCES = ["engine.cu", "probe.cu"]
-HEADERS = ["common.cuh", "components.cuh", "sample.cuh", "monitors.cuh"]
+SOURCES = ["engine.cu", "launch_fp32.cu", "launch_fp64.cu", "probe.cu"]
+HEADERS = ["common.cuh", "components.cuh", "sample.cuh", "monitors.cuh",
+           "kernels.cuh"]
+# per-source extra flags: the FP64 kernels round every multiply and add
+# separately, like the CPU restatement they are checked against
+EXTRA_FLAGS = {"launch_fp64.cu": ["--fmad=false"]}
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # FP32 code paths are written for approximate division and square root;
@@ -53,8 +57,8 @@ def stale():
 
 def _compile(src):
     obj = os.path.join(BUILD_DIR, os.path.splitext(src)[0] + ".o")
-    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, src), "-o",
-           obj]
+    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *EXTRA_FLAGS.get(src, []), "-c",
+           os.path.join(CSRC, src), "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed on {src}:\n{r.stdout}\n{r.stderr}")

@@ -76,7 +76,7 @@ class mcv_launch(ctypes.Structure):
         ("threads_per_block", ctypes.c_int32),
         ("blocks", ctypes.c_int32),
         ("chunk", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("variant", ctypes.c_int32),
     ]
 
 

@@ -20,18 +20,21 @@ constexpr double kPi = 3.14159265358979323846;
 
 // ------------------------------------------------------------ random streams
 // Philox4x32-10 (Salmon et al., SC'11): counter (index lo, index hi, block,
-// stream), key (seed lo, seed hi).  Four uniforms per block, kept in
-// registers and popped by shifting so no local-memory indexing happens.
+// stream), key (seed lo, seed hi).  Each 128-bit block w0..w3 gives five
+// 24-bit integers u (bits 0-23, 24-47, 48-71, 72-95, 96-119 of
+// w0 | w1<<32 | w2<<64 | w3<<96) and so five float32-exact uniforms
+// u * 2^-24; they are kept in registers and popped by shifting, so no
+// local-memory indexing happens.
 struct PhiloxStream {
   uint32_t k0, k1, c0, c1, c2, c3;
-  uint32_t b0, b1, b2, b3;
+  uint32_t b0, b1, b2, b3, b4;
   int left;
 
   __device__ __forceinline__ PhiloxStream(uint64_t seed, uint64_t index,
                                           uint32_t stream)
       : k0((uint32_t)seed), k1((uint32_t)(seed >> 32)), c0((uint32_t)index),
         c1((uint32_t)(index >> 32)), c2(0), c3(stream), b0(0), b1(0), b2(0),
-        b3(0), left(0) {}
+        b3(0), b4(0), left(0) {}
 
   __device__ __forceinline__ void refill() {
     uint32_t x0 = c0, x1 = c1, x2 = c2, x3 = c3, y0 = k0, y1 = k1;
@@ -49,23 +52,25 @@ struct PhiloxStream {
       x2 = n2;
       x3 = lo0;
     }
-    b0 = x0;
-    b1 = x1;
-    b2 = x2;
-    b3 = x3;
-    left = 4;
+    b0 = x0 & 0xFFFFFFu;
+    b1 = __funnelshift_r(x0, x1, 24) & 0xFFFFFFu;
+    b2 = __funnelshift_r(x1, x2, 16) & 0xFFFFFFu;
+    b3 = x2 >> 8;
+    b4 = x3 & 0xFFFFFFu;
+    left = 5;
     ++c2;
   }
 
-  // float32-exact uniform (w >> 8) * 2^-24 in [0, 1)
+  // float32-exact uniform u * 2^-24 in [0, 1)
   __device__ __forceinline__ float next() {
     if (left == 0) refill();
     uint32_t w = b0;
     b0 = b1;
     b1 = b2;
     b2 = b3;
+    b3 = b4;
     --left;
-    return __uint2float_rz(w >> 8) * 5.9604644775390625e-08f;
+    return __uint2float_rz(w) * 5.9604644775390625e-08f;
   }
   __device__ __forceinline__ int overrun() const { return 0; }
 };

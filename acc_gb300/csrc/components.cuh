@@ -99,99 +99,108 @@ __device__ __forceinline__ float reflectivity(float Q, float R0, float Qc,
   return R;
 }
 
-// Guide.propagate (acc/components/optics/guide.py:66-162).  Returns 1 when
-// the bounce loop ran out of its MCV_MAX_BOUNCES iterations.
+// Guide.propagate (acc/components/optics/guide.py:66-162), split into the
+// entry (propagate to z=0, absorb outside the opening: lines 74-83) and one
+// pass of the bounce loop (lines 85-159) so that the path-regeneration
+// kernel can advance a guide one bounce per step with the same arithmetic.
+// The loop's locals live in the neutron itself; they are what the reference
+// writes back at line 160.
+
+// false when the neutron is absorbed at the opening (only p changes then)
 template <typename R>
-__device__ __forceinline__ int guide(Neutron<R>& n, const mcv_component& c) {
-  const R ww = prm<R>(c, 0), hh = prm<R>(c, 1), hw1 = prm<R>(c, 2),
-          hh1 = prm<R>(c, 3), l = prm<R>(c, 4);
-  const R R0 = prm<R>(c, 5), Qc = prm<R>(c, 6), alpha = prm<R>(c, 7),
-          m = prm<R>(c, 8), W = prm<R>(c, 9);
-  R x = n.x, y = n.y, z = n.z, vx = n.vx, vy = n.vy, vz = n.vz, prob = n.p;
-  R dt = -z / vz;
-  x += vx * dt;
-  y += vy * dt;
-  z = R(0);
+__device__ __forceinline__ bool guide_enter(Neutron<R>& n,
+                                            const mcv_component& c) {
+  const R hw1 = prm<R>(c, 2), hh1 = prm<R>(c, 3);
+  R dt = -n.z / n.vz;
+  R x = n.x + n.vx * dt;
+  R y = n.y + n.vy * dt;
   if (x <= -hw1 || x >= hw1 || y <= -hh1 || y >= hh1) {
-    // absorb (acc/neutron.py:25-28); the moved position stays local
-    n.p = R(-1);
-    return 0;
-  }
-  n.t.add(dt);
-  // |n| of the vertical and horizontal mirror normals (loop invariants)
-  const R nlen2v = l * l + ww * ww, nlen2h = l * l + hh * hh;
-  int overflow = 1;
-  for (int nb = 0; nb < MCV_MAX_BOUNCES; ++nb) {
-    R av = l * vx, bv = ww * vz, ah = l * vy, bh = hh * vz;
-    R vdotn_v1 = bv + av, vdotn_v2 = bv - av;
-    R vdotn_h1 = bh + ah, vdotn_h2 = bh - ah;
-    R cv1 = -hw1 * l - z * ww, cv2 = x * l;
-    R ch1 = -hh1 * l - z * hh, ch2 = y * l;
-    R t1 = (l - z) / vz, t2;
-    int i = 0;
-    if (vdotn_v1 < 0) {
-      t2 = (cv1 - cv2) / vdotn_v1;
-      if (t2 < t1) { t1 = t2; i = 1; }
-    }
-    if (vdotn_v2 < 0) {
-      t2 = (cv1 + cv2) / vdotn_v2;
-      if (t2 < t1) { t1 = t2; i = 2; }
-    }
-    if (vdotn_h1 < 0) {
-      t2 = (ch1 - ch2) / vdotn_h1;
-      if (t2 < t1) { t1 = t2; i = 3; }
-    }
-    if (vdotn_h2 < 0) {
-      t2 = (ch1 + ch2) / vdotn_h2;
-      if (t2 < t1) { t1 = t2; i = 4; }
-    }
-    if (i == 0) {
-      overflow = 0;
-      break;
-    }
-    x += vx * t1;
-    y += vy * t1;
-    z += vz * t1;
-    n.t.add(t1);
-    R vdn = (i == 1) ? vdotn_v1 : (i == 2) ? vdotn_v2 : (i == 3) ? vdotn_h1
-                                                                 : vdotn_h2;
-    R nlen2 = (i <= 2) ? nlen2v : nlen2h;
-    R q, d;
-    if constexpr (sizeof(R) == 4) {
-      R rn = m_rsqrt(nlen2);
-      q = R(kV2K) * (-2) * vdn * rn;
-      d = 2 * vdn * (rn * rn);
-    } else {
-      q = R(kV2K) * (-2) * vdn / m_sqrt(nlen2);
-      d = 2 * vdn / nlen2;
-    }
-    if (i == 1) {
-      vx = vx - d * l;
-      vz = vz - d * ww;
-    } else if (i == 2) {
-      vx = vx + d * l;
-      vz = vz - d * ww;
-    } else if (i == 3) {
-      vy = vy - d * l;
-      vz = vz - d * hh;
-    } else {
-      vy = vy + d * l;
-      vz = vz - d * hh;
-    }
-    prob *= reflectivity(q, R0, Qc, alpha, m, W);
-    if (prob <= 0) {
-      overflow = 0;
-      break;
-    }
+    n.p = R(-1);  // absorb (acc/neutron.py:25-28)
+    return false;
   }
   n.x = x;
   n.y = y;
-  n.z = z;
-  n.vx = vx;
-  n.vy = vy;
-  n.vz = vz;
-  n.p = prob;
-  return overflow;
+  n.z = R(0);
+  n.t.add(dt);
+  return true;
+}
+
+// one pass of the bounce loop; true when the neutron has left the guide
+// (it stays at its last reflection point, guide.py:122-123) or its weight
+// is gone
+template <typename R>
+__device__ __forceinline__ bool guide_bounce(Neutron<R>& n,
+                                             const mcv_component& c) {
+  const R ww = prm<R>(c, 0), hh = prm<R>(c, 1), hw1 = prm<R>(c, 2),
+          hh1 = prm<R>(c, 3), l = prm<R>(c, 4);
+  R x = n.x, y = n.y, z = n.z, vx = n.vx, vy = n.vy, vz = n.vz;
+  R av = l * vx, bv = ww * vz, ah = l * vy, bh = hh * vz;
+  R vdotn_v1 = bv + av, vdotn_v2 = bv - av;
+  R vdotn_h1 = bh + ah, vdotn_h2 = bh - ah;
+  R cv1 = -hw1 * l - z * ww, cv2 = x * l;
+  R ch1 = -hh1 * l - z * hh, ch2 = y * l;
+  R t1 = (l - z) / vz, t2;
+  int i = 0;
+  if (vdotn_v1 < 0) {
+    t2 = (cv1 - cv2) / vdotn_v1;
+    if (t2 < t1) { t1 = t2; i = 1; }
+  }
+  if (vdotn_v2 < 0) {
+    t2 = (cv1 + cv2) / vdotn_v2;
+    if (t2 < t1) { t1 = t2; i = 2; }
+  }
+  if (vdotn_h1 < 0) {
+    t2 = (ch1 - ch2) / vdotn_h1;
+    if (t2 < t1) { t1 = t2; i = 3; }
+  }
+  if (vdotn_h2 < 0) {
+    t2 = (ch1 + ch2) / vdotn_h2;
+    if (t2 < t1) { t1 = t2; i = 4; }
+  }
+  if (i == 0) return true;  // the neutron left the guide
+  n.x = x + vx * t1;
+  n.y = y + vy * t1;
+  n.z = z + vz * t1;
+  n.t.add(t1);
+  R vdn = (i == 1) ? vdotn_v1 : (i == 2) ? vdotn_v2 : (i == 3) ? vdotn_h1
+                                                               : vdotn_h2;
+  R lw = (i <= 2) ? ww : hh;  // the mirror's slope term
+  R nlen2 = l * l + lw * lw;
+  R q, d;
+  if constexpr (sizeof(R) == 4) {
+    R rn = m_rsqrt(nlen2);
+    q = R(kV2K) * (-2) * vdn * rn;
+    d = 2 * vdn * (rn * rn);
+  } else {
+    q = R(kV2K) * (-2) * vdn / m_sqrt(nlen2);
+    d = 2 * vdn / nlen2;
+  }
+  if (i == 1) {
+    n.vx = vx - d * l;
+    n.vz = vz - d * ww;
+  } else if (i == 2) {
+    n.vx = vx + d * l;
+    n.vz = vz - d * ww;
+  } else if (i == 3) {
+    n.vy = vy - d * l;
+    n.vz = vz - d * hh;
+  } else {
+    n.vy = vy + d * l;
+    n.vz = vz - d * hh;
+  }
+  n.p *= reflectivity(q, prm<R>(c, 5), prm<R>(c, 6), prm<R>(c, 7),
+                      prm<R>(c, 8), prm<R>(c, 9));
+  return n.p <= 0;
+}
+
+// The whole guide; returns 1 when the bounce loop ran out of its
+// MCV_MAX_BOUNCES iterations.
+template <typename R>
+__device__ __forceinline__ int guide(Neutron<R>& n, const mcv_component& c) {
+  if (!guide_enter(n, c)) return 0;
+  for (int nb = 0; nb < MCV_MAX_BOUNCES; ++nb)
+    if (guide_bounce(n, c)) return 0;
+  return 1;
 }
 
 // Slit / Beamstop (acc/components/optics/slit.py:71-108,

@@ -1,345 +1,15 @@
-// engine.cu -- propagation kernels and the extern "C" entry points declared
-// in include/acc_gb300.h.
-//
-// One thread carries one neutron at a time through the whole chain; the
-// grid strides over neutron indices.  The chain description is a
-// __grid_constant__ kernel parameter, so component parameters are read from
-// the constant bank and every lane of a warp dispatches on the same opcode.
+// engine.cu -- the extern "C" entry points declared in include/acc_gb300.h
+// (host side; the kernels are instantiated in launch_fp32.cu and
+// launch_fp64.cu).
 
 #include <cstdio>
 #include <cstring>
 #include <new>
 
-#include "common.cuh"
-#include "components.cuh"
-#include "monitors.cuh"
-#include "sample.cuh"
+#include "kernels.cuh"
 
-namespace mcv {
-
-enum { kFlagIdentityRot = 1 };
-
-__device__ __forceinline__ uint64_t comp_nbins(const mcv_component& c) {
-  switch (c.opcode) {
-    case MCV_OP_PSD_MONITOR:
-    case MCV_OP_PSD_MONITOR_4PI:
-    case MCV_OP_POSDIV_MONITOR:
-    case MCV_OP_IQE_MONITOR:
-    case MCV_OP_THETA_TOF_4PI:
-    case MCV_OP_CYL_IQE_DETECTOR:
-      return (uint64_t)c.ip[0] * (uint64_t)c.ip[1];
-    case MCV_OP_WAVELENGTH_MONITOR:
-    case MCV_OP_ENERGY_MONITOR:
-      return (uint64_t)c.ip[0];
-    case MCV_OP_BANKED_DETECTOR:
-      return (uint64_t)c.ip[0] * c.ip[1] * c.ip[2] * c.ip[3];
-    default:
-      return 0;
-  }
-}
-
-// r' = rot (r - off), v' = rot v  (acc/vec3.py:148-159, acc/neutron.py:18-23)
-template <typename R>
-__device__ __forceinline__ void apply_transform(Neutron<R>& n,
-                                                const mcv_chain& ch, int k) {
-  const R* o = chain_off<R>(ch, k);
-  R tx = n.x - o[0], ty = n.y - o[1], tz = n.z - o[2];
-  if (ch.comp[k].flags & kFlagIdentityRot) {
-    n.x = tx;
-    n.y = ty;
-    n.z = tz;
-    return;
-  }
-  const R* m = chain_rot<R>(ch, k);
-  n.x = m[0] * tx + m[1] * ty + m[2] * tz;
-  n.y = m[3] * tx + m[4] * ty + m[5] * tz;
-  n.z = m[6] * tx + m[7] * ty + m[8] * tz;
-  R vx = m[0] * n.vx + m[1] * n.vy + m[2] * n.vz;
-  R vy = m[3] * n.vx + m[4] * n.vy + m[5] * n.vz;
-  R vz = m[6] * n.vx + m[7] * n.vy + m[8] * n.vz;
-  n.vx = vx;
-  n.vy = vy;
-  n.vz = vz;
-}
-
-// One component on one neutron; returns 1 when a guide ran out of bounces.
-template <typename R, typename Rng>
-__device__ __forceinline__ int run_component(Neutron<R>& n, Rng& rng,
-                                             const mcv_component& c) {
-  Tally tl{c.tally, comp_nbins(c)};
-  switch (c.opcode) {
-    case MCV_OP_SOURCE_SIMPLE:
-      source_simple<R>(n, rng, c);
-      return 0;
-    case MCV_OP_GUIDE:
-      return guide<R>(n, c);
-    case MCV_OP_HSS:
-      hss(n, rng, c);
-      return 0;
-    case MCV_OP_PSD_MONITOR:
-      psd_monitor<R>(n, c, tl);
-      return 0;
-    case MCV_OP_PSD_MONITOR_4PI:
-      psd_monitor_4pi<R>(n, c, tl);
-      return 0;
-    case MCV_OP_WAVELENGTH_MONITOR:
-      wavelength_monitor<R>(n, c, tl);
-      return 0;
-    case MCV_OP_POSDIV_MONITOR:
-      posdiv_monitor<R>(n, c, tl);
-      return 0;
-    case MCV_OP_IQE_MONITOR:
-      iqe_monitor<R>(n, c, tl);
-      return 0;
-    case MCV_OP_ENERGY_MONITOR:
-      energy_monitor<R>(n, c, tl);
-      return 0;
-    case MCV_OP_THETA_TOF_4PI:
-      theta_tof_4pi<R>(n, c, tl);
-      return 0;
-    case MCV_OP_CYL_IQE_DETECTOR:
-      cyl_iqe<R>(n, c, tl);
-      return 0;
-    case MCV_OP_BANKED_DETECTOR:
-      banked<R>(n, c, tl);
-      return 0;
-    case MCV_OP_SLIT:
-      slit_or_beamstop<R>(n, c, false);
-      return 0;
-    case MCV_OP_BEAMSTOP:
-      slit_or_beamstop<R>(n, c, true);
-      return 0;
-    default:  // MCV_OP_ARM
-      return 0;
-  }
-}
-
-struct Counters {
-  unsigned processed, overflow, nonfinite, overrun;
-};
-
-// Whole chain on one neutron (the body of the generated
-// process_kernel_no_buffer, acc/run_script.py:182-196).  A neutron leaves
-// the chain after a component that leaves its weight not positive.
-template <typename R, typename Rng>
-__device__ __forceinline__ int run_chain_one(Neutron<R>& n, Rng& rng,
-                                             const mcv_chain& ch,
-                                             Counters& k) {
-  int last = -1;
-  const int nc = ch.ncomp;
-  for (int c = 0; c < nc; ++c) {
-    if (c > 0) apply_transform<R>(n, ch, c);
-    last = c;
-    k.overflow += run_component<R>(n, rng, ch.comp[c]);
-    if (!(n.p > 0)) {
-      if (m_isnan(n.p)) k.nonfinite++;
-      break;
-    }
-  }
-  return last;
-}
-
-template <typename R>
-__device__ __forceinline__ void zero_neutron(Neutron<R>& n) {
-  n.x = n.y = n.z = n.vx = n.vy = n.vz = n.sx = n.sy = n.p = R(0);
-  n.t.set(R(0));
-}
-
-template <typename R>
-__device__ __forceinline__ void store_neutron(const Neutron<R>& n,
-                                              double* out) {
-  out[0] = n.x;
-  out[1] = n.y;
-  out[2] = n.z;
-  out[3] = n.vx;
-  out[4] = n.vy;
-  out[5] = n.vz;
-  out[6] = n.sx;
-  out[7] = n.sy;
-  out[8] = n.t.dval();
-  out[9] = n.p;
-}
-
-__device__ __forceinline__ void flush_counters(const Counters& k,
-                                               DevStatus* st) {
-  unsigned p = __reduce_add_sync(0xffffffffu, k.processed);
-  unsigned o = __reduce_add_sync(0xffffffffu, k.overflow);
-  unsigned f = __reduce_add_sync(0xffffffffu, k.nonfinite);
-  unsigned r = __reduce_add_sync(0xffffffffu, k.overrun);
-  if ((threadIdx.x & 31) == 0) {
-    if (p) atomicAdd(&st->processed, (unsigned long long)p);
-    if (o) atomicAdd(&st->bounce_overflow, (unsigned long long)o);
-    if (f) atomicAdd(&st->nonfinite, (unsigned long long)f);
-    if (r) atomicAdd(&st->rng_overrun, (unsigned long long)r);
-  }
-}
-
-constexpr int kMaxThreads = 256;
-
-// MODE 0: Philox; 1: Philox + record; 2: injected uniforms + record
-template <typename R, int MODE>
-__global__ void __launch_bounds__(kMaxThreads)
-    chain_kernel(const __grid_constant__ mcv_chain ch, uint64_t n,
-                 uint64_t first, uint64_t seed, const float* __restrict__ uni,
-                 int stride, double* __restrict__ out_n,
-                 int* __restrict__ out_last, DevStatus* st) {
-  Counters k{0, 0, 0, 0};
-  const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += step) {
-    Neutron<R> nt;
-    zero_neutron(nt);
-    int last;
-    if constexpr (MODE == 2) {
-      InjectedStream rng(uni + i * (uint64_t)stride, stride);
-      last = run_chain_one<R>(nt, rng, ch, k);
-      k.overrun += rng.overrun();
-    } else {
-      PhiloxStream rng(seed, first + i, 0u);
-      last = run_chain_one<R>(nt, rng, ch, k);
-    }
-    k.processed++;
-    if constexpr (MODE != 0) {
-      if (out_n) store_neutron(nt, out_n + i * 10);
-      if (out_last) out_last[i] = last;
-    }
-  }
-  flush_counters(k, st);
-}
-
-// Buffered mode (ComponentBase.process, ComponentBase.py:79-129): the chain
-// applied to a stored neutron array in place; component k draws from
-// Philox stream k+1.
-template <typename R>
-__global__ void __launch_bounds__(kMaxThreads)
-    buffer_kernel(const __grid_constant__ mcv_chain ch, R* __restrict__ buf,
-                  uint64_t n, uint64_t first, uint64_t seed, DevStatus* st) {
-  Counters k{0, 0, 0, 0};
-  const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += step) {
-    R* s = buf + i * 10;
-    Neutron<R> nt;
-    nt.x = s[0];
-    nt.y = s[1];
-    nt.z = s[2];
-    nt.vx = s[3];
-    nt.vy = s[4];
-    nt.vz = s[5];
-    nt.sx = s[6];
-    nt.sy = s[7];
-    nt.t.set(s[8]);
-    nt.p = s[9];
-    for (int c = 0; c < ch.ncomp; ++c) {
-      const mcv_component& cp = ch.comp[c];
-      if (cp.opcode != MCV_OP_SOURCE_SIMPLE && !(nt.p > 0)) break;
-      if (c > 0) apply_transform<R>(nt, ch, c);
-      PhiloxStream rng(seed, first + i, (uint32_t)(c + 1));
-      k.overflow += run_component<R>(nt, rng, cp);
-    }
-    k.processed++;
-    s[0] = nt.x;
-    s[1] = nt.y;
-    s[2] = nt.z;
-    s[3] = nt.vx;
-    s[4] = nt.vy;
-    s[5] = nt.vz;
-    s[6] = nt.sx;
-    s[7] = nt.sy;
-    s[8] = (R)nt.t.dval();
-    s[9] = nt.p;
-  }
-  flush_counters(k, st);
-}
-
-// Geometry probe: sorted hit times of rays with an HSS shape.
-template <typename R>
-__global__ void intersect_kernel(const __grid_constant__ mcv_component c,
-                                 const double* __restrict__ rays, uint64_t n,
-                                 double* __restrict__ out_ts,
-                                 int* __restrict__ out_n) {
-  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const double* r = rays + i * 6;
-  Hits<R> h = intersect_shape_from<R>(c, (R)r[0], (R)r[1], (R)r[2], (R)r[3],
-                                      (R)r[4], (R)r[5]);
-  double* o = out_ts + i * MCV_MAX_INTERSECTIONS;
-  for (int k = 0; k < MCV_MAX_INTERSECTIONS; ++k)
-    o[k] = k < h.n ? (double)h.get(k) : __longlong_as_double(0x7ff8000000000000ll);
-  out_n[i] = h.n;
-}
-
-// Batched persistent launch over many instrument variants.  Blocks take
-// work items of `chunk` neutrons from a device counter (DevStatus::
-// work_next); item k belongs to the variant whose cumulative item range
-// holds k.  The block stages that variant's chain in shared memory once per
-// change of variant.  Neutron i of variant v draws from Philox (seeds[v], i).
-template <typename R>
-__global__ void __launch_bounds__(kMaxThreads)
-    batched_kernel(const mcv_chain* __restrict__ variants, int nvar,
-                   const uint64_t* __restrict__ counts,
-                   const uint64_t* __restrict__ seeds, uint64_t chunk,
-                   DevStatus* st) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  mcv_chain& ch = *reinterpret_cast<mcv_chain*>(smem);
-  uint64_t* item_start = reinterpret_cast<uint64_t*>(
-      smem + (sizeof(mcv_chain) + 15) / 16 * 16);
-  __shared__ uint64_t s_item;
-  __shared__ int s_var;
-  if (threadIdx.x == 0) {
-    uint64_t acc = 0;
-    for (int v = 0; v < nvar; ++v) {
-      item_start[v] = acc;
-      acc += (counts[v] + chunk - 1) / chunk;
-    }
-    item_start[nvar] = acc;
-  }
-  __syncthreads();
-  const uint64_t total = item_start[nvar];
-  int cur = -1;
-  Counters k{0, 0, 0, 0};
-  for (;;) {
-    if (threadIdx.x == 0) {
-      uint64_t it = atomicAdd(&st->work_next, 1ull);
-      int lo = 0, hi = nvar;  // item_start[lo] <= it < item_start[hi]
-      while (hi - lo > 1) {
-        int mid = (lo + hi) >> 1;
-        if (item_start[mid] <= it) lo = mid;
-        else hi = mid;
-      }
-      s_item = it;
-      s_var = lo;
-    }
-    __syncthreads();
-    const uint64_t it = s_item;
-    const int v = s_var;
-    if (it >= total) break;
-    if (v != cur) {
-      const uint2* src = reinterpret_cast<const uint2*>(variants + v);
-      uint2* dst = reinterpret_cast<uint2*>(smem);
-      for (int i = threadIdx.x; i < (int)(sizeof(mcv_chain) / 8);
-           i += blockDim.x)
-        dst[i] = src[i];
-      cur = v;
-      __syncthreads();
-    }
-    const uint64_t a = (it - item_start[v]) * chunk;
-    const uint64_t cnt = counts[v];
-    const uint64_t b = a + chunk < cnt ? a + chunk : cnt;
-    const uint64_t seed = seeds[v];
-    for (uint64_t i = a + threadIdx.x; i < b; i += blockDim.x) {
-      Neutron<R> nt;
-      zero_neutron(nt);
-      PhiloxStream rng(seed, i, 0u);
-      run_chain_one<R>(nt, rng, ch, k);
-      k.processed++;
-    }
-    __syncthreads();
-  }
-  flush_counters(k, st);
-}
-
-}  // namespace mcv
+extern template struct mcv::Launchers<float>;
+extern template struct mcv::Launchers<double>;
 
 // =================================================================== host
 using namespace mcv;
@@ -490,16 +160,18 @@ int precision_ok(int precision, mcv_status* st) {
   return 1;
 }
 
-template <typename K>
-void launch_shape(const mcv_ctx* ctx, K kernel, uint64_t n,
-                  const mcv_launch* launch, int* blocks, int* threads) {
+int launch_threads(const mcv_launch* launch) {
   int t = (launch && launch->threads_per_block > 0) ? launch->threads_per_block
                                                     : kMaxThreads;
   if (t > kMaxThreads) t = kMaxThreads;
-  t = (t + 31) / 32 * 32;
-  int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, t, 0);
-  if (per_sm < 1) per_sm = 1;
+  return (t + 31) / 32 * 32;
+}
+
+template <typename Occ>
+void launch_shape(const mcv_ctx* ctx, Occ occupancy, uint64_t n,
+                  const mcv_launch* launch, int* blocks, int* threads) {
+  int t = launch_threads(launch);
+  int per_sm = occupancy(t);
   uint64_t want = (n + t - 1) / t;
   uint64_t full = (uint64_t)ctx->sm_count * per_sm;
   uint64_t b = (launch && launch->blocks > 0) ? (uint64_t)launch->blocks
@@ -510,17 +182,29 @@ void launch_shape(const mcv_ctx* ctx, K kernel, uint64_t n,
   *threads = t;
 }
 
-template <typename R, int MODE>
-int launch_chain(mcv_ctx* ctx, const mcv_chain* chain, uint64_t ncount,
-                 uint64_t first, uint64_t seed, const float* uni, int stride,
-                 double* out_n, int* out_last, const mcv_launch* launch,
-                 cudaStream_t s) {
+template <typename R>
+int launch_chain(mcv_ctx* ctx, int mode, const mcv_chain* chain,
+                 uint64_t ncount, uint64_t first, uint64_t seed,
+                 const float* uni, int stride, double* out_n, int* out_last,
+                 const mcv_launch* launch, cudaStream_t s) {
   int blocks, threads;
-  launch_shape(ctx, chain_kernel<R, MODE>, ncount, launch, &blocks, &threads);
-  chain_kernel<R, MODE><<<blocks, threads, 0, s>>>(
-      *chain, ncount, first, seed, uni, stride, out_n, out_last,
-      ctx->d_status);
+  launch_shape(
+      ctx, [mode](int t) { return Launchers<R>::occupancy_chain(mode, t); },
+      ncount, launch, &blocks, &threads);
+  Launchers<R>::chain(mode, blocks, threads, s, *chain, ncount, first, seed,
+                      uni, stride, out_n, out_last, ctx->d_status);
   return 0;
+}
+
+// The FP32 fused run uses path regeneration when asked to, or by default
+// when the chain has a guide (whose bounce count varies from neutron to
+// neutron); chains without one have near-uniform paths.
+bool use_regen(const mcv_chain* ch, const mcv_launch* launch) {
+  if (launch && launch->variant == 1) return false;
+  if (launch && launch->variant == 2) return true;
+  for (int k = 0; k < ch->ncomp; ++k)
+    if (ch->comp[k].opcode == MCV_OP_GUIDE) return true;
+  return false;
 }
 
 constexpr uint64_t kDefaultChunk = 8192;
@@ -563,6 +247,7 @@ int stage_batch(void* dst, const mcv_chain* variants, int nvar,
 template <typename R>
 void launch_batched_t(const mcv_ctx* ctx, const void* dbatch, int nvar,
                       const mcv_launch* launch, cudaStream_t s) {
+  // (the kernel itself is instantiated in launch_fp32.cu / launch_fp64.cu)
   const char* d = (const char*)dbatch;
   const mcv_chain* chains = (const mcv_chain*)d;
   const uint64_t* counts = (const uint64_t*)(d + nvar * sizeof(mcv_chain));
@@ -572,17 +257,14 @@ void launch_batched_t(const mcv_ctx* ctx, const void* dbatch, int nvar,
   if (t > kMaxThreads) t = kMaxThreads;
   t = (t + 31) / 32 * 32;
   size_t smem = (sizeof(mcv_chain) + 15) / 16 * 16 + 8 * (size_t)(nvar + 1);
-  int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batched_kernel<R>, t,
-                                                smem);
-  if (per_sm < 1) per_sm = 1;
+  int per_sm = Launchers<R>::occupancy_batched(t, smem);
   int blocks = (launch && launch->blocks > 0) ? launch->blocks
                                               : ctx->sm_count * per_sm;
   uint64_t chunk = (launch && launch->chunk > 0) ? (uint64_t)launch->chunk
                                                  : kDefaultChunk;
   cudaMemsetAsync(&ctx->d_status->work_next, 0, sizeof(unsigned long long), s);
-  batched_kernel<R><<<blocks, t, smem, s>>>(chains, nvar, counts, seeds, chunk,
-                                            ctx->d_status);
+  Launchers<R>::batched(blocks, t, smem, s, chains, nvar, counts, seeds,
+                        chunk, ctx->d_status);
 }
 
 void launch_batched(const mcv_ctx* ctx, const void* dbatch, int nvar,
@@ -706,12 +388,21 @@ int mcv_run_chain(mcv_ctx* ctx, const mcv_chain* chain, uint64_t ncount,
   if (ncount == 0) return st ? mcv_ctx_status(ctx, stream, 0, st) : MCV_OK;
   DeviceGuard g(ctx->device);
   cudaStream_t s = (cudaStream_t)stream;
-  if (precision == MCV_FP32)
-    launch_chain<float, 0>(ctx, chain, ncount, first, seed, nullptr, 0,
-                           nullptr, nullptr, launch, s);
-  else
-    launch_chain<double, 0>(ctx, chain, ncount, first, seed, nullptr, 0,
-                            nullptr, nullptr, launch, s);
+  if (precision == MCV_FP32) {
+    if (use_regen(chain, launch)) {
+      int blocks, threads;
+      launch_shape(ctx, Launchers<float>::occupancy_regen, ncount, launch,
+                   &blocks, &threads);
+      Launchers<float>::regen(blocks, threads, s, *chain, ncount, first, seed,
+                              ctx->d_status);
+    } else {
+      launch_chain<float>(ctx, 0, chain, ncount, first, seed, nullptr, 0,
+                          nullptr, nullptr, launch, s);
+    }
+  } else {
+    launch_chain<double>(ctx, 0, chain, ncount, first, seed, nullptr, 0,
+                         nullptr, nullptr, launch, s);
+  }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(st, e, "mcv_run_chain launch");
   if (st) return mcv_ctx_status(ctx, stream, ncount, st);
@@ -738,21 +429,13 @@ int mcv_replay_uniforms(mcv_ctx* ctx, const mcv_chain* chain, uint64_t ncount,
   if (ncount == 0) return st ? mcv_ctx_status(ctx, stream, 0, st) : MCV_OK;
   DeviceGuard g(ctx->device);
   cudaStream_t s = (cudaStream_t)stream;
-  if (precision == MCV_FP32) {
-    if (uniforms)
-      launch_chain<float, 2>(ctx, chain, ncount, first, seed, uniforms, stride,
-                             out_neutrons, out_last, launch, s);
-    else
-      launch_chain<float, 1>(ctx, chain, ncount, first, seed, nullptr, 0,
-                             out_neutrons, out_last, launch, s);
-  } else {
-    if (uniforms)
-      launch_chain<double, 2>(ctx, chain, ncount, first, seed, uniforms,
-                              stride, out_neutrons, out_last, launch, s);
-    else
-      launch_chain<double, 1>(ctx, chain, ncount, first, seed, nullptr, 0,
-                              out_neutrons, out_last, launch, s);
-  }
+  int mode = uniforms ? 2 : 1;
+  if (precision == MCV_FP32)
+    launch_chain<float>(ctx, mode, chain, ncount, first, seed, uniforms,
+                        stride, out_neutrons, out_last, launch, s);
+  else
+    launch_chain<double>(ctx, mode, chain, ncount, first, seed, uniforms,
+                         stride, out_neutrons, out_last, launch, s);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(st, e, "mcv_replay_uniforms launch");
   if (st) return mcv_ctx_status(ctx, stream, ncount, st);
@@ -779,13 +462,15 @@ int mcv_process_buffer(mcv_ctx* ctx, const mcv_chain* chain, void* neutrons,
   cudaStream_t s = (cudaStream_t)stream;
   int blocks, threads;
   if (precision == MCV_FP32) {
-    launch_shape(ctx, buffer_kernel<float>, n, launch, &blocks, &threads);
-    buffer_kernel<float><<<blocks, threads, 0, s>>>(
-        *chain, (float*)neutrons, n, first, seed, ctx->d_status);
+    launch_shape(ctx, Launchers<float>::occupancy_buffer, n, launch, &blocks,
+                 &threads);
+    Launchers<float>::buffer(blocks, threads, s, *chain, neutrons, n, first,
+                             seed, ctx->d_status);
   } else {
-    launch_shape(ctx, buffer_kernel<double>, n, launch, &blocks, &threads);
-    buffer_kernel<double><<<blocks, threads, 0, s>>>(
-        *chain, (double*)neutrons, n, first, seed, ctx->d_status);
+    launch_shape(ctx, Launchers<double>::occupancy_buffer, n, launch, &blocks,
+                 &threads);
+    Launchers<double>::buffer(blocks, threads, s, *chain, neutrons, n, first,
+                              seed, ctx->d_status);
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(st, e, "mcv_process_buffer launch");
@@ -909,11 +594,10 @@ int mcv_intersect(mcv_ctx* ctx, const mcv_component* hss, const double* rays,
   cudaStream_t s = (cudaStream_t)stream;
   unsigned blocks = (unsigned)((n + 127) / 128);
   if (precision == MCV_FP32)
-    intersect_kernel<float><<<blocks, 128, 0, s>>>(*hss, rays, n, out_ts,
-                                                   out_n);
+    Launchers<float>::intersect(blocks, 128, s, *hss, rays, n, out_ts, out_n);
   else
-    intersect_kernel<double><<<blocks, 128, 0, s>>>(*hss, rays, n, out_ts,
-                                                    out_n);
+    Launchers<double>::intersect(blocks, 128, s, *hss, rays, n, out_ts,
+                                 out_n);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(st, e, "mcv_intersect launch");
   if (st) {

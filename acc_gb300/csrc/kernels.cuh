@@ -1,0 +1,536 @@
+// kernels.cuh -- the propagation kernels and their per-precision launchers.
+//
+// One thread carries one neutron at a time through the whole chain; the
+// grid strides over neutron indices.  The chain description is a
+// __grid_constant__ kernel parameter, so component parameters are read from
+// the constant bank and every lane of a warp dispatches on the same opcode.
+//
+// Launchers<R> is instantiated once per precision in its own translation
+// unit (launch_fp32.cu, launch_fp64.cu) so that each can be compiled with
+// its own floating-point contraction setting.
+#pragma once
+
+#include "common.cuh"
+#include "components.cuh"
+#include "monitors.cuh"
+#include "sample.cuh"
+
+namespace mcv {
+
+enum { kFlagIdentityRot = 1 };
+
+__device__ __forceinline__ uint64_t comp_nbins(const mcv_component& c) {
+  switch (c.opcode) {
+    case MCV_OP_PSD_MONITOR:
+    case MCV_OP_PSD_MONITOR_4PI:
+    case MCV_OP_POSDIV_MONITOR:
+    case MCV_OP_IQE_MONITOR:
+    case MCV_OP_THETA_TOF_4PI:
+    case MCV_OP_CYL_IQE_DETECTOR:
+      return (uint64_t)c.ip[0] * (uint64_t)c.ip[1];
+    case MCV_OP_WAVELENGTH_MONITOR:
+    case MCV_OP_ENERGY_MONITOR:
+      return (uint64_t)c.ip[0];
+    case MCV_OP_BANKED_DETECTOR:
+      return (uint64_t)c.ip[0] * c.ip[1] * c.ip[2] * c.ip[3];
+    default:
+      return 0;
+  }
+}
+
+// r' = rot (r - off), v' = rot v  (acc/vec3.py:148-159, acc/neutron.py:18-23)
+template <typename R>
+__device__ __forceinline__ void apply_transform(Neutron<R>& n,
+                                                const mcv_chain& ch, int k) {
+  const R* o = chain_off<R>(ch, k);
+  R tx = n.x - o[0], ty = n.y - o[1], tz = n.z - o[2];
+  if (ch.comp[k].flags & kFlagIdentityRot) {
+    n.x = tx;
+    n.y = ty;
+    n.z = tz;
+    return;
+  }
+  const R* m = chain_rot<R>(ch, k);
+  n.x = m[0] * tx + m[1] * ty + m[2] * tz;
+  n.y = m[3] * tx + m[4] * ty + m[5] * tz;
+  n.z = m[6] * tx + m[7] * ty + m[8] * tz;
+  R vx = m[0] * n.vx + m[1] * n.vy + m[2] * n.vz;
+  R vy = m[3] * n.vx + m[4] * n.vy + m[5] * n.vz;
+  R vz = m[6] * n.vx + m[7] * n.vy + m[8] * n.vz;
+  n.vx = vx;
+  n.vy = vy;
+  n.vz = vz;
+}
+
+// One component on one neutron; returns 1 when a guide ran out of bounces.
+template <typename R, typename Rng>
+__device__ __forceinline__ int run_component(Neutron<R>& n, Rng& rng,
+                                             const mcv_component& c) {
+  Tally tl{c.tally, comp_nbins(c)};
+  switch (c.opcode) {
+    case MCV_OP_SOURCE_SIMPLE:
+      source_simple<R>(n, rng, c);
+      return 0;
+    case MCV_OP_GUIDE:
+      return guide<R>(n, c);
+    case MCV_OP_HSS:
+      hss(n, rng, c);
+      return 0;
+    case MCV_OP_PSD_MONITOR:
+      psd_monitor<R>(n, c, tl);
+      return 0;
+    case MCV_OP_PSD_MONITOR_4PI:
+      psd_monitor_4pi<R>(n, c, tl);
+      return 0;
+    case MCV_OP_WAVELENGTH_MONITOR:
+      wavelength_monitor<R>(n, c, tl);
+      return 0;
+    case MCV_OP_POSDIV_MONITOR:
+      posdiv_monitor<R>(n, c, tl);
+      return 0;
+    case MCV_OP_IQE_MONITOR:
+      iqe_monitor<R>(n, c, tl);
+      return 0;
+    case MCV_OP_ENERGY_MONITOR:
+      energy_monitor<R>(n, c, tl);
+      return 0;
+    case MCV_OP_THETA_TOF_4PI:
+      theta_tof_4pi<R>(n, c, tl);
+      return 0;
+    case MCV_OP_CYL_IQE_DETECTOR:
+      cyl_iqe<R>(n, c, tl);
+      return 0;
+    case MCV_OP_BANKED_DETECTOR:
+      banked<R>(n, c, tl);
+      return 0;
+    case MCV_OP_SLIT:
+      slit_or_beamstop<R>(n, c, false);
+      return 0;
+    case MCV_OP_BEAMSTOP:
+      slit_or_beamstop<R>(n, c, true);
+      return 0;
+    default:  // MCV_OP_ARM
+      return 0;
+  }
+}
+
+struct Counters {
+  unsigned processed, overflow, nonfinite, overrun;
+};
+
+// Whole chain on one neutron (the body of the generated
+// process_kernel_no_buffer, acc/run_script.py:182-196).  A neutron leaves
+// the chain after a component that leaves its weight not positive.
+template <typename R, typename Rng>
+__device__ __forceinline__ int run_chain_one(Neutron<R>& n, Rng& rng,
+                                             const mcv_chain& ch,
+                                             Counters& k) {
+  int last = -1;
+  const int nc = ch.ncomp;
+  for (int c = 0; c < nc; ++c) {
+    if (c > 0) apply_transform<R>(n, ch, c);
+    last = c;
+    k.overflow += run_component<R>(n, rng, ch.comp[c]);
+    if (!(n.p > 0)) {
+      if (m_isnan(n.p)) k.nonfinite++;
+      break;
+    }
+  }
+  return last;
+}
+
+template <typename R>
+__device__ __forceinline__ void zero_neutron(Neutron<R>& n) {
+  n.x = n.y = n.z = n.vx = n.vy = n.vz = n.sx = n.sy = n.p = R(0);
+  n.t.set(R(0));
+}
+
+template <typename R>
+__device__ __forceinline__ void store_neutron(const Neutron<R>& n,
+                                              double* out) {
+  out[0] = n.x;
+  out[1] = n.y;
+  out[2] = n.z;
+  out[3] = n.vx;
+  out[4] = n.vy;
+  out[5] = n.vz;
+  out[6] = n.sx;
+  out[7] = n.sy;
+  out[8] = n.t.dval();
+  out[9] = n.p;
+}
+
+__device__ __forceinline__ void flush_counters(const Counters& k,
+                                               DevStatus* st) {
+  unsigned p = __reduce_add_sync(0xffffffffu, k.processed);
+  unsigned o = __reduce_add_sync(0xffffffffu, k.overflow);
+  unsigned f = __reduce_add_sync(0xffffffffu, k.nonfinite);
+  unsigned r = __reduce_add_sync(0xffffffffu, k.overrun);
+  if ((threadIdx.x & 31) == 0) {
+    if (p) atomicAdd(&st->processed, (unsigned long long)p);
+    if (o) atomicAdd(&st->bounce_overflow, (unsigned long long)o);
+    if (f) atomicAdd(&st->nonfinite, (unsigned long long)f);
+    if (r) atomicAdd(&st->rng_overrun, (unsigned long long)r);
+  }
+}
+
+constexpr int kMaxThreads = 256;
+
+// MODE 0: Philox; 1: Philox + record; 2: injected uniforms + record
+template <typename R, int MODE>
+__global__ void __launch_bounds__(kMaxThreads)
+    chain_kernel(const __grid_constant__ mcv_chain ch, uint64_t n,
+                 uint64_t first, uint64_t seed, const float* __restrict__ uni,
+                 int stride, double* __restrict__ out_n,
+                 int* __restrict__ out_last, DevStatus* st) {
+  Counters k{0, 0, 0, 0};
+  const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += step) {
+    Neutron<R> nt;
+    zero_neutron(nt);
+    int last;
+    if constexpr (MODE == 2) {
+      InjectedStream rng(uni + i * (uint64_t)stride, stride);
+      last = run_chain_one<R>(nt, rng, ch, k);
+      k.overrun += rng.overrun();
+    } else {
+      PhiloxStream rng(seed, first + i, 0u);
+      last = run_chain_one<R>(nt, rng, ch, k);
+    }
+    k.processed++;
+    if constexpr (MODE != 0) {
+      if (out_n) store_neutron(nt, out_n + i * 10);
+      if (out_last) out_last[i] = last;
+    }
+  }
+  flush_counters(k, st);
+}
+
+// Path regeneration: the same per-neutron sequence as chain_kernel, but a
+// lane whose neutron leaves the chain immediately takes the next neutron of
+// its warp's index range, and a guide advances one bounce per loop pass.
+// Lanes of a warp therefore stay busy while a few neutrons bounce many
+// times, instead of idling until the warp's longest path ends.  Every
+// neutron is computed with the same functions in the same order as in
+// chain_kernel, so results are identical neutron by neutron.
+template <typename R>
+__global__ void __launch_bounds__(kMaxThreads)
+    regen_kernel(const __grid_constant__ mcv_chain ch, uint64_t n,
+                 uint64_t first, uint64_t seed, DevStatus* st) {
+  constexpr unsigned kFull = 0xffffffffu;
+  const unsigned lane = threadIdx.x & 31u;
+  const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  const uint64_t per = (n + nwarps - 1) / nwarps;
+  uint64_t next = warp * per;
+  const uint64_t end = next + per < n ? next + per : n;
+  Counters k{0, 0, 0, 0};
+  Neutron<R> nt;
+  zero_neutron(nt);
+  PhiloxStream rng(seed, 0, 0u);
+  int c = -1;      // component of the lane's neutron; -1 idle, -2 finished
+  int inside = 0;  // guide: entered and bouncing
+  int nb = 0;      // guide: bounces so far
+  const int nc = ch.ncomp;
+  for (;;) {
+    const unsigned idle = __ballot_sync(kFull, c == -1);
+    if (idle) {
+      const uint64_t idx = next + __popc(idle & ((1u << lane) - 1u));
+      next += __popc(idle);
+      if (c == -1) {
+        if (idx < end) {
+          zero_neutron(nt);
+          rng = PhiloxStream(seed, first + idx, 0u);
+          c = 0;
+          inside = 0;
+        } else {
+          c = -2;
+        }
+      }
+    }
+    if (__all_sync(kFull, c == -2)) break;
+    if (c < 0) continue;
+    const mcv_component& cp = ch.comp[c];
+    bool finished = true;  // the lane's neutron is done with component c
+    if (cp.opcode == MCV_OP_GUIDE) {
+      if (!inside) {
+        if (guide_enter<R>(nt, cp)) {
+          inside = 1;
+          nb = 0;
+          finished = guide_bounce<R>(nt, cp);
+          ++nb;
+        }
+      } else {
+        finished = guide_bounce<R>(nt, cp);
+        ++nb;
+      }
+      if (!finished && nb >= MCV_MAX_BOUNCES) {
+        finished = true;
+        k.overflow++;
+      }
+    } else {
+      k.overflow += run_component<R>(nt, rng, cp);
+    }
+    if (finished) {
+      inside = 0;
+      if (!(nt.p > 0)) {
+        if (m_isnan(nt.p)) k.nonfinite++;
+        c = -1;
+        k.processed++;
+      } else if (c + 1 < nc) {
+        ++c;
+        apply_transform<R>(nt, ch, c);
+      } else {
+        c = -1;
+        k.processed++;
+      }
+    }
+  }
+  flush_counters(k, st);
+}
+
+// Buffered mode (ComponentBase.process, ComponentBase.py:79-129): the chain
+// applied to a stored neutron array in place; component k draws from
+// Philox stream k+1.
+template <typename R>
+__global__ void __launch_bounds__(kMaxThreads)
+    buffer_kernel(const __grid_constant__ mcv_chain ch, R* __restrict__ buf,
+                  uint64_t n, uint64_t first, uint64_t seed, DevStatus* st) {
+  Counters k{0, 0, 0, 0};
+  const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += step) {
+    R* s = buf + i * 10;
+    Neutron<R> nt;
+    nt.x = s[0];
+    nt.y = s[1];
+    nt.z = s[2];
+    nt.vx = s[3];
+    nt.vy = s[4];
+    nt.vz = s[5];
+    nt.sx = s[6];
+    nt.sy = s[7];
+    nt.t.set(s[8]);
+    nt.p = s[9];
+    for (int c = 0; c < ch.ncomp; ++c) {
+      const mcv_component& cp = ch.comp[c];
+      if (cp.opcode != MCV_OP_SOURCE_SIMPLE && !(nt.p > 0)) break;
+      if (c > 0) apply_transform<R>(nt, ch, c);
+      PhiloxStream rng(seed, first + i, (uint32_t)(c + 1));
+      k.overflow += run_component<R>(nt, rng, cp);
+    }
+    k.processed++;
+    s[0] = nt.x;
+    s[1] = nt.y;
+    s[2] = nt.z;
+    s[3] = nt.vx;
+    s[4] = nt.vy;
+    s[5] = nt.vz;
+    s[6] = nt.sx;
+    s[7] = nt.sy;
+    s[8] = (R)nt.t.dval();
+    s[9] = nt.p;
+  }
+  flush_counters(k, st);
+}
+
+// Geometry probe: sorted hit times of rays with an HSS shape.
+template <typename R>
+__global__ void intersect_kernel(const __grid_constant__ mcv_component c,
+                                 const double* __restrict__ rays, uint64_t n,
+                                 double* __restrict__ out_ts,
+                                 int* __restrict__ out_n) {
+  uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double* r = rays + i * 6;
+  Hits<R> h = intersect_shape_from<R>(c, (R)r[0], (R)r[1], (R)r[2], (R)r[3],
+                                      (R)r[4], (R)r[5]);
+  double* o = out_ts + i * MCV_MAX_INTERSECTIONS;
+  for (int k = 0; k < MCV_MAX_INTERSECTIONS; ++k)
+    o[k] = k < h.n ? (double)h.get(k) : __longlong_as_double(0x7ff8000000000000ll);
+  out_n[i] = h.n;
+}
+
+// Batched persistent launch over many instrument variants.  Blocks take
+// work items of `chunk` neutrons from a device counter (DevStatus::
+// work_next); item k belongs to the variant whose cumulative item range
+// holds k.  The block stages that variant's chain in shared memory once per
+// change of variant.  Neutron i of variant v draws from Philox (seeds[v], i).
+template <typename R>
+__global__ void __launch_bounds__(kMaxThreads)
+    batched_kernel(const mcv_chain* __restrict__ variants, int nvar,
+                   const uint64_t* __restrict__ counts,
+                   const uint64_t* __restrict__ seeds, uint64_t chunk,
+                   DevStatus* st) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  mcv_chain& ch = *reinterpret_cast<mcv_chain*>(smem);
+  uint64_t* item_start = reinterpret_cast<uint64_t*>(
+      smem + (sizeof(mcv_chain) + 15) / 16 * 16);
+  __shared__ uint64_t s_item;
+  __shared__ int s_var;
+  if (threadIdx.x == 0) {
+    uint64_t acc = 0;
+    for (int v = 0; v < nvar; ++v) {
+      item_start[v] = acc;
+      acc += (counts[v] + chunk - 1) / chunk;
+    }
+    item_start[nvar] = acc;
+  }
+  __syncthreads();
+  const uint64_t total = item_start[nvar];
+  int cur = -1;
+  Counters k{0, 0, 0, 0};
+  for (;;) {
+    if (threadIdx.x == 0) {
+      uint64_t it = atomicAdd(&st->work_next, 1ull);
+      int lo = 0, hi = nvar;  // item_start[lo] <= it < item_start[hi]
+      while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (item_start[mid] <= it) lo = mid;
+        else hi = mid;
+      }
+      s_item = it;
+      s_var = lo;
+    }
+    __syncthreads();
+    const uint64_t it = s_item;
+    const int v = s_var;
+    if (it >= total) break;
+    if (v != cur) {
+      const uint2* src = reinterpret_cast<const uint2*>(variants + v);
+      uint2* dst = reinterpret_cast<uint2*>(smem);
+      for (int i = threadIdx.x; i < (int)(sizeof(mcv_chain) / 8);
+           i += blockDim.x)
+        dst[i] = src[i];
+      cur = v;
+      __syncthreads();
+    }
+    const uint64_t a = (it - item_start[v]) * chunk;
+    const uint64_t cnt = counts[v];
+    const uint64_t b = a + chunk < cnt ? a + chunk : cnt;
+    const uint64_t seed = seeds[v];
+    for (uint64_t i = a + threadIdx.x; i < b; i += blockDim.x) {
+      Neutron<R> nt;
+      zero_neutron(nt);
+      PhiloxStream rng(seed, i, 0u);
+      run_chain_one<R>(nt, rng, ch, k);
+      k.processed++;
+    }
+    __syncthreads();
+  }
+  flush_counters(k, st);
+}
+
+}  // namespace mcv
+
+
+namespace mcv {
+
+// Host-side launchers of the kernels above for one working precision.
+template <typename R>
+struct Launchers {
+  static int occupancy_chain(int mode, int threads);
+  static void chain(int mode, int blocks, int threads, cudaStream_t s,
+                    const mcv_chain& ch, uint64_t n, uint64_t first,
+                    uint64_t seed, const float* uni, int stride,
+                    double* out_n, int* out_last, DevStatus* st);
+  static int occupancy_regen(int threads);
+  static void regen(int blocks, int threads, cudaStream_t s,
+                    const mcv_chain& ch, uint64_t n, uint64_t first,
+                    uint64_t seed, DevStatus* st);
+  static int occupancy_buffer(int threads);
+  static void buffer(int blocks, int threads, cudaStream_t s,
+                     const mcv_chain& ch, void* buf, uint64_t n,
+                     uint64_t first, uint64_t seed, DevStatus* st);
+  static int occupancy_batched(int threads, size_t smem);
+  static void batched(int blocks, int threads, size_t smem, cudaStream_t s,
+                      const mcv_chain* variants, int nvar,
+                      const uint64_t* counts, const uint64_t* seeds,
+                      uint64_t chunk, DevStatus* st);
+  static void intersect(int blocks, int threads, cudaStream_t s,
+                        const mcv_component& c, const double* rays,
+                        uint64_t n, double* out_ts, int* out_n);
+};
+
+template <typename K>
+inline int occupancy_of(K kernel, int threads, size_t smem) {
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads,
+                                                smem);
+  return per_sm < 1 ? 1 : per_sm;
+}
+
+#ifdef MCV_DEFINE_LAUNCHERS
+template <typename R>
+int Launchers<R>::occupancy_chain(int mode, int threads) {
+  if (mode == 0) return occupancy_of(chain_kernel<R, 0>, threads, 0);
+  if (mode == 1) return occupancy_of(chain_kernel<R, 1>, threads, 0);
+  return occupancy_of(chain_kernel<R, 2>, threads, 0);
+}
+
+template <typename R>
+void Launchers<R>::chain(int mode, int blocks, int threads, cudaStream_t s,
+                         const mcv_chain& ch, uint64_t n, uint64_t first,
+                         uint64_t seed, const float* uni, int stride,
+                         double* out_n, int* out_last, DevStatus* st) {
+  if (mode == 0)
+    chain_kernel<R, 0><<<blocks, threads, 0, s>>>(ch, n, first, seed, uni,
+                                                  stride, out_n, out_last, st);
+  else if (mode == 1)
+    chain_kernel<R, 1><<<blocks, threads, 0, s>>>(ch, n, first, seed, uni,
+                                                  stride, out_n, out_last, st);
+  else
+    chain_kernel<R, 2><<<blocks, threads, 0, s>>>(ch, n, first, seed, uni,
+                                                  stride, out_n, out_last, st);
+}
+
+template <typename R>
+int Launchers<R>::occupancy_regen(int threads) {
+  return occupancy_of(regen_kernel<R>, threads, 0);
+}
+
+template <typename R>
+void Launchers<R>::regen(int blocks, int threads, cudaStream_t s,
+                         const mcv_chain& ch, uint64_t n, uint64_t first,
+                         uint64_t seed, DevStatus* st) {
+  regen_kernel<R><<<blocks, threads, 0, s>>>(ch, n, first, seed, st);
+}
+
+template <typename R>
+int Launchers<R>::occupancy_buffer(int threads) {
+  return occupancy_of(buffer_kernel<R>, threads, 0);
+}
+
+template <typename R>
+void Launchers<R>::buffer(int blocks, int threads, cudaStream_t s,
+                          const mcv_chain& ch, void* buf, uint64_t n,
+                          uint64_t first, uint64_t seed, DevStatus* st) {
+  buffer_kernel<R><<<blocks, threads, 0, s>>>(ch, (R*)buf, n, first, seed,
+                                              st);
+}
+
+template <typename R>
+int Launchers<R>::occupancy_batched(int threads, size_t smem) {
+  return occupancy_of(batched_kernel<R>, threads, smem);
+}
+
+template <typename R>
+void Launchers<R>::batched(int blocks, int threads, size_t smem,
+                           cudaStream_t s, const mcv_chain* variants,
+                           int nvar, const uint64_t* counts,
+                           const uint64_t* seeds, uint64_t chunk,
+                           DevStatus* st) {
+  batched_kernel<R><<<blocks, threads, smem, s>>>(variants, nvar, counts,
+                                                  seeds, chunk, st);
+}
+
+template <typename R>
+void Launchers<R>::intersect(int blocks, int threads, cudaStream_t s,
+                             const mcv_component& c, const double* rays,
+                             uint64_t n, double* out_ts, int* out_n) {
+  intersect_kernel<R><<<blocks, threads, 0, s>>>(c, rays, n, out_ts, out_n);
+}
+#endif  // MCV_DEFINE_LAUNCHERS
+
+}  // namespace mcv

@@ -586,7 +586,8 @@ __device__ __forceinline__ R sqe_lookup(const mcv_component& c, R Q, R E) {
 }
 
 // Gridded S(Q,E) kernel: the kinematics of E_Q._S (acc/kernels/E_Q.py:37-99)
-// with (Q, E) uniform over the table box and S from the grid.
+// with (Q, E) uniform over the table box and S from the grid; sin(theta)
+// from the factored (Q^2 - (ki-kf)^2)((ki+kf)^2 - Q^2) / (2 ki kf)^2.
 template <typename R, typename Rng>
 __device__ __forceinline__ void sqe_scatter(Neutron<R>& n, Rng& rng,
                                             const mcv_component& c) {
@@ -605,13 +606,15 @@ __device__ __forceinline__ void sqe_scatter(Neutron<R>& n, Rng& rng,
   }
   R vf = m_sqrt(Ef) * R(kSE2V);
   R ki = R(kV2K) * vi, kf = R(kV2K) * vf;
-  R cost = (ki * ki + kf * kf - Q * Q) / (2 * ki * kf);
-  R cost2 = cost * cost;
-  if (cost2 > 1) {
+  // 1 - cos^2 in factored form, well conditioned near 0 and 180 degrees
+  R Q2 = Q * Q, dk = ki - kf, sk = ki + kf;
+  R sint2 = (Q2 - dk * dk) * (sk * sk - Q2) / (4 * ki * ki * kf * kf);
+  if (sint2 < 0) {
     n.p = R(-1);
     return;
   }
-  R sint = m_sqrt(R(1.0) - cost2);
+  R cost = (ki * ki + kf * kf - Q2) / (2 * ki * kf);
+  R sint = m_sqrt(sint2);
   R sp, cp;
   m_sincos_2pi(u3, &sp, &cp);
   R v2 = vf * sint * cp, v3 = vf * sint * sp, v1 = vf * cost;

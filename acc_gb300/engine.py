@@ -55,12 +55,16 @@ def chain_for_instrument(instrument, binder=None):
     return build_chain(instrument.components, offsets, rotmats, binder)
 
 
-def _launch(threads_per_block=None, blocks=None):
-    if not threads_per_block and not blocks:
+VARIANTS = {None: 0, "auto": 0, "thread": 1, "regen": 2}
+
+
+def _launch(threads_per_block=None, blocks=None, variant=None):
+    if not threads_per_block and not blocks and not VARIANTS[variant]:
         return None
     L = nat.mcv_launch()
     L.threads_per_block = int(threads_per_block or 0)
     L.blocks = int(blocks or 0)
+    L.variant = VARIANTS[variant]
     return L
 
 
@@ -69,12 +73,14 @@ def _precision(floattype):
 
 
 def run_chain(chain, ncount, seed=None, floattype=None, first=0,
-              threads_per_block=None, blocks=None, sync=True, device=None):
-    """mcv_run_chain: ncount neutrons through the fused chain kernel.
-    Returns the mcv_status (sync=True) or None."""
+              threads_per_block=None, blocks=None, sync=True, device=None,
+              variant=None):
+    """mcv_run_chain: ncount neutrons through the fused chain kernel
+    (variant None/"auto", "thread" or "regen" for FP32).  Returns the
+    mcv_status (sync=True) or None."""
     ctx = nat.context(device)
     st = nat.mcv_status() if sync else None
-    L = _launch(threads_per_block, blocks)
+    L = _launch(threads_per_block, blocks, variant)
     seed = config.rng_seed if seed is None else seed
     rc = nat.lib().mcv_run_chain(
         ctx.handle, ctypes.byref(chain), int(ncount), int(first), int(seed),

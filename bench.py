@@ -150,7 +150,7 @@ class ClockSampler:
 
 # --------------------------------------------------------- GPU timing
 def time_chain(chain, ncount, steps, warmup, floattype, seed, first0, world,
-               rank, flush):
+               rank, flush, variant=None):
     """Warm up, then time exactly `steps` launches with CUDA events on the
     launching stream (L2 flushed between launches, outside the events).
     Returns per-step milliseconds."""
@@ -161,7 +161,7 @@ def time_chain(chain, ncount, steps, warmup, floattype, seed, first0, world,
     for w in range(warmup):
         engine.run_chain(chain, ncount, seed=seed, floattype=floattype,
                          first=first0 + (w * world + rank) * ncount,
-                         sync=False)
+                         sync=False, variant=variant)
     engine.read_status(expected=warmup * ncount if warmup else 0)
     evs = [(torch.cuda.Event(enable_timing=True),
             torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
@@ -173,7 +173,8 @@ def time_chain(chain, ncount, steps, warmup, floattype, seed, first0, world,
         flush.zero_()
         evs[k][0].record(stream)
         engine.run_chain(chain, ncount, seed=seed, floattype=floattype,
-                         first=base + (k * world + rank) * ncount, sync=False)
+                         first=base + (k * world + rank) * ncount, sync=False,
+                         variant=variant)
         evs[k][1].record(stream)
     torch.cuda.synchronize()
     if world > 1:
@@ -371,6 +372,12 @@ def ours_arm(a, rank, world, local_rank):
                       a.seed + 1, 0, world, rank, flush)
     clk = clocks.stop()
     t64 = max_over_ranks(sum(ms64) / 1e3, world)
+    # the FP32 kernel without path regeneration, for comparison
+    ins_t = build_instrument(a.workload)
+    ms_t = time_chain(engine.chain_for_instrument(ins_t), ncount, a.steps,
+                      a.warmup, "float32", a.seed, 0, world, rank, flush,
+                      variant="thread")
+    t_thread = max_over_ranks(sum(ms_t) / 1e3, world)
 
     # all ranks' tallies summed (the one collective of the sharded path)
     tallies = []
@@ -419,7 +426,7 @@ def ours_arm(a, rank, world, local_rank):
         "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
         "frac": achieved / fp32_peak if achieved else None,
         "traffic": dbn * ncount if dbn is not None else None,
-        "kernel": "mcv::chain_kernel<float,0>",
+        "kernel": "mcv::regen_kernel<float>",
         "peak_source": "FP32 FMA peak measured in this run "
                        "(mcv_probe_fma_peak); the measured peak file has "
                        "HBM and bf16-tensor peaks only",
@@ -452,6 +459,10 @@ def ours_arm(a, rank, world, local_rank):
         "fp64_plain": {"value": v64, "unit": UNIT,
                        "ms_per_step": 1e3 * t64 / a.steps, "dtype": "f64"},
         "fp32_over_fp64": value / v64,
+        "fp32_one_neutron_per_thread": {
+            "value": world * ncount * a.steps / t_thread, "unit": UNIT,
+            "ms_per_step": 1e3 * t_thread / a.steps,
+            "note": "same FP32 kernel body without path regeneration"},
         "chi2_fp32_vs_fp64": chi2,
         "bwd_over_fwd": None,
         "batched": batched,

@@ -159,12 +159,16 @@ typedef struct mcv_chain {
   float foff[MCV_MAX_COMPONENTS][3];
 } mcv_chain;
 
-/* Launch shape; zeros mean "engine default" (the autotuned value if any). */
+/* Launch shape; zeros mean "engine default". */
 typedef struct mcv_launch {
   int32_t threads_per_block;
   int32_t blocks;
   int32_t chunk;            /* neutrons per work item (batched launch) */
-  int32_t reserved;
+  int32_t variant;          /* fused FP32 kernel: 0 engine's choice,
+                               1 one neutron per thread to the end of the
+                               chain, 2 path regeneration (a lane whose
+                               neutron leaves the chain starts the next one;
+                               guides advance one bounce per step) */
 } mcv_launch;
 
 typedef struct mcv_status {
@@ -201,9 +205,10 @@ int mcv_ctx_status(mcv_ctx* ctx, void* stream, uint64_t expected,
  * acc/components/sources/SourceBase.py:36-52).  Runs neutrons with indices
  * [first, first+ncount) of the stream keyed by `seed` through the whole chain
  * in one kernel and adds into the component tallies.  Neutron i draws its
- * uniforms from Philox4x32-10 with counter (i, draw block), so the result
- * does not depend on the launch shape, and disjoint index ranges on several
- * devices sum to the single-device run.
+ * uniforms from Philox4x32-10 with counter (i, draw block), five 24-bit
+ * uniforms per 128-bit block, so the result does not depend on the launch
+ * shape, and disjoint index ranges on several devices sum to the
+ * single-device run.
  */
 int mcv_run_chain(mcv_ctx* ctx, const mcv_chain* chain, uint64_t ncount,
                   uint64_t first, uint64_t seed, int precision,

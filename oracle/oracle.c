@@ -17,8 +17,9 @@
  * Uniform random numbers come from Philox4x32-10 (Salmon, Moraes, Dror,
  * Shaw, "Parallel random numbers: as easy as 1, 2, 3", SC'11), counter
  * (neutron index lo, hi, draw block, stream), key (seed lo, seed hi); each
- * 32-bit word w gives the float32-exact uniform (w >> 8) * 2^-24 in [0, 1),
- * matching the float32 uniforms the reference draws
+ * 128-bit block gives five 24-bit integers u and so five float32-exact
+ * uniforms u * 2^-24 in [0, 1), the resolution of the float32 uniforms the
+ * reference draws
  * (xoroshiro128p_uniform_float32, e.g. source_simple.py:128-132).
  */
 #include <math.h>
@@ -77,8 +78,8 @@ void oracle_philox4x32_10(const uint32_t ctr_in[4], const uint32_t key_in[2],
 typedef struct {
   uint32_t key[2];
   uint32_t ctr[4];
-  uint32_t buf[4];
-  int pos;           /* next word in buf; 4 = empty */
+  uint32_t buf[5];
+  int pos;           /* next uniform in buf; 5 = empty */
   const float* inj;  /* injected uniforms, or NULL   */
   int inj_pos, inj_stride;
   int overrun;
@@ -92,7 +93,7 @@ static void rng_init(rng_t* r, uint64_t seed, uint64_t index, uint32_t stream,
   r->ctr[1] = (uint32_t)(index >> 32);
   r->ctr[2] = 0;
   r->ctr[3] = stream;
-  r->pos = 4;
+  r->pos = 5;
   r->inj = inj;
   r->inj_pos = 0;
   r->inj_stride = stride;
@@ -107,13 +108,20 @@ static double rng_uniform(rng_t* r) {
     }
     return (double)r->inj[r->inj_pos++];
   }
-  if (r->pos == 4) {
-    oracle_philox4x32_10(r->ctr, r->key, r->buf);
+  if (r->pos == 5) {
+    /* one 128-bit block w0..w3 gives five 24-bit uniforms: bits 0-23,
+     * 24-47, 48-71, 72-95 and 96-119 of w0 | w1 << 32 | w2 << 64 | w3 << 96 */
+    uint32_t w[4];
+    oracle_philox4x32_10(r->ctr, r->key, w);
     r->ctr[2]++;
+    r->buf[0] = w[0] & 0xFFFFFFu;
+    r->buf[1] = (w[0] >> 24) | ((w[1] & 0xFFFFu) << 8);
+    r->buf[2] = (w[1] >> 16) | ((w[2] & 0xFFu) << 16);
+    r->buf[3] = w[2] >> 8;
+    r->buf[4] = w[3] & 0xFFFFFFu;
     r->pos = 0;
   }
-  uint32_t w = r->buf[r->pos++];
-  return (double)(w >> 8) * (1.0 / 16777216.0);
+  return (double)r->buf[r->pos++] * (1.0 / 16777216.0);
 }
 
 /* ------------------------------------------------------ neutron / vec3 */
@@ -933,7 +941,8 @@ double oracle_sqe_lookup(const mcv_component* c, double Q, double E) {
  * uniformly over the table box (one draw each, no rejection loop) and S
  * from the bilinear grid (SANS2D_ongrid.py:16-56).  Weight
  * S (vf/vi) Q (Qmax-Qmin)(Emax-Emin) / (2 ki kf); kinematically closed
- * (Q, E) absorb. */
+ * (Q, E) absorb.  sin(theta) comes from the factored
+ * (Q^2 - (ki-kf)^2)((ki+kf)^2 - Q^2) / (2 ki kf)^2 instead of 1 - cos^2. */
 static void sqe_scatter(neutron_t* n, rng_t* rng, const mcv_component* c) {
   double Qmin = c->dp[10], Qmax = c->dp[11], Emin = c->dp[12], Emax = c->dp[13];
   double v[3] = {n->vx, n->vy, n->vz};
@@ -946,10 +955,12 @@ static void sqe_scatter(neutron_t* n, rng_t* rng, const mcv_component* c) {
   if (Ef <= 0) { n->p = -1; return; }
   double vf = sqrt(Ef) * SE2V;
   double ki = V2K * vi, kf = V2K * vf;
-  double cost = (ki * ki + kf * kf - Q * Q) / (2 * ki * kf);
-  double cost2 = cost * cost;
-  if (cost2 > 1) { n->p = -1; return; }
-  double sint = sqrt(1.0 - cost2);
+  /* 1 - cos^2 in factored form, well conditioned near 0 and 180 deg */
+  double Q2 = Q * Q, dk = ki - kf, sk = ki + kf;
+  double sint2 = (Q2 - dk * dk) * (sk * sk - Q2) / (4 * ki * ki * kf * kf);
+  if (sint2 < 0) { n->p = -1; return; }
+  double cost = (ki * ki + kf * kf - Q2) / (2 * ki * kf);
+  double sint = sqrt(sint2);
   double v2 = vf * sint * cos(phi), v3 = vf * sint * sin(phi), v1 = vf * cost;
   double e1[3] = {v[0], v[1], v[2]}, e2[3], e3[3], nrm[3];
   normalize3(e1);

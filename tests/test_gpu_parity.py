@@ -96,7 +96,8 @@ def test_fp32_same_stream_within_1e5(name):
     assert bad.sum() <= max(2, 1e-4 * cmp.sum()), \
         (name, bad.sum(), cmp.sum(), np.sort(err[cmp])[-5:])
     dead = ~cmp
-    assert (g_last[dead] == o_last[dead]).mean() >= 0.99
+    if dead.any():
+        assert (g_last[dead] == o_last[dead]).mean() >= 0.99
 
 
 @pytest.mark.parametrize("name", list(BUILDERS))
@@ -187,3 +188,22 @@ def test_guide_pass_through_on_gpu():
     dt = (16 - out[2]) / out[5]
     assert out[2] + out[5] * dt == 16.0
     assert out[8] + dt == 32.0 and out[9] == 1.0
+
+
+@pytest.mark.parametrize("name", ["guide_chain", "sphere_theta_tof"])
+def test_regeneration_kernel_equals_thread_kernel(name):
+    """Path regeneration changes which lane runs which neutron, not the
+    neutron's arithmetic: identical bin counts, sums equal up to the order
+    of FP64 atomic additions (1e-12)."""
+    n = 500_000
+    a, b = BUILDERS[name](), BUILDERS[name]()
+    sa = engine.run_instrument(a, n, seed=21, floattype="float32",
+                               variant="regen")
+    sb = engine.run_instrument(b, n, seed=21, floattype="float32",
+                               variant="thread")
+    assert sa.processed == sb.processed == n
+    for (_, ta), (_, tb) in zip(gpu_tallies(a).items(),
+                                gpu_tallies(b).items()):
+        np.testing.assert_array_equal(ta[0], tb[0])
+        np.testing.assert_allclose(ta[1:], tb[1:], rtol=1e-12, atol=1e-300)
+        assert ta[0].sum() > 0
