@@ -80,6 +80,14 @@ class mcv_launch(ctypes.Structure):
     ]
 
 
+class mcv_grad(ctypes.Structure):
+    _fields_ = [
+        ("dout", ctypes.c_void_p * MCV_MAX_COMPONENTS),
+        ("dparam", ctypes.c_void_p * MCV_MAX_COMPONENTS),
+        ("dtable", ctypes.c_void_p * MCV_MAX_COMPONENTS),
+    ]
+
+
 class mcv_status(ctypes.Structure):
     _fields_ = [
         ("code", ctypes.c_int32),
@@ -141,6 +149,11 @@ _SIGNATURES = {
         ctypes.POINTER(ctypes.c_void_p)]),
     "mcv_graph_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "mcv_graph_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "mcv_backward": (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.POINTER(mcv_chain), ctypes.POINTER(mcv_grad),
+        ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int,
+        ctypes.POINTER(mcv_launch), ctypes.c_void_p,
+        ctypes.POINTER(mcv_status)]),
     "mcv_probe_fma_peak": (ctypes.c_int, [ctypes.c_int, ctypes.c_int,
                                           ctypes.c_int,
                                           ctypes.POINTER(ctypes.c_double)]),

@@ -9,6 +9,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "track.cuh"
 
 namespace mcv {
 
@@ -128,9 +129,10 @@ __device__ __forceinline__ bool guide_enter(Neutron<R>& n,
 // one pass of the bounce loop; true when the neutron has left the guide
 // (it stays at its last reflection point, guide.py:122-123) or its weight
 // is gone
-template <typename R>
+template <typename R, typename Trk>
 __device__ __forceinline__ bool guide_bounce(Neutron<R>& n,
-                                             const mcv_component& c) {
+                                             const mcv_component& c,
+                                             Trk& trk) {
   const R ww = prm<R>(c, 0), hh = prm<R>(c, 1), hw1 = prm<R>(c, 2),
           hh1 = prm<R>(c, 3), l = prm<R>(c, 4);
   R x = n.x, y = n.y, z = n.z, vx = n.vx, vy = n.vy, vz = n.vz;
@@ -188,18 +190,21 @@ __device__ __forceinline__ bool guide_bounce(Neutron<R>& n,
     n.vy = vy + d * l;
     n.vz = vz - d * hh;
   }
-  n.p *= reflectivity(q, prm<R>(c, 5), prm<R>(c, 6), prm<R>(c, 7),
-                      prm<R>(c, 8), prm<R>(c, 9));
+  const R R0 = prm<R>(c, 5), Qc = prm<R>(c, 6), alpha = prm<R>(c, 7),
+          m = prm<R>(c, 8), W = prm<R>(c, 9);
+  trk.reflect(q, R0, Qc, alpha, m, W);
+  n.p *= reflectivity(q, R0, Qc, alpha, m, W);
   return n.p <= 0;
 }
 
 // The whole guide; returns 1 when the bounce loop ran out of its
 // MCV_MAX_BOUNCES iterations.
-template <typename R>
-__device__ __forceinline__ int guide(Neutron<R>& n, const mcv_component& c) {
+template <typename R, typename Trk>
+__device__ __forceinline__ int guide(Neutron<R>& n, const mcv_component& c,
+                                     Trk& trk) {
   if (!guide_enter(n, c)) return 0;
   for (int nb = 0; nb < MCV_MAX_BOUNCES; ++nb)
-    if (guide_bounce(n, c)) return 0;
+    if (guide_bounce(n, c, trk)) return 0;
   return 1;
 }
 

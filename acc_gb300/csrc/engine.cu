@@ -20,6 +20,8 @@ struct mcv_ctx {
   DevStatus* d_status;
   void* d_batch;        // staged variant descriptions (mcv_run_batched)
   size_t batch_bytes;
+  double* d_grad;       // powder gradient partial sums (mcv_backward)
+  size_t grad_bytes;
 };
 
 struct mcv_graph {
@@ -196,6 +198,23 @@ int launch_chain(mcv_ctx* ctx, int mode, const mcv_chain* chain,
   return 0;
 }
 
+bool host_is_monitor(const mcv_component& c) {
+  switch (c.opcode) {
+    case MCV_OP_PSD_MONITOR:
+    case MCV_OP_PSD_MONITOR_4PI:
+    case MCV_OP_WAVELENGTH_MONITOR:
+    case MCV_OP_POSDIV_MONITOR:
+    case MCV_OP_IQE_MONITOR:
+    case MCV_OP_ENERGY_MONITOR:
+    case MCV_OP_THETA_TOF_4PI:
+    case MCV_OP_CYL_IQE_DETECTOR:
+    case MCV_OP_BANKED_DETECTOR:
+      return true;
+    default:
+      return false;
+  }
+}
+
 // The FP32 fused run uses path regeneration when asked to, or by default
 // when the chain has a guide (whose bounce count varies from neutron to
 // neutron); chains without one have near-uniform paths.
@@ -311,6 +330,8 @@ int mcv_ctx_create(int device, mcv_ctx** out) {
   c->device = device;
   c->d_batch = nullptr;
   c->batch_bytes = 0;
+  c->d_grad = nullptr;
+  c->grad_bytes = 0;
   cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device);
   if (cudaMalloc(&c->d_status, sizeof(DevStatus)) != cudaSuccess) {
     cudaGetLastError();
@@ -332,6 +353,7 @@ int mcv_ctx_destroy(mcv_ctx* ctx) {
     DeviceGuard g(ctx->device);
     cudaFree(ctx->d_status);
     if (ctx->d_batch) cudaFree(ctx->d_batch);
+    if (ctx->d_grad) cudaFree(ctx->d_grad);
   }
   delete ctx;
   return MCV_OK;
@@ -572,6 +594,81 @@ int mcv_graph_destroy(mcv_graph* graph) {
     if (graph->d_batch) cudaFree(graph->d_batch);
   }
   delete graph;
+  return MCV_OK;
+}
+
+int mcv_backward(mcv_ctx* ctx, const mcv_chain* chain, const mcv_grad* grad,
+                 uint64_t ncount, uint64_t first, uint64_t seed,
+                 int precision, const mcv_launch* launch, void* stream,
+                 mcv_status* st) {
+  int rc = validate_chain(chain, st);
+  if (rc) return rc;
+  if (!precision_ok(precision, st)) return MCV_EINVAL;
+  if (!grad) {
+    set_msg(st, MCV_EINVAL, "gradient description is NULL%s", "");
+    return MCV_EINVAL;
+  }
+  int hss = -1;
+  for (int k = 0; k < chain->ncomp; ++k) {
+    const mcv_component& c = chain->comp[k];
+    if (c.opcode == MCV_OP_HSS) {
+      if (hss < 0) hss = k;
+      else if (grad->dparam[k] || grad->dtable[k]) {
+        set_msg(st, MCV_EINVAL,
+                "only the first sample is differentiated (component %s%lld)",
+                "", (long long)k);
+        return MCV_EINVAL;
+      }
+    }
+    if (grad->dout[k] && !host_is_monitor(c)) {
+      set_msg(st, MCV_EINVAL, "dout given for non-monitor component %s%lld",
+              "", (long long)k);
+      return MCV_EINVAL;
+    }
+  }
+  if (!ctx) {
+    set_msg(st, MCV_EINVAL, "context is NULL%s", "");
+    return MCV_EINVAL;
+  }
+  if (ncount == 0) return st ? mcv_ctx_status(ctx, stream, 0, st) : MCV_OK;
+  DeviceGuard g(ctx->device);
+  cudaStream_t s = (cudaStream_t)stream;
+  double *px = nullptr, *py = nullptr;
+  int npeaks = 0;
+  if (hss >= 0 && chain->comp[hss].ip[1] == MCV_KERNEL_POWDER &&
+      grad->dtable[hss]) {
+    npeaks = chain->comp[hss].ip[4];
+    size_t need = (2 * (size_t)npeaks + 1) * sizeof(double);
+    if (need > ctx->grad_bytes) {
+      cudaError_t e = cudaStreamSynchronize(s);
+      if (e != cudaSuccess) return cuda_fail(st, e, "mcv_backward");
+      if (ctx->d_grad) cudaFree(ctx->d_grad);
+      ctx->d_grad = nullptr;
+      ctx->grad_bytes = 0;
+      e = cudaMalloc(&ctx->d_grad, need);
+      if (e != cudaSuccess) return cuda_fail(st, e, "mcv_backward scratch");
+      ctx->grad_bytes = need;
+    }
+    cudaMemsetAsync(ctx->d_grad, 0, need, s);
+    px = ctx->d_grad;
+    py = ctx->d_grad + npeaks + 1;
+  }
+  int blocks, threads;
+  if (precision == MCV_FP32) {
+    launch_shape(ctx, Launchers<float>::occupancy_grad, ncount, launch,
+                 &blocks, &threads);
+    Launchers<float>::grad(blocks, threads, s, *chain, *grad, ncount, first,
+                           seed, px, py, ctx->d_status);
+  } else {
+    launch_shape(ctx, Launchers<double>::occupancy_grad, ncount, launch,
+                 &blocks, &threads);
+    Launchers<double>::grad(blocks, threads, s, *chain, *grad, ncount, first,
+                            seed, px, py, ctx->d_status);
+  }
+  if (px) powder_finalize(px, py, npeaks, grad->dtable[hss], s);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(st, e, "mcv_backward launch");
+  if (st) return mcv_ctx_status(ctx, stream, ncount, st);
   return MCV_OK;
 }
 

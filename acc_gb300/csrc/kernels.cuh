@@ -63,45 +63,46 @@ __device__ __forceinline__ void apply_transform(Neutron<R>& n,
 }
 
 // One component on one neutron; returns 1 when a guide ran out of bounces.
-template <typename R, typename Rng>
+template <typename R, typename Rng, typename Trk>
 __device__ __forceinline__ int run_component(Neutron<R>& n, Rng& rng,
-                                             const mcv_component& c) {
+                                             const mcv_component& c,
+                                             Trk& trk) {
   Tally tl{c.tally, comp_nbins(c)};
   switch (c.opcode) {
     case MCV_OP_SOURCE_SIMPLE:
       source_simple<R>(n, rng, c);
       return 0;
     case MCV_OP_GUIDE:
-      return guide<R>(n, c);
+      return guide<R>(n, c, trk);
     case MCV_OP_HSS:
-      hss(n, rng, c);
+      hss(n, rng, c, trk);
       return 0;
     case MCV_OP_PSD_MONITOR:
-      psd_monitor<R>(n, c, tl);
+      psd_monitor<R>(n, c, tl, trk);
       return 0;
     case MCV_OP_PSD_MONITOR_4PI:
-      psd_monitor_4pi<R>(n, c, tl);
+      psd_monitor_4pi<R>(n, c, tl, trk);
       return 0;
     case MCV_OP_WAVELENGTH_MONITOR:
-      wavelength_monitor<R>(n, c, tl);
+      wavelength_monitor<R>(n, c, tl, trk);
       return 0;
     case MCV_OP_POSDIV_MONITOR:
-      posdiv_monitor<R>(n, c, tl);
+      posdiv_monitor<R>(n, c, tl, trk);
       return 0;
     case MCV_OP_IQE_MONITOR:
-      iqe_monitor<R>(n, c, tl);
+      iqe_monitor<R>(n, c, tl, trk);
       return 0;
     case MCV_OP_ENERGY_MONITOR:
-      energy_monitor<R>(n, c, tl);
+      energy_monitor<R>(n, c, tl, trk);
       return 0;
     case MCV_OP_THETA_TOF_4PI:
-      theta_tof_4pi<R>(n, c, tl);
+      theta_tof_4pi<R>(n, c, tl, trk);
       return 0;
     case MCV_OP_CYL_IQE_DETECTOR:
-      cyl_iqe<R>(n, c, tl);
+      cyl_iqe<R>(n, c, tl, trk);
       return 0;
     case MCV_OP_BANKED_DETECTOR:
-      banked<R>(n, c, tl);
+      banked<R>(n, c, tl, trk);
       return 0;
     case MCV_OP_SLIT:
       slit_or_beamstop<R>(n, c, false);
@@ -121,16 +122,18 @@ struct Counters {
 // Whole chain on one neutron (the body of the generated
 // process_kernel_no_buffer, acc/run_script.py:182-196).  A neutron leaves
 // the chain after a component that leaves its weight not positive.
-template <typename R, typename Rng>
+template <typename R, typename Rng, typename Trk = NoTrack>
 __device__ __forceinline__ int run_chain_one(Neutron<R>& n, Rng& rng,
                                              const mcv_chain& ch,
-                                             Counters& k) {
+                                             Counters& k, Trk&& trk = Trk()) {
   int last = -1;
   const int nc = ch.ncomp;
+  trk.begin_neutron();
   for (int c = 0; c < nc; ++c) {
     if (c > 0) apply_transform<R>(n, ch, c);
     last = c;
-    k.overflow += run_component<R>(n, rng, ch.comp[c]);
+    trk.begin_component(ch, c);
+    k.overflow += run_component<R>(n, rng, ch.comp[c], trk);
     if (!(n.p > 0)) {
       if (m_isnan(n.p)) k.nonfinite++;
       break;
@@ -226,6 +229,7 @@ __global__ void __launch_bounds__(kMaxThreads)
   uint64_t next = warp * per;
   const uint64_t end = next + per < n ? next + per : n;
   Counters k{0, 0, 0, 0};
+  NoTrack trk;
   Neutron<R> nt;
   zero_neutron(nt);
   PhiloxStream rng(seed, 0, 0u);
@@ -258,11 +262,11 @@ __global__ void __launch_bounds__(kMaxThreads)
         if (guide_enter<R>(nt, cp)) {
           inside = 1;
           nb = 0;
-          finished = guide_bounce<R>(nt, cp);
+          finished = guide_bounce<R>(nt, cp, trk);
           ++nb;
         }
       } else {
-        finished = guide_bounce<R>(nt, cp);
+        finished = guide_bounce<R>(nt, cp, trk);
         ++nb;
       }
       if (!finished && nb >= MCV_MAX_BOUNCES) {
@@ -270,7 +274,7 @@ __global__ void __launch_bounds__(kMaxThreads)
         k.overflow++;
       }
     } else {
-      k.overflow += run_component<R>(nt, rng, cp);
+      k.overflow += run_component<R>(nt, rng, cp, trk);
     }
     if (finished) {
       inside = 0;
@@ -287,6 +291,29 @@ __global__ void __launch_bounds__(kMaxThreads)
       }
     }
   }
+  flush_counters(k, st);
+}
+
+// Backward replay: neutron i of the stream `seed` again, with the gradient
+// tracker (track.cuh) in place of the tallies.
+template <typename R>
+__global__ void __launch_bounds__(kMaxThreads)
+    grad_kernel(const __grid_constant__ mcv_chain ch,
+                const __grid_constant__ mcv_grad g, uint64_t n,
+                uint64_t first, uint64_t seed, double* powder_x,
+                double* powder_y, DevStatus* st) {
+  Counters k{0, 0, 0, 0};
+  GradTrack<R> trk(g, ch, powder_x, powder_y);
+  const uint64_t step = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += step) {
+    Neutron<R> nt;
+    zero_neutron(nt);
+    PhiloxStream rng(seed, first + i, 0u);
+    run_chain_one<R>(nt, rng, ch, k, trk);
+    k.processed++;
+  }
+  trk.flush(ch);
   flush_counters(k, st);
 }
 
@@ -318,7 +345,8 @@ __global__ void __launch_bounds__(kMaxThreads)
       if (cp.opcode != MCV_OP_SOURCE_SIMPLE && !(nt.p > 0)) break;
       if (c > 0) apply_transform<R>(nt, ch, c);
       PhiloxStream rng(seed, first + i, (uint32_t)(c + 1));
-      k.overflow += run_component<R>(nt, rng, cp);
+      NoTrack trk;
+      k.overflow += run_component<R>(nt, rng, cp, trk);
     }
     k.processed++;
     s[0] = nt.x;
@@ -439,6 +467,11 @@ struct Launchers {
   static void regen(int blocks, int threads, cudaStream_t s,
                     const mcv_chain& ch, uint64_t n, uint64_t first,
                     uint64_t seed, DevStatus* st);
+  static int occupancy_grad(int threads);
+  static void grad(int blocks, int threads, cudaStream_t s,
+                   const mcv_chain& ch, const mcv_grad& g, uint64_t n,
+                   uint64_t first, uint64_t seed, double* px, double* py,
+                   DevStatus* st);
   static int occupancy_buffer(int threads);
   static void buffer(int blocks, int threads, cudaStream_t s,
                      const mcv_chain& ch, void* buf, uint64_t n,
@@ -460,6 +493,10 @@ inline int occupancy_of(K kernel, int threads, size_t smem) {
                                                 smem);
   return per_sm < 1 ? 1 : per_sm;
 }
+
+// the one kernel that is not per-precision: instantiated in launch_fp64.cu
+void powder_finalize(const double* px, const double* py, int npeaks,
+                     double* dtable, cudaStream_t s);
 
 #ifdef MCV_DEFINE_LAUNCHERS
 template <typename R>
@@ -495,6 +532,20 @@ void Launchers<R>::regen(int blocks, int threads, cudaStream_t s,
                          const mcv_chain& ch, uint64_t n, uint64_t first,
                          uint64_t seed, DevStatus* st) {
   regen_kernel<R><<<blocks, threads, 0, s>>>(ch, n, first, seed, st);
+}
+
+template <typename R>
+int Launchers<R>::occupancy_grad(int threads) {
+  return occupancy_of(grad_kernel<R>, threads, 0);
+}
+
+template <typename R>
+void Launchers<R>::grad(int blocks, int threads, cudaStream_t s,
+                        const mcv_chain& ch, const mcv_grad& g, uint64_t n,
+                        uint64_t first, uint64_t seed, double* px, double* py,
+                        DevStatus* st) {
+  grad_kernel<R><<<blocks, threads, 0, s>>>(ch, g, n, first, seed, px, py,
+                                            st);
 }
 
 template <typename R>

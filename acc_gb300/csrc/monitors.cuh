@@ -6,29 +6,9 @@
 
 #include "common.cuh"
 #include "sample.cuh"
+#include "track.cuh"
 
 namespace mcv {
-
-struct Tally {
-  double* out;
-  uint64_t nbins;
-};
-
-__device__ __forceinline__ void tally_add(const Tally& t, uint64_t bin,
-                                          double p) {
-  if (!t.out) return;
-  atomicAdd(t.out + bin, 1.0);
-  atomicAdd(t.out + t.nbins + bin, p);
-  atomicAdd(t.out + 2 * t.nbins + bin, p * p);
-}
-__device__ __forceinline__ void tally_add(const Tally& t, uint64_t bin,
-                                          float p) {
-  if (!t.out) return;
-  atomicAdd(t.out + bin, 1.0);
-  const double pd = (double)p;
-  atomicAdd(t.out + t.nbins + bin, pd);
-  atomicAdd(t.out + 2 * t.nbins + bin, pd * pd);
-}
 
 // propagate to z = 0 without moving the neutron (prop_z0, acc/neutron.py:60-66);
 // false when that plane lies in the neutron's past.
@@ -55,10 +35,10 @@ __device__ __forceinline__ int bin_of(R v, R lo, R hi, int nb) {
 }
 
 // PSD_monitor.propagate (acc/components/monitors/psd_monitor.py:66-83)
-template <typename R>
+template <typename R, typename Trk>
 __device__ __forceinline__ void psd_monitor(const Neutron<R>& n,
                                             const mcv_component& c,
-                                            const Tally& tl) {
+                                            const Tally& tl, Trk& trk) {
   R xmin = prm<R>(c, 0), xmax = prm<R>(c, 1), ymin = prm<R>(c, 2),
     ymax = prm<R>(c, 3);
   int nx = c.ip[0], ny = c.ip[1];
@@ -66,14 +46,14 @@ __device__ __forceinline__ void psd_monitor(const Neutron<R>& n,
   if (!to_z0(n, x, y)) return;
   if (!(x > xmin && x < xmax && y > ymin && y < ymax)) return;
   int ix = bin_of(x, xmin, xmax, nx), iy = bin_of(y, ymin, ymax, ny);
-  tally_add(tl, (uint64_t)ix * ny + iy, n.p);
+  trk.tally(tl, (uint64_t)ix * ny + iy, n.p);
 }
 
 // Wavelength_monitor.propagate (wavelength_monitor.py:52-74)
-template <typename R>
+template <typename R, typename Trk>
 __device__ __forceinline__ void wavelength_monitor(const Neutron<R>& n,
                                                    const mcv_component& c,
-                                                   const Tally& tl) {
+                                                   const Tally& tl, Trk& trk) {
   R xmin = prm<R>(c, 0), xmax = prm<R>(c, 1), ymin = prm<R>(c, 2),
     ymax = prm<R>(c, 3), Lmin = prm<R>(c, 4), Lmax = prm<R>(c, 5);
   R x, y;
@@ -82,15 +62,15 @@ __device__ __forceinline__ void wavelength_monitor(const Neutron<R>& n,
   R v = m_sqrt(n.vx * n.vx + n.vy * n.vy + n.vz * n.vz);
   R L = R(2 * kPi) / (v * R(kV2K));
   if (!(L > Lmin && L < Lmax)) return;
-  tally_add(tl, (uint64_t)bin_of(L, Lmin, Lmax, c.ip[0]), n.p);
+  trk.tally(tl, (uint64_t)bin_of(L, Lmin, Lmax, c.ip[0]), n.p);
 }
 
 // Energy monitor: the wavelength monitor binned in E = v^2 VS2E
 // (acc/neutron.py:69-71)
-template <typename R>
+template <typename R, typename Trk>
 __device__ __forceinline__ void energy_monitor(const Neutron<R>& n,
                                                const mcv_component& c,
-                                               const Tally& tl) {
+                                               const Tally& tl, Trk& trk) {
   R xmin = prm<R>(c, 0), xmax = prm<R>(c, 1), ymin = prm<R>(c, 2),
     ymax = prm<R>(c, 3), Emin = prm<R>(c, 4), Emax = prm<R>(c, 5);
   R x, y;
@@ -98,14 +78,14 @@ __device__ __forceinline__ void energy_monitor(const Neutron<R>& n,
   if (!(x > xmin && x < xmax && y > ymin && y < ymax)) return;
   R E = (n.vx * n.vx + n.vy * n.vy + n.vz * n.vz) * R(kVS2E);
   if (!(E > Emin && E < Emax)) return;
-  tally_add(tl, (uint64_t)bin_of(E, Emin, Emax, c.ip[0]), n.p);
+  trk.tally(tl, (uint64_t)bin_of(E, Emin, Emax, c.ip[0]), n.p);
 }
 
 // PosDiv_monitor.propagate (posdiv_monitor.py:67-89)
-template <typename R>
+template <typename R, typename Trk>
 __device__ __forceinline__ void posdiv_monitor(const Neutron<R>& n,
                                                const mcv_component& c,
-                                               const Tally& tl) {
+                                               const Tally& tl, Trk& trk) {
   R xmin = prm<R>(c, 0), xmax = prm<R>(c, 1), ymin = prm<R>(c, 2),
     ymax = prm<R>(c, 3), maxdiv = prm<R>(c, 4);
   int npos = c.ip[0], ndiv = c.ip[1];
@@ -116,16 +96,16 @@ __device__ __forceinline__ void posdiv_monitor(const Neutron<R>& n,
   if (!(div < maxdiv && div > -maxdiv)) return;
   int ix = bin_of(x, xmin, xmax, npos);
   int id = bin_of(div + maxdiv, R(0), 2 * maxdiv, ndiv);
-  tally_add(tl, (uint64_t)ix * ndiv + id, n.p);
+  trk.tally(tl, (uint64_t)ix * ndiv + id, n.p);
 }
 
 // PSD_monitor_4Pi.propagate (psd_monitor_4pi.py:56-79) with the +0.5 of
 // its theta index (line 72); sin(theta) is clamped to [-1, 1] and a
 // neutron that misses the sphere is not tallied.
-template <typename R>
+template <typename R, typename Trk>
 __device__ __forceinline__ void psd_monitor_4pi(Neutron<R>& n,
                                                 const mcv_component& c,
-                                                const Tally& tl) {
+                                                const Tally& tl, Trk& trk) {
   R radius = prm<R>(c, 0);
   int nphi = c.ip[0], ntheta = c.ip[1];
   R t1, t2;
@@ -146,14 +126,14 @@ __device__ __forceinline__ void psd_monitor_4pi(Neutron<R>& n,
   int itheta = (int)(ntheta * (theta + R(kPi) / 2) / R(kPi) + R(0.5));
   if (itheta >= ntheta) itheta = ntheta - 1;
   else if (itheta < 0) itheta = 0;
-  tally_add(tl, (uint64_t)iphi * ntheta + itheta, n.p);
+  trk.tally(tl, (uint64_t)iphi * ntheta + itheta, n.p);
 }
 
 // IQE_monitor.propagate (iqe_monitor.py:80-113), angle gates included
-template <typename R>
+template <typename R, typename Trk>
 __device__ __forceinline__ void iqe_monitor(const Neutron<R>& n,
                                             const mcv_component& c,
-                                            const Tally& tl) {
+                                            const Tally& tl, Trk& trk) {
   R Ei = prm<R>(c, 0), Qmin = prm<R>(c, 1), Qmax = prm<R>(c, 2),
     Emin = prm<R>(c, 3), Emax = prm<R>(c, 4);
   R max_in = prm<R>(c, 5), min_in = prm<R>(c, 6), max_out = prm<R>(c, 7),
@@ -174,17 +154,17 @@ __device__ __forceinline__ void iqe_monitor(const Neutron<R>& n,
     R E = Ei - (vx * vx + vy * vy + vz * vz) * R(kVS2E);
     if (Q >= Qmin && Q < Qmax && E >= Emin && E < Emax) {
       int iQ = bin_of(Q, Qmin, Qmax, c.ip[0]), iE = bin_of(E, Emin, Emax, c.ip[1]);
-      tally_add(tl, (uint64_t)iQ * c.ip[1] + iE, n.p);
+      trk.tally(tl, (uint64_t)iQ * c.ip[1] + iE, n.p);
     }
   }
 }
 
 // theta x tof 4pi shell: the sphere crossing of PSD_monitor_4Pi binned by
 // the polar angle from +z, atan2(hypot(x, y), z), and the time of flight.
-template <typename R>
+template <typename R, typename Trk>
 __device__ __forceinline__ void theta_tof_4pi(Neutron<R>& n,
                                               const mcv_component& c,
-                                              const Tally& tl) {
+                                              const Tally& tl, Trk& trk) {
   R radius = prm<R>(c, 0), tmin = prm<R>(c, 1), tmax = prm<R>(c, 2);
   int nth = c.ip[0], nt = c.ip[1];
   R t1, t2;
@@ -201,7 +181,7 @@ __device__ __forceinline__ void theta_tof_4pi(Neutron<R>& n,
   if (!(t >= tmin && t < tmax)) return;
   int ith = bin_of(theta, R(0), R(kPi), nth);
   int it = bin_of(t, tmin, tmax, nt);
-  tally_add(tl, (uint64_t)ith * nt + it, n.p);
+  trk.tally(tl, (uint64_t)ith * nt + it, n.p);
 }
 
 // exit through the side of the vertical (axis y) cylinder x^2 + z^2 = R^2
@@ -222,9 +202,9 @@ __device__ __forceinline__ R vcyl_exit(const Neutron<R>& n, R Rad, R H) {
 }
 
 // cylinder detector binned in I(Q,E): Q and E as iqe_monitor.py:96-110
-template <typename R>
+template <typename R, typename Trk>
 __device__ __forceinline__ void cyl_iqe(Neutron<R>& n, const mcv_component& c,
-                                        const Tally& tl) {
+                                        const Tally& tl, Trk& trk) {
   R Rad = prm<R>(c, 0), H = prm<R>(c, 1), Ei = prm<R>(c, 2),
     Qmin = prm<R>(c, 3), Qmax = prm<R>(c, 4), Emin = prm<R>(c, 5),
     Emax = prm<R>(c, 6);
@@ -237,14 +217,14 @@ __device__ __forceinline__ void cyl_iqe(Neutron<R>& n, const mcv_component& c,
   R E = Ei - (vx * vx + vy * vy + vz * vz) * R(kVS2E);
   if (Q >= Qmin && Q < Qmax && E >= Emin && E < Emax) {
     int iQ = bin_of(Q, Qmin, Qmax, c.ip[0]), iE = bin_of(E, Emin, Emax, c.ip[1]);
-    tally_add(tl, (uint64_t)iQ * c.ip[1] + iE, n.p);
+    trk.tally(tl, (uint64_t)iQ * c.ip[1] + iE, n.p);
   }
 }
 
 // banked cylinder detector: banks are azimuthal windows of phi = atan2(x, z)
-template <typename R>
+template <typename R, typename Trk>
 __device__ __forceinline__ void banked(Neutron<R>& n, const mcv_component& c,
-                                       const Tally& tl) {
+                                       const Tally& tl, Trk& trk) {
   R Rad = prm<R>(c, 0), H = prm<R>(c, 1), a0 = prm<R>(c, 2), w = prm<R>(c, 3),
     g = prm<R>(c, 4), tmin = prm<R>(c, 5), tmax = prm<R>(c, 6);
   int nb = c.ip[0], ntube = c.ip[1], npix = c.ip[2], ntof = c.ip[3];
@@ -264,7 +244,7 @@ __device__ __forceinline__ void banked(Neutron<R>& n, const mcv_component& c,
   int pix = bin_of(n.y + H / 2, R(0), H, npix);
   int it = bin_of(tt, tmin, tmax, ntof);
   uint64_t bin = (((uint64_t)b * ntube + tube) * npix + pix) * ntof + it;
-  tally_add(tl, bin, n.p);
+  trk.tally(tl, bin, n.p);
 }
 
 }  // namespace mcv

@@ -3,6 +3,7 @@
 #pragma once
 
 #include "common.cuh"
+#include "track.cuh"
 
 namespace mcv {
 
@@ -498,9 +499,10 @@ __device__ __forceinline__ R powder_coeff(const Neutron<R>& n,
 // powderdiffr.scatter (acc/kernels/powderdiffr.py:27-109), including the
 // reference's peak count: without a break in `for peakindex in range(1,
 // Npeaks)` the count is Npeaks-1.
-template <typename R, typename Rng>
+template <typename R, typename Rng, typename Trk>
 __device__ __forceinline__ void powder_scatter(Neutron<R>& n, Rng& rng,
-                                               const mcv_component& c) {
+                                               const mcv_component& c,
+                                               Trk& trk) {
   const R* pk = powder_table<R>(c);
   int np = c.ip[4];
   R ucvol = prm<R>(c, 10), d_phi = prm<R>(c, 11);
@@ -525,6 +527,7 @@ __device__ __forceinline__ void powder_scatter(Neutron<R>& n, Rng& rng,
   R rt = R(rng.next()) * 2 - 1;
   R q = __ldg(&pk[4 * peak]), w = __ldg(&pk[4 * peak + 1]),
     s = __ldg(&pk[4 * peak + 2]);
+  trk.powder_peak(peak, s);
   R arg = q * (1 + w * rt) / (R(2.0) * vl);
   R scatter_xs = s / (vl * vl);
   scatter_xs *= nreach;
@@ -567,37 +570,66 @@ __device__ __forceinline__ void powder_scatter(Neutron<R>& n, Rng& rng,
 
 // Bilinear lookup of the S(Q,E) grid (node (iq, ie) at Qmin + iq dQ,
 // Emin + ie dE; indices clamp to [0, n-2] as SANS2D_ongrid.py:37-50 does).
-template <typename R>
-__device__ __forceinline__ R sqe_lookup(const mcv_component& c, R Q, R E) {
-  const float* S = c.ftable;
+// Grid coordinate of a value drawn as lo + u (hi - lo) on an n-node grid
+// spanning [lo, hi]: u (n - 1).  In FP32 it is formed exactly from the
+// uniform's 24-bit integer k (u = k 2^-24): node = k (n-1) >> 24,
+// fraction = (k (n-1) mod 2^24) 2^-24.
+__device__ __forceinline__ void grid_coord(float u, int n, int& i, float& f) {
+  uint64_t prod = (uint64_t)(uint32_t)(u * 16777216.f) * (uint64_t)(n - 1);
+  i = (int)(prod >> 24);
+  f = (float)(uint32_t)(prod & 0xFFFFFFu) * 5.9604644775390625e-08f;
+  if (i > n - 2) {
+    i = n - 2;
+    f = 1.f;
+  }
+}
+
+template <typename R, typename Trk>
+__device__ __forceinline__ R sqe_lookup(const mcv_component& c, R Q, R E,
+                                        R uQ, R uE, Trk& trk) {
+  const float* tab = c.ftable;
   int nQ = c.ip[4], nE = c.ip[5];
-  R Qmin = prm<R>(c, 10), Qmax = prm<R>(c, 11), Emin = prm<R>(c, 12),
-    Emax = prm<R>(c, 13);
-  R dQ = (Qmax - Qmin) / (nQ - 1), dE = (Emax - Emin) / (nE - 1);
-  int iq = (int)((Q - Qmin) / dQ), ie = (int)((E - Emin) / dE);
-  iq = iq < 0 ? 0 : (iq > nQ - 2 ? nQ - 2 : iq);
-  ie = ie < 0 ? 0 : (ie > nE - 2 ? nE - 2 : ie);
-  R fx = (Q - Qmin) / dQ - iq, fy = (E - Emin) / dE - ie;
-  R f00 = __ldg(&S[iq * nE + ie]), f10 = __ldg(&S[(iq + 1) * nE + ie]);
-  R f01 = __ldg(&S[iq * nE + ie + 1]), f11 = __ldg(&S[(iq + 1) * nE + ie + 1]);
+  int iq, ie;
+  R fx, fy;
+  if constexpr (sizeof(R) == 4) {
+    grid_coord(uQ, nQ, iq, fx);
+    grid_coord(uE, nE, ie, fy);
+  } else {
+    R Qmin = prm<R>(c, 10), Qmax = prm<R>(c, 11), Emin = prm<R>(c, 12),
+      Emax = prm<R>(c, 13);
+    R dQ = (Qmax - Qmin) / (nQ - 1), dE = (Emax - Emin) / (nE - 1);
+    iq = (int)((Q - Qmin) / dQ);
+    ie = (int)((E - Emin) / dE);
+    iq = iq < 0 ? 0 : (iq > nQ - 2 ? nQ - 2 : iq);
+    ie = ie < 0 ? 0 : (ie > nE - 2 ? nE - 2 : ie);
+    fx = (Q - Qmin) / dQ - iq;
+    fy = (E - Emin) / dE - ie;
+  }
+  R f00 = __ldg(&tab[iq * nE + ie]), f10 = __ldg(&tab[(iq + 1) * nE + ie]);
+  R f01 = __ldg(&tab[iq * nE + ie + 1]);
+  R f11 = __ldg(&tab[(iq + 1) * nE + ie + 1]);
   // bilinear_interp (SANS2D_ongrid.py:16-22)
   R a00 = f00, a10 = f10 - f00, a01 = f01 - f00, a11 = f11 - f10 - f01 + f00;
-  return a00 + a10 * fx + a01 * fy + a11 * fx * fy;
+  R S = a00 + a10 * fx + a01 * fy + a11 * fx * fy;
+  trk.sqe(iq * nE + ie, nE, fx, fy, S);
+  return S;
 }
 
 // Gridded S(Q,E) kernel: the kinematics of E_Q._S (acc/kernels/E_Q.py:37-99)
 // with (Q, E) uniform over the table box and S from the grid; sin(theta)
 // from the factored (Q^2 - (ki-kf)^2)((ki+kf)^2 - Q^2) / (2 ki kf)^2.
-template <typename R, typename Rng>
+template <typename R, typename Rng, typename Trk>
 __device__ __forceinline__ void sqe_scatter(Neutron<R>& n, Rng& rng,
-                                            const mcv_component& c) {
+                                            const mcv_component& c,
+                                            Trk& trk) {
   R Qmin = prm<R>(c, 10), Qmax = prm<R>(c, 11), Emin = prm<R>(c, 12),
     Emax = prm<R>(c, 13);
   R vx = n.vx, vy = n.vy, vz = n.vz;
   R vi = m_sqrt(vx * vx + vy * vy + vz * vz);
   R Ei = vi * vi * R(kVS2E);
-  R Q = R(rng.next()) * (Qmax - Qmin) + Qmin;
-  R E = R(rng.next()) * (Emax - Emin) + Emin;
+  R uQ = rng.next(), uE = rng.next();
+  R Q = uQ * (Qmax - Qmin) + Qmin;
+  R E = uE * (Emax - Emin) + Emin;
   R u3 = rng.next();
   R Ef = Ei - E;
   if (Ef <= 0) {
@@ -634,7 +666,7 @@ __device__ __forceinline__ void sqe_scatter(Neutron<R>& n, Rng& rng,
   n.vx = e1x * v1 + e2x * v2 + e3x * v3;
   n.vy = e1y * v1 + e2y * v2 + e3y * v3;
   n.vz = e1z * v1 + e2z * v2 + e3z * v3;
-  R S = sqe_lookup<R>(c, Q, E);
+  R S = sqe_lookup<R>(c, Q, E, uQ, uE, trk);
   R prob_f = S * (vf / vi) * Q * (Qmax - Qmin) * (Emax - Emin) / (kf * ki) / 2;
   n.p *= prob_f;
 }
@@ -654,32 +686,53 @@ __device__ __forceinline__ R hss_mu(const Neutron<R>& n,
   return prm<R>(c, 8) / v * 2200;
 }
 
-template <typename R, typename Rng>
+template <typename R, typename Rng, typename Trk>
 __device__ __forceinline__ void hss_kernel(Neutron<R>& n, Rng& rng,
-                                           const mcv_component& c) {
+                                           const mcv_component& c, Trk& trk) {
   switch (c.ip[1]) {
     case MCV_KERNEL_ISOTROPIC:
       n.p *= prm<R>(c, 9);  // kernels/__init__.py:42
+      trk.sigma_factor(prm<R>(c, 9));
       isotropic_S<R>(n, rng);
       break;
     case MCV_KERNEL_POWDER:
-      powder_scatter<R>(n, rng, c);
+      powder_scatter<R>(n, rng, c, trk);
       break;
     case MCV_KERNEL_SQE_GRID:
       n.p *= prm<R>(c, 9);
-      sqe_scatter<R>(n, rng, c);
+      trk.sigma_factor(prm<R>(c, 9));
+      sqe_scatter<R>(n, rng, c, trk);
       break;
     default:
       break;
   }
 }
 
+// The weight factor exp(-(mu(v) + sigma(v)) L) seen by the tracker:
+// d/dmu2200 = -2200 L / v; d/dsigma = -L for a constant scattering
+// coefficient, d/ds_j = -L / (v^2 Vcell) for the K reachable powder peaks.
+template <typename R, typename Trk>
+__device__ __forceinline__ void track_atten(const Neutron<R>& n,
+                                            const mcv_component& c, R L,
+                                            Trk& trk) {
+  if constexpr (Trk::kActive) {
+    R v = m_sqrt(n.vx * n.vx + n.vy * n.vy + n.vz * n.vz);
+    if (c.ip[1] == MCV_KERNEL_POWDER) {
+      trk.atten(R(-2200) * L / v, R(0));
+      int K = powder_reach(powder_table<R>(c), c.ip[4], v);
+      trk.powder_atten(K, -L / (v * v * prm<R>(c, 10)));
+    } else {
+      trk.atten(R(-2200) * L / v, -L);
+    }
+  }
+}
+
 // HomogeneousSingleScatterer.propagate
 // (acc/components/samples/homogeneous_single_scatterer.py:62-100), FP64:
 // the reference's sequence.
-template <typename Rng>
+template <typename Rng, typename Trk>
 __device__ __forceinline__ void hss(Neutron<double>& n, Rng& rng,
-                                    const mcv_component& c) {
+                                    const mcv_component& c, Trk& trk) {
   double x = n.x, y = n.y, z = n.z, vx = n.vx, vy = n.vy, vz = n.vz;
   Hits<double> h = intersect_shape<double>(c, x, y, z, vx, vy, vz);
   if (h.n < 2) return;
@@ -697,7 +750,8 @@ __device__ __forceinline__ void hss(Neutron<double>& n, Rng& rng,
   double mu = hss_mu<double>(n, c);
   double atten = exp(-(mu + sigma) * dist);
   n.p *= fulllen * atten;
-  hss_kernel<double>(n, rng, c);
+  track_atten<double>(n, c, dist, trk);
+  hss_kernel<double>(n, rng, c, trk);
   if (n.p <= 0) return;
   h = intersect_shape<double>(c, n.x, n.y, n.z, n.vx, n.vy, n.vz);
   double dt3 = total_time_in_shape<double>(h);
@@ -707,6 +761,7 @@ __device__ __forceinline__ void hss(Neutron<double>& n, Rng& rng,
   // the reference uses the incident speed v here (line 98)
   double atten2 = exp(-(mu + sigma) * v * dt3);
   n.p *= atten2;
+  track_atten<double>(n, c, v * dt3, trk);
 }
 
 // FP32 form of the same propagate.  The incoming ray is first moved to its
@@ -716,9 +771,9 @@ __device__ __forceinline__ void hss(Neutron<double>& n, Rng& rng,
 // "now" is formed as a difference of tau values.  In exact arithmetic this
 // is the reference's sequence; in float it avoids cancelling metre-scale
 // flight times against centimetre-scale chords.
-template <typename Rng>
+template <typename Rng, typename Trk>
 __device__ __forceinline__ void hss(Neutron<float>& n, Rng& rng,
-                                    const mcv_component& c) {
+                                    const mcv_component& c, Trk& trk) {
   float vx = n.vx, vy = n.vy, vz = n.vz;
   float v2 = vx * vx + vy * vy + vz * vz;
   float t0 = -(n.x * vx + n.y * vy + n.z * vz) / v2;
@@ -773,7 +828,8 @@ __device__ __forceinline__ void hss(Neutron<float>& n, Rng& rng,
   float sigma = hss_sigma<float>(n, c);
   float mu = hss_mu<float>(n, c);
   n.p *= fulllen * __expf(-(mu + sigma) * dist);
-  hss_kernel<float>(n, rng, c);
+  track_atten<float>(n, c, dist, trk);
+  hss_kernel<float>(n, rng, c, trk);
   if (n.p <= 0.f) return;
   h = intersect_shape<float>(c, n.x, n.y, n.z, n.vx, n.vy, n.vz);
   float dt3 = total_time_in_shape<float>(h);
@@ -781,6 +837,7 @@ __device__ __forceinline__ void hss(Neutron<float>& n, Rng& rng,
   sigma = hss_sigma<float>(n, c);
   mu = hss_mu<float>(n, c);
   n.p *= __expf(-(mu + sigma) * v * dt3);
+  track_atten<float>(n, c, v * dt3, trk);
 }
 
 }  // namespace mcv

@@ -1,0 +1,243 @@
+// track.cuh -- what a kernel does at the points where a neutron's weight
+// picks up a parameter-dependent factor, and at tallies.
+//
+// NoTrack (forward kernels) adds tallies and ignores the weight factors; it
+// compiles to nothing else.  GradTrack (the backward replay) follows the
+// same neutron -- same Philox counter, same arithmetic -- and accumulates
+// d ln p / d theta for the differentiable parameters; at a tally in bin b
+// it adds dL/d(sum p)_b * p * d ln p / d theta to the gradient.  Every
+// parameter handled here enters only the weight: with the random numbers
+// fixed the path does not depend on it, so this is the exact derivative of
+// the estimator (the common-random-number derivative).
+#pragma once
+
+#include "common.cuh"
+
+namespace mcv {
+
+struct Tally {
+  double* out;
+  uint64_t nbins;
+};
+
+__device__ __forceinline__ void tally_add(const Tally& t, uint64_t bin,
+                                          double p) {
+  if (!t.out) return;
+  atomicAdd(t.out + bin, 1.0);
+  atomicAdd(t.out + t.nbins + bin, p);
+  atomicAdd(t.out + 2 * t.nbins + bin, p * p);
+}
+__device__ __forceinline__ void tally_add(const Tally& t, uint64_t bin,
+                                          float p) {
+  if (!t.out) return;
+  atomicAdd(t.out + bin, 1.0);
+  const double pd = (double)p;
+  atomicAdd(t.out + t.nbins + bin, pd);
+  atomicAdd(t.out + 2 * t.nbins + bin, pd * pd);
+}
+
+struct NoTrack {
+  static constexpr bool kActive = false;
+  __device__ __forceinline__ void begin_neutron() {}
+  __device__ __forceinline__ void begin_component(const mcv_chain&, int) {}
+  template <typename R>
+  __device__ __forceinline__ void reflect(R, R, R, R, R, R) {}
+  template <typename R>
+  __device__ __forceinline__ void atten(R, R) {}
+  template <typename R>
+  __device__ __forceinline__ void sigma_factor(R) {}
+  template <typename R>
+  __device__ __forceinline__ void powder_atten(int, R) {}
+  template <typename R>
+  __device__ __forceinline__ void powder_peak(int, R) {}
+  template <typename R>
+  __device__ __forceinline__ void sqe(int, int, R, R, R) {}
+  template <typename R>
+  __device__ __forceinline__ void tally(const Tally& t, uint64_t bin, R p) {
+    tally_add(t, bin, p);
+  }
+};
+
+enum { kGradGuides = 2 };
+
+template <typename R>
+struct GradTrack {
+  static constexpr bool kActive = true;
+  const mcv_grad& g;
+  double* powder_x;  // [npeaks+1]: sum over neutrons reaching K peaks
+  double* powder_y;  // [npeaks]:   chosen-peak terms
+  int cur = 0, gslot = -1, is_hss = 0;
+  // per-neutron d ln p / d theta
+  R dg[kGradGuides][3];
+  R dmu, dsig;
+  int sqe_base;
+  R sqe_fx, sqe_fy, sqe_invS;
+  int pk1, pk2, peak;
+  R pc1, pc2, inv_s;
+  // per-thread gradient sums
+  double acc_g[kGradGuides][3];
+  double acc_mu, acc_sig;
+
+  int hss_comp = -1, sqe_nE = 0;
+
+  // the first HSS of the chain is the differentiated sample
+  __device__ GradTrack(const mcv_grad& grad, const mcv_chain& ch, double* px,
+                       double* py)
+      : g(grad), powder_x(px), powder_y(py) {
+    for (int c = ch.ncomp - 1; c >= 0; --c)
+      if (ch.comp[c].opcode == MCV_OP_HSS) hss_comp = c;
+    if (hss_comp >= 0) sqe_nE = ch.comp[hss_comp].ip[5];
+#pragma unroll
+    for (int s = 0; s < kGradGuides; ++s)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) acc_g[s][k] = 0.0;
+    acc_mu = acc_sig = 0.0;
+    begin_neutron();
+  }
+
+  __device__ __forceinline__ void begin_neutron() {
+#pragma unroll
+    for (int s = 0; s < kGradGuides; ++s)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) dg[s][k] = R(0);
+    dmu = dsig = R(0);
+    sqe_base = -1;
+    sqe_fx = sqe_fy = sqe_invS = R(0);
+    pk1 = pk2 = peak = -1;
+    pc1 = pc2 = inv_s = R(0);
+  }
+
+  // guides count 0, 1 in chain order; more guides are not differentiated
+  __device__ __forceinline__ void begin_component(const mcv_chain& ch,
+                                                  int c) {
+    cur = c;
+    int s = 0;
+    for (int k = 0; k < c; ++k) s += ch.comp[k].opcode == MCV_OP_GUIDE;
+    gslot = (ch.comp[c].opcode == MCV_OP_GUIDE && s < kGradGuides) ? s : -1;
+    is_hss = c == hss_comp;
+  }
+
+  // d ln R / d(m, alpha, W) of calc_reflectivity (_guide_utils.py:6-23):
+  // R = R0 (1 - tanh x)(1 - alpha (Q - Qc)) / 2, x = (Q - m Qc) / W, and
+  // d ln(1 - tanh x) / dx = -(1 + tanh x) = -2 / (1 + e^(-2x)).
+  __device__ __forceinline__ void reflect(R Q, R R0, R Qc, R alpha, R m,
+                                          R W) {
+    if (gslot < 0 || !(Q > Qc)) return;
+    R x = (Q - m * Qc) / W;
+    if (!(x < R(10))) return;
+    R one_plus_tanh = R(2) / (R(1) + m_exp(R(-2) * x));
+    R da = Q - Qc;
+    R s0 = one_plus_tanh * Qc / W, s2 = one_plus_tanh * x / W;
+    R s1 = -da / (R(1) - alpha * da);
+    if (gslot == 0) {
+      dg[0][0] += s0;
+      dg[0][1] += s1;
+      dg[0][2] += s2;
+    } else {
+      dg[1][0] += s0;
+      dg[1][1] += s1;
+      dg[1][2] += s2;
+    }
+  }
+  // attenuation exp(-(mu(v) + sigma) L): d/dmu2200 = -2200 L / v,
+  // d/dsigma = -L (a kernel with a constant scattering coefficient)
+  __device__ __forceinline__ void atten(R dmu_, R dsig_) {
+    if (!is_hss) return;
+    dmu += dmu_;
+    dsig += dsig_;
+  }
+  __device__ __forceinline__ void sigma_factor(R sigma) {
+    if (is_hss && sigma != R(0)) dsig += R(1) / sigma;
+  }
+  // powder attenuation: d ln p / d s_j = coef for the K reachable peaks
+  __device__ __forceinline__ void powder_atten(int K, R coef) {
+    if (!is_hss) return;
+    if (pk1 < 0 || pk1 == K) {
+      pk1 = K;
+      pc1 += coef;
+    } else {
+      pk2 = K;
+      pc2 += coef;
+    }
+  }
+  __device__ __forceinline__ void powder_peak(int j, R s) {
+    if (!is_hss) return;
+    peak = j;
+    inv_s = R(1) / s;
+  }
+  // bilinear S(Q,E): d ln p / d S_corner = weight_corner / S
+  __device__ __forceinline__ void sqe(int base, int nE, R fx, R fy, R S) {
+    if (!is_hss || !(S > R(0))) return;
+    sqe_base = base;
+    sqe_fx = fx;
+    sqe_fy = fy;
+    sqe_invS = R(1) / S;
+    (void)nE;
+  }
+
+  __device__ __forceinline__ void tally(const Tally&, uint64_t bin, R p) {
+    const double* d = g.dout[cur];
+    if (!d) return;
+    double gb = d[bin];
+    if (gb == 0.0) return;
+    double gp = gb * (double)p;
+#pragma unroll
+    for (int s = 0; s < kGradGuides; ++s)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) acc_g[s][k] += gp * (double)dg[s][k];
+    acc_mu += gp * (double)dmu;
+    acc_sig += gp * (double)dsig;
+    tables(gp);
+  }
+
+  __device__ __forceinline__ void tables(double gp) {
+    if (hss_comp < 0) return;
+    double* dt = g.dtable[hss_comp];
+    if (sqe_base >= 0 && dt) {
+      double w = gp * (double)sqe_invS;
+      double fx = sqe_fx, fy = sqe_fy;
+      atomicAdd(dt + sqe_base, w * (1 - fx) * (1 - fy));
+      atomicAdd(dt + sqe_base + sqe_nE, w * fx * (1 - fy));
+      atomicAdd(dt + sqe_base + 1, w * (1 - fx) * fy);
+      atomicAdd(dt + sqe_base + sqe_nE + 1, w * fx * fy);
+    }
+    if (powder_x) {
+      if (pk1 >= 0) atomicAdd(powder_x + pk1, gp * (double)pc1);
+      if (pk2 >= 0) atomicAdd(powder_x + pk2, gp * (double)pc2);
+      if (peak >= 0) atomicAdd(powder_y + peak, gp * (double)inv_s);
+    }
+  }
+
+  // warp-reduce the per-thread sums and add them to the gradient arrays
+  __device__ void flush(const mcv_chain& ch) {
+    int s = 0;
+    for (int c = 0; c < ch.ncomp; ++c) {
+      int op = ch.comp[c].opcode;
+      if (op == MCV_OP_GUIDE) {
+        if (s < kGradGuides) {
+#pragma unroll
+          for (int k = 0; k < 3; ++k) {
+            double v = s == 0 ? acc_g[0][k] : acc_g[1][k];
+            for (int o = 16; o > 0; o >>= 1)
+              v += __shfl_down_sync(0xffffffffu, v, o);
+            if ((threadIdx.x & 31) == 0 && g.dparam[c])
+              atomicAdd(g.dparam[c] + k, v);
+          }
+        }
+        ++s;
+      } else if (c == hss_comp) {
+        double v0 = acc_mu, v1 = acc_sig;
+        for (int o = 16; o > 0; o >>= 1) {
+          v0 += __shfl_down_sync(0xffffffffu, v0, o);
+          v1 += __shfl_down_sync(0xffffffffu, v1, o);
+        }
+        if ((threadIdx.x & 31) == 0 && g.dparam[c]) {
+          atomicAdd(g.dparam[c] + 0, v0);
+          atomicAdd(g.dparam[c] + 1, v1);
+        }
+      }
+    }
+  }
+};
+
+}  // namespace mcv

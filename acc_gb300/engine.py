@@ -282,3 +282,35 @@ class BatchedGraph:
             self.close()
         except Exception:
             pass
+
+
+# ------------------------------------------------------------ gradients
+def backward(chain, ncount, dout, dparam=None, dtable=None, seed=None,
+             floattype=None, first=0, threads_per_block=None, device=None):
+    """mcv_backward: replay `ncount` neutrons of `seed` and add the gradient
+    of L into the given device tensors.  dout {component index: float64
+    tensor (nbins,) = dL/d(sum p)}, dparam {index: float64 tensor (3,) for a
+    guide (m, alpha, W) or (2,) for the sample (mu, sigma)}, dtable {index:
+    float64 tensor (S(Q,E) nodes or powder peaks)}."""
+    ctx = nat.context(device)
+    g = nat.mcv_grad()
+    keep = []
+    for field, d in (("dout", dout), ("dparam", dparam or {}),
+                     ("dtable", dtable or {})):
+        arr = getattr(g, field)
+        for k, t in d.items():
+            if t.dtype.itemsize != 8 or not t.is_cuda or not t.is_contiguous():
+                raise ValueError(f"{field}[{k}] must be a contiguous CUDA "
+                                 "float64 tensor")
+            arr[k] = t.data_ptr()
+            keep.append(t)
+    st = nat.mcv_status()
+    L = _launch(threads_per_block)
+    seed = config.rng_seed if seed is None else seed
+    rc = nat.lib().mcv_backward(
+        ctx.handle, ctypes.byref(chain), ctypes.byref(g), int(ncount),
+        int(first), int(seed), _precision(floattype),
+        ctypes.byref(L) if L else None, nat.current_stream_handle(),
+        ctypes.byref(st))
+    nat.check(rc, st)
+    return st

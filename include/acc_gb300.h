@@ -275,6 +275,38 @@ int mcv_graph_launch(mcv_graph* graph, void* stream);
 int mcv_graph_destroy(mcv_graph* graph);
 
 /*
+ * Gradients of monitor tallies.  No counterpart in the reference.
+ * dout[k] (monitor k, float64 per bin) is dL/d(sum p) of that monitor's
+ * bins, NULL if the monitor is not in the loss.  Results are ADDED into:
+ *   dparam[k], GUIDE k:  {dL/dm, dL/dalpha, dL/dW}        (first two guides)
+ *   dparam[k], HSS k:    {dL/dmu_2200, dL/dsigma}  (mu at 2200 m/s, 1/m;
+ *                        sigma the constant scattering coefficient, 1/m)
+ *   dtable[k], HSS k:    SQE_GRID dL/dS (nQ*nE); POWDER dL/d my_s_v2
+ *                        (npeaks, the per-peak constant of powderdiffr.py:129)
+ * Only the first HSS of the chain is differentiated.
+ */
+typedef struct mcv_grad {
+  const double* dout[MCV_MAX_COMPONENTS];
+  double* dparam[MCV_MAX_COMPONENTS];
+  double* dtable[MCV_MAX_COMPONENTS];
+} mcv_grad;
+
+/*
+ * Backward run: replays neutrons [first, first+ncount) of the stream
+ * `seed` -- the same neutrons, random numbers and arithmetic as
+ * mcv_run_chain with the same arguments -- and accumulates the gradient of
+ * L through the tallies (see mcv_grad).  Every differentiated parameter
+ * enters only the neutron weight, so d(sum p)/d theta = sum p d ln p/d theta
+ * over the neutrons in the bin, exact for the estimator with its random
+ * numbers held fixed.  Table entries where the interpolated S is 0 receive
+ * no gradient.  Tallies are not touched.
+ */
+int mcv_backward(mcv_ctx* ctx, const mcv_chain* chain, const mcv_grad* grad,
+                 uint64_t ncount, uint64_t first, uint64_t seed,
+                 int precision, const mcv_launch* launch, void* stream,
+                 mcv_status* st);
+
+/*
  * Geometry probe: the intersection times of rays with the shape of an HSS
  * component (arrow_intersect.py render + intersect).  rays[n][6] float64;
  * out_ts[n][MCV_MAX_INTERSECTIONS] float64; out_n[n] int32.

@@ -1,0 +1,112 @@
+"""One component at a time, FP32 engine against the FP64 oracle.
+
+Each component is fed the same input neutron array (values rounded to
+float32 so that both sides start from identical numbers) in buffered mode
+(ComponentBase.process) and draws from the same Philox stream.  Tolerance:
+every neutron that leaves alive with a weight above 1e-30 (in either run)
+agrees within 1e-5 relative in every slot (denominator floored at the
+slot's RMS over the batch), except at most 1e-4 of them (paths that cross
+a branch within float rounding).  FP64 buffered runs agree within 1e-12.
+"""
+
+import numpy as np
+import pytest
+import torch
+
+from acc_gb300 import engine, instruments
+from acc_gb300.instrument import calcTransformations
+from acc_gb300.memory import HostBinder
+from helpers import oracle_run, rel_err
+
+pytestmark = pytest.mark.gpu
+
+N = 40_000
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _engine(engine_lib):
+    torch.cuda.init()
+    yield
+
+
+def transform(arr, rot, off):
+    a = arr.copy()
+    a[:, 0:3] = (a[:, 0:3] - off) @ np.asarray(rot).T
+    a[:, 3:6] = a[:, 3:6] @ np.asarray(rot).T
+    return a
+
+
+def alive(a):
+    return a[a[:, 9] > 0]
+
+
+def source_output(builder, seed=3):
+    import acc_gb300
+    ins = acc_gb300.instrument()
+    ins.append(builder().components[0])
+    _, _, out, _ = oracle_run(ins, N, seed=seed, record=True)
+    return out
+
+
+def compare(comp_factory, inputs, floattype, tol, flips):
+    from oracle import binding as O
+    inp = np.ascontiguousarray(inputs).astype(np.float32).astype(np.float64)
+    g = engine.process_buffer([comp_factory()], inp, seed=9,
+                              floattype=floattype)
+    o = O.process_buffer(engine.build_chain([comp_factory()],
+                                            binder=HostBinder()), inp, seed=9)
+    cmp = (g[:, 9] > 1e-30) | (o[:, 9] > 1e-30)
+    assert cmp.sum() > 50
+    err = rel_err(g, o)
+    worst = err.max(axis=1)
+    bad = cmp & (worst > tol)
+    k = np.argmax(np.where(cmp, worst, -1))
+    assert bad.sum() <= max(flips * cmp.sum(), 0), (
+        bad.sum(), cmp.sum(), worst[k], int(np.argmax(err[k])))
+
+
+def guide_inputs():
+    s = source_output(instruments.guide_chain)
+    return transform(s, np.eye(3), [0, 0, 1.0])
+
+
+def taper_inputs():
+    from oracle import binding as O
+    g1 = lambda: instruments.guide_chain().components[1]  # noqa: E731
+    out = O.process_buffer(engine.build_chain([g1()], binder=HostBinder()),
+                           guide_inputs(), seed=9)
+    return transform(alive(out), np.eye(3), [0, 0, 10.001])
+
+
+def sample_inputs(builder):
+    ins = builder()
+    off, rot = calcTransformations(ins)
+    return transform(source_output(builder), rot[0], off[0]), ins
+
+
+CASES = {
+    "source_disc": (lambda: instruments.guide_chain().components[0],
+                    lambda: np.zeros((N, 10))),
+    "guide_straight": (lambda: instruments.guide_chain().components[1],
+                       guide_inputs),
+    "guide_taper": (lambda: instruments.guide_chain().components[2],
+                    taper_inputs),
+    "hss_sphere_isotropic": (
+        lambda: instruments.sphere_theta_tof().components[1],
+        lambda: sample_inputs(instruments.sphere_theta_tof)[0]),
+    "hss_hollow_cylinder_sqe": (
+        lambda: instruments.sqe_hollow_cylinder().components[1],
+        lambda: sample_inputs(instruments.sqe_hollow_cylinder)[0]),
+}
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_component_fp32_within_1e5(name):
+    make, inputs = CASES[name]
+    compare(make, inputs(), "float32", 1e-5, 1e-4)
+
+
+@pytest.mark.parametrize("name", list(CASES))
+def test_component_fp64_within_1e12(name):
+    make, inputs = CASES[name]
+    compare(make, inputs(), "float64", 1e-12, 0)
