@@ -212,11 +212,14 @@ __global__ void __launch_bounds__(kMaxThreads)
 
 // Path regeneration: the same per-neutron sequence as chain_kernel, but a
 // lane whose neutron leaves the chain immediately takes the next neutron of
-// its warp's index range, and a guide advances one bounce per loop pass.
-// Lanes of a warp therefore stay busy while a few neutrons bounce many
-// times, instead of idling until the warp's longest path ends.  Every
-// neutron is computed with the same functions in the same order as in
-// chain_kernel, so results are identical neutron by neutron.
+// its warp's index range.  Each pass first moves lanes that are not inside
+// a guide through the following components up to the next guide entry
+// (a new neutron: source, transform, entry), then every lane inside a
+// guide advances one bounce in the same instruction stream.  Lanes of a
+// warp stay busy while a few neutrons bounce many times, instead of idling
+// until the warp's longest path ends.  Every neutron is computed with the
+// same functions in the same order as in chain_kernel, so results are
+// identical neutron by neutron.
 template <typename R>
 __global__ void __launch_bounds__(kMaxThreads)
     regen_kernel(const __grid_constant__ mcv_chain ch, uint64_t n,
@@ -254,40 +257,45 @@ __global__ void __launch_bounds__(kMaxThreads)
       }
     }
     if (__all_sync(kFull, c == -2)) break;
-    if (c < 0) continue;
-    const mcv_component& cp = ch.comp[c];
-    bool finished = true;  // the lane's neutron is done with component c
-    if (cp.opcode == MCV_OP_GUIDE) {
-      if (!inside) {
-        if (guide_enter<R>(nt, cp)) {
-          inside = 1;
-          nb = 0;
-          finished = guide_bounce<R>(nt, cp, trk);
-          ++nb;
+    if (c >= 0 && !inside) {
+      // advance through components up to the next guide's entry
+      for (;;) {
+        const mcv_component& cp = ch.comp[c];
+        if (cp.opcode == MCV_OP_GUIDE) {
+          if (guide_enter<R>(nt, cp)) {
+            inside = 1;
+            nb = 0;
+          }
+          break;
         }
-      } else {
-        finished = guide_bounce<R>(nt, cp, trk);
-        ++nb;
+        k.overflow += run_component<R>(nt, rng, cp, trk);
+        if (!(nt.p > 0) || c + 1 >= nc) break;
+        ++c;
+        apply_transform<R>(nt, ch, c);
       }
-      if (!finished && nb >= MCV_MAX_BOUNCES) {
-        finished = true;
-        k.overflow++;
-      }
-    } else {
-      k.overflow += run_component<R>(nt, rng, cp, trk);
-    }
-    if (finished) {
-      inside = 0;
-      if (!(nt.p > 0)) {
+      if (!inside) {  // absorbed, or through the last component
         if (m_isnan(nt.p)) k.nonfinite++;
         c = -1;
         k.processed++;
-      } else if (c + 1 < nc) {
-        ++c;
-        apply_transform<R>(nt, ch, c);
-      } else {
-        c = -1;
-        k.processed++;
+      }
+    }
+    if (inside) {
+      // one bounce, executed together by every lane inside a guide
+      bool finished = guide_bounce<R>(nt, ch.comp[c], trk);
+      if (!finished && ++nb >= MCV_MAX_BOUNCES) {
+        finished = true;
+        k.overflow++;
+      }
+      if (finished) {
+        inside = 0;
+        if (!(nt.p > 0) || c + 1 >= nc) {
+          if (m_isnan(nt.p)) k.nonfinite++;
+          c = -1;
+          k.processed++;
+        } else {
+          ++c;
+          apply_transform<R>(nt, ch, c);
+        }
       }
     }
   }

@@ -74,6 +74,7 @@ def parse_args(argv=None):
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-grad", action="store_true")
     a = ap.parse_args(argv)
     if a.warmup < 0 or a.steps < 1:
         ap.error("need --steps >= 1 and --warmup >= 0")
@@ -262,6 +263,71 @@ def batched_run(world, rank, replays=3):
             "note": "one persistent launch per CUDA-graph replay"}
 
 
+def grad_cost(name, ncount, params, reps=2):
+    """Kernel time of the FP32 forward (mcv_run_chain) and of the backward
+    replay (mcv_backward) on one workload, CUDA events, after a warm-up."""
+    import torch
+    from acc_gb300 import engine
+    from acc_gb300.autograd import GradRun
+    ins = build_instrument(name) if isinstance(name, str) else name
+    mon = [c for c in ins.components if hasattr(c, "hist_shape")][-1]
+    run = GradRun(ins, mon, ncount, seed=11, floattype="float32",
+                  params=params(ins))
+    dout = torch.randn(mon.nbins(), dtype=torch.float64, device="cuda")
+    dparam = {}
+    dtable = {}
+    for kind, target in run.params.values():
+        k = run._index(target[0] if isinstance(target, list) else target)
+        c = run.chain.comp[k]
+        if kind in ("sqe_table", "powder_F2"):
+            n = c.ip[4] * c.ip[5] if kind == "sqe_table" else c.ip[4]
+            dtable[k] = torch.zeros(n, dtype=torch.float64, device="cuda")
+        else:
+            dparam[k] = torch.zeros(3, dtype=torch.float64, device="cuda")
+
+    def fwd():
+        engine.run_chain(run.chain, ncount, seed=11, floattype="float32",
+                         sync=False)
+
+    def bwd():
+        engine.backward(run.chain, ncount, {run.mon_index: dout}, dparam,
+                        dtable, seed=11, floattype="float32")
+
+    out = {}
+    for label, fn in (("forward_ms", fwd), ("backward_ms", bwd)):
+        fn()
+        torch.cuda.synchronize()
+        best = float("inf")
+        for _ in range(reps):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            b.synchronize()
+            best = min(best, a.elapsed_time(b))
+        engine.read_status()
+        out[label] = best
+    out["bwd_over_fwd"] = out["backward_ms"] / out["forward_ms"]
+    out["neutrons"] = ncount
+    out["monitor_bins"] = mon.nbins()
+    return out
+
+
+def grad_costs():
+    from acc_gb300 import instruments
+    sqe = grad_cost(
+        "sqe_hollow_cylinder", int(1e8),
+        lambda ins: {"S": ("sqe_table", ins.components[1]),
+                     "mu": ("hss_mu", ins.components[1])})
+    pw = grad_cost(
+        instruments.powder_banked(), int(1e9),
+        lambda ins: {"F2": ("powder_F2", ins.components[5]),
+                     "m": ("guide_m", [ins.components[1],
+                                       ins.components[2]])})
+    return {"sqe_hollow_cylinder": sqe, "powder_banked": pw}
+
+
 # ---------------------------------------------------------- CPU baseline
 def cpu_oracle_rate(workload, seconds, seed, nthreads=0):
     """Neutrons/s of the CPU oracle on a bounded sample of the workload."""
@@ -402,6 +468,7 @@ def ours_arm(a, rank, world, local_rank):
     batched = None
     if not a.no_batched:
         batched = batched_run(world, rank)
+    grads = None if a.no_grad or rank != 0 else grad_costs()
 
     if rank != 0:
         return 0
@@ -464,7 +531,7 @@ def ours_arm(a, rank, world, local_rank):
             "ms_per_step": 1e3 * t_thread / a.steps,
             "note": "same FP32 kernel body without path regeneration"},
         "chi2_fp32_vs_fp64": chi2,
-        "bwd_over_fwd": None,
+        "bwd_over_fwd": grads,
         "batched": batched,
         "e2e": e2e,
         "roofline": roofline,
