@@ -86,14 +86,16 @@ __device__ __forceinline__ double reflectivity(double Q, double R0, double Qc,
   }
   return R;
 }
-// (1 - tanh(x)) / 2 == 1 / (1 + e^(2x)), which has no cancellation in float
+// (1 - tanh(x)) / 2 == 1 / (1 + e^(2x)), which has no cancellation in
+// float; expf (not the fast __expf, whose error grows with |x|) because the
+// supermirror edge is steep: d ln R / dQ = 2 / W per bounce.
 __device__ __forceinline__ float reflectivity(float Q, float R0, float Qc,
                                               float alpha, float m, float W) {
   float R = R0;
   if (Q > Qc) {
     float tmp = (Q - m * Qc) / W;
     if (tmp < 10.f)
-      R *= (1.f - alpha * (Q - Qc)) / (1.f + __expf(2.f * tmp));
+      R *= (1.f - alpha * (Q - Qc)) / (1.f + expf(2.f * tmp));
     else
       R = 0.f;
   }
@@ -167,28 +169,40 @@ __device__ __forceinline__ bool guide_bounce(Neutron<R>& n,
   R vdn = (i == 1) ? vdotn_v1 : (i == 2) ? vdotn_v2 : (i == 3) ? vdotn_h1
                                                                : vdotn_h2;
   R lw = (i <= 2) ? ww : hh;  // the mirror's slope term
-  R nlen2 = l * l + lw * lw;
-  R q, d;
-  if constexpr (sizeof(R) == 4) {
-    R rn = m_rsqrt(nlen2);
-    q = R(kV2K) * (-2) * vdn * rn;
-    d = 2 * vdn * (rn * rn);
+  R q;
+  if (sizeof(R) == 4 && lw == R(0)) {
+    // FP32, mirror parallel to z: the reflection flips one velocity
+    // component exactly, q = 2 V2K |v_perp|
+    if (i <= 2) {
+      q = R(2 * kV2K) * m_fabs(vx);
+      n.vx = -vx;
+    } else {
+      q = R(2 * kV2K) * m_fabs(vy);
+      n.vy = -vy;
+    }
   } else {
-    q = R(kV2K) * (-2) * vdn / m_sqrt(nlen2);
-    d = 2 * vdn / nlen2;
-  }
-  if (i == 1) {
-    n.vx = vx - d * l;
-    n.vz = vz - d * ww;
-  } else if (i == 2) {
-    n.vx = vx + d * l;
-    n.vz = vz - d * ww;
-  } else if (i == 3) {
-    n.vy = vy - d * l;
-    n.vz = vz - d * hh;
-  } else {
-    n.vy = vy + d * l;
-    n.vz = vz - d * hh;
+    R nlen2 = l * l + lw * lw, d;
+    if constexpr (sizeof(R) == 4) {
+      R rn = m_rsqrt(nlen2);
+      q = R(kV2K) * (-2) * vdn * rn;
+      d = 2 * vdn * (rn * rn);
+    } else {
+      q = R(kV2K) * (-2) * vdn / m_sqrt(nlen2);
+      d = 2 * vdn / nlen2;
+    }
+    if (i == 1) {
+      n.vx = vx - d * l;
+      n.vz = vz - d * ww;
+    } else if (i == 2) {
+      n.vx = vx + d * l;
+      n.vz = vz - d * ww;
+    } else if (i == 3) {
+      n.vy = vy - d * l;
+      n.vz = vz - d * hh;
+    } else {
+      n.vy = vy + d * l;
+      n.vz = vz - d * hh;
+    }
   }
   const R R0 = prm<R>(c, 5), Qc = prm<R>(c, 6), alpha = prm<R>(c, 7),
           m = prm<R>(c, 8), W = prm<R>(c, 9);

@@ -71,7 +71,8 @@ struct GradTrack {
   R dg[kGradGuides][3];
   R dmu, dsig;
   int sqe_base;
-  R sqe_fx, sqe_fy, sqe_invS;
+  R sqe_fx, sqe_fy;
+  double sqe_invS;  // 1/S can overflow float for tiny S
   int pk1, pk2, peak;
   R pc1, pc2, inv_s;
   // per-thread gradient sums
@@ -102,7 +103,8 @@ struct GradTrack {
       for (int k = 0; k < 3; ++k) dg[s][k] = R(0);
     dmu = dsig = R(0);
     sqe_base = -1;
-    sqe_fx = sqe_fy = sqe_invS = R(0);
+    sqe_fx = sqe_fy = R(0);
+    sqe_invS = 0.0;
     pk1 = pk2 = peak = -1;
     pc1 = pc2 = inv_s = R(0);
   }
@@ -171,7 +173,7 @@ struct GradTrack {
     sqe_base = base;
     sqe_fx = fx;
     sqe_fy = fy;
-    sqe_invS = R(1) / S;
+    sqe_invS = 1.0 / (double)S;
     (void)nE;
   }
 
@@ -194,7 +196,7 @@ struct GradTrack {
     if (hss_comp < 0) return;
     double* dt = g.dtable[hss_comp];
     if (sqe_base >= 0 && dt) {
-      double w = gp * (double)sqe_invS;
+      double w = gp * sqe_invS;
       double fx = sqe_fx, fy = sqe_fy;
       atomicAdd(dt + sqe_base, w * (1 - fx) * (1 - fy));
       atomicAdd(dt + sqe_base + sqe_nE, w * fx * (1 - fy));

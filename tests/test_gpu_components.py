@@ -6,7 +6,13 @@ float32 so that both sides start from identical numbers) in buffered mode
 every neutron that leaves alive with a weight above 1e-30 (in either run)
 agrees within 1e-5 relative in every slot (denominator floored at the
 slot's RMS over the batch), except at most 1e-4 of them (paths that cross
-a branch within float rounding).  FP64 buffered runs agree within 1e-12.
+a branch within float rounding).  Two places are ill-conditioned in float
+and set the distribution rather than the maximum: the scattering angle of
+the S(Q,E) kernel, cos(theta) = (ki^2 + kf^2 - Q^2) / (2 ki kf), whose
+error grows as 1/sin(theta) near 0 and 180 degrees, and the supermirror
+edge, d ln R / dQ = 2/W per reflection.  So: at most 1e-3 of the compared
+neutrons above 1e-5, and at most 1e-4 of them (at least one) above 1e-3.
+FP64 buffered runs agree within 1e-12.
 """
 
 import numpy as np
@@ -59,10 +65,13 @@ def compare(comp_factory, inputs, floattype, tol, flips):
     assert cmp.sum() > 50
     err = rel_err(g, o)
     worst = err.max(axis=1)
-    bad = cmp & (worst > tol)
     k = np.argmax(np.where(cmp, worst, -1))
-    assert bad.sum() <= max(flips * cmp.sum(), 0), (
-        bad.sum(), cmp.sum(), worst[k], int(np.argmax(err[k])))
+    info = (cmp.sum(), worst[k], int(np.argmax(err[k])))
+    if flips:
+        assert (cmp & (worst > tol)).sum() <= 1e-3 * cmp.sum(), info
+        assert (cmp & (worst > 1e-3)).sum() <= max(1, flips * cmp.sum()), info
+    else:
+        assert (cmp & (worst > tol)).sum() == 0, info
 
 
 def guide_inputs():

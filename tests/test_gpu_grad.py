@@ -6,8 +6,10 @@ differentiated parameter (they enter only neutron weights), so a central
 difference of the FP64 forward with the same seed converges to the
 replayed gradient.  Tolerances: 1e-6 relative for the coefficient-type
 parameters (central difference, step 1e-4 relative, O(step^2) truncation);
-S(Q,E) nodes enter linearly, checked to 1e-9 relative; FP32 backward
-against FP64 backward within 1e-3 relative on the largest gradients.
+S(Q,E) nodes enter linearly, checked to 1e-7 relative (the loss
+difference of a 1% node change is a sum over many bins); FP32 backward
+against FP64 backward within 1e-3 relative for dL/d ln S on the nodes
+that carry 1% or more of the largest sensitivity.
 """
 
 import numpy as np
@@ -80,7 +82,10 @@ def test_sqe_table_gradient_is_exact_for_linear_nodes():
     L.backward()
     g = S_r.grad.cpu().numpy()
     assert np.isfinite(g).all() and np.abs(g).max() > 0
-    for flat in np.argsort(-np.abs(g).ravel())[:4]:
+    # nodes whose change moves L the most (|dL/dS| S), so that a 1% change
+    # is resolved in double
+    effect = np.abs(g * S.cpu().numpy())
+    for flat in np.argsort(-effect.ravel())[:4]:
         i, j = np.unravel_index(flat, g.shape)
         base = float(S[i, j])
         Sp, Sm = S.clone(), S.clone()
@@ -89,7 +94,7 @@ def test_sqe_table_gradient_is_exact_for_linear_nodes():
         d = float(Sp[i, j]) - float(Sm[i, j])
         fd = (loss(run, w, S=Sp, mu=mu, sigma=sigma)
               - loss(run, w, S=Sm, mu=mu, sigma=sigma)) / d
-        assert g[i, j] == pytest.approx(fd, rel=1e-9, abs=1e-30), (i, j)
+        assert g[i, j] == pytest.approx(fd, rel=1e-7), (i, j)
 
 
 def test_guide_coating_gradients_match_crn_differences():
@@ -148,5 +153,10 @@ def test_fp32_backward_close_to_fp64():
         out[ft] = (S_r.grad.cpu().numpy(), float(mu_r.grad))
     g64, g32 = out["float64"], out["float32"]
     assert g32[1] == pytest.approx(g64[1], rel=1e-3)
-    big = np.abs(g64[0]) > 1e-2 * np.abs(g64[0]).max()
-    np.testing.assert_allclose(g32[0][big], g64[0][big], rtol=1e-3)
+    # compare dL/d ln S = S dL/dS: where S is tiny (far tails) the FP32
+    # weights are subnormal and dL/dS is large but moves L by nothing
+    S = sqe_run()[2].cpu().numpy()
+    e64, e32 = g64[0] * S, g32[0] * S
+    big = np.abs(e64) > 1e-2 * np.abs(e64).max()
+    assert big.sum() > 100
+    np.testing.assert_allclose(e32[big], e64[big], rtol=1e-3)
