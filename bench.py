@@ -48,14 +48,17 @@ WORKLOADS = {
         "200x200 S(Q,E) -> 3 m cylinder I(Q,E) 100x100"),
 }
 
-# Executed FP32 arithmetic (2*FFMA + FADD + FMUL, thread level) and warp
-# instructions per neutron of the FP32 chain kernel, counted by ncu on the
-# same workload (profiles/chain_kernel_fp32_guide_chain.md).  None until
-# a capture exists.
+# Per-neutron counts of the FP32 path-regeneration kernel on this workload,
+# from one ncu --set full capture of a 1e7-neutron launch (456 blocks x 256
+# threads): executed FP32 arithmetic (2*FFMA + FADD + FMUL, thread level),
+# warp instructions issued, and the DRAM bytes of that launch (tally bins
+# touched; it does not grow with the neutron count).
 KERNEL_COUNTS = {
-    "guide_chain": {"fp32_flops_per_neutron": None,
-                    "warp_inst_per_neutron": None,
-                    "dram_bytes_per_neutron": None},
+    "guide_chain": {"fp32_flops_per_neutron": 160.47,
+                    "warp_inst_per_neutron": 51.65,
+                    "thread_inst_per_neutron": 635.9,
+                    "dram_bytes_per_launch": 130048,
+                    "captured_neutrons": 10_000_000},
 }
 
 
@@ -487,19 +490,38 @@ def ours_arm(a, rank, world, local_rank):
     counts = KERNEL_COUNTS.get(a.workload, {})
     fpn = counts.get("fp32_flops_per_neutron")
     achieved = fpn * ncount / mean_s / 1e12 if fpn else None
-    dbn = counts.get("dram_bytes_per_neutron")
     roofline = {
         "bound": "compute",
         "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
         "frac": achieved / fp32_peak if achieved else None,
-        "traffic": dbn * ncount if dbn is not None else None,
+        "traffic": counts.get("dram_bytes_per_launch"),
         "kernel": "mcv::regen_kernel<float>",
         "peak_source": "FP32 FMA peak measured in this run "
                        "(mcv_probe_fma_peak); the measured peak file has "
                        "HBM and bf16-tensor peaks only",
-        "per_unit": "executed FP32 flops per neutron counted by ncu",
+        "per_unit": f"{fpn} executed FP32 flops per neutron (ncu count)",
+        "traffic_note": "DRAM bytes of one launch from ncu on a "
+                        f"{counts.get('captured_neutrons')}-neutron launch: "
+                        "the tally bins, independent of the neutron count",
         "fp64_peak_tflops": fp64_peak,
     }
+    wpn = counts.get("warp_inst_per_neutron")
+    if wpn and clk and clk.get("sm_mhz"):
+        # the binding limit: one warp instruction per cycle per SM sub-
+        # partition (4 per SM); divergence (SIMT efficiency) sets how many
+        # warp instructions a neutron costs
+        sms = torch.cuda.get_device_properties(
+            torch.cuda.current_device()).multi_processor_count
+        peak_issue = sms * 4 * clk["sm_mhz"] * 1e6
+        got = wpn * ncount / mean_s
+        roofline["issue"] = {
+            "achieved": got, "peak": peak_issue, "unit": "warp-inst/s",
+            "frac": got / peak_issue,
+            "per_unit": f"{wpn} warp instructions per neutron (ncu count), "
+                        f"{counts.get('thread_inst_per_neutron')} thread "
+                        "instructions",
+            "peak_source": "SMs x 4 issue slots x median SM clock sampled "
+                           "during the timed region"}
     cpu = None
     if world == 1 and not a.no_cpu_baseline:
         rate, n, cores = cpu_oracle_rate(a.workload, a.cpu_seconds, a.seed)

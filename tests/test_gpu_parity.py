@@ -12,9 +12,10 @@ Tolerances (stated per test):
    rounding).  The per-component bound is 1e-5 (test_gpu_components.py);
    over a chain with tens of reflections and a 3 m flight after a sample
    the float rounding of each component adds up.  Neutrons dead in both runs
-   are compared only by exit component (>= 99% equal): a float weight
-   underflows (< 1e-38) a few bounces earlier than a double one, which
-   moves the recorded state of an already-negligible neutron.
+   are compared only by exit component (>= 99% equal), leaving out those
+   the oracle ends with a positive weight below 1e-30: a float weight
+   underflows to 0 (S(Q,E) tail values, many guide bounces) where a double
+   one does not, and p <= 0 stops the neutron one component earlier.
  * Independent streams: chi^2/dof <= 1.1 between FP32 GPU and FP64 oracle
    histograms for monitors with >= 2000 populated bins; with fewer bins the
    bound is 1.1 + 3 sqrt(2/dof) (three standard deviations of chi^2/dof).
@@ -99,7 +100,12 @@ def test_fp32_same_stream_within_1e4(name):
     assert (cmp & (err > 1e-4)).sum() <= 1e-3 * cmp.sum(), info
     bad = cmp & ((g_last != o_last) | (err > 1e-3))
     assert bad.sum() <= max(2, 1e-4 * cmp.sum()), info
-    dead = ~cmp
+    # neutrons the oracle ends with a positive weight below 1e-30 can
+    # underflow to 0 in float (S(Q,E) tails: p * S below the smallest
+    # subnormal) and so stop one component earlier; the rest of the dead
+    # ones stop at the same component
+    tiny = (o_out[:, 9] > 0) & (o_out[:, 9] <= 1e-30)
+    dead = ~cmp & ~tiny
     if dead.any():
         assert (g_last[dead] == o_last[dead]).mean() >= 0.99
 
