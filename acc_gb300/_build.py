@@ -16,7 +16,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libacc_gb300.so")
 
-SOURCES = ["engine.cu", "launch_fp32.cu", "launch_fp64.cu", "probe.cu"]
+SOURCES = ["engine.cu", "launch_fp32.cu", "launch_fp64.cu", "probe.cu",
+           "noalloc.cu"]
 HEADERS = ["common.cuh", "components.cuh", "sample.cuh", "monitors.cuh",
            "kernels.cuh"]
 # per-source extra flags: the FP64 kernels round every multiply and add

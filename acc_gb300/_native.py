@@ -17,6 +17,7 @@ MCV_NIPARAM = 8
 MCV_MAX_INTERSECTIONS = 10
 MCV_MAX_BOUNCES = 100000
 MCV_MAX_VARIANTS = 1024
+MCV_NOALLOC_MAX_VARIANTS = 64
 
 MCV_OK, MCV_EINVAL, MCV_ECUDA, MCV_ECOUNT, MCV_EBOUNCE = 0, 1, 2, 3, 4
 MCV_ENONFINITE, MCV_EBIN, MCV_ENODEV, MCV_ECAPACITY = 5, 6, 7, 8
@@ -147,6 +148,10 @@ _SIGNATURES = {
         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,
         ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(mcv_launch),
         ctypes.POINTER(ctypes.c_void_p)]),
+    "mcv_run_batched_noalloc": (ctypes.c_int, [
+        ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+        ctypes.c_int, ctypes.POINTER(mcv_launch), ctypes.c_void_p,
+        ctypes.POINTER(mcv_status)]),
     "mcv_graph_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "mcv_graph_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "mcv_backward": (ctypes.c_int, [

@@ -302,6 +302,11 @@ uint64_t sum_counts(const uint64_t* counts, int nvar) {
 
 }  // namespace
 
+// chain validation for the other entry-point unit (noalloc.cu)
+int mcv::validate_chain_for(const mcv_chain* ch, mcv_status* st) {
+  return validate_chain(ch, st);
+}
+
 extern "C" {
 
 int mcv_abi_version(void) { return MCV_ABI_VERSION; }

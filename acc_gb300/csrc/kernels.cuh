@@ -502,6 +502,9 @@ inline int occupancy_of(K kernel, int threads, size_t smem) {
   return per_sm < 1 ? 1 : per_sm;
 }
 
+// the chain validation of the entry points (engine.cu)
+int validate_chain_for(const mcv_chain* ch, mcv_status* st);
+
 // the one kernel that is not per-precision: instantiated in launch_fp64.cu
 void powder_finalize(const double* px, const double* py, int npeaks,
                      double* dtable, cudaStream_t s);

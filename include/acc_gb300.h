@@ -275,6 +275,31 @@ int mcv_graph_launch(mcv_graph* graph, void* stream);
 int mcv_graph_destroy(mcv_graph* graph);
 
 /*
+ * mcv_run_batched without any allocation.  No counterpart in the reference.
+ * For callers that must not allocate device memory: a plugin inside a host
+ * application that hands out every byte of device memory from its own pool,
+ * or a caller that cannot take the device-wide synchronisation of freeing
+ * and re-allocating a growing staging buffer.  Same arguments and results as
+ * mcv_run_batched, but no context: the variant descriptions, counts, seeds,
+ * counters and work-queue head live in one static device array of
+ * MCV_NOALLOC_MAX_VARIANTS variants (about 0.7 MB, held by every GPU that
+ * loads the library until the process exits); more variants are rejected
+ * with MCV_ECAPACITY.  The first call on a device looks up the array's
+ * device address, so make that first call before any stream capture.  The
+ * call itself zeroes the counters and the work-queue head in the array
+ * before its launch; the tallies add to what they hold, as with
+ * mcv_run_batched.  Every call shares the one array: calls that overlap on
+ * the GPU (other streams, other host threads) race, so order them on one
+ * stream.  st != NULL synchronises the stream and reads the counters back;
+ * with st == NULL they are lost when the next call clears them.
+ */
+#define MCV_NOALLOC_MAX_VARIANTS 64
+int mcv_run_batched_noalloc(const mcv_chain* variants, int32_t nvariants,
+                            const uint64_t* counts, const uint64_t* seeds,
+                            int precision, const mcv_launch* launch,
+                            void* stream, mcv_status* st);
+
+/*
  * Gradients of monitor tallies.  No counterpart in the reference.
  * dout[k] (monitor k, float64 per bin) is dL/d(sum p) of that monitor's
  * bins, NULL if the monitor is not in the loss.  Results are ADDED into:
