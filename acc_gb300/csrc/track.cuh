@@ -20,20 +20,49 @@ struct Tally {
   uint64_t nbins;
 };
 
+// Warp-aggregated tally: the lanes that reach this call together and hit the
+// same bin of the same tally (__match_any_sync on the bin's address) add
+// their count, p and p^2 in a tree inside the warp, and one lane (the
+// group's lowest) makes the three global atomics.  A transmitted beam puts
+// a large share of all neutrons into a few bins; without aggregation those
+// become same-address atomics serialised in one L2 slice.  When no two
+// lanes share a bin the call is three plain atomics per lane.
 __device__ __forceinline__ void tally_add(const Tally& t, uint64_t bin,
                                           double p) {
   if (!t.out) return;
-  atomicAdd(t.out + bin, 1.0);
-  atomicAdd(t.out + t.nbins + bin, p);
-  atomicAdd(t.out + 2 * t.nbins + bin, p * p);
+  double* a = t.out + bin;
+  const unsigned mask = __activemask();
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned peers =
+      __match_any_sync(mask, (unsigned long long)(uintptr_t)a);
+  const unsigned me = 1u << lane;
+  double s1 = p, s2 = p * p;
+  if (!__all_sync(mask, peers == me)) {
+    // tree over ranks within the group: rank r adds rank r + k while
+    // r is a multiple of 2k; the group's lowest lane ends with the sum
+    const int size = __popc(peers);
+    const int rank = __popc(peers & (me - 1u));
+    const int most = __reduce_max_sync(mask, (unsigned)size);
+    for (int k = 1; k < most; k <<= 1) {
+      const unsigned src = __fns(peers, lane, k + 1);
+      const unsigned from = src < 32u ? src : lane;
+      const double o1 = __shfl_sync(mask, s1, from);
+      const double o2 = __shfl_sync(mask, s2, from);
+      if ((rank & (2 * k - 1)) == 0 && rank + k < size) {
+        s1 += o1;
+        s2 += o2;
+      }
+    }
+    if (peers & (me - 1u)) return;  // not the group's lowest lane
+  }
+  atomicAdd(a, (double)__popc(peers));
+  atomicAdd(a + t.nbins, s1);
+  atomicAdd(a + 2 * t.nbins, s2);
 }
 __device__ __forceinline__ void tally_add(const Tally& t, uint64_t bin,
                                           float p) {
-  if (!t.out) return;
-  atomicAdd(t.out + bin, 1.0);
-  const double pd = (double)p;
-  atomicAdd(t.out + t.nbins + bin, pd);
-  atomicAdd(t.out + 2 * t.nbins + bin, pd * pd);
+  // p^2 is formed in double: a float weight of 1e-25 would underflow
+  tally_add(t, bin, (double)p);
 }
 
 struct NoTrack {

@@ -46,6 +46,10 @@ WORKLOADS = {
     "sqe_hollow_cylinder": (
         "sqe_hollow_cylinder: 60 meV 1x1 cm beam -> hollow cylinder with "
         "200x200 S(Q,E) -> 3 m cylinder I(Q,E) 100x100"),
+    "powder_banked": (
+        "powder_banked: the guide_chain guides -> powder cylinder r=0.5 cm "
+        "h=4 cm, 50 peaks -> banked detector R=3 m, 8 banks x 128 tubes x "
+        "256 pixels x 1000 tof bins (2.62e8 bins)"),
 }
 
 # Per-neutron counts of the FP32 path-regeneration kernel on this workload,
@@ -54,10 +58,10 @@ WORKLOADS = {
 # warp instructions issued, and the DRAM bytes of that launch (tally bins
 # touched; it does not grow with the neutron count).
 KERNEL_COUNTS = {
-    "guide_chain": {"fp32_flops_per_neutron": 160.47,
-                    "warp_inst_per_neutron": 51.65,
-                    "thread_inst_per_neutron": 635.9,
-                    "dram_bytes_per_launch": 130048,
+    "guide_chain": {"fp32_flops_per_neutron": 151.63,
+                    "warp_inst_per_neutron": 51.73,
+                    "thread_inst_per_neutron": 623.0,
+                    "dram_bytes_per_launch": 129024,
                     "captured_neutrons": 10_000_000},
 }
 
@@ -476,13 +480,14 @@ def ours_arm(a, rank, world, local_rank):
     if rank != 0:
         return 0
 
-    from acc_gb300.stats import chi2_per_dof
+    from acc_gb300.stats import chi2_per_dof, z_summary
     chi2 = {}
     names = [c.name for c in ins32.components if isinstance(c, MonitorBase)]
     for nm, g32, g64 in zip(names, tallies[0], tallies[1]):
-        c2, dof = chi2_per_dof(g32.cpu().numpy().reshape(3, -1),
-                               g64.cpu().numpy().reshape(3, -1))
-        chi2[nm] = {"chi2_per_dof": c2, "bins": dof}
+        a = g32.cpu().numpy().reshape(3, -1)
+        b = g64.cpu().numpy().reshape(3, -1)
+        c2, dof = chi2_per_dof(a, b)
+        chi2[nm] = {"chi2_per_dof": c2, "bins": dof, "z": z_summary(a, b)}
 
     fp32_peak = engine.probe_fma_peak(32)
     fp64_peak = engine.probe_fma_peak(64)

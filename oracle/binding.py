@@ -63,6 +63,10 @@ def lib():
             ctypes.c_void_p, c_double_p, ctypes.c_uint64, ctypes.c_uint64,
             ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(ctypes.c_uint64)]
         L.oracle_process_buffer.restype = ctypes.c_int
+        L.oracle_guide_reflections.argtypes = [
+            ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,
+            ctypes.c_int, ctypes.c_void_p, ctypes.c_int]
+        L.oracle_guide_reflections.restype = ctypes.c_int
         L.oracle_guide_one.argtypes = [ctypes.c_void_p, c_double_p]
         L.oracle_guide_one.restype = ctypes.c_int
         L.oracle_source_one.argtypes = [ctypes.c_void_p, ctypes.c_void_p, c_double_p]
@@ -218,6 +222,20 @@ def run_chain(chain, ncount, seed=1, first=0, uniforms=None, record=False,
         raise RuntimeError(f"oracle_run_chain failed ({rc}); stats {list(stats)}")
     return ({"processed": stats[0], "bounce_overflow": stats[1],
              "nonfinite": stats[2]}, out, last)
+
+
+def guide_reflections(chain, ncount, seed=1, first=0, nbins=64,
+                      nthreads=0):
+    """Histogram (ncomp, nbins) of reflections per guide traversal: row k
+    counts the neutrons that entered guide component k by how many
+    reflections they made there (last bin: nbins - 1 or more)."""
+    h = np.zeros((chain.ncomp, nbins), dtype=np.uint64)
+    rc = lib().oracle_guide_reflections(ctypes.byref(chain), int(ncount),
+                                        int(first), int(seed), int(nthreads),
+                                        h.ctypes.data, int(nbins))
+    if rc != 0:
+        raise RuntimeError(f"oracle_guide_reflections failed ({rc})")
+    return h
 
 
 def process_buffer(chain, neutrons, seed=1, first=0, nthreads=0):

@@ -273,8 +273,9 @@ double oracle_reflectivity(double Q, double R0, double Qc, double alpha,
 }
 
 /* Guide.propagate (acc/components/optics/guide.py:66-162).  Returns 1 if
- * the bounce loop ran out. */
-static int guide(neutron_t* n, const mcv_component* c) {
+ * the bounce loop ran out.  *nrefl (if given) = reflections made, -1 when
+ * the neutron misses the opening. */
+static int guide(neutron_t* n, const mcv_component* c, int* nrefl) {
   const double* d = c->dp;
   double ww = d[0], hh = d[1], hw1 = d[2], hh1 = d[3], l = d[4];
   double R0 = d[5], Qc = d[6], alpha = d[7], m = d[8], W = d[9];
@@ -285,11 +286,12 @@ static int guide(neutron_t* n, const mcv_component* c) {
   y += vy * dt;
   z = 0.;
   t += dt;
+  if (nrefl) *nrefl = -1;
   if (x <= -hw1 || x >= hw1 || y <= -hh1 || y >= hh1) {
     n->p = -1; /* absorb (acc/neutron.py:25-28) */
     return 0;
   }
-  int overflow = 1;
+  int overflow = 1, refl = 0;
   for (int nb = 0; nb < MCV_MAX_BOUNCES; ++nb) {
     double av = l * vx, bv = ww * vz, ah = l * vy, bh = hh * vz;
     double vdotn_v1 = bv + av, vdotn_v2 = bv - av;
@@ -347,8 +349,10 @@ static int guide(neutron_t* n, const mcv_component* c) {
     }
     double R = oracle_reflectivity(q, R0, Qc, alpha, m, W);
     prob *= R;
+    ++refl;
     if (prob <= 0) { overflow = 0; break; }
   }
+  if (nrefl) *nrefl = refl;
   n->x = x; n->y = y; n->z = z;
   n->vx = vx; n->vy = vy; n->vz = vz;
   n->t = t;
@@ -1301,7 +1305,7 @@ static void run_component(neutron_t* n, rng_t* rng, const mcv_component* c,
   switch (c->opcode) {
     case MCV_OP_ARM: break;
     case MCV_OP_SOURCE_SIMPLE: source_simple(n, rng, c); break;
-    case MCV_OP_GUIDE: st->bounce_overflow += guide(n, c); break;
+    case MCV_OP_GUIDE: st->bounce_overflow += guide(n, c, NULL); break;
     case MCV_OP_HSS: hss(n, rng, c); break;
     case MCV_OP_PSD_MONITOR: psd_monitor(n, c, tl); break;
     case MCV_OP_PSD_MONITOR_4PI: psd_monitor_4pi(n, c, tl); break;
@@ -1420,6 +1424,55 @@ int oracle_run_chain(const mcv_chain* chain, uint64_t ncount, uint64_t first,
 }
 
 /*
+ * Reflections per guide traversal: hist[k * nbins + min(r, nbins - 1)]
+ * counts the neutrons that entered guide component k and made r
+ * reflections there (the last bin collects r >= nbins - 1).  Same streams
+ * and sequence as oracle_run_chain, without tallies; used to describe the
+ * divergence of the guide chain, not to check results.
+ */
+int oracle_guide_reflections(const mcv_chain* chain, uint64_t ncount,
+                             uint64_t first, uint64_t seed, int nthreads,
+                             uint64_t* hist, int nbins) {
+  int nc = chain->ncomp;
+  if (nc < 1 || nc > MCV_MAX_COMPONENTS || nbins < 1 || !hist)
+    return MCV_EINVAL;
+#ifdef _OPENMP
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+#else
+  nthreads = 1;
+#endif
+  memset(hist, 0, sizeof(uint64_t) * (size_t)nc * nbins);
+#pragma omp parallel num_threads(nthreads)
+  {
+    uint64_t* h = (uint64_t*)calloc((size_t)nc * nbins, sizeof(uint64_t));
+    ostat_t st = {0, 0, 0, 0};
+#pragma omp for schedule(static)
+    for (int64_t ii = 0; ii < (int64_t)ncount; ++ii) {
+      rng_t rng;
+      rng_init(&rng, seed, first + (uint64_t)ii, 0, NULL, 0);
+      neutron_t n;
+      memset(&n, 0, sizeof n);
+      for (int k = 0; k < nc; ++k) {
+        const mcv_component* c = &chain->comp[k];
+        if (k > 0) apply_transform(&n, chain->rot[k], chain->off[k]);
+        if (c->opcode == MCV_OP_GUIDE) {
+          int r;
+          guide(&n, c, &r);
+          if (r >= 0) h[(size_t)k * nbins + (r < nbins ? r : nbins - 1)]++;
+        } else {
+          run_component(&n, &rng, c, NULL, &st);
+        }
+        if (!(n.p > 0)) break;
+      }
+    }
+#pragma omp critical
+    for (size_t b = 0; b < (size_t)nc * nbins; ++b) hist[b] += h[b];
+    free(h);
+  }
+  return MCV_OK;
+}
+
+/*
  * Buffered mode (ComponentBase.process, ComponentBase.py:79-129): apply the
  * components to neutrons[n][10] in place; component k draws from stream k+1.
  * Neutrons whose weight is not positive are skipped by later components.
@@ -1476,7 +1529,7 @@ int oracle_process_buffer(const mcv_chain* chain, double* neutrons, uint64_t n,
 
 /* single-component probes used by the known-answer tests */
 int oracle_guide_one(const mcv_component* c, double* st) {
-  return guide((neutron_t*)st, c);
+  return guide((neutron_t*)st, c, NULL);
 }
 void oracle_source_one(const mcv_component* c, const float* u, double* st) {
   rng_t rng;

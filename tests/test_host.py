@@ -143,3 +143,25 @@ def test_sharding_ranges_cover_exactly():
         for f, c in parts:
             assert f == pos
             pos += c
+
+
+def test_chi2_and_z_scores_of_independent_tallies():
+    from acc_gb300.stats import chi2_per_dof, z_summary
+    rng = np.random.default_rng(0)
+
+    def tally(n):
+        # 400 bins, Poisson entries with exponential weights
+        cnt = rng.poisson(200, 400).astype(float)
+        w = [rng.exponential(1.0, int(c)) for c in cnt]
+        return np.stack([cnt, [x.sum() for x in w],
+                         [(x * x).sum() for x in w]])
+
+    a, b = tally(0), tally(0)
+    c2, dof = chi2_per_dof(a, b)
+    z = z_summary(a, b)
+    assert dof == 400 and abs(c2 - 1) < 0.25
+    assert abs(z["mean_z"]) < 0.2 and abs(z["std_z"] - 1) < 0.15
+    assert z["frac_abs_z_gt_3"] < 0.02
+    b2 = b.copy()
+    b2[1] *= 1.5  # a 50% bias is seen
+    assert chi2_per_dof(a, b2)[0] > 3
