@@ -43,6 +43,7 @@ CSG_PRIMITIVE, CSG_DIFFERENCE, CSG_UNION, CSG_INTERSECTION = 0, 1, 2, 3
 KERNEL_ISOTROPIC, KERNEL_POWDER, KERNEL_SQE_GRID = 1, 2, 3
 
 FLAG_IDENTITY_ROT = 1
+FLAG_AGGREGATE = 2
 FP32, FP64 = 32, 64
 
 
@@ -64,6 +65,8 @@ class mcv_chain(ctypes.Structure):
     _fields_ = [
         ("ncomp", ctypes.c_int32),
         ("flags", ctypes.c_int32),
+        ("weight_exp2", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
         ("comp", mcv_component * MCV_MAX_COMPONENTS),
         ("rot", (ctypes.c_double * 9) * MCV_MAX_COMPONENTS),
         ("off", (ctypes.c_double * 3) * MCV_MAX_COMPONENTS),

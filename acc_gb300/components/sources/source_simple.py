@@ -46,6 +46,14 @@ class Source_simple(SourceBase):
             xw, yh, dist, pmul,
         )
 
+    def nominal_weight(self):
+        """The weight of a neutron aimed at the target's centre:
+        pmul * xw * yh / dist^2 (propagate, source_simple.py:143-161)."""
+        xw, yh, dist, pmul = self.propagate_params[9:13]
+        if dist <= 0 or xw <= 0 or yh <= 0:
+            return None
+        return pmul * xw * yh / (dist * dist)
+
     def pack(self, c, binder):
         (square, width, height, radius, wl_distr, Lambda0, dLambda, E0, dE,
          xw, yh, dist, pmul) = self.propagate_params

@@ -128,22 +128,80 @@ __device__ __forceinline__ bool guide_enter(Neutron<R>& n,
   return true;
 }
 
-// one pass of the bounce loop; true when the neutron has left the guide
-// (it stays at its last reflection point, guide.py:122-123) or its weight
-// is gone
-template <typename R, typename Trk>
-__device__ __forceinline__ bool guide_bounce(Neutron<R>& n,
-                                             const mcv_component& c,
-                                             Trk& trk) {
-  const R ww = prm<R>(c, 0), hh = prm<R>(c, 1), hw1 = prm<R>(c, 2),
-          hh1 = prm<R>(c, 3), l = prm<R>(c, 4);
-  R x = n.x, y = n.y, z = n.z, vx = n.vx, vy = n.vy, vz = n.vz;
-  R av = l * vx, bv = ww * vz, ah = l * vy, bh = hh * vz;
-  R vdotn_v1 = bv + av, vdotn_v2 = bv - av;
-  R vdotn_h1 = bh + ah, vdotn_h2 = bh - ah;
-  R cv1 = -hw1 * l - z * ww, cv2 = x * l;
-  R ch1 = -hh1 * l - z * hh, ch2 = y * l;
-  R t1 = (l - z) / vz, t2;
+// One pass of the bounce loop in FP32, without branches: lanes of a warp
+// reach the same bounce with different walls ahead, so every candidate
+// time is formed and the earliest is kept by selects (same comparison order
+// as the reference, guide.py:100-123); the reflection and the reflectivity
+// are selected the same way.  Division by a zero normal product gives an
+// infinity that the "approaching" test never selects.
+template <typename Trk>
+__device__ __forceinline__ bool guide_bounce_fp32(Neutron<float>& n,
+                                                  const mcv_component& c,
+                                                  Trk& trk) {
+  const float ww = prm<float>(c, 0), hh = prm<float>(c, 1),
+              hw1 = prm<float>(c, 2), hh1 = prm<float>(c, 3),
+              l = prm<float>(c, 4);
+  const float x = n.x, y = n.y, z = n.z, vx = n.vx, vy = n.vy, vz = n.vz;
+  const float av = l * vx, bv = ww * vz, ah = l * vy, bh = hh * vz;
+  const float vn1 = bv + av, vn2 = bv - av, vn3 = bh + ah, vn4 = bh - ah;
+  const float cv1 = -hw1 * l - z * ww, cv2 = x * l;
+  const float ch1 = -hh1 * l - z * hh, ch2 = y * l;
+  float t1 = (l - z) / vz;
+  int i = 0;
+  const float s1 = (cv1 - cv2) / vn1, s2 = (cv1 + cv2) / vn2;
+  const float s3 = (ch1 - ch2) / vn3, s4 = (ch1 + ch2) / vn4;
+  if (vn1 < 0.f && s1 < t1) { t1 = s1; i = 1; }
+  if (vn2 < 0.f && s2 < t1) { t1 = s2; i = 2; }
+  if (vn3 < 0.f && s3 < t1) { t1 = s3; i = 3; }
+  if (vn4 < 0.f && s4 < t1) { t1 = s4; i = 4; }
+  if (i == 0) return true;  // the neutron left the guide
+  n.x = fmaf(vx, t1, x);
+  n.y = fmaf(vy, t1, y);
+  n.z = fmaf(vz, t1, z);
+  n.t.add(t1);
+  const bool xw = i <= 2;
+  const float vdn = i == 1 ? vn1 : i == 2 ? vn2 : i == 3 ? vn3 : vn4;
+  const float lw = xw ? ww : hh;
+  // mirror parallel to z: the reflection flips one component exactly,
+  // q = 2 V2K |v_perp|; inclined mirror: v -= 2 (v.n) n / |n|^2
+  const float rn = rsqrtf(fmaf(l, l, lw * lw));
+  const float d = 2.f * vdn * (rn * rn);
+  const float sg = (i == 1 || i == 3) ? -1.f : 1.f;
+  const bool flat = lw == 0.f;
+  const float vperp = xw ? vx : vy;
+  const float q = flat ? float(2 * kV2K) * fabsf(vperp)
+                       : float(kV2K) * (-2.f) * vdn * rn;
+  const float vperp_new = flat ? -vperp : fmaf(sg * d, l, vperp);
+  n.vx = xw ? vperp_new : vx;
+  n.vy = xw ? vy : vperp_new;
+  n.vz = flat ? vz : fmaf(-d, lw, vz);
+  const float R0 = prm<float>(c, 5), Qc = prm<float>(c, 6),
+              alpha = prm<float>(c, 7), m = prm<float>(c, 8),
+              W = prm<float>(c, 9);
+  trk.reflect(q, R0, Qc, alpha, m, W);
+  // calc_reflectivity (_guide_utils.py:6-23) with (1 - tanh x) / 2 =
+  // 1 / (1 + e^(2x)), evaluated for every lane and selected
+  const float tmp = (q - m * Qc) / W;
+  const float edge = R0 * (1.f - alpha * (q - Qc)) / (1.f + expf(2.f * tmp));
+  const float refl = q > Qc ? (tmp < 10.f ? edge : 0.f) : R0;
+  n.p *= refl;
+  return n.p <= 0.f;
+}
+
+// One pass of the bounce loop in FP64, in the reference's operation order.
+template <typename Trk>
+__device__ __forceinline__ bool guide_bounce_fp64(Neutron<double>& n,
+                                                  const mcv_component& c,
+                                                  Trk& trk) {
+  const double ww = c.dp[0], hh = c.dp[1], hw1 = c.dp[2], hh1 = c.dp[3],
+               l = c.dp[4];
+  double x = n.x, y = n.y, z = n.z, vx = n.vx, vy = n.vy, vz = n.vz;
+  double av = l * vx, bv = ww * vz, ah = l * vy, bh = hh * vz;
+  double vdotn_v1 = bv + av, vdotn_v2 = bv - av;
+  double vdotn_h1 = bh + ah, vdotn_h2 = bh - ah;
+  double cv1 = -hw1 * l - z * ww, cv2 = x * l;
+  double ch1 = -hh1 * l - z * hh, ch2 = y * l;
+  double t1 = (l - z) / vz, t2;
   int i = 0;
   if (vdotn_v1 < 0) {
     t2 = (cv1 - cv2) / vdotn_v1;
@@ -166,49 +224,43 @@ __device__ __forceinline__ bool guide_bounce(Neutron<R>& n,
   n.y = y + vy * t1;
   n.z = z + vz * t1;
   n.t.add(t1);
-  R vdn = (i == 1) ? vdotn_v1 : (i == 2) ? vdotn_v2 : (i == 3) ? vdotn_h1
-                                                               : vdotn_h2;
-  R lw = (i <= 2) ? ww : hh;  // the mirror's slope term
-  R q;
-  if (sizeof(R) == 4 && lw == R(0)) {
-    // FP32, mirror parallel to z: the reflection flips one velocity
-    // component exactly, q = 2 V2K |v_perp|
-    if (i <= 2) {
-      q = R(2 * kV2K) * m_fabs(vx);
-      n.vx = -vx;
-    } else {
-      q = R(2 * kV2K) * m_fabs(vy);
-      n.vy = -vy;
-    }
+  double vdn = (i == 1) ? vdotn_v1 : (i == 2) ? vdotn_v2 : (i == 3) ? vdotn_h1
+                                                                   : vdotn_h2;
+  double lw = (i <= 2) ? ww : hh;  // the mirror's slope term
+  double nlen2 = l * l + lw * lw;
+  double q = kV2K * (-2) * vdn / sqrt(nlen2);
+  double d = 2 * vdn / nlen2;
+  if (i == 1) {
+    n.vx = vx - d * l;
+    n.vz = vz - d * ww;
+  } else if (i == 2) {
+    n.vx = vx + d * l;
+    n.vz = vz - d * ww;
+  } else if (i == 3) {
+    n.vy = vy - d * l;
+    n.vz = vz - d * hh;
   } else {
-    R nlen2 = l * l + lw * lw, d;
-    if constexpr (sizeof(R) == 4) {
-      R rn = m_rsqrt(nlen2);
-      q = R(kV2K) * (-2) * vdn * rn;
-      d = 2 * vdn * (rn * rn);
-    } else {
-      q = R(kV2K) * (-2) * vdn / m_sqrt(nlen2);
-      d = 2 * vdn / nlen2;
-    }
-    if (i == 1) {
-      n.vx = vx - d * l;
-      n.vz = vz - d * ww;
-    } else if (i == 2) {
-      n.vx = vx + d * l;
-      n.vz = vz - d * ww;
-    } else if (i == 3) {
-      n.vy = vy - d * l;
-      n.vz = vz - d * hh;
-    } else {
-      n.vy = vy + d * l;
-      n.vz = vz - d * hh;
-    }
+    n.vy = vy + d * l;
+    n.vz = vz - d * hh;
   }
-  const R R0 = prm<R>(c, 5), Qc = prm<R>(c, 6), alpha = prm<R>(c, 7),
-          m = prm<R>(c, 8), W = prm<R>(c, 9);
+  const double R0 = c.dp[5], Qc = c.dp[6], alpha = c.dp[7], m = c.dp[8],
+               W = c.dp[9];
   trk.reflect(q, R0, Qc, alpha, m, W);
   n.p *= reflectivity(q, R0, Qc, alpha, m, W);
   return n.p <= 0;
+}
+
+// one pass of the bounce loop; true when the neutron has left the guide
+// (it stays at its last reflection point, guide.py:122-123) or its weight
+// is gone
+template <typename R, typename Trk>
+__device__ __forceinline__ bool guide_bounce(Neutron<R>& n,
+                                             const mcv_component& c,
+                                             Trk& trk) {
+  if constexpr (sizeof(R) == 4)
+    return guide_bounce_fp32(n, c, trk);
+  else
+    return guide_bounce_fp64(n, c, trk);
 }
 
 // The whole guide; returns 1 when the bounce loop ran out of its
@@ -224,12 +276,13 @@ __device__ __forceinline__ int guide(Neutron<R>& n, const mcv_component& c,
 
 // Slit / Beamstop (acc/components/optics/slit.py:71-108,
 // beamstop.py:75-112); dp = {xmin, xmax, ymin, ymax, radius^2, cut}
+// (`up`: the chain's FP32 weight scale, which the cut is compared in)
 template <typename R>
 __device__ __forceinline__ void slit_or_beamstop(Neutron<R>& n,
                                                  const mcv_component& c,
-                                                 bool stop) {
+                                                 bool stop, R up) {
   R xmin = prm<R>(c, 0), xmax = prm<R>(c, 1), ymin = prm<R>(c, 2),
-    ymax = prm<R>(c, 3), r2 = prm<R>(c, 4), cut = prm<R>(c, 5);
+    ymax = prm<R>(c, 3), r2 = prm<R>(c, 4), cut = prm<R>(c, 5) * up;
   R x = n.x, y = n.y, z = n.z, vx = n.vx, vy = n.vy, vz = n.vz;
   if ((z < 0 && vz <= 0) || (z > 0 && vz >= 0)) return;
   if (n.p < cut) {

@@ -146,6 +146,11 @@ int validate_chain(const mcv_chain* ch, mcv_status* st) {
             (long long)ch->ncomp);
     return MCV_EINVAL;
   }
+  if (ch->weight_exp2 < -126 || ch->weight_exp2 > 126) {
+    set_msg(st, MCV_EINVAL, "weight_exp2 %s%lld outside -126..126", "",
+            (long long)ch->weight_exp2);
+    return MCV_EINVAL;
+  }
   for (int k = 0; k < ch->ncomp; ++k) {
     int rc = validate_component(ch->comp[k], k, st);
     if (rc) return rc;

@@ -17,7 +17,8 @@
 
 namespace mcv {
 
-enum { kFlagIdentityRot = 1 };
+enum { kFlagIdentityRot = MCV_COMP_IDENTITY_ROT,
+       kFlagAggregate = MCV_COMP_AGGREGATE };
 
 __device__ __forceinline__ uint64_t comp_nbins(const mcv_component& c) {
   switch (c.opcode) {
@@ -66,11 +67,13 @@ __device__ __forceinline__ void apply_transform(Neutron<R>& n,
 template <typename R, typename Rng, typename Trk>
 __device__ __forceinline__ int run_component(Neutron<R>& n, Rng& rng,
                                              const mcv_component& c,
-                                             Trk& trk) {
-  Tally tl{c.tally, comp_nbins(c)};
+                                             Trk& trk, const mcv_chain& ch) {
+  Tally tl{c.tally, comp_nbins(c), weight_down<R>(ch),
+           (c.flags & kFlagAggregate) != 0};
   switch (c.opcode) {
     case MCV_OP_SOURCE_SIMPLE:
       source_simple<R>(n, rng, c);
+      if constexpr (sizeof(R) == 4) n.p *= weight_up<R>(ch);
       return 0;
     case MCV_OP_GUIDE:
       return guide<R>(n, c, trk);
@@ -105,10 +108,10 @@ __device__ __forceinline__ int run_component(Neutron<R>& n, Rng& rng,
       banked<R>(n, c, tl, trk);
       return 0;
     case MCV_OP_SLIT:
-      slit_or_beamstop<R>(n, c, false);
+      slit_or_beamstop<R>(n, c, false, weight_up<R>(ch));
       return 0;
     case MCV_OP_BEAMSTOP:
-      slit_or_beamstop<R>(n, c, true);
+      slit_or_beamstop<R>(n, c, true, weight_up<R>(ch));
       return 0;
     default:  // MCV_OP_ARM
       return 0;
@@ -126,17 +129,22 @@ template <typename R, typename Rng, typename Trk = NoTrack>
 __device__ __forceinline__ int run_chain_one(Neutron<R>& n, Rng& rng,
                                              const mcv_chain& ch,
                                              Counters& k, Trk&& trk = Trk()) {
+  // The loop runs over every component for every lane (a dead neutron
+  // skips the body) so that c stays warp-uniform: component parameters are
+  // then read at uniform constant-bank addresses.
   int last = -1;
+  bool alive = true;
   const int nc = ch.ncomp;
   trk.begin_neutron();
   for (int c = 0; c < nc; ++c) {
+    if (!alive) continue;
     if (c > 0) apply_transform<R>(n, ch, c);
     last = c;
     trk.begin_component(ch, c);
-    k.overflow += run_component<R>(n, rng, ch.comp[c], trk);
+    k.overflow += run_component<R>(n, rng, ch.comp[c], trk, ch);
     if (!(n.p > 0)) {
       if (m_isnan(n.p)) k.nonfinite++;
-      break;
+      alive = false;
     }
   }
   return last;
@@ -150,7 +158,7 @@ __device__ __forceinline__ void zero_neutron(Neutron<R>& n) {
 
 template <typename R>
 __device__ __forceinline__ void store_neutron(const Neutron<R>& n,
-                                              double* out) {
+                                              double* out, double down) {
   out[0] = n.x;
   out[1] = n.y;
   out[2] = n.z;
@@ -160,7 +168,7 @@ __device__ __forceinline__ void store_neutron(const Neutron<R>& n,
   out[6] = n.sx;
   out[7] = n.sy;
   out[8] = n.t.dval();
-  out[9] = n.p;
+  out[9] = (double)n.p * down;
 }
 
 __device__ __forceinline__ void flush_counters(const Counters& k,
@@ -203,7 +211,7 @@ __global__ void __launch_bounds__(kMaxThreads)
     }
     k.processed++;
     if constexpr (MODE != 0) {
-      if (out_n) store_neutron(nt, out_n + i * 10);
+      if (out_n) store_neutron(nt, out_n + i * 10, weight_down<R>(ch));
       if (out_last) out_last[i] = last;
     }
   }
@@ -211,15 +219,19 @@ __global__ void __launch_bounds__(kMaxThreads)
 }
 
 // Path regeneration: the same per-neutron sequence as chain_kernel, but a
-// lane whose neutron leaves the chain immediately takes the next neutron of
-// its warp's index range.  Each pass first moves lanes that are not inside
-// a guide through the following components up to the next guide entry
-// (a new neutron: source, transform, entry), then every lane inside a
-// guide advances one bounce in the same instruction stream.  Lanes of a
-// warp stay busy while a few neutrons bounce many times, instead of idling
-// until the warp's longest path ends.  Every neutron is computed with the
-// same functions in the same order as in chain_kernel, so results are
-// identical neutron by neutron.
+// lane whose neutron leaves the chain takes the next neutron of its warp's
+// index range at the start of the next pass.  A pass sweeps the components
+// in chain order with a warp-uniform index k: the lanes whose neutron is at
+// component k run it (a guide: its entry), and a lane that gets through
+// moves on to k+1 within the same sweep.  Then every lane inside a guide,
+// whichever guide, makes one bounce in the same instruction stream.  Lanes
+// of a warp stay busy while a few neutrons bounce many times, instead of
+// idling until the warp's longest path ends; because k is uniform the
+// component parameters are read at uniform constant-bank addresses and the
+// opcode dispatch does not diverge (only the bounce reads its guide's
+// parameters per lane).  Every neutron is computed with the same functions
+// in the same order as in chain_kernel, so results agree neutron by neutron
+// (up to the compiler's contraction choices).
 template <typename R>
 __global__ void __launch_bounds__(kMaxThreads)
     regen_kernel(const __grid_constant__ mcv_chain ch, uint64_t n,
@@ -257,36 +269,35 @@ __global__ void __launch_bounds__(kMaxThreads)
       }
     }
     if (__all_sync(kFull, c == -2)) break;
-    if (c >= 0 && !inside) {
-      // advance through components up to the next guide's entry
-      for (;;) {
-        const mcv_component& cp = ch.comp[c];
-        if (cp.opcode == MCV_OP_GUIDE) {
-          if (guide_enter<R>(nt, cp)) {
-            inside = 1;
-            nb = 0;
-          }
-          break;
-        }
-        k.overflow += run_component<R>(nt, rng, cp, trk);
-        if (!(nt.p > 0) || c + 1 >= nc) break;
-        ++c;
-        apply_transform<R>(nt, ch, c);
+    for (int kc = 0; kc < nc; ++kc) {
+      if (c != kc || inside) continue;  // inside a guide: bounces below
+      const mcv_component& cp = ch.comp[kc];
+      if (cp.opcode == MCV_OP_GUIDE) {
+        // the entry here; the bounces below, shared by all guides
+        inside = guide_enter<R>(nt, cp);
+        nb = 0;
+        if (inside) continue;
+      } else {
+        k.overflow += run_component<R>(nt, rng, cp, trk, ch);
       }
-      if (!inside) {  // absorbed, or through the last component
+      if (!(nt.p > 0) || kc + 1 >= nc) {
         if (m_isnan(nt.p)) k.nonfinite++;
         c = -1;
         k.processed++;
+      } else {
+        c = kc + 1;
+        apply_transform<R>(nt, ch, kc + 1);
       }
     }
     if (inside) {
-      // one bounce, executed together by every lane inside a guide
-      bool finished = guide_bounce<R>(nt, ch.comp[c], trk);
-      if (!finished && ++nb >= MCV_MAX_BOUNCES) {
-        finished = true;
+      // one bounce for every lane inside a guide, whichever guide it is in
+      // (that guide's parameters are read per lane)
+      bool done = guide_bounce<R>(nt, ch.comp[c], trk);
+      if (!done && ++nb >= MCV_MAX_BOUNCES) {
+        done = true;
         k.overflow++;
       }
-      if (finished) {
+      if (done) {
         inside = 0;
         if (!(nt.p > 0) || c + 1 >= nc) {
           if (m_isnan(nt.p)) k.nonfinite++;
@@ -347,14 +358,14 @@ __global__ void __launch_bounds__(kMaxThreads)
     nt.sx = s[6];
     nt.sy = s[7];
     nt.t.set(s[8]);
-    nt.p = s[9];
+    nt.p = s[9] * weight_up<R>(ch);
     for (int c = 0; c < ch.ncomp; ++c) {
       const mcv_component& cp = ch.comp[c];
       if (cp.opcode != MCV_OP_SOURCE_SIMPLE && !(nt.p > 0)) break;
       if (c > 0) apply_transform<R>(nt, ch, c);
       PhiloxStream rng(seed, first + i, (uint32_t)(c + 1));
       NoTrack trk;
-      k.overflow += run_component<R>(nt, rng, cp, trk);
+      k.overflow += run_component<R>(nt, rng, cp, trk, ch);
     }
     k.processed++;
     s[0] = nt.x;
@@ -366,7 +377,7 @@ __global__ void __launch_bounds__(kMaxThreads)
     s[6] = nt.sx;
     s[7] = nt.sy;
     s[8] = (R)nt.t.dval();
-    s[9] = nt.p;
+    s[9] = (R)((double)nt.p * weight_down<R>(ch));
   }
   flush_counters(k, st);
 }

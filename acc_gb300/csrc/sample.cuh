@@ -574,6 +574,9 @@ __device__ __forceinline__ void powder_scatter(Neutron<R>& n, Rng& rng,
 // spanning [lo, hi]: u (n - 1).  In FP32 it is formed exactly from the
 // uniform's 24-bit integer k (u = k 2^-24): node = k (n-1) >> 24,
 // fraction = (k (n-1) mod 2^24) 2^-24.
+// scale of the FP32 S(Q,E) interpolation (an exact power of two)
+constexpr float kSqeScale = 0x1p64f;
+
 __device__ __forceinline__ void grid_coord(float u, int n, int& i, float& f) {
   uint64_t prod = (uint64_t)(uint32_t)(u * 16777216.f) * (uint64_t)(n - 1);
   i = (int)(prod >> 24);
@@ -605,13 +608,18 @@ __device__ __forceinline__ R sqe_lookup(const mcv_component& c, R Q, R E,
     fx = (Q - Qmin) / dQ - iq;
     fy = (E - Emin) / dE - ie;
   }
-  R f00 = __ldg(&tab[iq * nE + ie]), f10 = __ldg(&tab[(iq + 1) * nE + ie]);
-  R f01 = __ldg(&tab[iq * nE + ie + 1]);
-  R f11 = __ldg(&tab[(iq + 1) * nE + ie + 1]);
+  // FP32: the nodes are scaled by 2^64 (exact) so that table tails below
+  // float's normal range (subnormal entries) interpolate at full precision;
+  // the caller divides the scale out of the weight.
+  const R ks = sizeof(R) == 4 ? R(kSqeScale) : R(1);
+  R f00 = __ldg(&tab[iq * nE + ie]) * ks;
+  R f10 = __ldg(&tab[(iq + 1) * nE + ie]) * ks;
+  R f01 = __ldg(&tab[iq * nE + ie + 1]) * ks;
+  R f11 = __ldg(&tab[(iq + 1) * nE + ie + 1]) * ks;
   // bilinear_interp (SANS2D_ongrid.py:16-22)
   R a00 = f00, a10 = f10 - f00, a01 = f01 - f00, a11 = f11 - f10 - f01 + f00;
   R S = a00 + a10 * fx + a01 * fy + a11 * fx * fy;
-  trk.sqe(iq * nE + ie, nE, fx, fy, S);
+  trk.sqe(iq * nE + ie, nE, fx, fy, (double)S / (double)ks);
   return S;
 }
 
@@ -668,7 +676,15 @@ __device__ __forceinline__ void sqe_scatter(Neutron<R>& n, Rng& rng,
   n.vz = e1z * v1 + e2z * v2 + e3z * v3;
   R S = sqe_lookup<R>(c, Q, E, uQ, uE, trk);
   R prob_f = S * (vf / vi) * Q * (Qmax - Qmin) * (Emax - Emin) / (kf * ki) / 2;
-  n.p *= prob_f;
+  if constexpr (sizeof(R) == 4) {
+    // prob_f carries the table scale 2^64: take it out of the factor when
+    // the factor stays normal, else out of the weight first (p is near
+    // 2^64 times its relative size, so p * 2^-64 stays normal)
+    const float f = prob_f * (1.f / kSqeScale);
+    n.p = f >= 0x1p-126f ? n.p * f : (n.p * (1.f / kSqeScale)) * prob_f;
+  } else {
+    n.p *= prob_f;
+  }
 }
 
 template <typename R>

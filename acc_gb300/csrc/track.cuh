@@ -18,19 +18,39 @@ namespace mcv {
 struct Tally {
   double* out;
   uint64_t nbins;
+  double down;     // 2^-weight_exp2: the FP32 weight scale divided out
+  bool aggregate;  // MCV_COMP_AGGREGATE: warp-aggregated atomics
 };
 
-// Warp-aggregated tally: the lanes that reach this call together and hit the
-// same bin of the same tally (__match_any_sync on the bin's address) add
-// their count, p and p^2 in a tree inside the warp, and one lane (the
-// group's lowest) makes the three global atomics.  A transmitted beam puts
-// a large share of all neutrons into a few bins; without aggregation those
-// become same-address atomics serialised in one L2 slice.  When no two
-// lanes share a bin the call is three plain atomics per lane.
-__device__ __forceinline__ void tally_add(const Tally& t, uint64_t bin,
-                                          double p) {
-  if (!t.out) return;
-  double* a = t.out + bin;
+// The FP32 weight scale of a chain (mcv_chain.weight_exp2, |e| <= 126):
+// the source's weight is multiplied by 2^e, tallies and outputs by 2^-e,
+// both exact powers of two built from the exponent bits where they are
+// used (the chain lives in the constant bank, so nothing stays in a
+// register).  The FP64 kernels use 1 and 1.
+template <typename R>
+__device__ __forceinline__ R weight_up(const mcv_chain& ch) {
+  if constexpr (sizeof(R) == 4)
+    return __int_as_float((127 + ch.weight_exp2) << 23);
+  else
+    return R(1);
+}
+template <typename R>
+__device__ __forceinline__ double weight_down(const mcv_chain& ch) {
+  if constexpr (sizeof(R) == 4)
+    return __longlong_as_double((long long)(1023 - ch.weight_exp2) << 52);
+  else
+    return 1.0;
+}
+
+// Warp-aggregated entry (MCV_COMP_AGGREGATE): the lanes that reach this
+// call together and hit the same bin of the same tally (__match_any_sync on
+// the bin's address) first add their count, p and p^2 in a tree inside the
+// warp, and one lane (the group's lowest) makes the three atomics.  Not
+// inlined, so that its registers do not weigh on the kernels that do not
+// take it.
+static __device__ __noinline__ void tally_add_aggregated(double* a,
+                                                         uint64_t nbins,
+                                                         double p) {
   const unsigned mask = __activemask();
   const unsigned lane = threadIdx.x & 31u;
   const unsigned peers =
@@ -56,13 +76,31 @@ __device__ __forceinline__ void tally_add(const Tally& t, uint64_t bin,
     if (peers & (me - 1u)) return;  // not the group's lowest lane
   }
   atomicAdd(a, (double)__popc(peers));
-  atomicAdd(a + t.nbins, s1);
-  atomicAdd(a + 2 * t.nbins, s2);
+  atomicAdd(a + nbins, s1);
+  atomicAdd(a + 2 * nbins, s2);
+}
+
+// One entry (1, p, p^2) into bin `bin`: three FP64 atomics into the
+// L2-resident histogram.  Warp aggregation trades a match and shuffles
+// against same-address atomics; on GB300 the plain atomics measured faster
+// on the bench workloads (a transmitted beam into a few theta x tof bins
+// included), so it is a per-monitor option.
+__device__ __forceinline__ void tally_add(const Tally& t, uint64_t bin,
+                                          double p) {
+  if (!t.out) return;
+  double* a = t.out + bin;
+  if (t.aggregate) {
+    tally_add_aggregated(a, t.nbins, p);
+    return;
+  }
+  atomicAdd(a, 1.0);
+  atomicAdd(a + t.nbins, p);
+  atomicAdd(a + 2 * t.nbins, p * p);
 }
 __device__ __forceinline__ void tally_add(const Tally& t, uint64_t bin,
                                           float p) {
-  // p^2 is formed in double: a float weight of 1e-25 would underflow
-  tally_add(t, bin, (double)p);
+  // the weight scale is divided out and p^2 formed in double
+  tally_add(t, bin, (double)p * t.down);
 }
 
 struct NoTrack {
@@ -80,7 +118,7 @@ struct NoTrack {
   template <typename R>
   __device__ __forceinline__ void powder_peak(int, R) {}
   template <typename R>
-  __device__ __forceinline__ void sqe(int, int, R, R, R) {}
+  __device__ __forceinline__ void sqe(int, int, R, R, double) {}
   template <typename R>
   __device__ __forceinline__ void tally(const Tally& t, uint64_t bin, R p) {
     tally_add(t, bin, p);
@@ -197,21 +235,22 @@ struct GradTrack {
     inv_s = R(1) / s;
   }
   // bilinear S(Q,E): d ln p / d S_corner = weight_corner / S
-  __device__ __forceinline__ void sqe(int base, int nE, R fx, R fy, R S) {
-    if (!is_hss || !(S > R(0))) return;
+  // S: the interpolated table value, unscaled, in double
+  __device__ __forceinline__ void sqe(int base, int nE, R fx, R fy, double S) {
+    if (!is_hss || !(S > 0.0)) return;
     sqe_base = base;
     sqe_fx = fx;
     sqe_fy = fy;
-    sqe_invS = 1.0 / (double)S;
+    sqe_invS = 1.0 / S;
     (void)nE;
   }
 
-  __device__ __forceinline__ void tally(const Tally&, uint64_t bin, R p) {
+  __device__ __forceinline__ void tally(const Tally& t, uint64_t bin, R p) {
     const double* d = g.dout[cur];
     if (!d) return;
     double gb = d[bin];
     if (gb == 0.0) return;
-    double gp = gb * (double)p;
+    double gp = gb * ((double)p * t.down);
 #pragma unroll
     for (int s = 0; s < kGradGuides; ++s)
 #pragma unroll

@@ -47,7 +47,28 @@ def build_chain(components, offsets=None, rotmats=None, binder=None):
             ch.foff[i][k] = float(off[k])
         if np.array_equal(rot, eye):
             c.flags |= nat.FLAG_IDENTITY_ROT
+    ch.weight_exp2 = weight_exp2(components)
     return ch
+
+
+# where the FP32 kernels place a source's nominal weight: 2^64 leaves 64
+# binary orders for weights to grow and 126 + 23 + 64 to shrink before a
+# float underflows
+WEIGHT_TARGET_EXP2 = 64
+
+
+def weight_exp2(components):
+    """The power of two the FP32 kernels multiply every weight by
+    (mcv_chain.weight_exp2): it brings the first component's nominal weight
+    (a source's weight on its central ray) to about 2^64.  0 when the chain
+    does not start with a source that states one."""
+    first = components[0] if components else None
+    nominal = getattr(first, "nominal_weight", None)
+    w = nominal() if callable(nominal) else None
+    if not w or not np.isfinite(w) or w <= 0:
+        return 0
+    e = int(round(WEIGHT_TARGET_EXP2 - np.log2(w)))
+    return max(-100, min(100, e))
 
 
 def chain_for_instrument(instrument, binder=None):

@@ -482,12 +482,23 @@ def ours_arm(a, rank, world, local_rank):
 
     from acc_gb300.stats import chi2_per_dof, z_summary
     chi2 = {}
-    names = [c.name for c in ins32.components if isinstance(c, MonitorBase)]
-    for nm, g32, g64 in zip(names, tallies[0], tallies[1]):
-        a = g32.cpu().numpy().reshape(3, -1)
-        b = g64.cpu().numpy().reshape(3, -1)
-        c2, dof = chi2_per_dof(a, b)
-        chi2[nm] = {"chi2_per_dof": c2, "bins": dof, "z": z_summary(a, b)}
+    mons = [c for c in ins32.components if isinstance(c, MonitorBase)]
+    for mon, g32, g64 in zip(mons, tallies[0], tallies[1]):
+        shape = (3,) + tuple(getattr(mon, "shape4", mon.hist_shape))
+        h32 = g32.cpu().numpy().reshape(shape)
+        h64 = g64.cpu().numpy().reshape(shape)
+        c2, dof = chi2_per_dof(h32, h64)
+        entry = {"chi2_per_dof": c2, "bins": dof}
+        if dof < 100 and len(shape) > 3:
+            # too sparse at this neutron count: compare the projection on
+            # the first and last axes (sums of N, p, p^2 over the others)
+            axes = tuple(range(2, len(shape) - 1))
+            h32, h64 = h32.sum(axis=axes), h64.sum(axis=axes)
+            c2, dof = chi2_per_dof(h32, h64)
+            entry = {"chi2_per_dof": c2, "bins": dof,
+                     "projection": "first and last axes"}
+        entry["z"] = z_summary(h32, h64)
+        chi2[mon.name] = entry
 
     fp32_peak = engine.probe_fma_peak(32)
     fp64_peak = engine.probe_fma_peak(64)

@@ -30,7 +30,7 @@
 extern "C" {
 #endif
 
-#define MCV_ABI_VERSION 1
+#define MCV_ABI_VERSION 2
 
 #define MCV_MAX_COMPONENTS 16
 #define MCV_NPARAM 40
@@ -132,6 +132,10 @@ enum {
  * Every monitor tallies into `tally`: float64 [3][n0][n1] holding
  * (N, sum p, sum p^2) per bin, the `out` array of psd_monitor.py:61-65.
  */
+/* mcv_component.flags */
+#define MCV_COMP_IDENTITY_ROT 1   /* rot of this hop is the identity         */
+#define MCV_COMP_AGGREGATE 2      /* monitors: warp-aggregate tally atomics  */
+
 typedef struct mcv_component {
   int32_t opcode;
   int32_t flags;
@@ -152,6 +156,13 @@ typedef struct mcv_component {
 typedef struct mcv_chain {
   int32_t ncomp;
   int32_t flags;
+  /* FP32 kernels carry every weight as p * 2^weight_exp2 (an exact power of
+   * two, |weight_exp2| <= 126) and divide it out in double at tallies and
+   * outputs, so that the float exponent range covers the chain's weights
+   * (p0 * 2^weight_exp2 near 2^64 leaves 64 binary orders above the source
+   * weight and 213 below).  FP64 kernels ignore it; 0 = no scaling. */
+  int32_t weight_exp2;
+  int32_t reserved;
   mcv_component comp[MCV_MAX_COMPONENTS];
   double rot[MCV_MAX_COMPONENTS][9];
   double off[MCV_MAX_COMPONENTS][3];

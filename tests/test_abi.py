@@ -38,7 +38,7 @@ def test_struct_layout_matches(engine_lib, oracle_lib):
     assert oracle_lib.oracle_sizeof_chain() == ctypes.sizeof(nat.mcv_chain)
     assert oracle_lib.oracle_sizeof_component() == \
         ctypes.sizeof(nat.mcv_component)
-    assert engine_lib.mcv_abi_version() == 1
+    assert engine_lib.mcv_abi_version() == 2
 
 
 def _bad_chain():
@@ -105,3 +105,15 @@ def test_context_create(engine_lib):
         engine_lib.mcv_ctx_destroy(h)
     else:
         assert rc == nat.MCV_ENODEV
+
+
+def test_weight_exp2_out_of_range_rejected(engine_lib):
+    from acc_gb300.memory import HostBinder
+    from acc_gb300.components.optics.arm import Arm
+    from acc_gb300.engine import build_chain
+    ch = build_chain([Arm("a")], binder=HostBinder())
+    ch.weight_exp2 = 127
+    st = nat.mcv_status()
+    rc = engine_lib.mcv_run_chain(None, ctypes.byref(ch), 1, 0, 1, 32, None,
+                                  None, ctypes.byref(st))
+    assert rc == nat.MCV_EINVAL and b"weight_exp2" in st.message

@@ -220,3 +220,42 @@ def test_regeneration_kernel_equals_thread_kernel(name):
         moved = np.abs(ta[0] - tb[0]).sum() / 2
         assert moved <= max(2, 1e-5 * ta[0].sum()), moved
         assert ta[1].sum() == pytest.approx(tb[1].sum(), rel=1e-6)
+
+
+def test_fp32_weight_scale_keeps_weights_below_float_range():
+    """S(Q,E) tails put weights near 1e-45 (below float's normal range, 1.2e-38):
+    with the chain's power-of-two weight scale the FP32 kernel keeps them.
+    Same stream: the neutrons alive at the detector are the same set as in
+    FP64 (up to 1e-4 of them), and those with an FP64 weight below 1e-38
+    agree within 1e-4 relative."""
+    n, seed = 100_000, 21
+    ins = instruments.sqe_hollow_cylinder()
+    g32, l32 = gpu_record(ins, n, seed, "float32")
+    g64, l64 = gpu_record(instruments.sqe_hollow_cylinder(), n, seed,
+                          "float64")
+    last = len(ins.components) - 1
+    a32 = (l32 == last) & (g32[:, 9] > 0)
+    a64 = (l64 == last) & (g64[:, 9] > 0)
+    assert a64.sum() > 1000
+    assert (a32 != a64).sum() <= max(2, 1e-4 * a64.sum())
+    tiny = a32 & a64 & (g64[:, 9] < 1e-38)
+    assert tiny.sum() > 100
+    rel = np.abs(g32[tiny, 9] - g64[tiny, 9]) / g64[tiny, 9]
+    assert (rel > 1e-4).mean() <= 1e-3, np.sort(rel)[-5:]
+
+
+def test_aggregated_tallies_equal_plain_atomics():
+    """MCV_COMP_AGGREGATE (warp-aggregated atomics) gives the same histogram
+    as plain atomics: identical counts, sums within 1e-12 (only the order of
+    additions differs)."""
+    n, seed = 1_000_000, 4
+    out = []
+    for agg in (False, True):
+        ins = instruments.sphere_theta_tof()
+        ins.components[-1].aggregate_tallies = agg
+        engine.run_instrument(ins, n, seed=seed, floattype="float64")
+        out.append(ins.components[-1].out.reshape(3, -1))
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_allclose(out[0][1:], out[1][1:], rtol=1e-12,
+                               atol=1e-300)
+    assert out[0][0].max() > 1000  # the transmitted beam shares bins

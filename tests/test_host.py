@@ -165,3 +165,16 @@ def test_chi2_and_z_scores_of_independent_tallies():
     b2 = b.copy()
     b2[1] *= 1.5  # a 50% bias is seen
     assert chi2_per_dof(a, b2)[0] > 3
+
+
+def test_weight_exp2_places_the_source_weight_near_2_64():
+    from acc_gb300 import engine, instruments
+    for name in ("guide_chain", "sphere_theta_tof", "sqe_hollow_cylinder"):
+        comps = getattr(instruments, name)().components
+        e = engine.weight_exp2(comps)
+        w = comps[0].nominal_weight()
+        assert abs(np.log2(w) + e - engine.WEIGHT_TARGET_EXP2) <= 0.5
+        ch = build_chain(comps, binder=HostBinder())
+        assert ch.weight_exp2 == e
+    # no source first: no scaling
+    assert engine.weight_exp2([Arm("a")]) == 0
