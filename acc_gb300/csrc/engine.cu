@@ -225,10 +225,23 @@ bool host_is_monitor(const mcv_component& c) {
 // neutron); chains without one have near-uniform paths.
 bool use_regen(const mcv_chain* ch, const mcv_launch* launch) {
   if (launch && launch->variant == 1) return false;
-  if (launch && launch->variant == 2) return true;
+  if (launch && (launch->variant == 2 || launch->variant == 3)) return true;
   for (int k = 0; k < ch->ncomp; ++k)
     if (ch->comp[k].opcode == MCV_OP_GUIDE) return true;
   return false;
+}
+
+// Shared memory of the regeneration kernel's tail queue for blocks of
+// `threads`: one queue per warp when components follow the chain's last
+// guide (variant 3 runs without it).
+size_t regen_tail_bytes(const mcv_chain* ch, const mcv_launch* launch,
+                        int threads) {
+  if (launch && launch->variant == 3) return 0;
+  int last = -1;
+  for (int k = 0; k < ch->ncomp; ++k)
+    if (ch->comp[k].opcode == MCV_OP_GUIDE) last = k;
+  if (last < 0 || last + 1 >= ch->ncomp) return 0;
+  return (size_t)(threads / 32) * kTailBytesPerWarp;
 }
 
 constexpr uint64_t kDefaultChunk = 8192;
@@ -423,10 +436,16 @@ int mcv_run_chain(mcv_ctx* ctx, const mcv_chain* chain, uint64_t ncount,
   if (precision == MCV_FP32) {
     if (use_regen(chain, launch)) {
       int blocks, threads;
-      launch_shape(ctx, Launchers<float>::occupancy_regen, ncount, launch,
-                   &blocks, &threads);
-      Launchers<float>::regen(blocks, threads, s, *chain, ncount, first, seed,
-                              ctx->d_status);
+      launch_shape(
+          ctx,
+          [chain, launch](int t) {
+            return Launchers<float>::occupancy_regen(
+                t, regen_tail_bytes(chain, launch, t));
+          },
+          ncount, launch, &blocks, &threads);
+      Launchers<float>::regen(blocks, threads,
+                              regen_tail_bytes(chain, launch, threads), s,
+                              *chain, ncount, first, seed, ctx->d_status);
     } else {
       launch_chain<float>(ctx, 0, chain, ncount, first, seed, nullptr, 0,
                           nullptr, nullptr, launch, s);

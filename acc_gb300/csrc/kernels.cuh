@@ -218,26 +218,89 @@ __global__ void __launch_bounds__(kMaxThreads)
   flush_counters(k, st);
 }
 
+// The tail queue of the FP32 regeneration kernel: per warp, a ring of
+// kTailCap neutrons that have left the chain's last guide alive, each with
+// its position in its Philox stream (20 words, stored word-major so that
+// the lanes of a warp touch consecutive banks).
+constexpr int kTailWords = 20;
+constexpr int kTailCap = 64;
+constexpr size_t kTailBytesPerWarp = sizeof(uint32_t) * kTailWords * kTailCap;
+
+__device__ __forceinline__ void tail_store(uint32_t* q, int slot,
+                                           const Neutron<float>& n,
+                                           const PhiloxStream& r) {
+  const uint32_t w[kTailWords] = {
+      __float_as_uint(n.x),  __float_as_uint(n.y),    __float_as_uint(n.z),
+      __float_as_uint(n.vx), __float_as_uint(n.vy),   __float_as_uint(n.vz),
+      __float_as_uint(n.sx), __float_as_uint(n.sy),   __float_as_uint(n.t.hi),
+      __float_as_uint(n.t.lo), __float_as_uint(n.p),  r.c0,
+      r.c1,                  r.c2,                    r.b0,
+      r.b1,                  r.b2,                    r.b3,
+      r.b4,                  (uint32_t)r.left};
+#pragma unroll
+  for (int k = 0; k < kTailWords; ++k) q[k * kTailCap + slot] = w[k];
+}
+
+__device__ __forceinline__ void tail_load(const uint32_t* q, int slot,
+                                          Neutron<float>& n,
+                                          PhiloxStream& r) {
+  uint32_t w[kTailWords];
+#pragma unroll
+  for (int k = 0; k < kTailWords; ++k) w[k] = q[k * kTailCap + slot];
+  n.x = __uint_as_float(w[0]);
+  n.y = __uint_as_float(w[1]);
+  n.z = __uint_as_float(w[2]);
+  n.vx = __uint_as_float(w[3]);
+  n.vy = __uint_as_float(w[4]);
+  n.vz = __uint_as_float(w[5]);
+  n.sx = __uint_as_float(w[6]);
+  n.sy = __uint_as_float(w[7]);
+  n.t.hi = __uint_as_float(w[8]);
+  n.t.lo = __uint_as_float(w[9]);
+  n.p = __uint_as_float(w[10]);
+  r.c0 = w[11];
+  r.c1 = w[12];
+  r.c2 = w[13];
+  r.b0 = w[14];
+  r.b1 = w[15];
+  r.b2 = w[16];
+  r.b3 = w[17];
+  r.b4 = w[18];
+  r.left = (int)w[19];
+}
+
 // Path regeneration: the same per-neutron sequence as chain_kernel, but a
-// lane whose neutron leaves the chain takes the next neutron of its warp's
-// index range at the start of the next pass.  A pass sweeps the components
-// in chain order with a warp-uniform index k: the lanes whose neutron is at
-// component k run it (a guide: its entry), and a lane that gets through
-// moves on to k+1 within the same sweep.  Then every lane inside a guide,
-// whichever guide, makes one bounce in the same instruction stream.  Lanes
-// of a warp stay busy while a few neutrons bounce many times, instead of
-// idling until the warp's longest path ends; because k is uniform the
-// component parameters are read at uniform constant-bank addresses and the
-// opcode dispatch does not diverge (only the bounce reads its guide's
-// parameters per lane).  Every neutron is computed with the same functions
-// in the same order as in chain_kernel, so results agree neutron by neutron
-// (up to the compiler's contraction choices).
+// lane whose neutron leaves the chain takes new work at the start of the
+// next pass.  A pass sweeps the components in chain order with a
+// warp-uniform index k: the lanes whose neutron is at component k run it
+// (a guide: its entry), and a lane that gets through moves on to k+1
+// within the same sweep.  Then every lane inside a guide, whichever guide,
+// makes one bounce in the same instruction stream.  Lanes of a warp stay
+// busy while a few neutrons bounce many times, instead of idling until the
+// warp's longest path ends; because k is uniform the component parameters
+// are read at uniform constant-bank addresses and the opcode dispatch does
+// not diverge (only the bounce reads its guide's parameters per lane).
+//
+// FP32 with shared memory (tail_queue): a neutron that leaves the last
+// guide alive is parked in the warp's tail queue and its lane takes new
+// work; once the queue holds a neutron for every idle lane (or no new
+// neutrons are left), the idle lanes take queued neutrons together, so
+// the components after the last guide -- monitors, a sample, a detector,
+// which only a few percent of the neutrons reach -- run with the lanes of
+// a warp converged.  A full queue leaves the neutron on its lane.
+//
+// Every neutron is computed with the same functions, in the same order and
+// with its own Philox stream, as in chain_kernel, so results agree neutron
+// by neutron (up to the compiler's contraction choices).
 template <typename R>
 __global__ void __launch_bounds__(kMaxThreads)
     regen_kernel(const __grid_constant__ mcv_chain ch, uint64_t n,
-                 uint64_t first, uint64_t seed, DevStatus* st) {
+                 uint64_t first, uint64_t seed, int tail_queue,
+                 DevStatus* st) {
+  extern __shared__ uint32_t tail_smem[];
   constexpr unsigned kFull = 0xffffffffu;
   const unsigned lane = threadIdx.x & 31u;
+  const unsigned below = (1u << lane) - 1u;
   const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
   const uint64_t per = (n + nwarps - 1) / nwarps;
@@ -252,21 +315,46 @@ __global__ void __launch_bounds__(kMaxThreads)
   int inside = 0;  // guide: entered and bouncing
   int nb = 0;      // guide: bounces so far
   const int nc = ch.ncomp;
+  int last_guide = -1;
+  for (int i = 0; i < nc; ++i)
+    if (ch.comp[i].opcode == MCV_OP_GUIDE) last_guide = i;
+  // the queue: FP32 only, when something follows the last guide
+  bool queue = false;
+  if constexpr (sizeof(R) == 4)
+    queue = tail_queue && last_guide >= 0 && last_guide + 1 < nc;
+  uint32_t* q = tail_smem + (threadIdx.x >> 5) * (kTailWords * kTailCap);
+  int qhead = 0, qcount = 0;  // warp-uniform
   for (;;) {
+    const bool more = next < end;  // new neutrons left (warp-uniform)
     const unsigned idle = __ballot_sync(kFull, c == -1);
     if (idle) {
-      const uint64_t idx = next + __popc(idle & ((1u << lane) - 1u));
-      next += __popc(idle);
+      const int nidle = __popc(idle);
+      const int rank = __popc(idle & below);
+      int npop = 0;
+      if (queue && qcount > 0 && (qcount >= nidle || !more))
+        npop = qcount < nidle ? qcount : nidle;
       if (c == -1) {
-        if (idx < end) {
-          zero_neutron(nt);
-          rng = PhiloxStream(seed, first + idx, 0u);
-          c = 0;
+        if (rank < npop) {
+          if constexpr (sizeof(R) == 4)
+            tail_load(q, (qhead + rank) % kTailCap, nt, rng);
+          c = last_guide + 1;
           inside = 0;
         } else {
-          c = -2;
+          const uint64_t idx = next + (uint64_t)(rank - npop);
+          if (idx < end) {
+            zero_neutron(nt);
+            rng = PhiloxStream(seed, first + idx, 0u);
+            c = 0;
+            inside = 0;
+          } else {
+            c = -2;
+          }
         }
       }
+      qhead = (qhead + npop) % kTailCap;
+      qcount -= npop;
+      next += (uint64_t)(nidle - npop);
+      if (next > end) next = end;
     }
     if (__all_sync(kFull, c == -2)) break;
     for (int kc = 0; kc < nc; ++kc) {
@@ -289,6 +377,7 @@ __global__ void __launch_bounds__(kMaxThreads)
         apply_transform<R>(nt, ch, kc + 1);
       }
     }
+    bool park = false;
     if (inside) {
       // one bounce for every lane inside a guide, whichever guide it is in
       // (that guide's parameters are read per lane)
@@ -306,8 +395,24 @@ __global__ void __launch_bounds__(kMaxThreads)
         } else {
           ++c;
           apply_transform<R>(nt, ch, c);
+          park = queue && more && c == last_guide + 1;
         }
       }
+    }
+    if (queue) {
+      // park the neutrons that left the last guide, if they all fit
+      const unsigned pm = __ballot_sync(kFull, park);
+      const int npush = __popc(pm);
+      if (npush && qcount + npush <= kTailCap) {
+        if (park) {
+          if constexpr (sizeof(R) == 4)
+            tail_store(q, (qhead + qcount + __popc(pm & below)) % kTailCap,
+                       nt, rng);
+          c = -1;
+        }
+        qcount += npush;
+      }
+      __syncwarp();  // the stores are seen by the lanes that take them
     }
   }
   flush_counters(k, st);
@@ -482,8 +587,9 @@ struct Launchers {
                     const mcv_chain& ch, uint64_t n, uint64_t first,
                     uint64_t seed, const float* uni, int stride,
                     double* out_n, int* out_last, DevStatus* st);
-  static int occupancy_regen(int threads);
-  static void regen(int blocks, int threads, cudaStream_t s,
+  // smem: the tail queue's bytes (0 = no queue)
+  static int occupancy_regen(int threads, size_t smem);
+  static void regen(int blocks, int threads, size_t smem, cudaStream_t s,
                     const mcv_chain& ch, uint64_t n, uint64_t first,
                     uint64_t seed, DevStatus* st);
   static int occupancy_grad(int threads);
@@ -545,15 +651,16 @@ void Launchers<R>::chain(int mode, int blocks, int threads, cudaStream_t s,
 }
 
 template <typename R>
-int Launchers<R>::occupancy_regen(int threads) {
-  return occupancy_of(regen_kernel<R>, threads, 0);
+int Launchers<R>::occupancy_regen(int threads, size_t smem) {
+  return occupancy_of(regen_kernel<R>, threads, smem);
 }
 
 template <typename R>
-void Launchers<R>::regen(int blocks, int threads, cudaStream_t s,
-                         const mcv_chain& ch, uint64_t n, uint64_t first,
-                         uint64_t seed, DevStatus* st) {
-  regen_kernel<R><<<blocks, threads, 0, s>>>(ch, n, first, seed, st);
+void Launchers<R>::regen(int blocks, int threads, size_t smem,
+                         cudaStream_t s, const mcv_chain& ch, uint64_t n,
+                         uint64_t first, uint64_t seed, DevStatus* st) {
+  regen_kernel<R><<<blocks, threads, smem, s>>>(ch, n, first, seed,
+                                                 smem > 0 ? 1 : 0, st);
 }
 
 template <typename R>

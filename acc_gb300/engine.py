@@ -76,7 +76,8 @@ def chain_for_instrument(instrument, binder=None):
     return build_chain(instrument.components, offsets, rotmats, binder)
 
 
-VARIANTS = {None: 0, "auto": 0, "thread": 1, "regen": 2}
+VARIANTS = {None: 0, "auto": 0, "thread": 1, "regen": 2,
+            "regen_noqueue": 3}
 
 
 def _launch(threads_per_block=None, blocks=None, variant=None):

@@ -179,7 +179,10 @@ typedef struct mcv_launch {
                                1 one neutron per thread to the end of the
                                chain, 2 path regeneration (a lane whose
                                neutron leaves the chain starts the next one;
-                               guides advance one bounce per step) */
+                               guides advance one bounce per step; the
+                               components after the last guide run from a
+                               per-warp queue in shared memory), 3 path
+                               regeneration without that queue */
 } mcv_launch;
 
 typedef struct mcv_status {

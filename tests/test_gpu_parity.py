@@ -200,17 +200,28 @@ def test_guide_pass_through_on_gpu():
     assert out[8] + dt == 32.0 and out[9] == 1.0
 
 
-@pytest.mark.parametrize("name", ["guide_chain", "sphere_theta_tof"])
-def test_regeneration_kernel_equals_thread_kernel(name):
-    """Path regeneration changes which lane runs which neutron, not the
-    neutron's arithmetic.  The two kernels inline the same functions into
-    different code, where the compiler may contract a different multiply-add
-    into an FMA: a coordinate within an ulp of a bin edge can change bins.
-    Bound: at most 1e-5 of the entries move, sums within 1e-6 relative."""
+REGEN_CHAINS = {
+    "guide_chain": instruments.guide_chain,
+    # a sample and a detector after the guides: the tail draws random
+    # numbers after the neutron waited in the tail queue
+    "powder_banked": lambda: instruments.powder_banked(ntubes=16, npixels=16,
+                                                       ntof=50),
+}
+
+
+@pytest.mark.parametrize("variant", ["regen", "regen_noqueue"])
+@pytest.mark.parametrize("name", list(REGEN_CHAINS))
+def test_regeneration_kernel_equals_thread_kernel(name, variant):
+    """Path regeneration (with or without the tail queue) changes which lane
+    runs which neutron, not the neutron's arithmetic or its random numbers.
+    The kernels inline the same functions into different code, where the
+    compiler may contract a different multiply-add into an FMA: a
+    coordinate within an ulp of a bin edge can change bins.  Bound: at most
+    1e-5 of the entries move, sums within 1e-6 relative."""
     n = 500_000
-    a, b = BUILDERS[name](), BUILDERS[name]()
+    a, b = REGEN_CHAINS[name](), REGEN_CHAINS[name]()
     sa = engine.run_instrument(a, n, seed=21, floattype="float32",
-                               variant="regen")
+                               variant=variant)
     sb = engine.run_instrument(b, n, seed=21, floattype="float32",
                                variant="thread")
     assert sa.processed == sb.processed == n
