@@ -683,7 +683,28 @@ int mcv_backward(mcv_ctx* ctx, const mcv_chain* chain, const mcv_grad* grad,
     py = ctx->d_grad + npeaks + 1;
   }
   int blocks, threads;
-  if (precision == MCV_FP32) {
+  if (precision == MCV_FP32 && use_regen(chain, launch)) {
+    // the forward's structure (regeneration, tail queue) for the replay
+    auto bytes = [chain, launch](int t) {
+      return regen_tail_bytes(chain, launch, t) ? (size_t)(t / 32) *
+                                                      kGradTailBytesPerWarp
+                                                : (size_t)0;
+    };
+    launch_shape(
+        ctx,
+        [&bytes](int t) {
+          return Launchers<float>::occupancy_grad_regen(t, bytes(t));
+        },
+        ncount, launch, &blocks, &threads);
+    size_t smem = bytes(threads);
+    if (smem > 48 * 1024) {
+      cudaError_t ea = Launchers<float>::allow_grad_regen_smem(smem);
+      if (ea != cudaSuccess) return cuda_fail(st, ea, "mcv_backward smem");
+    }
+    Launchers<float>::grad_regen(blocks, threads, smem, s, *chain, *grad,
+                                 ncount, first, seed, px, py,
+                                 ctx->d_status);
+  } else if (precision == MCV_FP32) {
     launch_shape(ctx, Launchers<float>::occupancy_grad, ncount, launch,
                  &blocks, &threads);
     Launchers<float>::grad(blocks, threads, s, *chain, *grad, ncount, first,

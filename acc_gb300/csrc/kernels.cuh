@@ -225,6 +225,9 @@ __global__ void __launch_bounds__(kMaxThreads)
 constexpr int kTailWords = 20;
 constexpr int kTailCap = 64;
 constexpr size_t kTailBytesPerWarp = sizeof(uint32_t) * kTailWords * kTailCap;
+// the backward's queue also carries the gradient tracker's state
+constexpr size_t kGradTailBytesPerWarp =
+    sizeof(uint32_t) * (kTailWords + GradTrack<float>::kQueueWords) * kTailCap;
 
 __device__ __forceinline__ void tail_store(uint32_t* q, int slot,
                                            const Neutron<float>& n,
@@ -292,11 +295,11 @@ __device__ __forceinline__ void tail_load(const uint32_t* q, int slot,
 // Every neutron is computed with the same functions, in the same order and
 // with its own Philox stream, as in chain_kernel, so results agree neutron
 // by neutron (up to the compiler's contraction choices).
-template <typename R>
-__global__ void __launch_bounds__(kMaxThreads)
-    regen_kernel(const __grid_constant__ mcv_chain ch, uint64_t n,
-                 uint64_t first, uint64_t seed, int tail_queue,
-                 DevStatus* st) {
+template <typename R, typename Trk>
+__device__ __forceinline__ void regen_body(const mcv_chain& ch, uint64_t n,
+                                           uint64_t first, uint64_t seed,
+                                           int tail_queue, DevStatus* st,
+                                           Trk& trk) {
   extern __shared__ uint32_t tail_smem[];
   constexpr unsigned kFull = 0xffffffffu;
   const unsigned lane = threadIdx.x & 31u;
@@ -307,7 +310,6 @@ __global__ void __launch_bounds__(kMaxThreads)
   uint64_t next = warp * per;
   const uint64_t end = next + per < n ? next + per : n;
   Counters k{0, 0, 0, 0};
-  NoTrack trk;
   Neutron<R> nt;
   zero_neutron(nt);
   PhiloxStream rng(seed, 0, 0u);
@@ -322,7 +324,11 @@ __global__ void __launch_bounds__(kMaxThreads)
   bool queue = false;
   if constexpr (sizeof(R) == 4)
     queue = tail_queue && last_guide >= 0 && last_guide + 1 < nc;
-  uint32_t* q = tail_smem + (threadIdx.x >> 5) * (kTailWords * kTailCap);
+  // per slot: the neutron and its stream (kTailWords), then the tracker's
+  // per-neutron state
+  constexpr int kWords = kTailWords + Trk::kQueueWords;
+  uint32_t* q = tail_smem + (threadIdx.x >> 5) * (kWords * kTailCap);
+  uint32_t* qt = q + kTailWords * kTailCap;
   int qhead = 0, qcount = 0;  // warp-uniform
   for (;;) {
     const bool more = next < end;  // new neutrons left (warp-uniform)
@@ -335,8 +341,10 @@ __global__ void __launch_bounds__(kMaxThreads)
         npop = qcount < nidle ? qcount : nidle;
       if (c == -1) {
         if (rank < npop) {
-          if constexpr (sizeof(R) == 4)
+          if constexpr (sizeof(R) == 4) {
             tail_load(q, (qhead + rank) % kTailCap, nt, rng);
+            trk.load(qt, kTailCap, (qhead + rank) % kTailCap);
+          }
           c = last_guide + 1;
           inside = 0;
         } else {
@@ -344,6 +352,7 @@ __global__ void __launch_bounds__(kMaxThreads)
           if (idx < end) {
             zero_neutron(nt);
             rng = PhiloxStream(seed, first + idx, 0u);
+            trk.begin_neutron();
             c = 0;
             inside = 0;
           } else {
@@ -360,6 +369,7 @@ __global__ void __launch_bounds__(kMaxThreads)
     for (int kc = 0; kc < nc; ++kc) {
       if (c != kc || inside) continue;  // inside a guide: bounces below
       const mcv_component& cp = ch.comp[kc];
+      trk.begin_component(ch, kc);
       if (cp.opcode == MCV_OP_GUIDE) {
         // the entry here; the bounces below, shared by all guides
         inside = guide_enter<R>(nt, cp);
@@ -405,9 +415,11 @@ __global__ void __launch_bounds__(kMaxThreads)
       const int npush = __popc(pm);
       if (npush && qcount + npush <= kTailCap) {
         if (park) {
-          if constexpr (sizeof(R) == 4)
-            tail_store(q, (qhead + qcount + __popc(pm & below)) % kTailCap,
-                       nt, rng);
+          if constexpr (sizeof(R) == 4) {
+            const int slot = (qhead + qcount + __popc(pm & below)) % kTailCap;
+            tail_store(q, slot, nt, rng);
+            trk.save(qt, kTailCap, slot);
+          }
           c = -1;
         }
         qcount += npush;
@@ -416,6 +428,29 @@ __global__ void __launch_bounds__(kMaxThreads)
     }
   }
   flush_counters(k, st);
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kMaxThreads)
+    regen_kernel(const __grid_constant__ mcv_chain ch, uint64_t n,
+                 uint64_t first, uint64_t seed, int tail_queue,
+                 DevStatus* st) {
+  NoTrack trk;
+  regen_body<R>(ch, n, first, seed, tail_queue, st, trk);
+}
+
+// The backward replay with the regeneration kernel's structure: the same
+// neutrons, lanes and queue as the forward, with the gradient tracker
+// (its per-neutron state travels through the tail queue with the neutron).
+template <typename R>
+__global__ void __launch_bounds__(kMaxThreads)
+    grad_regen_kernel(const __grid_constant__ mcv_chain ch,
+                      const __grid_constant__ mcv_grad g, uint64_t n,
+                      uint64_t first, uint64_t seed, double* powder_x,
+                      double* powder_y, int tail_queue, DevStatus* st) {
+  GradTrack<R> trk(g, ch, powder_x, powder_y);
+  regen_body<R>(ch, n, first, seed, tail_queue, st, trk);
+  trk.flush(ch);
 }
 
 // Backward replay: neutron i of the stream `seed` again, with the gradient
@@ -592,6 +627,14 @@ struct Launchers {
   static void regen(int blocks, int threads, size_t smem, cudaStream_t s,
                     const mcv_chain& ch, uint64_t n, uint64_t first,
                     uint64_t seed, DevStatus* st);
+  static int occupancy_grad_regen(int threads, size_t smem);
+  // dynamic shared memory above 48 KB must be allowed per kernel
+  static cudaError_t allow_grad_regen_smem(size_t smem);
+  static void grad_regen(int blocks, int threads, size_t smem,
+                         cudaStream_t s, const mcv_chain& ch,
+                         const mcv_grad& g, uint64_t n, uint64_t first,
+                         uint64_t seed, double* px, double* py,
+                         DevStatus* st);
   static int occupancy_grad(int threads);
   static void grad(int blocks, int threads, cudaStream_t s,
                    const mcv_chain& ch, const mcv_grad& g, uint64_t n,
@@ -661,6 +704,29 @@ void Launchers<R>::regen(int blocks, int threads, size_t smem,
                          uint64_t first, uint64_t seed, DevStatus* st) {
   regen_kernel<R><<<blocks, threads, smem, s>>>(ch, n, first, seed,
                                                  smem > 0 ? 1 : 0, st);
+}
+
+template <typename R>
+int Launchers<R>::occupancy_grad_regen(int threads, size_t smem) {
+  if (smem > 48 * 1024) allow_grad_regen_smem(smem);
+  return occupancy_of(grad_regen_kernel<R>, threads, smem);
+}
+
+template <typename R>
+cudaError_t Launchers<R>::allow_grad_regen_smem(size_t smem) {
+  return cudaFuncSetAttribute(grad_regen_kernel<R>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)smem);
+}
+
+template <typename R>
+void Launchers<R>::grad_regen(int blocks, int threads, size_t smem,
+                              cudaStream_t s, const mcv_chain& ch,
+                              const mcv_grad& g, uint64_t n, uint64_t first,
+                              uint64_t seed, double* px, double* py,
+                              DevStatus* st) {
+  grad_regen_kernel<R><<<blocks, threads, smem, s>>>(
+      ch, g, n, first, seed, px, py, smem > 0 ? 1 : 0, st);
 }
 
 template <typename R>

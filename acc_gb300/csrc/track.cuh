@@ -105,6 +105,10 @@ __device__ __forceinline__ void tally_add(const Tally& t, uint64_t bin,
 
 struct NoTrack {
   static constexpr bool kActive = false;
+  // per-neutron words the regeneration kernel's tail queue carries
+  static constexpr int kQueueWords = 0;
+  __device__ __forceinline__ void save(uint32_t*, int, int) const {}
+  __device__ __forceinline__ void load(const uint32_t*, int, int) {}
   __device__ __forceinline__ void begin_neutron() {}
   __device__ __forceinline__ void begin_component(const mcv_chain&, int) {}
   template <typename R>
@@ -147,6 +151,55 @@ struct GradTrack {
   double acc_mu, acc_sig;
 
   int hss_comp = -1, sqe_nE = 0;
+
+  // The per-neutron state above, as queue words (FP32): word w of the
+  // neutron in `slot` lives at q[w * stride + slot].
+  static constexpr int kQueueWords = 19;
+  __device__ __forceinline__ void save(uint32_t* q, int stride,
+                                       int slot) const {
+    const uint32_t w[kQueueWords] = {
+        rbits(dg[0][0]), rbits(dg[0][1]), rbits(dg[0][2]),
+        rbits(dg[1][0]), rbits(dg[1][1]), rbits(dg[1][2]),
+        rbits(dmu),      rbits(dsig),     (uint32_t)sqe_base,
+        rbits(sqe_fx),   rbits(sqe_fy),
+        (uint32_t)__double2loint(sqe_invS),
+        (uint32_t)__double2hiint(sqe_invS),
+        (uint32_t)pk1,   (uint32_t)pk2,   (uint32_t)peak,
+        rbits(pc1),      rbits(pc2),      rbits(inv_s)};
+#pragma unroll
+    for (int k = 0; k < kQueueWords; ++k) q[k * stride + slot] = w[k];
+  }
+  __device__ __forceinline__ void load(const uint32_t* q, int stride,
+                                       int slot) {
+    uint32_t w[kQueueWords];
+#pragma unroll
+    for (int k = 0; k < kQueueWords; ++k) w[k] = q[k * stride + slot];
+    dg[0][0] = rval(w[0]);
+    dg[0][1] = rval(w[1]);
+    dg[0][2] = rval(w[2]);
+    dg[1][0] = rval(w[3]);
+    dg[1][1] = rval(w[4]);
+    dg[1][2] = rval(w[5]);
+    dmu = rval(w[6]);
+    dsig = rval(w[7]);
+    sqe_base = (int)w[8];
+    sqe_fx = rval(w[9]);
+    sqe_fy = rval(w[10]);
+    sqe_invS = __hiloint2double((int)w[12], (int)w[11]);
+    pk1 = (int)w[13];
+    pk2 = (int)w[14];
+    peak = (int)w[15];
+    pc1 = rval(w[16]);
+    pc2 = rval(w[17]);
+    inv_s = rval(w[18]);
+  }
+  // (queue words hold FP32 values: the queue is used by the FP32 kernel)
+  static __device__ __forceinline__ uint32_t rbits(R v) {
+    return __float_as_uint((float)v);
+  }
+  static __device__ __forceinline__ R rval(uint32_t w) {
+    return R(__uint_as_float(w));
+  }
 
   // the first HSS of the chain is the differentiated sample
   __device__ GradTrack(const mcv_grad& grad, const mcv_chain& ch, double* px,

@@ -308,12 +308,14 @@ class BatchedGraph:
 
 # ------------------------------------------------------------ gradients
 def backward(chain, ncount, dout, dparam=None, dtable=None, seed=None,
-             floattype=None, first=0, threads_per_block=None, device=None):
+             floattype=None, first=0, threads_per_block=None, device=None,
+             variant=None):
     """mcv_backward: replay `ncount` neutrons of `seed` and add the gradient
     of L into the given device tensors.  dout {component index: float64
     tensor (nbins,) = dL/d(sum p)}, dparam {index: float64 tensor (3,) for a
     guide (m, alpha, W) or (2,) for the sample (mu, sigma)}, dtable {index:
-    float64 tensor (S(Q,E) nodes or powder peaks)}."""
+    float64 tensor (S(Q,E) nodes or powder peaks)}.  `variant` as for
+    run_chain (the FP32 replay has the forward's kernel structures)."""
     ctx = nat.context(device)
     g = nat.mcv_grad()
     keep = []
@@ -327,7 +329,7 @@ def backward(chain, ncount, dout, dparam=None, dtable=None, seed=None,
             arr[k] = t.data_ptr()
             keep.append(t)
     st = nat.mcv_status()
-    L = _launch(threads_per_block)
+    L = _launch(threads_per_block, None, variant)
     seed = config.rng_seed if seed is None else seed
     rc = nat.lib().mcv_backward(
         ctx.handle, ctypes.byref(chain), ctypes.byref(g), int(ncount),

@@ -160,3 +160,42 @@ def test_fp32_backward_close_to_fp64():
     big = np.abs(e64) > 1e-2 * np.abs(e64).max()
     assert big.sum() > 100
     np.testing.assert_allclose(e32[big], e64[big], rtol=1e-3)
+
+
+@pytest.mark.parametrize("variant", ["regen", "regen_noqueue"])
+def test_fp32_regeneration_backward_equals_thread_backward(variant):
+    """The FP32 replay of a chain with guides runs with the forward's
+    structure (regeneration, tail queue carrying the tracker state); it
+    replays the same neutrons with the same arithmetic as the one-neutron-
+    per-thread replay.  The kernels may contract different multiply-adds
+    into FMAs, which moves a neutron within an ulp of a bin edge into the
+    next bin (a different dL/d(sum p) weight); the sums have random-sign
+    terms, so the bound is on the gradient vector's scale: every component
+    within 1e-6 relative or 2e-5 of the largest component.  A lost tracker
+    state would move components by their own size."""
+    from acc_gb300 import engine
+    ins = instruments.powder_banked(ntubes=16, npixels=16, ntof=50)
+    sample, det = ins.components[5], ins.components[6]
+    run = GradRun(ins, det, N, seed=8, floattype="float32",
+                  params={"F2": ("powder_F2", sample),
+                          "m": ("guide_m", [ins.components[1],
+                                            ins.components[2]])})
+    dout = weights(det.hist_shape, seed=6).reshape(-1).contiguous()
+    kF = run._index(sample)
+    kg = [run._index(ins.components[1]), run._index(ins.components[2])]
+    out = {}
+    for v in (variant, "thread"):
+        dF = torch.zeros(run.chain.comp[kF].ip[4], dtype=torch.float64,
+                         device="cuda")
+        dm = {k: torch.zeros(3, dtype=torch.float64, device="cuda")
+              for k in kg}
+        engine.backward(run.chain, N, {run.mon_index: dout}, dm, {kF: dF},
+                        seed=8, floattype="float32", variant=v)
+        out[v] = (dF.cpu().numpy(), [dm[k].cpu().numpy() for k in kg])
+    a, b = out[variant], out["thread"]
+    assert np.abs(b[0]).max() > 0 and np.abs(b[1][0]).max() > 0
+    np.testing.assert_allclose(a[0], b[0], rtol=1e-6,
+                               atol=2e-5 * np.abs(b[0]).max())
+    for x, y in zip(a[1], b[1]):
+        np.testing.assert_allclose(x, y, rtol=1e-6,
+                                   atol=2e-5 * np.abs(y).max())
