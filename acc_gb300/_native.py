@@ -17,6 +17,7 @@ MCV_NIPARAM = 8
 MCV_MAX_INTERSECTIONS = 10
 MCV_MAX_BOUNCES = 100000
 MCV_MAX_VARIANTS = 1024
+MCV_MS_MAX_SCATTERED = 16
 MCV_NOALLOC_MAX_VARIANTS = 64
 
 MCV_OK, MCV_EINVAL, MCV_ECUDA, MCV_ECOUNT, MCV_EBOUNCE = 0, 1, 2, 3, 4
@@ -37,6 +38,7 @@ OP_CYL_IQE_DETECTOR = 11
 OP_BANKED_DETECTOR = 12
 OP_SLIT = 13
 OP_BEAMSTOP = 14
+OP_HMS = 15
 
 SHAPE_SPHERE, SHAPE_CYLINDER, SHAPE_BOX = 1, 2, 3
 CSG_PRIMITIVE, CSG_DIFFERENCE, CSG_UNION, CSG_INTERSECTION = 0, 1, 2, 3

@@ -99,8 +99,18 @@ int validate_component(const mcv_component& c, int k, mcv_status* st) {
         return MCV_EINVAL;
       }
       break;
-    case MCV_OP_HSS: {
+    case MCV_OP_HSS:
+    case MCV_OP_HMS: {
       int op = c.ip[0], ker = c.ip[1];
+      if (c.opcode == MCV_OP_HMS &&
+          (c.ip[6] < 1 || c.ip[6] > MCV_MS_MAX_SCATTERED ||
+           (c.ip[7] & 0xffff) > 64 || (c.ip[7] >> 16) > 64 || c.ip[7] < 0)) {
+        set_msg(st, MCV_ECAPACITY,
+                "component %s%lld: multiple scatterer needs 1 <= "
+                "max_scattered_neutrons <= 16 and loop counts <= 64",
+                "", (long long)k);
+        return MCV_ECAPACITY;
+      }
       bool shape_ok = c.ip[2] >= MCV_SHAPE_SPHERE && c.ip[2] <= MCV_SHAPE_BOX &&
                       op >= MCV_CSG_PRIMITIVE && op <= MCV_CSG_INTERSECTION &&
                       (op == MCV_CSG_PRIMITIVE ||
@@ -151,11 +161,24 @@ int validate_chain(const mcv_chain* ch, mcv_status* st) {
             (long long)ch->weight_exp2);
     return MCV_EINVAL;
   }
+  int nhms = 0;
   for (int k = 0; k < ch->ncomp; ++k) {
     int rc = validate_component(ch->comp[k], k, st);
     if (rc) return rc;
+    nhms += ch->comp[k].opcode == MCV_OP_HMS;
+  }
+  if (nhms > 1) {
+    set_msg(st, MCV_EINVAL, "a chain holds at most one multiple scatterer%s",
+            "");
+    return MCV_EINVAL;
   }
   return MCV_OK;
+}
+
+bool has_hms(const mcv_chain* ch) {
+  for (int k = 0; k < ch->ncomp; ++k)
+    if (ch->comp[k].opcode == MCV_OP_HMS) return true;
+  return false;
 }
 
 int precision_ok(int precision, mcv_status* st) {
@@ -224,6 +247,7 @@ bool host_is_monitor(const mcv_component& c) {
 // when the chain has a guide (whose bounce count varies from neutron to
 // neutron); chains without one have near-uniform paths.
 bool use_regen(const mcv_chain* ch, const mcv_launch* launch) {
+  if (has_hms(ch)) return false;  // the fan-out runs in the thread kernel
   if (launch && launch->variant == 1) return false;
   if (launch && (launch->variant == 2 || launch->variant == 3)) return true;
   for (int k = 0; k < ch->ncomp; ++k)
@@ -259,6 +283,11 @@ int validate_batch(const mcv_chain* variants, int nvar, const uint64_t* counts,
   }
   for (int v = 0; v < nvar; ++v) {
     int rc = validate_chain(variants + v, st);
+    if (!rc && has_hms(variants + v)) {
+      set_msg(st, MCV_EINVAL,
+              "batched run: no multiple scatterer in a variant%s", "");
+      rc = MCV_EINVAL;
+    }
     if (rc) {
       if (st) st->first_bad_component = v;
       return rc;
@@ -322,7 +351,13 @@ uint64_t sum_counts(const uint64_t* counts, int nvar) {
 
 // chain validation for the other entry-point unit (noalloc.cu)
 int mcv::validate_chain_for(const mcv_chain* ch, mcv_status* st) {
-  return validate_chain(ch, st);
+  int rc = validate_chain(ch, st);
+  if (!rc && has_hms(ch)) {
+    set_msg(st, MCV_EINVAL,
+            "batched run: no multiple scatterer in a variant%s", "");
+    rc = MCV_EINVAL;
+  }
+  return rc;
 }
 
 extern "C" {
@@ -447,12 +482,12 @@ int mcv_run_chain(mcv_ctx* ctx, const mcv_chain* chain, uint64_t ncount,
                               regen_tail_bytes(chain, launch, threads), s,
                               *chain, ncount, first, seed, ctx->d_status);
     } else {
-      launch_chain<float>(ctx, 0, chain, ncount, first, seed, nullptr, 0,
-                          nullptr, nullptr, launch, s);
+      launch_chain<float>(ctx, has_hms(chain) ? 3 : 0, chain, ncount, first,
+                          seed, nullptr, 0, nullptr, nullptr, launch, s);
     }
   } else {
-    launch_chain<double>(ctx, 0, chain, ncount, first, seed, nullptr, 0,
-                         nullptr, nullptr, launch, s);
+    launch_chain<double>(ctx, has_hms(chain) ? 3 : 0, chain, ncount, first,
+                         seed, nullptr, 0, nullptr, nullptr, launch, s);
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(st, e, "mcv_run_chain launch");
@@ -468,6 +503,12 @@ int mcv_replay_uniforms(mcv_ctx* ctx, const mcv_chain* chain, uint64_t ncount,
                         mcv_status* st) {
   int rc = validate_chain(chain, st);
   if (rc) return rc;
+  if (has_hms(chain)) {
+    set_msg(st, MCV_EINVAL,
+            "mcv_replay_uniforms: a multiple scatterer's outputs are tallied, "
+            "not recorded; use mcv_run_chain%s", "");
+    return MCV_EINVAL;
+  }
   if (!precision_ok(precision, st)) return MCV_EINVAL;
   if (!ctx) {
     set_msg(st, MCV_EINVAL, "context is NULL%s", "");
@@ -499,6 +540,12 @@ int mcv_process_buffer(mcv_ctx* ctx, const mcv_chain* chain, void* neutrons,
                        mcv_status* st) {
   int rc = validate_chain(chain, st);
   if (rc) return rc;
+  if (has_hms(chain)) {
+    set_msg(st, MCV_EINVAL,
+            "mcv_process_buffer: the multiple scatterer's fan-out needs the "
+            "fused run (mcv_run_chain)%s", "");
+    return MCV_EINVAL;
+  }
   if (!precision_ok(precision, st)) return MCV_EINVAL;
   if (!ctx) {
     set_msg(st, MCV_EINVAL, "context is NULL%s", "");
@@ -632,6 +679,11 @@ int mcv_backward(mcv_ctx* ctx, const mcv_chain* chain, const mcv_grad* grad,
                  mcv_status* st) {
   int rc = validate_chain(chain, st);
   if (rc) return rc;
+  if (has_hms(chain)) {
+    set_msg(st, MCV_EINVAL,
+            "mcv_backward: no gradients through the multiple scatterer%s", "");
+    return MCV_EINVAL;
+  }
   if (!precision_ok(precision, st)) return MCV_EINVAL;
   if (!grad) {
     set_msg(st, MCV_EINVAL, "gradient description is NULL%s", "");

@@ -10,9 +10,12 @@
 // its own floating-point contraction setting.
 #pragma once
 
+#include <type_traits>
+
 #include "common.cuh"
 #include "components.cuh"
 #include "monitors.cuh"
+#include "ms.cuh"
 #include "sample.cuh"
 
 namespace mcv {
@@ -125,7 +128,7 @@ struct Counters {
 // Whole chain on one neutron (the body of the generated
 // process_kernel_no_buffer, acc/run_script.py:182-196).  A neutron leaves
 // the chain after a component that leaves its weight not positive.
-template <typename R, typename Rng, typename Trk = NoTrack>
+template <typename R, bool kMS = false, typename Rng, typename Trk = NoTrack>
 __device__ __forceinline__ int run_chain_one(Neutron<R>& n, Rng& rng,
                                              const mcv_chain& ch,
                                              Counters& k, Trk&& trk = Trk()) {
@@ -141,6 +144,29 @@ __device__ __forceinline__ int run_chain_one(Neutron<R>& n, Rng& rng,
     if (c > 0) apply_transform<R>(n, ch, c);
     last = c;
     trk.begin_component(ch, c);
+    if constexpr (kMS && !std::decay_t<Trk>::kActive) {
+      if (ch.comp[c].opcode == MCV_OP_HMS) {
+        // fan-out: the rest of the chain for every output neutron, in
+        // order, on the same stream (run_script.py:66-92, 245-260)
+        Neutron<R> outs[MCV_MS_MAX_SCATTERED];
+        const int nout =
+            ms_scatter<R>(ch.comp[c], rng, outs, n, weight_up<R>(ch));
+        for (int j = 0; j < nout; ++j) {
+          n = outs[j];
+          for (int c2 = c + 1; c2 < nc; ++c2) {
+            apply_transform<R>(n, ch, c2);
+            last = c2;
+            k.overflow += run_component<R>(n, rng, ch.comp[c2], trk, ch);
+            if (!(n.p > 0)) {
+              if (m_isnan(n.p)) k.nonfinite++;
+              break;
+            }
+          }
+        }
+        alive = false;
+        continue;
+      }
+    }
     k.overflow += run_component<R>(n, rng, ch.comp[c], trk, ch);
     if (!(n.p > 0)) {
       if (m_isnan(n.p)) k.nonfinite++;
@@ -187,7 +213,9 @@ __device__ __forceinline__ void flush_counters(const Counters& k,
 
 constexpr int kMaxThreads = 256;
 
-// MODE 0: Philox; 1: Philox + record; 2: injected uniforms + record
+// MODE 0: Philox; 1: Philox + record; 2: injected uniforms + record;
+// 3: Philox, with the multiple scatterer's fan-out (its own instantiation:
+// the per-thread work lists would weigh on every other chain)
 template <typename R, int MODE>
 __global__ void __launch_bounds__(kMaxThreads)
     chain_kernel(const __grid_constant__ mcv_chain ch, uint64_t n,
@@ -207,10 +235,10 @@ __global__ void __launch_bounds__(kMaxThreads)
       k.overrun += rng.overrun();
     } else {
       PhiloxStream rng(seed, first + i, 0u);
-      last = run_chain_one<R>(nt, rng, ch, k);
+      last = run_chain_one<R, MODE == 3>(nt, rng, ch, k);
     }
     k.processed++;
-    if constexpr (MODE != 0) {
+    if constexpr (MODE == 1 || MODE == 2) {
       if (out_n) store_neutron(nt, out_n + i * 10, weight_down<R>(ch));
       if (out_last) out_last[i] = last;
     }
@@ -674,6 +702,7 @@ template <typename R>
 int Launchers<R>::occupancy_chain(int mode, int threads) {
   if (mode == 0) return occupancy_of(chain_kernel<R, 0>, threads, 0);
   if (mode == 1) return occupancy_of(chain_kernel<R, 1>, threads, 0);
+  if (mode == 3) return occupancy_of(chain_kernel<R, 3>, threads, 0);
   return occupancy_of(chain_kernel<R, 2>, threads, 0);
 }
 
@@ -687,6 +716,9 @@ void Launchers<R>::chain(int mode, int blocks, int threads, cudaStream_t s,
                                                   stride, out_n, out_last, st);
   else if (mode == 1)
     chain_kernel<R, 1><<<blocks, threads, 0, s>>>(ch, n, first, seed, uni,
+                                                  stride, out_n, out_last, st);
+  else if (mode == 3)
+    chain_kernel<R, 3><<<blocks, threads, 0, s>>>(ch, n, first, seed, uni,
                                                   stride, out_n, out_last, st);
   else
     chain_kernel<R, 2><<<blocks, threads, 0, s>>>(ch, n, first, seed, uni,

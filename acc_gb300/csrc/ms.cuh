@@ -1,0 +1,316 @@
+// ms.cuh -- the homogeneous multiple scatterer
+// (acc/components/samples/homogeneous_multiple_scatterer.py:22-342) and
+// the propagation helpers it uses (acc/geometry/propagation.py:11-215).
+//
+// One incident neutron gives up to max_scattered_neutrons output neutrons
+// (transmitted and scattered branches, iterated max_ms_loops x
+// max_ms_loops_path1 times).  The work lists are per-thread arrays of
+// MCV_MS_MAX_SCATTERED neutrons, as the reference's are per-thread local
+// arrays; the caller runs the rest of the chain on each output.  The FP64
+// forms follow the reference's operation order; FP32 takes its hit times
+// from the ray's closest approach (intersect_shape_from), and the event
+// probability cut is compared in the chain's weight scale.
+#pragma once
+
+#include "sample.cuh"
+
+namespace mcv {
+
+// The geometry below is called from many places of the multiple-scattering
+// tree, on lanes that are at different places of it: one out-of-line copy
+// each (not inlined) keeps the kernel's code small enough for the
+// instruction cache, which otherwise dominates its stalls.
+template <typename R>
+__device__ __noinline__ Hits<R> ms_hits(const mcv_component& c, R x, R y, R z,
+                                        R vx, R vy, R vz) {
+  return intersect_shape_from<R>(c, x, y, z, vx, vy, vz);
+}
+template <typename R>
+__device__ __noinline__ int ms_locate(const mcv_component& c, R x, R y, R z) {
+  return locate_shape<R>(c, x, y, z);
+}
+
+// forward_intersect (propagation.py:11-22): the hit times >= 0, in order
+template <typename R>
+__device__ __forceinline__ Hits<R> forward_hits(const mcv_component& c,
+                                                const Neutron<R>& n) {
+  Hits<R> h = ms_hits<R>(c, n.x, n.y, n.z, n.vx, n.vy, n.vz);
+  int m = h.n;
+#pragma unroll
+  for (int i = 3; i >= 0; --i)
+    if (i < h.n && h.get(i) >= R(0)) m = i;
+  Hits<R> f;
+  f.n = h.n - m;
+  f.t0 = h.get(m < 4 ? m : 3);
+  f.t1 = h.get(m + 1 < 4 ? m + 1 : 3);
+  f.t2 = h.get(m + 2 < 4 ? m + 2 : 3);
+  f.t3 = h.get(m + 3 < 4 ? m + 3 : 3);
+  return f;
+}
+
+template <typename R>
+__device__ __forceinline__ int locate_at(const mcv_component& c,
+                                         const Neutron<R>& n, R t) {
+  return ms_locate<R>(c, n.x + n.vx * t, n.y + n.vy * t, n.z + n.vz * t);
+}
+
+// _is_exiting (propagation.py:24-50)
+template <typename R>
+__device__ __noinline__ bool ms_is_exiting(const mcv_component& c,
+                                              const Neutron<R>& n) {
+  const int loc = ms_locate<R>(c, n.x, n.y, n.z);
+  if (loc == kInside) return false;
+  const Hits<R> h = forward_hits(c, n);
+  if (h.n == 0) return true;
+  if (loc == kOutside) return false;
+  R previous = 0;
+  for (int it = 0; it < h.n; ++it) {
+    const R now = h.get(it), middle = (previous + now) / R(2);
+    if (locate_at(c, n, middle) != kOnBorder) return false;
+    previous = now;
+  }
+  return true;
+}
+
+// _propagate_out (propagation.py:52-59)
+template <typename R>
+__device__ __forceinline__ void ms_propagate_out(const mcv_component& c,
+                                                 Neutron<R>& n) {
+  const Hits<R> h = forward_hits(c, n);
+  if (h.n == 0) return;
+  prop_dt(n, h.get(h.n - 1));
+}
+
+// _tof_before_first_exit (propagation.py:154-191); -1 where the reference
+// raises (a point outside the shape)
+template <typename R>
+__device__ __forceinline__ R ms_tof_before_first_exit(const mcv_component& c,
+                                                      const Neutron<R>& n) {
+  const int loc = ms_locate<R>(c, n.x, n.y, n.z);
+  if (loc == kOutside) return R(-1);
+  const Hits<R> h = forward_hits(c, n);
+  if (h.n == 0) return R(0);
+  if (loc == kInside) return h.t0;
+  R t = 0;
+  for (int i = 0; i < h.n; ++i) {
+    const int l1 = locate_at(c, n, h.get(i) / R(2));
+    if (l1 == kOutside) return R(0);
+    if (l1 == kInside) {
+      t = h.get(i);
+      break;
+    }
+  }
+  return t;
+}
+
+// _propagate_to_next_incident_surface (propagation.py:61-105); a point
+// inside the shape (where the reference raises) is left where it is
+template <typename R>
+__device__ __forceinline__ void ms_to_incident(const mcv_component& c,
+                                               Neutron<R>& n) {
+  const int loc = ms_locate<R>(c, n.x, n.y, n.z);
+  if (loc == kInside) return;
+  const Hits<R> h = forward_hits(c, n);
+  if (h.n == 0) return;
+  R t;
+  if (loc == kOutside) {
+    t = h.t0;
+  } else {
+    bool found = false;
+    for (int i = 0; i < h.n; ++i) {
+      const int l1 = locate_at(c, n, h.get(i) / R(2));
+      if (l1 == kInside) return;
+      if (l1 == kOutside) {
+        t = h.get(i);
+        found = true;
+        break;
+      }
+    }
+    if (!found) return;
+  }
+  prop_dt(n, t);
+}
+
+// _propagate_to_next_exiting_surface (propagation.py:107-152)
+template <typename R>
+__device__ __noinline__ void ms_to_exiting(const mcv_component& c,
+                                              Neutron<R>& n) {
+  const int loc = ms_locate<R>(c, n.x, n.y, n.z);
+  R t;
+  if (loc == kInside) {
+    t = forward_hits(c, n).t0;
+  } else {
+    if (loc == kOutside) ms_to_incident(c, n);
+    const Hits<R> h = forward_hits(c, n);
+    bool found = false;
+    for (int i = 0; i < h.n; ++i) {
+      const int l1 = locate_at(c, n, h.get(i) / R(2));
+      if (l1 == kOutside) return;
+      if (l1 == kInside) {
+        t = h.get(i);
+        found = true;
+        break;
+      }
+    }
+    if (!found) return;
+  }
+  prop_dt(n, t);
+}
+
+// _calc_atten_coeff (homogeneous_multiple_scatterer.py:67-71)
+template <typename R>
+__device__ __forceinline__ R ms_atten_coeff(const Neutron<R>& n,
+                                            const mcv_component& c) {
+  return hss_sigma<R>(n, c) + hss_mu<R>(n, c);
+}
+
+// _propagate_to_next_exiting_surface_with_attenuation (:73-84)
+template <typename R>
+__device__ __forceinline__ void ms_exit_attenuated(const mcv_component& c,
+                                                   Neutron<R>& n) {
+  const R tof = ms_tof_before_first_exit(c, n);
+  const R v = m_sqrt(n.vx * n.vx + n.vy * n.vy + n.vz * n.vz);
+  const R distance = tof * v;
+  const R atten = ms_atten_coeff(n, c);
+  const R transmission_prob = m_exp(-atten * distance);
+  ms_to_exiting(c, n);
+  n.p *= transmission_prob;
+}
+
+// _interactM1 (:86-121): the transmitted and the scattered neutron.  The
+// absorbed copy (:106-110) is overwritten by the scattered one and the
+// kernels' absorb is a no-op (kernels/__init__.py:164-166), so it is not
+// formed.  A point left outside the shape (the reference raises) gives no
+// output.
+template <typename R, typename Rng>
+__device__ __noinline__ int ms_interact_m1(const mcv_component& c,
+                                              Rng& rng, Neutron<R>* out,
+                                              Neutron<R>& n) {
+  const R vx = n.vx, vy = n.vy, vz = n.vz;
+  if (ms_locate<R>(c, n.x, n.y, n.z) != kInside) ms_to_incident(c, n);
+  const R tof = ms_tof_before_first_exit(c, n);
+  if (!(tof > R(0))) return 0;
+  const R v = m_sqrt(vx * vx + vy * vy + vz * vz);
+  const R distance = tof * v;
+  const R sigma = hss_sigma<R>(n, c);
+  const R mu = hss_mu<R>(n, c);
+  const R transmission_prob = m_exp(-(mu + sigma) * distance);
+  out[0] = n;
+  ms_to_exiting(c, out[0]);
+  out[0].p *= transmission_prob;
+  const R rand = rng.next();
+  const R x = distance * rand;
+  const R prob = distance * m_exp(-(mu + sigma) * x);
+  out[1] = n;
+  out[1].p *= prob;
+  prop_dt(out[1], x / v);
+  NoTrack trk;
+  hss_kernel<R>(out[1], rng, c, trk);
+  return 2;
+}
+
+// _interactM_path1 (:123-177): out holds max_scattered_neutrons
+template <typename R, typename Rng>
+__device__ __noinline__ int ms_path1(const mcv_component& c, Rng& rng,
+                                     Neutron<R>* out, const Neutron<R>& n0,
+                                     R min_prob) {
+  const int max_sc = c.ip[6], loops1 = c.ip[7] >> 16;
+  Neutron<R> buf_a[MCV_MS_MAX_SCATTERED], buf_b[MCV_MS_MAX_SCATTERED];
+  Neutron<R> sc[2];
+  Neutron<R>* tbs = buf_a;
+  Neutron<R>* tbs2 = buf_b;
+  if (n0.p < min_prob) return 0;
+  int ntbs = 1, out_index = 0;
+  tbs[0] = n0;
+  for (int iloop = 0; iloop < loops1; ++iloop) {
+    int s2 = 0;
+    for (int i = 0; i < ntbs; ++i) {
+      const int ns = ms_interact_m1(c, rng, sc, tbs[i]);
+      for (int j = 0; j < ns; ++j) {
+        const Neutron<R>& s1 = sc[j];
+        if (s1.p < min_prob) continue;
+        if (ms_locate<R>(c, s1.x, s1.y, s1.z) != kInside) {
+          out[out_index++] = s1;
+          if (out_index >= max_sc) return out_index;
+          continue;
+        }
+        tbs2[s2++] = s1;
+        if (s2 >= max_sc) break;
+      }
+      if (s2 >= max_sc) break;
+    }
+    Neutron<R>* tmp = tbs2;
+    tbs2 = tbs;
+    tbs = tmp;
+    ntbs = s2;
+    if (!ntbs) break;
+  }
+  for (int i = 0; i < ntbs; ++i) {
+    if (out_index >= max_sc) break;
+    out[out_index++] = tbs[i];
+  }
+  return out_index;
+}
+
+// _scatterM (:196-256): the output neutrons of one incident neutron.
+// `up`: the chain's FP32 weight scale (the probability cut is compared in
+// it).
+template <typename R, typename Rng>
+__device__ __noinline__ int ms_scatter(const mcv_component& c, Rng& rng,
+                                       Neutron<R>* out, const Neutron<R>& n0,
+                                       R up) {
+  const int max_sc = c.ip[6], loops = c.ip[7] & 0xffff;
+  const R min_prob = prm<R>(c, 14) * up;
+  Neutron<R> buf_a[MCV_MS_MAX_SCATTERED], buf_b[MCV_MS_MAX_SCATTERED];
+  Neutron<R> sc[MCV_MS_MAX_SCATTERED];
+  Neutron<R>* tbs = buf_a;
+  Neutron<R>* tbs2 = buf_b;
+  if (ms_is_exiting(c, n0)) {
+    out[0] = n0;
+    return 1;
+  }
+  int ntbs = 1, out_index = 0;
+  tbs[0] = n0;
+  for (int iloop = 0; iloop < loops; ++iloop) {
+    int s2 = 0;
+    for (int i = 0; i < ntbs; ++i) {
+      const int ns1 = ms_path1<R>(c, rng, sc, tbs[i], min_prob);
+      for (int j = 0; j < ns1; ++j) {
+        Neutron<R>& s1 = sc[j];
+        if (s1.p < min_prob) continue;
+        if (!(m_sqrt(s1.vx * s1.vx + s1.vy * s1.vy + s1.vz * s1.vz) >
+              R(1.e-6)))
+          continue;  // is_moving (acc/neutron.py:39-42)
+        if (ms_locate<R>(c, s1.x, s1.y, s1.z) == kInside)
+          ms_exit_attenuated(c, s1);
+        if (ms_is_exiting(c, s1)) {
+          out[out_index++] = s1;
+          if (out_index >= max_sc) return out_index;
+          continue;
+        }
+        tbs2[s2++] = s1;
+        if (s2 >= max_sc) break;
+      }
+      if (s2 >= max_sc) break;
+    }
+    Neutron<R>* tmp = tbs2;
+    tbs2 = tbs;
+    tbs = tmp;
+    ntbs = s2;
+    if (!ntbs) break;
+  }
+  for (int i = 0; i < ntbs; ++i) {
+    if (out_index >= max_sc) break;
+    Neutron<R>& m = tbs[i];
+    const R x = m.x, y = m.y, z = m.z;
+    ms_propagate_out(c, m);
+    const R dx = m.x - x, dy = m.y - y, dz = m.z - z;
+    const R dist = m_sqrt(dx * dx + dy * dy + dz * dz);
+    const R atten = ms_atten_coeff(m, c);
+    m.p *= m_exp(-atten * dist);
+    out[out_index++] = m;
+  }
+  return out_index;
+}
+
+}  // namespace mcv

@@ -20,11 +20,12 @@ from .components.monitors.cylinder_detectors import (BankedCylinder_detector,
                                                      CylinderIQE_detector)
 from .components.monitors.energy_monitor import Energy_monitor
 from .components.monitors.psd_monitor import PSD_monitor
+from .components.monitors.psd_monitor_4pi import PSD_monitor_4Pi
 from .components.monitors.theta_tof_monitor_4pi import ThetaTOF_monitor_4Pi
 from .components.optics.guide import Guide
 from .components.samples.homogeneous_single_scatterer import factory
 from .components.sources.source_simple import Source_simple
-from .geometry import Cylinder, HollowCylinder, Sphere
+from .geometry import Cylinder, Difference, HollowCylinder, Sphere
 from .instrument import instrument
 from .kernels import (IsotropicKernel, Peak, SimplePowderDiffractionKernel,
                       SQEGridKernel, coefficient_from_cross_section)
@@ -157,6 +158,35 @@ def powder_banked(peaks=None, unitcell_volume=66.4, nbanks=8, ntubes=128,
     z = 16.002 + 0.5
     ins.append(HSS("sample"), position=(0, 0, z), orientation=(90, 0, 0))
     ins.append(det, position=(0, 0, z))
+    return ins
+
+
+def ms_hollow_cylinder(max_scattered_neutrons=16, max_ms_loops=2,
+                       max_ms_loops_path1=5):
+    """Multiple scattering: a 1 x 1 cm source 1 m from an 8 x 8 mm target,
+    wavelength 10 +- 9.5 A, onto an isotropic hollow cylinder 2 m
+    downstream (radii 1 and 2 cm, heights 7 and 6 cm, axis vertical,
+    absorption and scattering 10/m), with a 4pi PSD of radius 1 m (90 x 90)
+    around it: the test instrument of the reference's multiple scatterer
+    (tests/components/samples/acc_ss_test_instrument.py,
+    HMS_isotropic_hollowcylinder.py, test_homogeneous_multiple_scatterer.py
+    :15-31)."""
+    from .components.samples.homogeneous_multiple_scatterer import \
+        factory as ms_factory
+    ins = instrument("ms_hollow_cylinder")
+    src = Source_simple("src", radius=0., width=0.01, height=0.01, dist=1.,
+                        xw=0.008, yh=0.008, Lambda0=10., dLambda=9.5,
+                        E0=0., dE=0.0, flux=1, gauss=0)
+    shape = Difference(Cylinder(0.02, 0.06), Cylinder(0.01, 0.07))
+    HMS = ms_factory(shape, IsotropicKernel(10., 10.),
+                     max_scattered_neutrons=max_scattered_neutrons,
+                     max_ms_loops=max_ms_loops,
+                     max_ms_loops_path1=max_ms_loops_path1)
+    mon = PSD_monitor_4Pi("psd_4pi", radius=1., nphi=90, ntheta=90,
+                          filename="psd_4pi.h5")
+    ins.append(src, position=(0, 0, 0))
+    ins.append(HMS("sample"), position=(0, 0, 2.0), orientation=(90, 0, 0))
+    ins.append(mon, position=(0, 0, 2.0))
     return ins
 
 

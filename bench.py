@@ -46,6 +46,10 @@ WORKLOADS = {
     "sqe_hollow_cylinder": (
         "sqe_hollow_cylinder: 60 meV 1x1 cm beam -> hollow cylinder with "
         "200x200 S(Q,E) -> 3 m cylinder I(Q,E) 100x100"),
+    "ms_hollow_cylinder": (
+        "ms_hollow_cylinder: 1x1 cm source, 10 +- 9.5 A -> isotropic hollow "
+        "cylinder r 1-2 cm with multiple scattering (<= 16 outputs per "
+        "neutron, 2 x 5 loops) -> 4pi PSD 90x90"),
     "powder_banked": (
         "powder_banked: the guide_chain guides -> powder cylinder r=0.5 cm "
         "h=4 cm, 50 peaks -> banked detector R=3 m, 8 banks x 128 tubes x "

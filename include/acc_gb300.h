@@ -37,6 +37,8 @@ extern "C" {
 #define MCV_NIPARAM 8
 #define MCV_MAX_INTERSECTIONS 10  /* acc/geometry/arrow_intersect.py:16 */
 #define MCV_MAX_BOUNCES 100000    /* acc/components/optics/guide.py:17 */
+#define MCV_MS_MAX_SCATTERED 16   /* output neutrons per HMS event (the
+                                     reference default is 10) */
 
 /* ---- error codes ---------------------------------------------------- */
 enum {
@@ -68,7 +70,8 @@ enum {
   MCV_OP_BANKED_DETECTOR = 12,  /* no reference counterpart (banks x tubes x pixels x tof) */
   MCV_OP_SLIT = 13,             /* acc/components/optics/slit.py            */
   MCV_OP_BEAMSTOP = 14,         /* acc/components/optics/beamstop.py        */
-  MCV_OP_COUNT = 15
+  MCV_OP_HMS = 15,              /* acc/components/samples/homogeneous_multiple_scatterer.py */
+  MCV_OP_COUNT = 16
 };
 
 /* ---- shapes of the homogeneous scatterer (acc/geometry/arrow_intersect.py)
@@ -126,6 +129,15 @@ enum {
  * CYL_IQE_DETECTOR               ip: nQ nE; dp: radius height Ei Qmin Qmax Emin Emax
  * BANKED_DETECTOR                ip: nbanks ntubes npixels ntof
  *   dp: radius height bank_angle0 bank_width(rad) bank_gap(rad) tmin tmax
+ * HMS (homogeneous_multiple_scatterer.py:22-342): the HSS slots, plus
+ *   ip[6]=max_scattered_neutrons (1..MCV_MS_MAX_SCATTERED)
+ *   ip[7]=max_ms_loops | max_ms_loops_path1 << 16
+ *   dp[14]=minimum_neutron_event_probability
+ *   One incident neutron gives up to max_scattered_neutrons output
+ *   neutrons; the components after it run on each output in turn, drawing
+ *   from the incident neutron's stream.  At most one HMS per chain; the
+ *   fused thread kernel and the batched launch run it (mcv_process_buffer,
+ *   mcv_backward and the regeneration kernel reject it).
  * SLIT / BEAMSTOP (slit.py:20-108, beamstop.py:18-112)
  *                                dp: xmin xmax ymin ymax radius^2 cut
  *

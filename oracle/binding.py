@@ -67,6 +67,10 @@ def lib():
             ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,
             ctypes.c_int, ctypes.c_void_p, ctypes.c_int]
         L.oracle_guide_reflections.restype = ctypes.c_int
+        L.oracle_ms_step.argtypes = [
+            ctypes.c_void_p, ctypes.c_int, c_double_p, ctypes.c_uint64,
+            ctypes.c_uint64, ctypes.c_void_p, ctypes.c_int, c_double_p]
+        L.oracle_ms_step.restype = ctypes.c_int
         L.oracle_guide_one.argtypes = [ctypes.c_void_p, c_double_p]
         L.oracle_guide_one.restype = ctypes.c_int
         L.oracle_source_one.argtypes = [ctypes.c_void_p, ctypes.c_void_p, c_double_p]
@@ -236,6 +240,24 @@ def guide_reflections(chain, ncount, seed=1, first=0, nbins=64,
     if rc != 0:
         raise RuntimeError(f"oracle_guide_reflections failed ({rc})")
     return h
+
+
+MS_STEPS = {"interactM1": 0, "interactM_path1": 1, "scatterM": 2}
+
+
+def ms_step(comp, step, neutron, seed=1, index=0, uniforms=None):
+    """One step of the multiple scatterer (homogeneous_multiple_scatterer.py)
+    on a neutron state: returns (output neutrons (N, 10), the input state as
+    the step left it)."""
+    st = np.array(neutron, dtype=np.float64).reshape(10).copy()
+    out = np.zeros((64, 10))
+    uptr, stride = None, 0
+    if uniforms is not None:
+        u = np.ascontiguousarray(uniforms, dtype=np.float32).reshape(-1)
+        uptr, stride = u.ctypes.data, u.size
+    n = lib().oracle_ms_step(ctypes.byref(comp), MS_STEPS[step], _dp(st),
+                             int(seed), int(index), uptr, stride, _dp(out))
+    return out[:n].copy(), st
 
 
 def process_buffer(chain, neutrons, seed=1, first=0, nthreads=0):

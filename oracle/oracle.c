@@ -987,6 +987,27 @@ static double hss_sigma(const neutron_t* n, const mcv_component* c) {
   return c->dp[9];
 }
 
+/* the kernel's scatter function (scatter_func_factory.render,
+ * acc/kernels/__init__.py:10-22, 36-44): p *= sigma for the kernels with a
+ * constant scattering coefficient, then the kernel's S */
+static void kernel_scatter(neutron_t* n, rng_t* rng, const mcv_component* c) {
+  switch (c->ip[1]) {
+    case MCV_KERNEL_ISOTROPIC:
+      n->p *= c->dp[9]; /* kernels/__init__.py:42 */
+      isotropic_S(n, rng);
+      break;
+    case MCV_KERNEL_POWDER:
+      powder_scatter(n, rng, c);
+      break;
+    case MCV_KERNEL_SQE_GRID:
+      n->p *= c->dp[9];
+      sqe_scatter(n, rng, c);
+      break;
+    default:
+      break;
+  }
+}
+
 /* HomogeneousSingleScatterer.propagate
  * (acc/components/samples/homogeneous_single_scatterer.py:62-100) */
 static void hss(neutron_t* n, rng_t* rng, const mcv_component* c) {
@@ -1008,21 +1029,7 @@ static void hss(neutron_t* n, rng_t* rng, const mcv_component* c) {
   double mu = abs_coeff(n, c->dp[8]);
   double atten = exp(-(mu + sigma) * dist);
   n->p *= fulllen * atten;
-  switch (c->ip[1]) {
-    case MCV_KERNEL_ISOTROPIC:
-      n->p *= c->dp[9]; /* kernels/__init__.py:42 */
-      isotropic_S(n, rng);
-      break;
-    case MCV_KERNEL_POWDER:
-      powder_scatter(n, rng, c);
-      break;
-    case MCV_KERNEL_SQE_GRID:
-      n->p *= c->dp[9];
-      sqe_scatter(n, rng, c);
-      break;
-    default:
-      break;
-  }
+  kernel_scatter(n, rng, c);
   if (n->p <= 0) return;
   ninter = oracle_intersect(c, n->x, n->y, n->z, n->vx, n->vy, n->vz, ts);
   double dt3 = oracle_total_time_in_shape(ts, ninter);
@@ -1032,6 +1039,180 @@ static void hss(neutron_t* n, rng_t* rng, const mcv_component* c) {
   /* the reference uses the incident speed v here (line 98) */
   double atten2 = exp(-(mu + sigma) * v * dt3);
   n->p *= atten2;
+}
+
+/* ------------------------------------------------ multiple scattering */
+/* HomogeneousMultipleScatterer
+ * (acc/components/samples/homogeneous_multiple_scatterer.py:22-342) for
+ * one neutron: up to max_scattered_neutrons output neutrons.  Parameters
+ * as for the HSS component, plus ip[6] = max_scattered_neutrons,
+ * ip[7] = max_ms_loops | max_ms_loops_path1 << 16 and
+ * dp[14] = minimum_neutron_event_probability. */
+#define ORACLE_MS_CAP 64
+
+static double atten_coeff(const neutron_t* n, const mcv_component* c) {
+  /* _calc_atten_coeff (:67-71) */
+  return hss_sigma(n, c) + abs_coeff(n, c->dp[8]);
+}
+
+static int is_moving(const neutron_t* n) {
+  /* acc/neutron.py:39-42, MIN_VELOCITY = 1e-6 */
+  return sqrt(n->vx * n->vx + n->vy * n->vy + n->vz * n->vz) > 1.e-6;
+}
+
+/* _is_exiting (acc/geometry/propagation.py:24-50) */
+static int is_exiting(const mcv_component* c, const neutron_t* n) {
+  double ts[MCV_MAX_INTERSECTIONS];
+  int loc = oracle_locate(c, n->x, n->y, n->z);
+  if (loc == LOC_INSIDE) return 0;
+  int N = forward_intersect(c, n, ts);
+  if (N == 0) return 1;
+  if (loc == LOC_OUTSIDE) return 0;
+  double previous = 0.;
+  for (int it = 0; it < N; ++it) {
+    double now = ts[it], middle = (previous + now) / 2.;
+    if (oracle_locate(c, n->x + n->vx * middle, n->y + n->vy * middle,
+                      n->z + n->vz * middle) != LOC_ONBORDER)
+      return 0;
+    previous = now;
+  }
+  return 1;
+}
+
+/* _propagate_to_next_exiting_surface_with_attenuation (:73-84) */
+static void exit_with_attenuation(const mcv_component* c, neutron_t* n) {
+  double tof = oracle_tof_before_first_exit(c, (const double*)n);
+  double v = sqrt(n->vx * n->vx + n->vy * n->vy + n->vz * n->vz);
+  double distance = tof * v;
+  double atten = atten_coeff(n, c);
+  double transmission_prob = exp(-atten * distance);
+  oracle_propagate_to_next_exiting_surface(c, (double*)n);
+  n->p *= transmission_prob;
+}
+
+/* _interactM1 (:86-121): the transmitted and the scattered neutron.  The
+ * absorbed copy (:106-110) is overwritten by the scattered one and the
+ * kernels' absorb is a no-op (kernels/__init__.py:164-166), so it is not
+ * formed.  A neutron outside the shape after propagating to the incident
+ * surface, where the reference raises, gives no output. */
+static int interact_m1(const mcv_component* c, rng_t* rng, neutron_t* out,
+                       neutron_t* n) {
+  double vx = n->vx, vy = n->vy, vz = n->vz;
+  if (oracle_locate(c, n->x, n->y, n->z) != LOC_INSIDE)
+    oracle_propagate_to_next_incident_surface(c, (double*)n);
+  double tof = oracle_tof_before_first_exit(c, (const double*)n);
+  if (!(tof > 0.)) return 0; /* 0: :97; < 0 or NaN: the reference raises */
+  double v = sqrt(vx * vx + vy * vy + vz * vz);
+  double distance = tof * v;
+  double sigma = hss_sigma(n, c);
+  double mu = abs_coeff(n, c->dp[8]);
+  double transmission_prob = exp(-(mu + sigma) * distance);
+  out[0] = *n;
+  oracle_propagate_to_next_exiting_surface(c, (double*)&out[0]);
+  out[0].p *= transmission_prob;
+  double rand = rng_uniform(rng);
+  double x = distance * rand;
+  double prob = distance * exp(-(mu + sigma) * x);
+  out[1] = *n;
+  out[1].p *= prob;
+  prop_dt(&out[1], x / v);
+  kernel_scatter(&out[1], rng, c);
+  return 2;
+}
+
+/* _interactM_path1 (:123-177), out holding `cap` neutrons */
+static int interact_m_path1(const mcv_component* c, rng_t* rng,
+                            neutron_t* out, int cap, const neutron_t* n0) {
+  const int max_sc = c->ip[6], loops1 = c->ip[7] >> 16;
+  const double min_prob = c->dp[14];
+  neutron_t buf_a[ORACLE_MS_CAP], buf_b[ORACLE_MS_CAP], scattered[2];
+  neutron_t *tbs = buf_a, *tbs2 = buf_b;
+  if (n0->p < min_prob) return 0;
+  int ntbs = 1, out_index = 0;
+  const int lim = max_sc < cap ? max_sc : cap;
+  tbs[0] = *n0;
+  for (int iloop = 0; iloop < loops1; ++iloop) {
+    int s2 = 0;
+    for (int i = 0; i < ntbs; ++i) {
+      int ns = interact_m1(c, rng, scattered, &tbs[i]);
+      for (int j = 0; j < ns; ++j) {
+        neutron_t* s1 = &scattered[j];
+        if (s1->p < min_prob) continue;
+        if (oracle_locate(c, s1->x, s1->y, s1->z) != LOC_INSIDE) {
+          out[out_index++] = *s1;
+          if (out_index >= lim) return out_index;
+          continue;
+        }
+        tbs2[s2++] = *s1;
+        if (s2 >= max_sc) break;
+      }
+      if (s2 >= max_sc) break;
+    }
+    neutron_t* tmp = tbs2;
+    tbs2 = tbs;
+    tbs = tmp;
+    ntbs = s2;
+    if (!ntbs) break;
+  }
+  for (int i = 0; i < ntbs; ++i) {
+    if (out_index >= lim) break;
+    out[out_index++] = tbs[i];
+  }
+  return out_index;
+}
+
+/* _scatterM (:196-256): the output neutrons of one incident neutron */
+static int scatter_m(const mcv_component* c, rng_t* rng, neutron_t* out,
+                     const neutron_t* n0) {
+  const int max_sc = c->ip[6], loops = c->ip[7] & 0xffff;
+  const double min_prob = c->dp[14];
+  neutron_t buf_a[ORACLE_MS_CAP], buf_b[ORACLE_MS_CAP],
+      scattered[ORACLE_MS_CAP];
+  neutron_t *tbs = buf_a, *tbs2 = buf_b;
+  if (is_exiting(c, n0)) {
+    out[0] = *n0;
+    return 1;
+  }
+  int ntbs = 1, out_index = 0;
+  tbs[0] = *n0;
+  for (int iloop = 0; iloop < loops; ++iloop) {
+    int s2 = 0;
+    for (int i = 0; i < ntbs; ++i) {
+      int ns1 = interact_m_path1(c, rng, scattered, max_sc, &tbs[i]);
+      for (int j = 0; j < ns1; ++j) {
+        neutron_t* s1 = &scattered[j];
+        if (s1->p < min_prob) continue;
+        if (!is_moving(s1)) continue;
+        if (oracle_locate(c, s1->x, s1->y, s1->z) == LOC_INSIDE)
+          exit_with_attenuation(c, s1);
+        if (is_exiting(c, s1)) {
+          out[out_index++] = *s1;
+          if (out_index >= max_sc) return out_index;
+          continue;
+        }
+        tbs2[s2++] = *s1;
+        if (s2 >= max_sc) break;
+      }
+      if (s2 >= max_sc) break;
+    }
+    neutron_t* tmp = tbs2;
+    tbs2 = tbs;
+    tbs = tmp;
+    ntbs = s2;
+    if (!ntbs) break;
+  }
+  for (int i = 0; i < ntbs; ++i) {
+    if (out_index >= max_sc) break;
+    neutron_t* m = &tbs[i];
+    double x = m->x, y = m->y, z = m->z;
+    oracle_propagate_out(c, (double*)m);
+    double dx = m->x - x, dy = m->y - y, dz = m->z - z;
+    double dist = sqrt(dx * dx + dy * dy + dz * dz);
+    double atten = atten_coeff(m, c);
+    m->p *= exp(-atten * dist);
+    out[out_index++] = *m;
+  }
+  return out_index;
 }
 
 /* ----------------------------------------------------------- monitors */
@@ -1383,6 +1564,25 @@ int oracle_run_chain(const mcv_chain* chain, uint64_t ncount, uint64_t first,
         const mcv_component* c = &chain->comp[k];
         if (k > 0) apply_transform(&n, chain->rot[k], chain->off[k]);
         last = k;
+        if (c->opcode == MCV_OP_HMS) {
+          /* fan-out: the rest of the chain for every output neutron, in
+           * order, on the same stream (run_script.py:66-92, 245-260) */
+          neutron_t outs[ORACLE_MS_CAP];
+          int nout = scatter_m(c, &rng, outs, &n);
+          for (int j = 0; j < nout; ++j) {
+            n = outs[j];
+            for (int k2 = k + 1; k2 < nc; ++k2) {
+              apply_transform(&n, chain->rot[k2], chain->off[k2]);
+              last = k2;
+              run_component(&n, &rng, &chain->comp[k2], &tl[k2], &st);
+              if (!(n.p > 0)) {
+                if (isnan(n.p)) st.nonfinite++;
+                break;
+              }
+            }
+          }
+          break;
+        }
         run_component(&n, &rng, c, &tl[k], &st);
         if (!(n.p > 0)) {
           if (isnan(n.p)) st.nonfinite++;
@@ -1547,3 +1747,23 @@ void oracle_apply_transform(const double* rot, const double* off, double* st) {
 }
 int oracle_sizeof_chain(void) { return (int)sizeof(mcv_chain); }
 int oracle_sizeof_component(void) { return (int)sizeof(mcv_component); }
+
+/* The multiple scatterer's steps on one neutron state (tests): which = 0
+ * _interactM1, 1 _interactM_path1, 2 _scatterM; out holds up to
+ * ORACLE_MS_CAP states; uniforms from Philox (seed, index) stream 0 or
+ * from `uniforms` (count `stride`) when given.  Returns the number of
+ * output neutrons. */
+int oracle_ms_step(const mcv_component* c, int which, double* st,
+                   uint64_t seed, uint64_t index, const float* uniforms,
+                   int stride, double* out) {
+  rng_t rng;
+  rng_init(&rng, seed, index, 0, uniforms, stride);
+  neutron_t* n = (neutron_t*)st;
+  neutron_t o[ORACLE_MS_CAP];
+  int N = 0;
+  if (which == 0) N = interact_m1(c, &rng, o, n);
+  else if (which == 1) N = interact_m_path1(c, &rng, o, c->ip[6], n);
+  else N = scatter_m(c, &rng, o, n);
+  memcpy(out, o, sizeof(neutron_t) * (size_t)N);
+  return N;
+}

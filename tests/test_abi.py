@@ -117,3 +117,39 @@ def test_weight_exp2_out_of_range_rejected(engine_lib):
     rc = engine_lib.mcv_run_chain(None, ctypes.byref(ch), 1, 0, 1, 32, None,
                                   None, ctypes.byref(st))
     assert rc == nat.MCV_EINVAL and b"weight_exp2" in st.message
+
+
+def test_multiple_scatterer_rejected_where_unsupported(engine_lib):
+    """The fan-out runs in the fused run only: buffered mode, replay,
+    backward and batched launches reject a chain with an HMS before any
+    device work."""
+    from acc_gb300 import instruments
+    from acc_gb300.engine import build_chain
+    from acc_gb300.instrument import calcTransformations
+    from acc_gb300.memory import HostBinder
+    ins = instruments.ms_hollow_cylinder()
+    off, rot = calcTransformations(ins)
+    ch = build_chain(ins.components, off, rot, HostBinder())
+    st = nat.mcv_status()
+    rc = engine_lib.mcv_process_buffer(None, ctypes.byref(ch), None, 0, 0, 1,
+                                       64, None, None, ctypes.byref(st))
+    assert rc == nat.MCV_EINVAL and b"multiple scatterer" in st.message
+    g = nat.mcv_grad()
+    rc = engine_lib.mcv_backward(None, ctypes.byref(ch), ctypes.byref(g), 1,
+                                 0, 1, 64, None, None, ctypes.byref(st))
+    assert rc == nat.MCV_EINVAL and b"multiple scatterer" in st.message
+    rc = engine_lib.mcv_replay_uniforms(None, ctypes.byref(ch), 1, 0, 1, 64,
+                                        None, 0, None, None, None, None,
+                                        ctypes.byref(st))
+    assert rc == nat.MCV_EINVAL and b"multiple scatterer" in st.message
+    cnt = (ctypes.c_uint64 * 1)(1)
+    sd = (ctypes.c_uint64 * 1)(1)
+    rc = engine_lib.mcv_run_batched(None, ctypes.byref(ch), 1, cnt, sd, 64,
+                                    None, None, ctypes.byref(st))
+    assert rc == nat.MCV_EINVAL and b"multiple scatterer" in st.message
+    # more than one multiple scatterer
+    ch2 = build_chain([ins.components[1], ins.components[1]],
+                      binder=HostBinder())
+    rc = engine_lib.mcv_run_chain(None, ctypes.byref(ch2), 1, 0, 1, 64, None,
+                                  None, ctypes.byref(st))
+    assert rc == nat.MCV_EINVAL and b"at most one" in st.message

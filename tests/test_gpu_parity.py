@@ -270,3 +270,36 @@ def test_aggregated_tallies_equal_plain_atomics():
     np.testing.assert_allclose(out[0][1:], out[1][1:], rtol=1e-12,
                                atol=1e-300)
     assert out[0][0].max() > 1000  # the transmitted beam shares bins
+
+
+def test_multiple_scattering_fp64_matches_oracle():
+    """The multiple scatterer's fan-out (homogeneous_multiple_scatterer.py
+    :22-342, run_script.py:66-92): FP64 kernel and oracle on the same
+    stream give identical bin counts and sums within 1e-12."""
+    n, seed = 100_000, 5
+    ins = instruments.ms_hollow_cylinder()
+    st = engine.run_instrument(ins, n, seed=seed, floattype="float64")
+    assert st.processed == n
+    ot, _, _, _ = oracle_run(instruments.ms_hollow_cylinder(), n, seed=seed)
+    (gc, g), = gpu_tallies(ins).items()
+    (oc, o), = ot.items()
+    np.testing.assert_array_equal(g[0], o[0])
+    np.testing.assert_allclose(g[1], o[1], rtol=1e-12, atol=1e-300)
+    np.testing.assert_allclose(g[2], o[2], rtol=1e-12, atol=1e-300)
+    assert g[0].sum() > 5 * n  # several output neutrons per incident one
+
+
+def test_multiple_scattering_fp32_chi2():
+    """FP32 multiple scattering against the FP64 oracle on independent
+    streams: chi^2/dof within the bound of test_fp32_independent_stream_chi2
+    over the populated bins."""
+    n = 1_000_000
+    ins = instruments.ms_hollow_cylinder()
+    engine.run_instrument(ins, n, seed=101, floattype="float32")
+    ot, _, _, _ = oracle_run(instruments.ms_hollow_cylinder(), n, seed=202)
+    (_, g), = gpu_tallies(ins).items()
+    (_, o), = ot.items()
+    c2, dof = chi2_per_dof(g.reshape(3, -1), o.reshape(3, -1))
+    assert dof > 1000
+    bound = 1.1 if dof >= 2000 else 1.1 + 3 * np.sqrt(2 / dof)
+    assert c2 <= bound, (c2, dof)

@@ -160,3 +160,43 @@ def test_reflectivity_formula(oracle_lib):
         # libm tanh implementations is ~1e-16 absolute
         assert O.reflectivity(Q, R0, Qc, alpha, m, W) == pytest.approx(
             expected, rel=1e-14, abs=1e-15)
+
+
+def _ms_component(k):
+    from acc_gb300.components.samples.homogeneous_multiple_scatterer import \
+        factory
+    from acc_gb300.engine import build_chain
+    from acc_gb300.geometry import Cylinder, Difference
+    from acc_gb300.kernels import IsotropicKernel
+    from acc_gb300.memory import HostBinder
+    shape = Difference(Cylinder(*k["shape"]["outer"]),
+                       Cylinder(*k["shape"]["inner"]))
+    HMS = factory(shape, IsotropicKernel(k["mu"], k["sigma"]),
+                  max_ms_loops=k["max_ms_loops"],
+                  max_ms_loops_path1=k["max_ms_loops_path1"],
+                  max_scattered_neutrons=16)
+    ch = build_chain([HMS("sample")], binder=HostBinder())
+    return ch, ch.comp[0]
+
+
+def test_multiple_scatterer_known_answers(oracle_lib):
+    """test_interactM1 / test_interactM_path1 of the reference (its
+    max_scattered_neutrons=100 only bounds the lists; 16 holds them)."""
+    from oracle import binding as O
+    k = KATS["ms_hollow_cylinder"]
+    ch, comp = _ms_component(k)
+    for seed in range(8):
+        out, _ = O.ms_step(comp, "interactM1", k["neutron"], seed=seed)
+        assert len(out) == 2
+        np.testing.assert_allclose(out[0][:9], k["interactM1_transmitted"],
+                                   atol=1e-12)
+        lo, hi = k["interactM1_scattered_x_range"]
+        assert lo < out[1][0] < hi
+        out, _ = O.ms_step(comp, "interactM_path1", k["neutron"], seed=seed)
+        assert len(out) == k["max_ms_loops_path1"] + 1
+        # scatterM: every output has left the shape
+        out, _ = O.ms_step(comp, "scatterM", k["neutron"], seed=seed)
+        assert 1 <= len(out) <= 16
+        for n in out:
+            r = np.hypot(n[0], n[1])
+            assert r >= 0.02 - 1e-9 or r <= 0.01 + 1e-9 or abs(n[2]) >= 0.03
