@@ -274,6 +274,147 @@ __device__ __forceinline__ int guide(Neutron<R>& n, const mcv_component& c,
   return 1;
 }
 
+// guide_tapering.Guide.propagate (acc/components/optics/guide_tapering.py
+// :140-291): nseg equal segments, each a tapered channel, read from the
+// component's table (rows w1 w2 h1 h2 ww hh whalf hhalf lwhalf lhhalf).
+// Returns 1 when a bounce loop ran out of MCV_MAX_BOUNCES iterations.
+template <typename R>
+__device__ __forceinline__ const R* taper_table(const mcv_component& c) {
+  if constexpr (sizeof(R) == 4)
+    return c.ftable;
+  else
+    return static_cast<const double*>(c.table);
+}
+
+template <typename R>
+__device__ __forceinline__ int guide_tapering(Neutron<R>& n,
+                                              const mcv_component& c) {
+  const int nseg = c.ip[0];
+  const R* d = taper_table<R>(c);
+  const R *w1 = d, *h1 = d + 2 * nseg, *ww = d + 4 * nseg, *hh = d + 5 * nseg,
+          *whalf = d + 6 * nseg, *hhalf = d + 7 * nseg;
+  const R l_seg = prm<R>(c, 0), R0 = prm<R>(c, 1), Qcx = prm<R>(c, 2),
+          Qcy = prm<R>(c, 3), alphax = prm<R>(c, 4), alphay = prm<R>(c, 5),
+          mx = prm<R>(c, 6), my = prm<R>(c, 7), W = prm<R>(c, 8);
+  R x = n.x, y = n.y, z = n.z, vx = n.vx, vy = n.vy, vz = n.vz;
+  Tof<R> t = n.t;
+  R prob = n.p;
+  // propagate to z=0 (:163-167)
+  R dt = -z / vz;
+  x += vx * dt;
+  y += vy * dt;
+  z = R(0);
+  t.add(dt);
+  int overflow = 0;
+  for (int seg = 0; seg < nseg; ++seg) {
+    const R zr = seg * l_seg;
+    const R w1s = __ldg(&w1[seg]), hhalfs = __ldg(&hhalf[seg]);
+    const R wws = __ldg(&ww[seg]), hhs = __ldg(&hh[seg]),
+            whalfs = __ldg(&whalf[seg]);
+    // propagate to the segment entrance (:171-175)
+    dt = (zr - z) / vz;
+    x += vx * dt;
+    y += vy * dt;
+    z += vz * dt;
+    if (x <= R(-0.5) * w1s || x >= R(0.5) * w1s || y <= -hhalfs ||
+        y >= hhalfs) {
+      n.p = R(0);
+      return 0;
+    }
+    // shift origin to the center of the channel hit (:180-186)
+    x += R(0.5) * w1s;
+    const R edge = floor(x / w1s) * w1s;
+    if (x - edge > w1s) {
+      n.p = R(0);
+      return 0;
+    }
+    x -= (edge + R(0.5) * w1s);
+    const R hadj = edge + (R(0.5) * w1s) - R(0.5) * w1s;
+    int nb;
+    for (nb = 0; nb < MCV_MAX_BOUNCES; ++nb) {
+      const R av = l_seg * vx, bv = wws * vz, ah = l_seg * vy, bh = hhs * vz;
+      const R vdotn_v1 = bv + av, vdotn_v2 = bv - av;
+      const R vdotn_h1 = bh + ah, vdotn_h2 = bh - ah;
+      const R cv1 = -whalfs * l_seg - (z - zr) * wws, cv2 = x * l_seg;
+      const R ch1 = -hhalfs * l_seg - (z - zr) * hhs, ch2 = y * l_seg;
+      R t1 = (zr + l_seg - z) / vz, t2;
+      int i = 0;
+      if (vdotn_v1 < 0) {
+        t2 = (cv1 - cv2) / vdotn_v1;
+        if (t2 < t1) { t1 = t2; i = 1; }
+      }
+      if (vdotn_v2 < 0) {
+        t2 = (cv1 + cv2) / vdotn_v2;
+        if (t2 < t1) { t1 = t2; i = 2; }
+      }
+      if (vdotn_h1 < 0) {
+        t2 = (ch1 - ch2) / vdotn_h1;
+        if (t2 < t1) { t1 = t2; i = 3; }
+      }
+      if (vdotn_h2 < 0) {
+        t2 = (ch1 + ch2) / vdotn_h2;
+        if (t2 < t1) { t1 = t2; i = 4; }
+      }
+      if (i == 0) break;  // left the segment
+      x += vx * t1;
+      y += vy * t1;
+      z += vz * t1;
+      t.add(t1);
+      const R vdn = i == 1 ? vdotn_v1 : i == 2 ? vdotn_v2
+                                               : i == 3 ? vdotn_h1 : vdotn_h2;
+      const R slope = i <= 2 ? wws : hhs;
+      const R nlen2 = l_seg * l_seg + slope * slope;
+      const R q = R(kV2K) * R(-2.0) * vdn / m_sqrt(nlen2);
+      const R dd = R(2.0) * vdn / nlen2;
+      if (i == 1) {
+        vx = vx - dd * l_seg;
+        vz = vz - dd * wws;
+      } else if (i == 2) {
+        vx = vx + dd * l_seg;
+        vz = vz - dd * wws;
+      } else if (i == 3) {
+        vy = vy - dd * l_seg;
+        vz = vz - dd * hhs;
+      } else {
+        vy = vy + dd * l_seg;
+        vz = vz - dd * hhs;
+      }
+      // an m = 0 mirror ends the segment's loop (:256-258)
+      if ((i <= 2 && mx == R(0)) || (i > 2 && my == R(0))) {
+        x += hadj;
+        break;
+      }
+      R m, Rf;
+      if (i <= 2) {
+        m = mx;
+        if (m <= R(0)) m = m_fabs(mx * __ldg(&w1[0]) / w1s);
+        Rf = reflectivity(q, R0, Qcx, alphax, m, W);
+      } else {
+        m = my;
+        if (m <= R(0)) m = m_fabs(my * __ldg(&h1[0]) / __ldg(&h1[seg]));
+        Rf = reflectivity(q, R0, Qcy, alphay, m, W);
+      }
+      if (Rf > R(1e-10)) {
+        prob *= Rf;
+      } else {
+        n.p = R(0);
+        return 0;
+      }
+    }
+    if (nb == MCV_MAX_BOUNCES) overflow = 1;
+    x += hadj;
+  }
+  n.x = x;
+  n.y = y;
+  n.z = z;
+  n.vx = vx;
+  n.vy = vy;
+  n.vz = vz;
+  n.t = t;
+  n.p = prob;
+  return overflow;
+}
+
 // Slit / Beamstop (acc/components/optics/slit.py:71-108,
 // beamstop.py:75-112); dp = {xmin, xmax, ymin, ymax, radius^2, cut}
 // (`up`: the chain's FP32 weight scale, which the cut is compared in)

@@ -99,6 +99,16 @@ int validate_component(const mcv_component& c, int k, mcv_status* st) {
         return MCV_EINVAL;
       }
       break;
+    case MCV_OP_GUIDE_TAPERING:
+      if (c.ip[0] < 1 || !c.table || !c.ftable ||
+          c.table_len < (uint64_t)10 * c.ip[0] || !(c.dp[0] > 0)) {
+        set_msg(st, MCV_EINVAL,
+                "component %s%lld: tapered guide needs >= 1 segment, its "
+                "10 x nseg table and a positive segment length", "",
+                (long long)k);
+        return MCV_EINVAL;
+      }
+      break;
     case MCV_OP_HSS:
     case MCV_OP_HMS: {
       int op = c.ip[0], ker = c.ip[1];

@@ -80,6 +80,8 @@ __device__ __forceinline__ int run_component(Neutron<R>& n, Rng& rng,
       return 0;
     case MCV_OP_GUIDE:
       return guide<R>(n, c, trk);
+    case MCV_OP_GUIDE_TAPERING:
+      return guide_tapering<R>(n, c);
     case MCV_OP_HSS:
       hss(n, rng, c, trk);
       return 0;

@@ -161,6 +161,47 @@ def powder_banked(peaks=None, unitcell_volume=66.4, nbanks=8, ntubes=128,
     return ins
 
 
+def elliptic_segments(nseg=100, w_in=0.05, w_mid=0.08, w_out=0.04,
+                      h_in=0.05, h_mid=0.07, h_out=0.04):
+    """(h1, h2, w1, w2) of `nseg` equal segments approximating a guide whose
+    width and height follow half-ellipses through the entrance, middle and
+    exit openings (a synthetic profile for tests and benchmarks)."""
+    z = np.linspace(0.0, 1.0, nseg + 1)
+
+    def profile(a_in, a_mid, a_out):
+        # ellipse through (0, a_in), (0.5, a_mid), (1, a_out) in its
+        # semi-axis form a(z) = a_mid * sqrt(1 - ((z - 0.5) / b)^2) + skew
+        lin = a_in + (a_out - a_in) * z
+        bulge = (a_mid - 0.5 * (a_in + a_out)) * np.sqrt(
+            np.clip(1 - (2 * z - 1) ** 2, 0, None))
+        return lin + bulge
+
+    w, h = profile(w_in, w_mid, w_out), profile(h_in, h_mid, h_out)
+    return h[:-1], h[1:], w[:-1], w[1:]
+
+
+def tapered_guide_chain(nseg=100, length=10.99, mx=6., my=6.):
+    """A 3 x 3 cm source (10 +- 9.5 A) 2 m before the 5 x 5 cm entrance of
+    a segmented tapered guide of `length` m (elliptic profile, see
+    elliptic_segments), a position-divergence monitor 1 mm after its exit
+    (as the reference's acc_tapered_guide_instrument.py, with a synthetic
+    profile in place of its segment file)."""
+    from .components.monitors.posdiv_monitor import PosDiv_monitor
+    from .components.optics.guide_tapering import Guide as TaperedGuide
+    ins = instrument("tapered_guide_chain")
+    src = Source_simple("source", radius=0., width=0.03, height=0.03,
+                        dist=2.0, xw=0.05, yh=0.05, Lambda0=10.,
+                        dLambda=9.5)
+    guide = TaperedGuide("guide", l=length, mx=mx, my=my,
+                         segments=elliptic_segments(nseg))
+    mon = PosDiv_monitor("Ixdivx", npos=250, ndiv=250, xwidth=0.25,
+                         yheight=0.25, maxdiv=0.5, filename="Ixdivx.h5")
+    ins.append(src, position=(0, 0, 0))
+    ins.append(guide, position=(0, 0, 2.0))
+    ins.append(mon, position=(0, 0, 2.0 + length + 1e-3))
+    return ins
+
+
 def ms_hollow_cylinder(max_scattered_neutrons=16, max_ms_loops=2,
                        max_ms_loops_path1=5):
     """Multiple scattering: a 1 x 1 cm source 1 m from an 8 x 8 mm target,

@@ -46,6 +46,10 @@ WORKLOADS = {
     "sqe_hollow_cylinder": (
         "sqe_hollow_cylinder: 60 meV 1x1 cm beam -> hollow cylinder with "
         "200x200 S(Q,E) -> 3 m cylinder I(Q,E) 100x100"),
+    "tapered_guide_chain": (
+        "tapered_guide_chain: 3x3 cm source, 10 +- 9.5 A -> 10.99 m "
+        "segmented tapered guide (100 elliptic segments, m=6) -> "
+        "position-divergence monitor 250x250"),
     "ms_hollow_cylinder": (
         "ms_hollow_cylinder: 1x1 cm source, 10 +- 9.5 A -> isotropic hollow "
         "cylinder r 1-2 cm with multiple scattering (<= 16 outputs per "

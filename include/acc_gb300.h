@@ -71,7 +71,8 @@ enum {
   MCV_OP_SLIT = 13,             /* acc/components/optics/slit.py            */
   MCV_OP_BEAMSTOP = 14,         /* acc/components/optics/beamstop.py        */
   MCV_OP_HMS = 15,              /* acc/components/samples/homogeneous_multiple_scatterer.py */
-  MCV_OP_COUNT = 16
+  MCV_OP_GUIDE_TAPERING = 16,   /* acc/components/optics/guide_tapering.py  */
+  MCV_OP_COUNT = 17
 };
 
 /* ---- shapes of the homogeneous scatterer (acc/geometry/arrow_intersect.py)
@@ -138,6 +139,12 @@ enum {
  *   from the incident neutron's stream.  At most one HMS per chain; the
  *   fused thread kernel and the batched launch run it (mcv_process_buffer,
  *   mcv_backward and the regeneration kernel reject it).
+ * GUIDE_TAPERING (guide_tapering.py:22-291): nseg equal segments
+ *   ip[0]=nseg
+ *   dp: 0 l_seg 1 R0 2 Qcx 3 Qcy 4 alphax 5 alphay 6 mx 7 my 8 W
+ *   table: float64 [10][nseg] rows w1 w2 h1 h2 ww hh whalf hhalf lwhalf
+ *          lhhalf (the reference's data block, prep_inputs_kernel :122-138);
+ *          ftable: its float32 copy
  * SLIT / BEAMSTOP (slit.py:20-108, beamstop.py:18-112)
  *                                dp: xmin xmax ymin ymax radius^2 cut
  *

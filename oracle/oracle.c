@@ -360,6 +360,137 @@ static int guide(neutron_t* n, const mcv_component* c, int* nrefl) {
   return overflow;
 }
 
+/* guide_tapering.Guide.propagate
+ * (acc/components/optics/guide_tapering.py:140-291): nseg equal segments,
+ * each a tapered channel; table rows w1 w2 h1 h2 ww hh whalf hhalf lwhalf
+ * lhhalf (float64, nseg each).  Returns 1 if a bounce loop ran out. */
+static int guide_tapering(neutron_t* n, const mcv_component* c) {
+  const int nseg = c->ip[0];
+  const double* d = (const double*)c->table;
+  const double *w1 = d, *hh = d + 5 * nseg, *ww = d + 4 * nseg,
+               *whalf = d + 6 * nseg, *hhalf = d + 7 * nseg, *h1 = d + 2 * nseg;
+  const double l_seg = c->dp[0], R0 = c->dp[1], Qcx = c->dp[2],
+               Qcy = c->dp[3], alphax = c->dp[4], alphay = c->dp[5],
+               mx = c->dp[6], my = c->dp[7], W = c->dp[8];
+  double x = n->x, y = n->y, z = n->z, vx = n->vx, vy = n->vy, vz = n->vz;
+  double t = n->t, prob = n->p;
+  /* propagate to z=0 (:163-167) */
+  double dt = -z / vz;
+  x += vx * dt;
+  y += vy * dt;
+  z = 0.0;
+  t += dt;
+  int overflow = 0;
+  for (int seg = 0; seg < nseg; ++seg) {
+    double zr = seg * l_seg;
+    /* propagate to segment entrance (:171-175) */
+    dt = (zr - z) / vz;
+    x += vx * dt;
+    y += vy * dt;
+    z += vz * dt;
+    if (x <= -0.5 * w1[seg] || x >= 0.5 * w1[seg] || y <= -hhalf[seg] ||
+        y >= hhalf[seg]) {
+      n->p = 0;
+      return 0;
+    }
+    /* shift origin to center of channel hit (:180-186) */
+    x += 0.5 * w1[seg];
+    double edge = floor(x / w1[seg]) * w1[seg];
+    if (x - edge > w1[seg]) {
+      n->p = 0;
+      return 0;
+    }
+    x -= (edge + 0.5 * w1[seg]);
+    double hadj = edge + (0.5 * w1[seg]) - 0.5 * w1[seg];
+    int nb;
+    for (nb = 0; nb < MCV_MAX_BOUNCES; ++nb) {
+      double av = l_seg * vx, bv = ww[seg] * vz;
+      double ah = l_seg * vy, bh = hh[seg] * vz;
+      double vdotn_v1 = bv + av, vdotn_v2 = bv - av;
+      double vdotn_h1 = bh + ah, vdotn_h2 = bh - ah;
+      double cv1 = -whalf[seg] * l_seg - (z - zr) * ww[seg], cv2 = x * l_seg;
+      double ch1 = -hhalf[seg] * l_seg - (z - zr) * hh[seg], ch2 = y * l_seg;
+      double t1 = (zr + l_seg - z) / vz, t2;
+      int i = 0;
+      if (vdotn_v1 < 0) {
+        t2 = (cv1 - cv2) / vdotn_v1;
+        if (t2 < t1) { t1 = t2; i = 1; }
+      }
+      if (vdotn_v2 < 0) {
+        t2 = (cv1 + cv2) / vdotn_v2;
+        if (t2 < t1) { t1 = t2; i = 2; }
+      }
+      if (vdotn_h1 < 0) {
+        t2 = (ch1 - ch2) / vdotn_h1;
+        if (t2 < t1) { t1 = t2; i = 3; }
+      }
+      if (vdotn_h2 < 0) {
+        t2 = (ch1 + ch2) / vdotn_h2;
+        if (t2 < t1) { t1 = t2; i = 4; }
+      }
+      if (i == 0) break; /* left the segment */
+      x += vx * t1;
+      y += vy * t1;
+      z += vz * t1;
+      t += t1;
+      double nlen2, q, dd;
+      if (i == 1) {
+        nlen2 = l_seg * l_seg + ww[seg] * ww[seg];
+        q = V2K * (-2.0) * vdotn_v1 / sqrt(nlen2);
+        dd = 2.0 * vdotn_v1 / nlen2;
+        vx = vx - dd * l_seg;
+        vz = vz - dd * ww[seg];
+      } else if (i == 2) {
+        nlen2 = l_seg * l_seg + ww[seg] * ww[seg];
+        q = V2K * (-2.0) * vdotn_v2 / sqrt(nlen2);
+        dd = 2.0 * vdotn_v2 / nlen2;
+        vx = vx + dd * l_seg;
+        vz = vz - dd * ww[seg];
+      } else if (i == 3) {
+        nlen2 = l_seg * l_seg + hh[seg] * hh[seg];
+        q = V2K * (-2.0) * vdotn_h1 / sqrt(nlen2);
+        dd = 2.0 * vdotn_h1 / nlen2;
+        vy = vy - dd * l_seg;
+        vz = vz - dd * hh[seg];
+      } else {
+        nlen2 = l_seg * l_seg + hh[seg] * hh[seg];
+        q = V2K * (-2.0) * vdotn_h2 / sqrt(nlen2);
+        dd = 2.0 * vdotn_h2 / nlen2;
+        vy = vy + dd * l_seg;
+        vz = vz - dd * hh[seg];
+      }
+      /* an m = 0 mirror ends the segment's loop (:256-258) */
+      if ((i <= 2 && mx == 0) || (i > 2 && my == 0)) {
+        x += hadj;
+        break;
+      }
+      double m, R;
+      if (i <= 2) {
+        m = mx;
+        if (m <= 0.0) m = fabs(mx * w1[0] / w1[seg]);
+        R = oracle_reflectivity(q, R0, Qcx, alphax, m, W);
+      } else {
+        m = my;
+        if (m <= 0.0) m = fabs(my * h1[0] / h1[seg]);
+        R = oracle_reflectivity(q, R0, Qcy, alphay, m, W);
+      }
+      if (R > 1e-10) {
+        prob *= R;
+      } else {
+        n->p = 0;
+        return 0;
+      }
+    }
+    if (nb == MCV_MAX_BOUNCES) overflow = 1;
+    x += hadj;
+  }
+  n->x = x; n->y = y; n->z = z;
+  n->vx = vx; n->vy = vy; n->vz = vz;
+  n->t = t;
+  n->p = prob;
+  return overflow;
+}
+
 /* Slit.propagate / Beamstop.propagate (acc/components/optics/slit.py:71-108,
  * beamstop.py:75-112); dp = {xmin, xmax, ymin, ymax, radius^2, cut} */
 static void slit_or_beamstop(neutron_t* n, const mcv_component* c, int stop) {
@@ -1487,6 +1618,9 @@ static void run_component(neutron_t* n, rng_t* rng, const mcv_component* c,
     case MCV_OP_ARM: break;
     case MCV_OP_SOURCE_SIMPLE: source_simple(n, rng, c); break;
     case MCV_OP_GUIDE: st->bounce_overflow += guide(n, c, NULL); break;
+    case MCV_OP_GUIDE_TAPERING:
+      st->bounce_overflow += guide_tapering(n, c);
+      break;
     case MCV_OP_HSS: hss(n, rng, c); break;
     case MCV_OP_PSD_MONITOR: psd_monitor(n, c, tl); break;
     case MCV_OP_PSD_MONITOR_4PI: psd_monitor_4pi(n, c, tl); break;

@@ -37,6 +37,7 @@ BUILDERS = {
     "sphere_theta_tof": instruments.sphere_theta_tof,
     "guide_chain": instruments.guide_chain,
     "sqe_hollow_cylinder": instruments.sqe_hollow_cylinder,
+    "tapered_guide_chain": instruments.tapered_guide_chain,
 }
 
 

@@ -200,3 +200,40 @@ def test_multiple_scatterer_known_answers(oracle_lib):
         for n in out:
             r = np.hypot(n[0], n[1])
             assert r >= 0.02 - 1e-9 or r <= 0.01 + 1e-9 or abs(n[2]) >= 0.03
+
+
+def test_single_segment_tapered_guide_is_the_plain_guide(oracle_lib):
+    """guide_tapering.py with one segment, equal coatings on both mirror
+    pairs and the same opening is guide.py's propagate (the two restate the
+    same bounce loop): identical final states, except where the tapered
+    guide's 1e-10 reflectivity cut (:263-275) ends a neutron the plain
+    guide keeps with a smaller weight."""
+    import acc_gb300
+    from acc_gb300.components.optics.guide import Guide
+    from acc_gb300.components.optics.guide_tapering import Guide as Tapered
+    from acc_gb300.components.sources.source_simple import Source_simple
+    from helpers import oracle_run
+    out = []
+    for kind in ("plain", "tapered"):
+        ins = acc_gb300.instrument()
+        ins.append(Source_simple("s", radius=0.05, dist=1.0, xw=0.05,
+                                 yh=0.05, E0=52.5, dE=47.5),
+                   position=(0, 0, 0))
+        coat = dict(R0=0.99, W=0.003)
+        if kind == "plain":
+            g = Guide("g", w1=0.05, h1=0.05, w2=0.03, h2=0.02, l=10.,
+                      Qc=0.0219, alpha=3., m=3., **coat)
+        else:
+            g = Tapered("g", l=10., mx=3., my=3., Qcx=0.0219, Qcy=0.0219,
+                        alphax=3., alphay=3.,
+                        segments=([0.05], [0.02], [0.05], [0.03]), **coat)
+        ins.append(g, position=(0, 0, 1.0))
+        _, _, o, last = oracle_run(ins, 100000, seed=4, record=True)
+        out.append((o, last))
+    (a, la), (b, lb) = out
+    alive_a, alive_b = a[:, 9] > 0, b[:, 9] > 0
+    differ = alive_a != alive_b
+    assert differ.sum() <= 100 and not (alive_b & ~alive_a).any()
+    both = alive_a & alive_b
+    assert both.sum() > 1000
+    np.testing.assert_allclose(b[both], a[both], rtol=1e-12, atol=1e-15)
