@@ -71,6 +71,164 @@ __device__ __forceinline__ void source_simple(Neutron<R>& n, Rng& rng,
   n.p = pmul * solidangle;
 }
 
+// ================================================== SNS moderator source
+// SNS_source (acc/components/sources/SNS_source.py:20-207): E and the
+// emission time from the moderator's cumulative tables (the host computes
+// them as _SNS_source_utils.py:187-223 does), in FP64 in both precisions.
+// The two loops of zero_find, unbounded in the reference, stop after 64 /
+// 200 passes, as in the oracle.
+constexpr int kSnsExpandMax = 64;
+constexpr int kSnsBisectMax = 200;
+
+// a table column, or P(t) interpolated between two E rows at weight wl
+struct SnsVec {
+  const double* a;
+  const double* b;  // null: plain column
+  double wl;
+  __device__ __forceinline__ double at(int i) const {
+    return b ? __ldg(&a[i]) * wl + __ldg(&b[i]) * (1 - wl) : __ldg(&a[i]);
+  }
+};
+
+// quadint (SNS_source.py:59-64)
+__device__ __forceinline__ double sns_quadint(double xdes, double x1,
+                                              double x2, double x3,
+                                              double y1, double y2,
+                                              double y3) {
+  double t1 = ((xdes - x2) * (xdes - x3) * y1) / ((x1 - x2) * (x1 - x3));
+  double t2 = ((xdes - x1) * (xdes - x3) * y2) / ((x2 - x1) * (x2 - x3));
+  double t3 = ((xdes - x1) * (xdes - x2) * y3) / ((x3 - x1) * (x3 - x2));
+  return t1 + t2 + t3;
+}
+
+// quadfuncint (:66-75).  The reference scans up from index 1 for the first
+// point not below xdes; on the ascending tables a binary search finds the
+// same index.  Past the last point the reference reads beyond the array
+// (undefined); the last bracket extrapolates here.  Index -1 wraps to the
+// last point, as numba indexes.
+__device__ __forceinline__ double sns_quadfuncint(double xdes, int xylen,
+                                                  const double* vecx,
+                                                  const SnsVec& vecy) {
+  int lo = 1, hi = xylen;  // first idx in [1, xylen) with !(vecx < xdes)
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(&vecx[mid]) < xdes) lo = mid + 1;
+    else hi = mid;
+  }
+  int idx = lo >= xylen ? xylen - 1 : lo;
+  const double xi = __ldg(&vecx[idx]);
+  if (xi == xdes) return vecy.at(idx);
+  const int i0 = idx - 2 < 0 ? idx - 2 + xylen : idx - 2;
+  return sns_quadint(xdes, __ldg(&vecx[i0]), __ldg(&vecx[idx - 1]), xi,
+                     vecy.at(i0), vecy.at(idx - 1), vecy.at(idx));
+}
+
+// zero_find (:78-96)
+__device__ __forceinline__ double sns_zero_find(const double* vecx, int len,
+                                                const SnsVec& vecy,
+                                                double yval, double xmin,
+                                                double xmax, double tol) {
+  double xl = xmin;
+  double xh = pow(10.0, (log10(xmin) + yval * (log10(xmax) - log10(xmin))));
+  double f = sns_quadfuncint(xl, len, vecx, vecy) - yval;
+  double fmid = sns_quadfuncint(xh, len, vecx, vecy) - yval;
+  for (int k = 0; k < kSnsExpandMax && fmid * f >= 0.0; ++k) {
+    xh = xh + (xh - xl) * 2.0;
+    fmid = sns_quadfuncint(xh, len, vecx, vecy) - yval;
+  }
+  double dx = xh - xl, rtb = xl;
+  for (int k = 0; k < kSnsBisectMax &&
+                  fabs(sns_quadfuncint(rtb, len, vecx, vecy) - yval) > tol;
+       ++k) {
+    dx = dx * 0.5;
+    const double xmid = rtb + dx;
+    fmid = sns_quadfuncint(xmid, len, vecx, vecy) - yval;
+    if (fmid < 0) rtb = xmid;
+  }
+  return rtb;
+}
+
+// generate (:22-54): E (meV) and t (s) from two uniforms.  Out of line:
+// one copy for the kernels that contain a source.
+static __device__ __noinline__ void sns_generate(const mcv_component& c,
+                                                 double randE, double randt,
+                                                 double* Eout,
+                                                 double* tout) {
+  const int nE = c.ip[1], nt = c.ip[2];
+  const int Eidx_start = c.ip[3], Eidx_stop = c.ip[4];
+  const int tidx_start = c.ip[5], tidx_stop = c.ip[6];
+  const double* Es = static_cast<const double*>(c.table);
+  const double* Pvec = Es + nE;
+  const double* ts = Pvec + nE;
+  const double* Ptmat = ts + nt;
+  const double EPmin = c.dp[6], EPmax = c.dp[7];
+  double randp = EPmin + randE * (EPmax - EPmin);
+  const SnsVec pv{Pvec, nullptr, 0.0};
+  const double Eval = sns_zero_find(Es, nE, pv, randp, __ldg(&Es[Eidx_start]),
+                                    __ldg(&Es[Eidx_stop]), 1e-7);
+  int lo = 0, hi = nE;  // first idx with !(Es < Eval): the reference's scan
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(&Es[mid]) < Eval) lo = mid + 1;
+    else hi = mid;
+  }
+  const int Eidxh = lo, Eidxl = lo - 1;
+  const double wl = (__ldg(&Es[Eidxh]) - Eval) /
+                    (__ldg(&Es[Eidxh]) - __ldg(&Es[Eidxl]));
+  const SnsVec pt{Ptmat + (size_t)Eidxl * nt, Ptmat + (size_t)Eidxh * nt, wl};
+  const double p0 = pt.at(tidx_start), p1 = pt.at(tidx_stop - 1);
+  randp = p0 + randt * (p1 - p0);
+  double tval = 0;
+  if (randp > 0.0)
+    tval = sns_zero_find(ts, nt, pt, randp, __ldg(&ts[tidx_start]),
+                         __ldg(&ts[tidx_stop - 1]), 1e-5);
+  *Eout = Eval * 1000.0;
+  *tout = tval * 1e-6;
+}
+
+// SNS_source.propagate (:157-207)
+template <typename R, typename Rng>
+__device__ __forceinline__ void sns_source(Neutron<R>& n, Rng& rng,
+                                           const mcv_component& c) {
+  const R randx = rng.next(), randy = rng.next();
+  const R rand_theta = rng.next(), rand_phi = rng.next();
+  const double randE = rng.next(), randt = rng.next();
+  const R xwidth = prm<R>(c, 0), yheight = prm<R>(c, 1),
+          radius = prm<R>(c, 2);
+  const R focus_xw = prm<R>(c, 3), focus_yh = prm<R>(c, 4),
+          dist = prm<R>(c, 5);
+  R x, y;
+  if (c.ip[0]) {
+    x = xwidth * (randx - R(0.5));
+    y = yheight * (randy - R(0.5));
+  } else {
+    R s, co;
+    m_sincos_2pi(randx, &s, &co);
+    const R r = m_sqrt(randy) * radius;
+    x = r * co;
+    y = r * s;
+  }
+  const R hdivmax = atan((focus_xw / R(2.0) - x) / dist);
+  const R hdivmin = atan(-(focus_xw / R(2.0) + x) / dist);
+  const R vdivmax = atan((focus_yh / R(2.0) - y) / dist);
+  const R vdivmin = atan(-(focus_yh / R(2.0) + y) / dist);
+  const R theta = hdivmin + (hdivmax - hdivmin) * rand_theta;
+  const R phi = vdivmin + (vdivmax - vdivmin) * rand_phi;
+  double E, t;
+  sns_generate(c, randE, randt, &E, &t);
+  const R v = R(kSE2V * sqrt(E));
+  n.x = x;
+  n.y = y;
+  n.z = R(0);
+  n.vx = v * cos(phi) * sin(theta);
+  n.vy = v * sin(phi);
+  n.vz = v * cos(phi) * cos(theta);
+  n.sx = R(0);
+  n.sy = R(0);
+  n.t.set(R(t));
+  n.p = prm<R>(c, 8);
+}
+
 // ====================================================================== guide
 // calc_reflectivity (acc/components/optics/_guide_utils.py:6-23)
 __device__ __forceinline__ double reflectivity(double Q, double R0, double Qc,

@@ -99,6 +99,23 @@ int validate_component(const mcv_component& c, int k, mcv_status* st) {
         return MCV_EINVAL;
       }
       break;
+    case MCV_OP_SNS_SOURCE: {
+      const int nE = c.ip[1], nt = c.ip[2];
+      const bool ok = c.table && nE >= 3 && nt >= 3 &&
+                      c.table_len >= (uint64_t)(2 * nE + nt) +
+                                         (uint64_t)nE * nt &&
+                      c.ip[3] >= 1 && c.ip[3] < nE && c.ip[4] >= 1 &&
+                      c.ip[4] < nE && c.ip[5] >= 0 && c.ip[6] >= 1 &&
+                      c.ip[6] <= nt && c.ip[5] < c.ip[6] && c.dp[5] > 0;
+      if (!ok) {
+        set_msg(st, MCV_EINVAL,
+                "component %s%lld: SNS source needs its E / t tables "
+                "(>= 3 points each) and index ranges inside them",
+                "", (long long)k);
+        return MCV_EINVAL;
+      }
+      break;
+    }
     case MCV_OP_GUIDE_TAPERING:
       if (c.ip[0] < 1 || !c.table || !c.ftable ||
           c.table_len < (uint64_t)10 * c.ip[0] || !(c.dp[0] > 0)) {
@@ -191,6 +208,18 @@ bool has_hms(const mcv_chain* ch) {
   return false;
 }
 
+// The rarer components run in their own kernel instantiations (kX): the
+// SNS source, the tapered guide, the multiple scatterer.
+bool is_exotic(const mcv_chain* ch) {
+  for (int k = 0; k < ch->ncomp; ++k) {
+    const int op = ch->comp[k].opcode;
+    if (op == MCV_OP_HMS || op == MCV_OP_SNS_SOURCE ||
+        op == MCV_OP_GUIDE_TAPERING)
+      return true;
+  }
+  return false;
+}
+
 int precision_ok(int precision, mcv_status* st) {
   if (precision != MCV_FP32 && precision != MCV_FP64) {
     set_msg(st, MCV_EINVAL, "precision must be 32 or 64, got %s%lld", "",
@@ -228,11 +257,13 @@ int launch_chain(mcv_ctx* ctx, int mode, const mcv_chain* chain,
                  const float* uni, int stride, double* out_n, int* out_last,
                  const mcv_launch* launch, cudaStream_t s) {
   int blocks, threads;
+  const bool x = is_exotic(chain);
   launch_shape(
-      ctx, [mode](int t) { return Launchers<R>::occupancy_chain(mode, t); },
+      ctx,
+      [mode, x](int t) { return Launchers<R>::occupancy_chain(mode, x, t); },
       ncount, launch, &blocks, &threads);
-  Launchers<R>::chain(mode, blocks, threads, s, *chain, ncount, first, seed,
-                      uni, stride, out_n, out_last, ctx->d_status);
+  Launchers<R>::chain(mode, x, blocks, threads, s, *chain, ncount, first,
+                      seed, uni, stride, out_n, out_last, ctx->d_status);
   return 0;
 }
 
@@ -293,9 +324,10 @@ int validate_batch(const mcv_chain* variants, int nvar, const uint64_t* counts,
   }
   for (int v = 0; v < nvar; ++v) {
     int rc = validate_chain(variants + v, st);
-    if (!rc && has_hms(variants + v)) {
+    if (!rc && is_exotic(variants + v)) {
       set_msg(st, MCV_EINVAL,
-              "batched run: no multiple scatterer in a variant%s", "");
+              "batched run: no multiple scatterer, SNS source or tapered "
+              "guide in a variant%s", "");
       rc = MCV_EINVAL;
     }
     if (rc) {
@@ -362,9 +394,10 @@ uint64_t sum_counts(const uint64_t* counts, int nvar) {
 // chain validation for the other entry-point unit (noalloc.cu)
 int mcv::validate_chain_for(const mcv_chain* ch, mcv_status* st) {
   int rc = validate_chain(ch, st);
-  if (!rc && has_hms(ch)) {
+  if (!rc && is_exotic(ch)) {
     set_msg(st, MCV_EINVAL,
-            "batched run: no multiple scatterer in a variant%s", "");
+            "batched run: no multiple scatterer, SNS source or tapered "
+            "guide in a variant%s", "");
     rc = MCV_EINVAL;
   }
   return rc;
@@ -481,23 +514,24 @@ int mcv_run_chain(mcv_ctx* ctx, const mcv_chain* chain, uint64_t ncount,
   if (precision == MCV_FP32) {
     if (use_regen(chain, launch)) {
       int blocks, threads;
+      const bool x = is_exotic(chain);
       launch_shape(
           ctx,
-          [chain, launch](int t) {
+          [chain, launch, x](int t) {
             return Launchers<float>::occupancy_regen(
-                t, regen_tail_bytes(chain, launch, t));
+                t, regen_tail_bytes(chain, launch, t), x);
           },
           ncount, launch, &blocks, &threads);
       Launchers<float>::regen(blocks, threads,
-                              regen_tail_bytes(chain, launch, threads), s,
+                              regen_tail_bytes(chain, launch, threads), x, s,
                               *chain, ncount, first, seed, ctx->d_status);
     } else {
-      launch_chain<float>(ctx, has_hms(chain) ? 3 : 0, chain, ncount, first,
-                          seed, nullptr, 0, nullptr, nullptr, launch, s);
+      launch_chain<float>(ctx, 0, chain, ncount, first, seed, nullptr, 0,
+                          nullptr, nullptr, launch, s);
     }
   } else {
-    launch_chain<double>(ctx, has_hms(chain) ? 3 : 0, chain, ncount, first,
-                         seed, nullptr, 0, nullptr, nullptr, launch, s);
+    launch_chain<double>(ctx, 0, chain, ncount, first, seed, nullptr, 0,
+                         nullptr, nullptr, launch, s);
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(st, e, "mcv_run_chain launch");
@@ -569,16 +603,19 @@ int mcv_process_buffer(mcv_ctx* ctx, const mcv_chain* chain, void* neutrons,
   DeviceGuard g(ctx->device);
   cudaStream_t s = (cudaStream_t)stream;
   int blocks, threads;
+  const bool x = is_exotic(chain);
   if (precision == MCV_FP32) {
-    launch_shape(ctx, Launchers<float>::occupancy_buffer, n, launch, &blocks,
-                 &threads);
-    Launchers<float>::buffer(blocks, threads, s, *chain, neutrons, n, first,
-                             seed, ctx->d_status);
+    launch_shape(
+        ctx, [x](int t) { return Launchers<float>::occupancy_buffer(t, x); },
+        n, launch, &blocks, &threads);
+    Launchers<float>::buffer(blocks, threads, x, s, *chain, neutrons, n,
+                             first, seed, ctx->d_status);
   } else {
-    launch_shape(ctx, Launchers<double>::occupancy_buffer, n, launch, &blocks,
-                 &threads);
-    Launchers<double>::buffer(blocks, threads, s, *chain, neutrons, n, first,
-                              seed, ctx->d_status);
+    launch_shape(
+        ctx, [x](int t) { return Launchers<double>::occupancy_buffer(t, x); },
+        n, launch, &blocks, &threads);
+    Launchers<double>::buffer(blocks, threads, x, s, *chain, neutrons, n,
+                              first, seed, ctx->d_status);
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(st, e, "mcv_process_buffer launch");
@@ -689,9 +726,10 @@ int mcv_backward(mcv_ctx* ctx, const mcv_chain* chain, const mcv_grad* grad,
                  mcv_status* st) {
   int rc = validate_chain(chain, st);
   if (rc) return rc;
-  if (has_hms(chain)) {
+  if (is_exotic(chain)) {
     set_msg(st, MCV_EINVAL,
-            "mcv_backward: no gradients through the multiple scatterer%s", "");
+            "mcv_backward: no gradients through the multiple scatterer, the "
+            "SNS source or the tapered guide%s", "");
     return MCV_EINVAL;
   }
   if (!precision_ok(precision, st)) return MCV_EINVAL;

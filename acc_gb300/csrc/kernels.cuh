@@ -67,7 +67,11 @@ __device__ __forceinline__ void apply_transform(Neutron<R>& n,
 }
 
 // One component on one neutron; returns 1 when a guide ran out of bounces.
-template <typename R, typename Rng, typename Trk>
+// kX: the instantiation for chains with the rarer components (SNS source,
+// tapered guide, multiple scatterer); the common kernels leave their code
+// out so that it weighs on neither their registers nor their instruction
+// stream (the host launches the kX kernels for such chains only).
+template <typename R, bool kX = false, typename Rng, typename Trk>
 __device__ __forceinline__ int run_component(Neutron<R>& n, Rng& rng,
                                              const mcv_component& c,
                                              Trk& trk, const mcv_chain& ch) {
@@ -78,10 +82,17 @@ __device__ __forceinline__ int run_component(Neutron<R>& n, Rng& rng,
       source_simple<R>(n, rng, c);
       if constexpr (sizeof(R) == 4) n.p *= weight_up<R>(ch);
       return 0;
+    case MCV_OP_SNS_SOURCE:
+      if constexpr (kX) {
+        sns_source<R>(n, rng, c);
+        if constexpr (sizeof(R) == 4) n.p *= weight_up<R>(ch);
+      }
+      return 0;
     case MCV_OP_GUIDE:
       return guide<R>(n, c, trk);
     case MCV_OP_GUIDE_TAPERING:
-      return guide_tapering<R>(n, c);
+      if constexpr (kX) return guide_tapering<R>(n, c);
+      return 0;
     case MCV_OP_HSS:
       hss(n, rng, c, trk);
       return 0;
@@ -130,7 +141,7 @@ struct Counters {
 // Whole chain on one neutron (the body of the generated
 // process_kernel_no_buffer, acc/run_script.py:182-196).  A neutron leaves
 // the chain after a component that leaves its weight not positive.
-template <typename R, bool kMS = false, typename Rng, typename Trk = NoTrack>
+template <typename R, bool kX = false, typename Rng, typename Trk = NoTrack>
 __device__ __forceinline__ int run_chain_one(Neutron<R>& n, Rng& rng,
                                              const mcv_chain& ch,
                                              Counters& k, Trk&& trk = Trk()) {
@@ -146,7 +157,7 @@ __device__ __forceinline__ int run_chain_one(Neutron<R>& n, Rng& rng,
     if (c > 0) apply_transform<R>(n, ch, c);
     last = c;
     trk.begin_component(ch, c);
-    if constexpr (kMS && !std::decay_t<Trk>::kActive) {
+    if constexpr (kX && !std::decay_t<Trk>::kActive) {
       if (ch.comp[c].opcode == MCV_OP_HMS) {
         // fan-out: the rest of the chain for every output neutron, in
         // order, on the same stream (run_script.py:66-92, 245-260)
@@ -158,7 +169,8 @@ __device__ __forceinline__ int run_chain_one(Neutron<R>& n, Rng& rng,
           for (int c2 = c + 1; c2 < nc; ++c2) {
             apply_transform<R>(n, ch, c2);
             last = c2;
-            k.overflow += run_component<R>(n, rng, ch.comp[c2], trk, ch);
+            k.overflow +=
+                run_component<R, kX>(n, rng, ch.comp[c2], trk, ch);
             if (!(n.p > 0)) {
               if (m_isnan(n.p)) k.nonfinite++;
               break;
@@ -169,7 +181,7 @@ __device__ __forceinline__ int run_chain_one(Neutron<R>& n, Rng& rng,
         continue;
       }
     }
-    k.overflow += run_component<R>(n, rng, ch.comp[c], trk, ch);
+    k.overflow += run_component<R, kX>(n, rng, ch.comp[c], trk, ch);
     if (!(n.p > 0)) {
       if (m_isnan(n.p)) k.nonfinite++;
       alive = false;
@@ -215,10 +227,9 @@ __device__ __forceinline__ void flush_counters(const Counters& k,
 
 constexpr int kMaxThreads = 256;
 
-// MODE 0: Philox; 1: Philox + record; 2: injected uniforms + record;
-// 3: Philox, with the multiple scatterer's fan-out (its own instantiation:
-// the per-thread work lists would weigh on every other chain)
-template <typename R, int MODE>
+// MODE 0: Philox; 1: Philox + record; 2: injected uniforms + record.
+// kX: the instantiation with the rarer components (run_component).
+template <typename R, int MODE, bool kX = false>
 __global__ void __launch_bounds__(kMaxThreads)
     chain_kernel(const __grid_constant__ mcv_chain ch, uint64_t n,
                  uint64_t first, uint64_t seed, const float* __restrict__ uni,
@@ -233,11 +244,11 @@ __global__ void __launch_bounds__(kMaxThreads)
     int last;
     if constexpr (MODE == 2) {
       InjectedStream rng(uni + i * (uint64_t)stride, stride);
-      last = run_chain_one<R>(nt, rng, ch, k);
+      last = run_chain_one<R, kX>(nt, rng, ch, k);
       k.overrun += rng.overrun();
     } else {
       PhiloxStream rng(seed, first + i, 0u);
-      last = run_chain_one<R, MODE == 3>(nt, rng, ch, k);
+      last = run_chain_one<R, kX>(nt, rng, ch, k);
     }
     k.processed++;
     if constexpr (MODE == 1 || MODE == 2) {
@@ -325,7 +336,7 @@ __device__ __forceinline__ void tail_load(const uint32_t* q, int slot,
 // Every neutron is computed with the same functions, in the same order and
 // with its own Philox stream, as in chain_kernel, so results agree neutron
 // by neutron (up to the compiler's contraction choices).
-template <typename R, typename Trk>
+template <typename R, bool kX, typename Trk>
 __device__ __forceinline__ void regen_body(const mcv_chain& ch, uint64_t n,
                                            uint64_t first, uint64_t seed,
                                            int tail_queue, DevStatus* st,
@@ -406,7 +417,7 @@ __device__ __forceinline__ void regen_body(const mcv_chain& ch, uint64_t n,
         nb = 0;
         if (inside) continue;
       } else {
-        k.overflow += run_component<R>(nt, rng, cp, trk, ch);
+        k.overflow += run_component<R, kX>(nt, rng, cp, trk, ch);
       }
       if (!(nt.p > 0) || kc + 1 >= nc) {
         if (m_isnan(nt.p)) k.nonfinite++;
@@ -460,13 +471,13 @@ __device__ __forceinline__ void regen_body(const mcv_chain& ch, uint64_t n,
   flush_counters(k, st);
 }
 
-template <typename R>
+template <typename R, bool kX = false>
 __global__ void __launch_bounds__(kMaxThreads)
     regen_kernel(const __grid_constant__ mcv_chain ch, uint64_t n,
                  uint64_t first, uint64_t seed, int tail_queue,
                  DevStatus* st) {
   NoTrack trk;
-  regen_body<R>(ch, n, first, seed, tail_queue, st, trk);
+  regen_body<R, kX>(ch, n, first, seed, tail_queue, st, trk);
 }
 
 // The backward replay with the regeneration kernel's structure: the same
@@ -479,7 +490,7 @@ __global__ void __launch_bounds__(kMaxThreads)
                       uint64_t first, uint64_t seed, double* powder_x,
                       double* powder_y, int tail_queue, DevStatus* st) {
   GradTrack<R> trk(g, ch, powder_x, powder_y);
-  regen_body<R>(ch, n, first, seed, tail_queue, st, trk);
+  regen_body<R, false>(ch, n, first, seed, tail_queue, st, trk);
   trk.flush(ch);
 }
 
@@ -509,7 +520,7 @@ __global__ void __launch_bounds__(kMaxThreads)
 // Buffered mode (ComponentBase.process, ComponentBase.py:79-129): the chain
 // applied to a stored neutron array in place; component k draws from
 // Philox stream k+1.
-template <typename R>
+template <typename R, bool kX = false>
 __global__ void __launch_bounds__(kMaxThreads)
     buffer_kernel(const __grid_constant__ mcv_chain ch, R* __restrict__ buf,
                   uint64_t n, uint64_t first, uint64_t seed, DevStatus* st) {
@@ -535,7 +546,7 @@ __global__ void __launch_bounds__(kMaxThreads)
       if (c > 0) apply_transform<R>(nt, ch, c);
       PhiloxStream rng(seed, first + i, (uint32_t)(c + 1));
       NoTrack trk;
-      k.overflow += run_component<R>(nt, rng, cp, trk, ch);
+      k.overflow += run_component<R, kX>(nt, rng, cp, trk, ch);
     }
     k.processed++;
     s[0] = nt.x;
@@ -647,16 +658,17 @@ namespace mcv {
 // Host-side launchers of the kernels above for one working precision.
 template <typename R>
 struct Launchers {
-  static int occupancy_chain(int mode, int threads);
-  static void chain(int mode, int blocks, int threads, cudaStream_t s,
-                    const mcv_chain& ch, uint64_t n, uint64_t first,
-                    uint64_t seed, const float* uni, int stride,
-                    double* out_n, int* out_last, DevStatus* st);
+  // x: the chain holds one of the rarer components (kX instantiations)
+  static int occupancy_chain(int mode, bool x, int threads);
+  static void chain(int mode, bool x, int blocks, int threads,
+                    cudaStream_t s, const mcv_chain& ch, uint64_t n,
+                    uint64_t first, uint64_t seed, const float* uni,
+                    int stride, double* out_n, int* out_last, DevStatus* st);
   // smem: the tail queue's bytes (0 = no queue)
-  static int occupancy_regen(int threads, size_t smem);
-  static void regen(int blocks, int threads, size_t smem, cudaStream_t s,
-                    const mcv_chain& ch, uint64_t n, uint64_t first,
-                    uint64_t seed, DevStatus* st);
+  static int occupancy_regen(int threads, size_t smem, bool x);
+  static void regen(int blocks, int threads, size_t smem, bool x,
+                    cudaStream_t s, const mcv_chain& ch, uint64_t n,
+                    uint64_t first, uint64_t seed, DevStatus* st);
   static int occupancy_grad_regen(int threads, size_t smem);
   // dynamic shared memory above 48 KB must be allowed per kernel
   static cudaError_t allow_grad_regen_smem(size_t smem);
@@ -670,8 +682,8 @@ struct Launchers {
                    const mcv_chain& ch, const mcv_grad& g, uint64_t n,
                    uint64_t first, uint64_t seed, double* px, double* py,
                    DevStatus* st);
-  static int occupancy_buffer(int threads);
-  static void buffer(int blocks, int threads, cudaStream_t s,
+  static int occupancy_buffer(int threads, bool x);
+  static void buffer(int blocks, int threads, bool x, cudaStream_t s,
                      const mcv_chain& ch, void* buf, uint64_t n,
                      uint64_t first, uint64_t seed, DevStatus* st);
   static int occupancy_batched(int threads, size_t smem);
@@ -701,43 +713,55 @@ void powder_finalize(const double* px, const double* py, int npeaks,
 
 #ifdef MCV_DEFINE_LAUNCHERS
 template <typename R>
-int Launchers<R>::occupancy_chain(int mode, int threads) {
+int Launchers<R>::occupancy_chain(int mode, bool x, int threads) {
+  if (x) {
+    if (mode == 0) return occupancy_of(chain_kernel<R, 0, true>, threads, 0);
+    if (mode == 1) return occupancy_of(chain_kernel<R, 1, true>, threads, 0);
+    return occupancy_of(chain_kernel<R, 2, true>, threads, 0);
+  }
   if (mode == 0) return occupancy_of(chain_kernel<R, 0>, threads, 0);
   if (mode == 1) return occupancy_of(chain_kernel<R, 1>, threads, 0);
-  if (mode == 3) return occupancy_of(chain_kernel<R, 3>, threads, 0);
   return occupancy_of(chain_kernel<R, 2>, threads, 0);
 }
 
 template <typename R>
-void Launchers<R>::chain(int mode, int blocks, int threads, cudaStream_t s,
-                         const mcv_chain& ch, uint64_t n, uint64_t first,
-                         uint64_t seed, const float* uni, int stride,
-                         double* out_n, int* out_last, DevStatus* st) {
-  if (mode == 0)
-    chain_kernel<R, 0><<<blocks, threads, 0, s>>>(ch, n, first, seed, uni,
-                                                  stride, out_n, out_last, st);
-  else if (mode == 1)
-    chain_kernel<R, 1><<<blocks, threads, 0, s>>>(ch, n, first, seed, uni,
-                                                  stride, out_n, out_last, st);
-  else if (mode == 3)
-    chain_kernel<R, 3><<<blocks, threads, 0, s>>>(ch, n, first, seed, uni,
-                                                  stride, out_n, out_last, st);
-  else
-    chain_kernel<R, 2><<<blocks, threads, 0, s>>>(ch, n, first, seed, uni,
-                                                  stride, out_n, out_last, st);
+void Launchers<R>::chain(int mode, bool x, int blocks, int threads,
+                         cudaStream_t s, const mcv_chain& ch, uint64_t n,
+                         uint64_t first, uint64_t seed, const float* uni,
+                         int stride, double* out_n, int* out_last,
+                         DevStatus* st) {
+#define MCV_CHAIN_LAUNCH(M, X)                                              \
+  chain_kernel<R, M, X><<<blocks, threads, 0, s>>>(ch, n, first, seed, uni, \
+                                                   stride, out_n, out_last, \
+                                                   st)
+  if (x) {
+    if (mode == 0) MCV_CHAIN_LAUNCH(0, true);
+    else if (mode == 1) MCV_CHAIN_LAUNCH(1, true);
+    else MCV_CHAIN_LAUNCH(2, true);
+  } else {
+    if (mode == 0) MCV_CHAIN_LAUNCH(0, false);
+    else if (mode == 1) MCV_CHAIN_LAUNCH(1, false);
+    else MCV_CHAIN_LAUNCH(2, false);
+  }
+#undef MCV_CHAIN_LAUNCH
 }
 
 template <typename R>
-int Launchers<R>::occupancy_regen(int threads, size_t smem) {
-  return occupancy_of(regen_kernel<R>, threads, smem);
+int Launchers<R>::occupancy_regen(int threads, size_t smem, bool x) {
+  return x ? occupancy_of(regen_kernel<R, true>, threads, smem)
+           : occupancy_of(regen_kernel<R, false>, threads, smem);
 }
 
 template <typename R>
-void Launchers<R>::regen(int blocks, int threads, size_t smem,
+void Launchers<R>::regen(int blocks, int threads, size_t smem, bool x,
                          cudaStream_t s, const mcv_chain& ch, uint64_t n,
                          uint64_t first, uint64_t seed, DevStatus* st) {
-  regen_kernel<R><<<blocks, threads, smem, s>>>(ch, n, first, seed,
-                                                 smem > 0 ? 1 : 0, st);
+  if (x)
+    regen_kernel<R, true><<<blocks, threads, smem, s>>>(
+        ch, n, first, seed, smem > 0 ? 1 : 0, st);
+  else
+    regen_kernel<R, false><<<blocks, threads, smem, s>>>(
+        ch, n, first, seed, smem > 0 ? 1 : 0, st);
 }
 
 template <typename R>
@@ -778,16 +802,21 @@ void Launchers<R>::grad(int blocks, int threads, cudaStream_t s,
 }
 
 template <typename R>
-int Launchers<R>::occupancy_buffer(int threads) {
-  return occupancy_of(buffer_kernel<R>, threads, 0);
+int Launchers<R>::occupancy_buffer(int threads, bool x) {
+  return x ? occupancy_of(buffer_kernel<R, true>, threads, 0)
+           : occupancy_of(buffer_kernel<R, false>, threads, 0);
 }
 
 template <typename R>
-void Launchers<R>::buffer(int blocks, int threads, cudaStream_t s,
+void Launchers<R>::buffer(int blocks, int threads, bool x, cudaStream_t s,
                           const mcv_chain& ch, void* buf, uint64_t n,
                           uint64_t first, uint64_t seed, DevStatus* st) {
-  buffer_kernel<R><<<blocks, threads, 0, s>>>(ch, (R*)buf, n, first, seed,
-                                              st);
+  if (x)
+    buffer_kernel<R, true><<<blocks, threads, 0, s>>>(ch, (R*)buf, n, first,
+                                                      seed, st);
+  else
+    buffer_kernel<R, false><<<blocks, threads, 0, s>>>(ch, (R*)buf, n,
+                                                       first, seed, st);
 }
 
 template <typename R>

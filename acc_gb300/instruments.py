@@ -13,6 +13,7 @@ densities) and documented beside each builder.
 """
 
 import math
+import os
 
 import numpy as np
 
@@ -158,6 +159,66 @@ def powder_banked(peaks=None, unitcell_volume=66.4, nbanks=8, ntubes=128,
     z = 16.002 + 0.5
     ins.append(HSS("sample"), position=(0, 0, z), orientation=(90, 0, 0))
     ins.append(det, position=(0, 0, z))
+    return ins
+
+
+def synthetic_moderator_file(path=None, nE=60, nt=50):
+    """Write a moderator file in the format SNS_source reads
+    (acc/components/sources/_SNS_source_utils.py:12-57) with a synthetic
+    spectrum and pulse shapes (no measured data) and return its path (a
+    temporary file when `path` is None):
+
+      f(E) = E / kT^2 exp(-E / kT) + 0.02 / E   (Maxwellian at kT = 25 meV
+                                                 with an epithermal tail)
+      I(t, E) = (t / tau) exp(-t / tau),  tau = 20 us + 40 us sqrt(kT / E)
+
+    on nE log-spaced energies in [1e-4, 10] eV and nt log-spaced times in
+    [0.05, 3000] us."""
+    import tempfile
+    if path is None:
+        fd, path = tempfile.mkstemp(suffix=".dat", prefix="moderator_")
+        os.close(fd)
+    kT = 0.025
+    E = np.logspace(-4, 1, nE)
+    lam = 9.044567 / np.sqrt(E * 1000.0)
+    fE = E / kT ** 2 * np.exp(-E / kT) + 0.02 / E
+    t = np.logspace(np.log10(0.05), np.log10(3000.0), nt)
+    lines = ["## synthetic moderator file (acc_gb300.instruments)",
+             "## section 1: E, wavelength, f(E), err, f(l), err"]
+    for e, l, f in zip(E, lam, fE):
+        lines.append(f"  {e:.6e}   {l:.6e}   {f:.6e}   {0.01 * f:.6e}"
+                     f"   {f:.6e}   {0.01 * f:.6e}")
+    lines += ["", "", "## section1end", "## section 2: t, E, I, err"]
+    for e in E:
+        tau = 20.0 + 40.0 * np.sqrt(kT / e)
+        I = (t / tau) * np.exp(-t / tau)
+        for tt, ii in zip(t, I):
+            lines.append(f"  {tt:.6e}   {e:.6e}   {ii:.6e}   {0.01 * ii:.6e}")
+        lines.append("")
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")
+    return path
+
+
+def sns_source_chain(filename=None, Emin=5., Emax=20.):
+    """An SNS moderator source (3 x 3 cm face, energies Emin-Emax meV from
+    `filename`, a synthetic moderator file when None) aimed at a 3 x 3 cm
+    window 5 m away, where a PSD (100 x 100 over +-3 cm) and an energy
+    monitor (100 bins over 0-25 meV) sit: the reference's SNS source test
+    set-up (tests/components/sources/test_SNS_source.py:12-15)."""
+    from .components.sources.SNS_source import SNS_source
+    if filename is None:
+        filename = synthetic_moderator_file()
+    ins = instrument("sns_source_chain")
+    src = SNS_source("src", filename, Emin, Emax, 0.03, 0.03, 5., .03, .03)
+    psd = PSD_monitor("psd", xmin=-0.03, xmax=0.03, ymin=-0.03, ymax=0.03,
+                      nx=100, ny=100, filename="psd.h5")
+    emon = Energy_monitor("energy", xmin=-0.03, xmax=0.03, ymin=-0.03,
+                          ymax=0.03, Emin=0.0, Emax=25.0, nchan=100,
+                          filename="energy.h5")
+    ins.append(src, position=(0, 0, 0))
+    ins.append(psd, position=(0, 0, 5.0))
+    ins.append(emon, position=(0, 0, 5.0))
     return ins
 
 

@@ -46,6 +46,9 @@ WORKLOADS = {
     "sqe_hollow_cylinder": (
         "sqe_hollow_cylinder: 60 meV 1x1 cm beam -> hollow cylinder with "
         "200x200 S(Q,E) -> 3 m cylinder I(Q,E) 100x100"),
+    "sns_source_chain": (
+        "sns_source_chain: SNS moderator source (synthetic moderator file, "
+        "5-20 meV, 3x3 cm) -> PSD 100x100 + energy 100 bins at 5 m"),
     "tapered_guide_chain": (
         "tapered_guide_chain: 3x3 cm source, 10 +- 9.5 A -> 10.99 m "
         "segmented tapered guide (100 elliptic segments, m=6) -> "

@@ -72,7 +72,8 @@ enum {
   MCV_OP_BEAMSTOP = 14,         /* acc/components/optics/beamstop.py        */
   MCV_OP_HMS = 15,              /* acc/components/samples/homogeneous_multiple_scatterer.py */
   MCV_OP_GUIDE_TAPERING = 16,   /* acc/components/optics/guide_tapering.py  */
-  MCV_OP_COUNT = 17
+  MCV_OP_SNS_SOURCE = 17,       /* acc/components/sources/SNS_source.py     */
+  MCV_OP_COUNT = 18
 };
 
 /* ---- shapes of the homogeneous scatterer (acc/geometry/arrow_intersect.py)
@@ -145,6 +146,14 @@ enum {
  *   table: float64 [10][nseg] rows w1 w2 h1 h2 ww hh whalf hhalf lwhalf
  *          lhhalf (the reference's data block, prep_inputs_kernel :122-138);
  *          ftable: its float32 copy
+ * SNS_SOURCE (SNS_source.py:20-207, _SNS_source_utils.py:187-223)
+ *   ip: 0 square 1 nE 2 nt 3 Eidx_start 4 Eidx_stop 5 tidx_start
+ *       6 tidx_stop
+ *   dp: 0 xwidth 1 yheight 2 radius 3 focus_xw 4 focus_yh 5 dist 6 EPmin
+ *       7 EPmax 8 prob
+ *   table: float64 Es[nE] (eV), Pvec[nE], ts[nt] (us), Ptmat[nE][nt]
+ *          (cumulative probabilities from the host's set-up)
+ *   E and t are drawn in FP64 in both precisions (the tables are FP64).
  * SLIT / BEAMSTOP (slit.py:20-108, beamstop.py:18-112)
  *                                dp: xmin xmax ymin ymax radius^2 cut
  *

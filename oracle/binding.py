@@ -71,6 +71,9 @@ def lib():
             ctypes.c_void_p, ctypes.c_int, c_double_p, ctypes.c_uint64,
             ctypes.c_uint64, ctypes.c_void_p, ctypes.c_int, c_double_p]
         L.oracle_ms_step.restype = ctypes.c_int
+        L.oracle_sns_generate.argtypes = [
+            ctypes.c_void_p, ctypes.c_double, ctypes.c_double, c_double_p,
+            c_double_p]
         L.oracle_guide_one.argtypes = [ctypes.c_void_p, c_double_p]
         L.oracle_guide_one.restype = ctypes.c_int
         L.oracle_source_one.argtypes = [ctypes.c_void_p, ctypes.c_void_p, c_double_p]
@@ -258,6 +261,15 @@ def ms_step(comp, step, neutron, seed=1, index=0, uniforms=None):
     n = lib().oracle_ms_step(ctypes.byref(comp), MS_STEPS[step], _dp(st),
                              int(seed), int(index), uptr, stride, _dp(out))
     return out[:n].copy(), st
+
+
+def sns_generate(comp, randE, randt):
+    """The SNS source's (E in meV, t in s) for two uniforms
+    (SNS_source.generate)."""
+    E, t = ctypes.c_double(), ctypes.c_double()
+    lib().oracle_sns_generate(ctypes.byref(comp), float(randE), float(randt),
+                              ctypes.byref(E), ctypes.byref(t))
+    return E.value, t.value
 
 
 def process_buffer(chain, neutrons, seed=1, first=0, nthreads=0):

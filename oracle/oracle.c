@@ -258,6 +258,148 @@ static void source_simple(neutron_t* n, rng_t* rng, const mcv_component* c) {
 }
 
 /* -------------------------------------------------------------- guide */
+/* ------------------------------------------------ SNS moderator source */
+/* SNS_source (acc/components/sources/SNS_source.py:20-207).  Table
+ * (float64): Es[nE], Pvec[nE], ts[nt], Ptmat[nE][nt]; ip: 0 square 1 nE
+ * 2 nt 3 Eidx_start 4 Eidx_stop 5 tidx_start 6 tidx_stop; dp: 0 xwidth
+ * 1 yheight 2 radius 3 focus_xw 4 focus_yh 5 dist 6 EPmin 7 EPmax 8 prob.
+ * The two loops of zero_find, unbounded in the reference, stop after
+ * SNS_EXPAND_MAX / SNS_BISECT_MAX passes (the GPU kernels use the same
+ * caps). */
+#define SNS_EXPAND_MAX 64
+#define SNS_BISECT_MAX 200
+
+/* a row of values: a table column, or P(t) interpolated between two E
+ * rows at weight wl (generate, :44-47) */
+typedef struct {
+  const double* a;
+  const double* b; /* NULL: plain column */
+  double wl;
+} snsvec_t;
+
+static inline double snsvec_at(const snsvec_t* v, int i) {
+  return v->b ? v->a[i] * v->wl + v->b[i] * (1 - v->wl) : v->a[i];
+}
+
+/* quadint (:59-64) */
+static double sns_quadint(double xdes, double x1, double x2, double x3,
+                          double y1, double y2, double y3) {
+  double t1 = ((xdes - x2) * (xdes - x3) * y1) / ((x1 - x2) * (x1 - x3));
+  double t2 = ((xdes - x1) * (xdes - x3) * y2) / ((x2 - x1) * (x2 - x3));
+  double t3 = ((xdes - x1) * (xdes - x2) * y3) / ((x3 - x1) * (x3 - x2));
+  return t1 + t2 + t3;
+}
+
+/* quadfuncint (:66-75).  Past the last point the reference reads beyond
+ * the array (undefined); here the last bracket extrapolates.  Index -1
+ * wraps to the last point, as numba indexes. */
+static double sns_quadfuncint(double xdes, int xylen, const double* vecx,
+                              const snsvec_t* vecy) {
+  int idx = 1;
+  while (idx < xylen && vecx[idx] < xdes) idx += 1;
+  if (idx >= xylen) idx = xylen - 1;
+  if (vecx[idx] == xdes) return snsvec_at(vecy, idx);
+  int i0 = idx - 2 < 0 ? idx - 2 + xylen : idx - 2;
+  return sns_quadint(xdes, vecx[i0], vecx[idx - 1], vecx[idx],
+                     snsvec_at(vecy, i0), snsvec_at(vecy, idx - 1),
+                     snsvec_at(vecy, idx));
+}
+
+/* zero_find (:78-96) */
+static double sns_zero_find(const double* vecx, int len,
+                            const snsvec_t* vecy, double yval, double xmin,
+                            double xmax, double tol) {
+  double xl = xmin;
+  double xh = pow(10, (log10(xmin) + yval * (log10(xmax) - log10(xmin))));
+  double f = sns_quadfuncint(xl, len, vecx, vecy) - yval;
+  double fmid = sns_quadfuncint(xh, len, vecx, vecy) - yval;
+  for (int k = 0; k < SNS_EXPAND_MAX && fmid * f >= 0.0; ++k) {
+    xh = xh + (xh - xl) * 2.0;
+    fmid = sns_quadfuncint(xh, len, vecx, vecy) - yval;
+  }
+  double dx = xh - xl, rtb = xl;
+  for (int k = 0; k < SNS_BISECT_MAX &&
+                  fabs(sns_quadfuncint(rtb, len, vecx, vecy) - yval) > tol;
+       ++k) {
+    dx = dx * 0.5;
+    double xmid = rtb + dx;
+    fmid = sns_quadfuncint(xmid, len, vecx, vecy) - yval;
+    if (fmid < 0) rtb = xmid;
+  }
+  return rtb;
+}
+
+/* generate (:22-54): E (meV) and t (s) from two uniforms */
+static void sns_generate(const mcv_component* c, double randE, double randt,
+                         double* Eout, double* tout) {
+  const int nE = c->ip[1], nt = c->ip[2];
+  const int Eidx_start = c->ip[3], Eidx_stop = c->ip[4];
+  const int tidx_start = c->ip[5], tidx_stop = c->ip[6];
+  const double* Es = (const double*)c->table;
+  const double* Pvec = Es + nE;
+  const double* ts = Pvec + nE;
+  const double* Ptmat = ts + nt;
+  const double EPmin = c->dp[6], EPmax = c->dp[7];
+  double randp = EPmin + randE * (EPmax - EPmin);
+  snsvec_t pv = {Pvec, NULL, 0.};
+  double Eval = sns_zero_find(Es, nE, &pv, randp, Es[Eidx_start],
+                              Es[Eidx_stop], 1e-7);
+  int idx1 = 0;
+  while (idx1 < nE && Es[idx1] < Eval) idx1 += 1;
+  int Eidxh = idx1, Eidxl = idx1 - 1;
+  double wl = (Es[Eidxh] - Eval) / (Es[Eidxh] - Es[Eidxl]);
+  snsvec_t pt = {Ptmat + (size_t)Eidxl * nt, Ptmat + (size_t)Eidxh * nt, wl};
+  double p0 = snsvec_at(&pt, tidx_start), p1 = snsvec_at(&pt, tidx_stop - 1);
+  randp = p0 + randt * (p1 - p0);
+  double tval = 0;
+  if (randp > 0.0)
+    tval = sns_zero_find(ts, nt, &pt, randp, ts[tidx_start],
+                         ts[tidx_stop - 1], 1e-5);
+  *Eout = Eval * 1000.0;
+  *tout = tval * 1e-6;
+}
+
+/* SNS_source.propagate (:157-207) */
+static void sns_source(neutron_t* n, rng_t* rng, const mcv_component* c) {
+  double randx = rng_uniform(rng), randy = rng_uniform(rng);
+  double rand_theta = rng_uniform(rng), rand_phi = rng_uniform(rng);
+  double randE = rng_uniform(rng), randt = rng_uniform(rng);
+  const double xwidth = c->dp[0], yheight = c->dp[1], radius = c->dp[2];
+  const double focus_xw = c->dp[3], focus_yh = c->dp[4], dist = c->dp[5];
+  double x, y;
+  if (c->ip[0]) {
+    x = xwidth * (randx - 0.5);
+    y = yheight * (randy - 0.5);
+  } else {
+    double chi = 2 * M_PI * randx, r = sqrt(randy) * radius;
+    x = r * cos(chi);
+    y = r * sin(chi);
+  }
+  double hdivmax = atan((focus_xw / 2.0 - x) / dist);
+  double hdivmin = atan(-(focus_xw / 2.0 + x) / dist);
+  double vdivmax = atan((focus_yh / 2.0 - y) / dist);
+  double vdivmin = atan(-(focus_yh / 2.0 + y) / dist);
+  double theta = hdivmin + (hdivmax - hdivmin) * rand_theta;
+  double phi = vdivmin + (vdivmax - vdivmin) * rand_phi;
+  double E, t;
+  sns_generate(c, randE, randt, &E, &t);
+  double v = SE2V * sqrt(E);
+  n->x = x;
+  n->y = y;
+  n->z = 0.;
+  n->vx = v * cos(phi) * sin(theta);
+  n->vy = v * sin(phi);
+  n->vz = v * cos(phi) * cos(theta);
+  n->t = t;
+  n->p = c->dp[8];
+}
+
+/* generate() alone, for tests */
+void oracle_sns_generate(const mcv_component* c, double randE, double randt,
+                         double* E, double* t) {
+  sns_generate(c, randE, randt, E, t);
+}
+
 /* calc_reflectivity (acc/components/optics/_guide_utils.py:6-23) */
 double oracle_reflectivity(double Q, double R0, double Qc, double alpha,
                            double m, double W) {
@@ -1617,6 +1759,7 @@ static void run_component(neutron_t* n, rng_t* rng, const mcv_component* c,
   switch (c->opcode) {
     case MCV_OP_ARM: break;
     case MCV_OP_SOURCE_SIMPLE: source_simple(n, rng, c); break;
+    case MCV_OP_SNS_SOURCE: sns_source(n, rng, c); break;
     case MCV_OP_GUIDE: st->bounce_overflow += guide(n, c, NULL); break;
     case MCV_OP_GUIDE_TAPERING:
       st->bounce_overflow += guide_tapering(n, c);

@@ -33,11 +33,22 @@ from helpers import chi2_per_dof, gpu_tallies, oracle_run, rel_err
 
 pytestmark = pytest.mark.gpu
 
+_MODERATOR = []
+
+
+def _sns_source_chain():
+    # one synthetic moderator file for the session
+    if not _MODERATOR:
+        _MODERATOR.append(instruments.synthetic_moderator_file())
+    return instruments.sns_source_chain(_MODERATOR[0])
+
+
 BUILDERS = {
     "sphere_theta_tof": instruments.sphere_theta_tof,
     "guide_chain": instruments.guide_chain,
     "sqe_hollow_cylinder": instruments.sqe_hollow_cylinder,
     "tapered_guide_chain": instruments.tapered_guide_chain,
+    "sns_source_chain": _sns_source_chain,
 }
 
 
