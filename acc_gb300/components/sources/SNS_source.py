@@ -21,13 +21,40 @@ from .SourceBase import SourceBase
 category = 'sources'
 
 
-def sns_source_load(filename, xcol=0, ycol=2):
+def sts_params_load(stream):
+    """The STS file's section 0 (_SNS_source_utils.py:62-78): one number
+    per line (first token) up to '## section 0 end'; the last must be the
+    check value 12345678.  Returns (PPower, Freq, MRadius, MOffangle,
+    PHeight, PWidth, TRadius)."""
+    params = []
+    while True:
+        line = stream.readline()
+        if not line:
+            raise RuntimeError("no '## section 0 end' line")
+        if line.startswith("## section 0 end"):
+            break
+        if line.startswith("#"):
+            continue
+        if len(line.strip()) != 0:
+            params.append(float(line.strip().split()[0]))
+    if not params or params[-1] != 12345678.0:
+        raise RuntimeError("ERROR: Inconsistent parameter data set. Expected "
+                           "check string 12345678, got "
+                           f"{params[-1] if params else None}")
+    return np.array(params[:-1])
+
+
+def sns_source_load(filename, xcol=0, ycol=2, sts=False):
     """The moderator file (_SNS_source_utils.py:12-57): section 1, one row
     per energy (eV) with the spectrum in column `ycol`, ends at the first
     blank line; section 2 holds one block per energy of rows (t in us, E,
     brightness, error), blocks separated by blank lines, '#' lines are
-    comments.  Returns (E, I(E), veclen, t, I[E][t])."""
+    comments.  Returns (E, I(E), veclen, t, I[E][t]), and the STS
+    parameters first when `sts` (the file then opens with section 0)."""
+    params = None
     with open(filename, "rt") as stream:
+        if sts:
+            params = sts_params_load(stream)
         first_block = []
         while True:
             line = stream.readline()
@@ -70,8 +97,9 @@ def sns_source_load(filename, xcol=0, ycol=2):
     for i in range(nE):
         if not np.allclose(mat[i, :, 0], tvec):
             raise RuntimeError(f"{filename}: times of section 2 differ")
-    return (np.ascontiguousarray(xvec), np.ascontiguousarray(yvec), veclen,
-            np.ascontiguousarray(tvec), np.ascontiguousarray(mat[:, :, 2]))
+    out = (np.ascontiguousarray(xvec), np.ascontiguousarray(yvec), veclen,
+           np.ascontiguousarray(tvec), np.ascontiguousarray(mat[:, :, 2]))
+    return out + (params,) if sts else out
 
 
 def Pcalc(func, llim, hlim, xvec, Prob, veclen):
@@ -103,13 +131,15 @@ def Pcalc(func, llim, hlim, xvec, Prob, veclen):
     return idxstart, idxstop
 
 
-def init(Emin, Emax, datafile):
+def init(Emin, Emax, datafile, sts_load=False):
     """_SNS_source_utils.init (:187-223): Emin, Emax in meV.  Returns
     (INorm2, Es, Pvec, ts, Ptmat, EPmin, EPmax, (Eidx_start, Eidx_stop),
-    (tidx_start, tidx_stop))."""
+    (tidx_start, tidx_stop)), and the STS parameters last when
+    `sts_load`."""
     import scipy.integrate as si
     import scipy.interpolate as sinterp
-    inxvec, inyvec, xylength, tvec, mat = sns_source_load(datafile, 0, 2)
+    loaded = sns_source_load(datafile, 0, 2, sts=sts_load)
+    inxvec, inyvec, xylength, tvec, mat = loaded[:5]
     nE, nt = mat.shape
     llim, hlim = inxvec[1], inxvec[xylength]
     I_E = sinterp.interp1d(inxvec, inyvec, kind="quadratic")
@@ -124,8 +154,9 @@ def init(Emin, Emax, datafile):
     f = sinterp.interp1d(inxvec, Pvec, kind="quadratic")
     EPmax = float(f(Emax / 1000.0))
     EPmin = float(f(Emin / 1000.0))
-    return (INorm2, inxvec, Pvec, tvec, Ptmat, EPmin, EPmax,
-            (idxstart, idxstop), (tidxstart, tidxstop))
+    out = (INorm2, inxvec, Pvec, tvec, Ptmat, EPmin, EPmax,
+           (idxstart, idxstop), (tidxstart, tidxstop))
+    return out + (loaded[5],) if sts_load else out
 
 
 class SNS_source(SourceBase):
@@ -180,3 +211,92 @@ class SNS_source(SourceBase):
         flat = np.concatenate([Es, Pvec, ts, np.asarray(Ptmat).reshape(-1)])
         c.table = binder.table(self, "moderator", flat, np.float64)
         c.table_len = flat.size
+        self.pack_geometry(c)
+
+    def pack_geometry(self, c):
+        c.ip[7] = 0
+
+
+class STS_source(SNS_source):
+    """STS moderator source (acc/components/sources/STS_source.py:107-284):
+    the SNS source's energy and time draws, on a cylindrical moderator
+    whose radius, port size and flight angle come from the file's
+    section 0."""
+
+    def __init__(self, name, filename, Emin, Emax, xwidth, yheight, dist,
+                 focus_xw, focus_yh, PPower=0.0, frequency=0.0,
+                 MOffangle=-1000.0, dmode=1.0, radius=0.0):
+        self.name = name
+        self.Emin, self.Emax = Emin, Emax
+        (self.INorm2, Es, Pvec, ts, Ptmat, EPmin, EPmax, Eidx_range,
+         tidx_range, sts_params) = init(Emin, Emax, filename, sts_load=True)
+        self.xwidth, self.yheight, self.radius = xwidth, yheight, radius
+        self.PPower, self.frequency = PPower, frequency
+        (self.PPower0, self.Freq0, self.MRadius0, MOffangle0, PHeight,
+         PWidth, TRadius) = sts_params
+        # the file's flight angle is used (:134-138)
+        self.MOffangle = MOffangle0
+        if MOffangle != MOffangle0 and MOffangle > -1000.0:
+            warnings.warn("Requested MOffangle different from value in "
+                          "source file")
+        self.MOffangle_rad = math.pi / 180.0 * self.MOffangle
+        self.tanMOa = 1.0
+        # the reference sets the cylinder only for square ports (:160-175)
+        self.cylx = self.cylz = self.cylphi1 = self.cylphi2 = 0.0
+        if TRadius > 0.0:
+            Anorm = np.pi * TRadius * TRadius
+            if self.radius > TRadius or self.radius <= 0.0:
+                self.radius = TRadius
+                warnings.warn("radius not set or requested is larger than "
+                              "TRadius. Setting radius=TRadius.")
+            self.square = False
+            srcArea = np.pi * self.radius * self.radius
+            self.tanMOa = math.tan(self.MOffangle_rad)
+        else:
+            Anorm = PWidth * PHeight
+            if self.xwidth > PWidth or self.xwidth <= 0.0:
+                self.xwidth = PWidth
+                warnings.warn("xwidth not set or requested larger than "
+                              "PWidth. Setting xwidth=PWidth")
+            if self.yheight > PHeight or self.yheight <= 0.0:
+                self.yheight = PHeight
+                warnings.warn("yheight not set or requested larger than "
+                              "PHeight. Setting yheight=PHeight")
+            self.square = True
+            srcArea = self.xwidth * self.yheight
+            MR = self.MRadius0
+            self.cylz = -MR * math.cos(self.MOffangle_rad)
+            self.cylx = -MR * math.sin(self.MOffangle_rad)
+            arg = math.sqrt(MR * MR - (self.xwidth / 2.0 - self.cylx) ** 2) \
+                + self.cylz
+            self.cylphi1 = 2.0 * math.asin(
+                math.sqrt(arg * arg + 0.25 * self.xwidth * self.xwidth)
+                / 2.0 / MR)
+            arg = math.sqrt(MR * MR - (-self.xwidth / 2.0 - self.cylx) ** 2) \
+                + self.cylz
+            self.cylphi2 = 2.0 * math.asin(
+                math.sqrt(arg * arg + 0.25 * self.xwidth * self.xwidth)
+                / 2.0 / MR)
+        self.p_in = focus_xw * focus_yh / (dist * dist) * srcArea / Anorm
+        if self.PPower > 0.0:
+            self.p_in *= self.PPower / self.PPower0
+        if self.frequency > 0.0:
+            self.p_in *= self.Freq0 / self.frequency
+        self.dmode = dmode == 1.0
+        self._prob = self.p_in * self.INorm2
+        self.dist, self.focus_xw, self.focus_yh = dist, focus_xw, focus_yh
+        self.Anorm = Anorm
+        self.tables = (Es, Pvec, ts, Ptmat)
+        # as the reference, the sampling uses the requested xwidth, yheight
+        # and radius (:203-206), the area the adjusted ones
+        self.propagate_params = (
+            self.square, xwidth, yheight, radius, focus_xw, focus_yh, dist,
+            EPmin, EPmax, Es, Eidx_range[0], Eidx_range[1], Pvec, ts,
+            tidx_range[0], tidx_range[1], Ptmat, self._prob)
+
+    def pack_geometry(self, c):
+        c.ip[7] = 1 | (2 if self.dmode else 0)
+        for k, v in enumerate((self.tanMOa, self.cylx, self.cylz,
+                               self.cylphi1, self.cylphi2, self.MRadius0,
+                               self.MOffangle_rad)):
+            set_param(c, 9 + k, v)

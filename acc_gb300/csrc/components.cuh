@@ -197,8 +197,31 @@ __device__ __forceinline__ void sns_source(Neutron<R>& n, Rng& rng,
           radius = prm<R>(c, 2);
   const R focus_xw = prm<R>(c, 3), focus_yh = prm<R>(c, 4),
           dist = prm<R>(c, 5);
-  R x, y;
-  if (c.ip[0]) {
+  R x, y, z = R(0);
+  if (c.ip[7] & 1) {
+    // STS_source.propagate (STS_source.py:242-259)
+    const R tanMOa = prm<R>(c, 9), cylx = prm<R>(c, 10), cylz = prm<R>(c, 11);
+    const R cylphi1 = prm<R>(c, 12), cylphi2 = prm<R>(c, 13);
+    const R MR = prm<R>(c, 14), MOa = prm<R>(c, 15);
+    if (c.ip[0]) {
+      y = yheight * (randy - R(0.5));
+      if (c.ip[7] & 2) {
+        x = xwidth * (randx - R(0.5));
+        z = m_sqrt(MR * MR - (x - cylx) * (x - cylx)) + cylz;
+      } else {
+        const R ang = -cylphi1 + randx * (cylphi1 + cylphi2) + MOa;
+        z = cylz + MR * cos(ang);
+        x = cylx + MR * sin(ang);
+      }
+    } else {
+      R s, co;
+      m_sincos_2pi(randx, &s, &co);
+      const R r = m_sqrt(randy) * radius;
+      x = r * co;
+      y = r * s;
+      z = tanMOa * x;
+    }
+  } else if (c.ip[0]) {
     x = xwidth * (randx - R(0.5));
     y = yheight * (randy - R(0.5));
   } else {
@@ -219,7 +242,7 @@ __device__ __forceinline__ void sns_source(Neutron<R>& n, Rng& rng,
   const R v = R(kSE2V * sqrt(E));
   n.x = x;
   n.y = y;
-  n.z = R(0);
+  n.z = z;
   n.vx = v * cos(phi) * sin(theta);
   n.vy = v * sin(phi);
   n.vz = v * cos(phi) * cos(theta);

@@ -162,7 +162,7 @@ def powder_banked(peaks=None, unitcell_volume=66.4, nbanks=8, ntubes=128,
     return ins
 
 
-def synthetic_moderator_file(path=None, nE=60, nt=50):
+def synthetic_moderator_file(path=None, nE=60, nt=50, sts=False):
     """Write a moderator file in the format SNS_source reads
     (acc/components/sources/_SNS_source_utils.py:12-57) with a synthetic
     spectrum and pulse shapes (no measured data) and return its path (a
@@ -173,7 +173,9 @@ def synthetic_moderator_file(path=None, nE=60, nt=50):
       I(t, E) = (t / tau) exp(-t / tau),  tau = 20 us + 40 us sqrt(kT / E)
 
     on nE log-spaced energies in [1e-4, 10] eV and nt log-spaced times in
-    [0.05, 3000] us."""
+    [0.05, 3000] us.  `sts`: with the STS file's section 0 first (power
+    700 kW, 15 Hz, moderator radius 3 cm, flight angle 5 deg, port 3 x
+    3 cm, no disk)."""
     import tempfile
     if path is None:
         fd, path = tempfile.mkstemp(suffix=".dat", prefix="moderator_")
@@ -183,8 +185,13 @@ def synthetic_moderator_file(path=None, nE=60, nt=50):
     lam = 9.044567 / np.sqrt(E * 1000.0)
     fE = E / kT ** 2 * np.exp(-E / kT) + 0.02 / E
     t = np.logspace(np.log10(0.05), np.log10(3000.0), nt)
-    lines = ["## synthetic moderator file (acc_gb300.instruments)",
-             "## section 1: E, wavelength, f(E), err, f(l), err"]
+    lines = ["## synthetic moderator file (acc_gb300.instruments)"]
+    if sts:
+        lines += ["## section 0: PPower, Freq, MRadius, MOffangle, PHeight,"
+                  " PWidth, TRadius, check", "  700.0", "  15.0", "  0.03",
+                  "  5.0", "  0.03", "  0.03", "  0.0", "  12345678.0",
+                  "## section 0 end"]
+    lines += ["## section 1: E, wavelength, f(E), err, f(l), err"]
     for e, l, f in zip(E, lam, fE):
         lines.append(f"  {e:.6e}   {l:.6e}   {f:.6e}   {0.01 * f:.6e}"
                      f"   {f:.6e}   {0.01 * f:.6e}")
@@ -211,6 +218,26 @@ def sns_source_chain(filename=None, Emin=5., Emax=20.):
         filename = synthetic_moderator_file()
     ins = instrument("sns_source_chain")
     src = SNS_source("src", filename, Emin, Emax, 0.03, 0.03, 5., .03, .03)
+    psd = PSD_monitor("psd", xmin=-0.03, xmax=0.03, ymin=-0.03, ymax=0.03,
+                      nx=100, ny=100, filename="psd.h5")
+    emon = Energy_monitor("energy", xmin=-0.03, xmax=0.03, ymin=-0.03,
+                          ymax=0.03, Emin=0.0, Emax=25.0, nchan=100,
+                          filename="energy.h5")
+    ins.append(src, position=(0, 0, 0))
+    ins.append(psd, position=(0, 0, 5.0))
+    ins.append(emon, position=(0, 0, 5.0))
+    return ins
+
+
+def sts_source_chain(filename=None, Emin=5., Emax=20., dmode=1.0):
+    """An STS moderator source (the sns_source_chain set-up on the
+    cylindrical moderator of a synthetic STS file)."""
+    from .components.sources.SNS_source import STS_source
+    if filename is None:
+        filename = synthetic_moderator_file(sts=True)
+    ins = instrument("sts_source_chain")
+    src = STS_source("src", filename, Emin, Emax, 0.03, 0.03, 5., .03, .03,
+                     dmode=dmode)
     psd = PSD_monitor("psd", xmin=-0.03, xmax=0.03, ymin=-0.03, ymax=0.03,
                       nx=100, ny=100, filename="psd.h5")
     emon = Energy_monitor("energy", xmin=-0.03, xmax=0.03, ymin=-0.03,

@@ -154,6 +154,10 @@ enum {
  *   table: float64 Es[nE] (eV), Pvec[nE], ts[nt] (us), Ptmat[nE][nt]
  *          (cumulative probabilities from the host's set-up)
  *   E and t are drawn in FP64 in both precisions (the tables are FP64).
+ *   STS_source (STS_source.py:107-284): ip[7] bit 0 set, bit 1 = dmode;
+ *   dp: 9 tanMOa 10 cylx 11 cylz 12 cylphi1 13 cylphi2 14 MRadius0
+ *       15 MOffangle (rad): the face point lies on the cylindrical
+ *       moderator (square ports) or on the tilted disk
  * SLIT / BEAMSTOP (slit.py:20-108, beamstop.py:18-112)
  *                                dp: xmin xmax ymin ymax radius^2 cut
  *

@@ -366,8 +366,29 @@ static void sns_source(neutron_t* n, rng_t* rng, const mcv_component* c) {
   double randE = rng_uniform(rng), randt = rng_uniform(rng);
   const double xwidth = c->dp[0], yheight = c->dp[1], radius = c->dp[2];
   const double focus_xw = c->dp[3], focus_yh = c->dp[4], dist = c->dp[5];
-  double x, y;
-  if (c->ip[0]) {
+  double x, y, z = 0.;
+  if (c->ip[7] & 1) {
+    /* STS_source.propagate (STS_source.py:242-259) */
+    const double tanMOa = c->dp[9], cylx = c->dp[10], cylz = c->dp[11];
+    const double cylphi1 = c->dp[12], cylphi2 = c->dp[13];
+    const double MR = c->dp[14], MOa = c->dp[15];
+    if (c->ip[0]) {
+      y = yheight * (randy - 0.5);
+      if (c->ip[7] & 2) {
+        x = xwidth * (randx - 0.5);
+        z = sqrt(MR * MR - (x - cylx) * (x - cylx)) + cylz;
+      } else {
+        double ang = -cylphi1 + randx * (cylphi1 + cylphi2) + MOa;
+        z = cylz + MR * cos(ang);
+        x = cylx + MR * sin(ang);
+      }
+    } else {
+      double chi = 2.0 * M_PI * randx, r = sqrt(randy) * radius;
+      x = r * cos(chi);
+      y = r * sin(chi);
+      z = tanMOa * x;
+    }
+  } else if (c->ip[0]) {
     x = xwidth * (randx - 0.5);
     y = yheight * (randy - 0.5);
   } else {
@@ -386,7 +407,7 @@ static void sns_source(neutron_t* n, rng_t* rng, const mcv_component* c) {
   double v = SE2V * sqrt(E);
   n->x = x;
   n->y = y;
-  n->z = 0.;
+  n->z = z;
   n->vx = v * cos(phi) * sin(theta);
   n->vy = v * sin(phi);
   n->vz = v * cos(phi) * cos(theta);

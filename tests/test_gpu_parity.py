@@ -40,7 +40,16 @@ def _sns_source_chain():
     # one synthetic moderator file for the session
     if not _MODERATOR:
         _MODERATOR.append(instruments.synthetic_moderator_file())
+        _MODERATOR.append(instruments.synthetic_moderator_file(sts=True))
     return instruments.sns_source_chain(_MODERATOR[0])
+
+
+def _sts_source_chain():
+    import warnings
+    _sns_source_chain()
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        return instruments.sts_source_chain(_MODERATOR[1])
 
 
 BUILDERS = {
@@ -49,6 +58,7 @@ BUILDERS = {
     "sqe_hollow_cylinder": instruments.sqe_hollow_cylinder,
     "tapered_guide_chain": instruments.tapered_guide_chain,
     "sns_source_chain": _sns_source_chain,
+    "sts_source_chain": _sts_source_chain,
 }
 
 

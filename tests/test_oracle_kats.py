@@ -270,3 +270,29 @@ def test_sns_source_draws_follow_the_moderator_spectrum(oracle_lib):
         frac = (F(E) - F(Emin)) / (F(Emax) - F(Emin))
         assert abs(frac - u) < 2e-3, (u, frac)
         assert 0.0 < t < 3000e-6
+
+
+@pytest.mark.parametrize("dmode", [1.0, 0.0])
+def test_sts_source_face_points_on_the_moderator_cylinder(oracle_lib, dmode):
+    """STS_source.propagate (STS_source.py:242-259): on a square port the
+    emission point lies on the cylindrical moderator of radius MRadius
+    around (cylx, cylz), for the flat-projection (dmode 1) and the
+    flat-area (dmode 0) distributions; y spans the port height."""
+    import warnings
+    from acc_gb300 import instruments
+    from acc_gb300.engine import build_chain
+    from acc_gb300.memory import HostBinder
+    from oracle import binding as O
+    path = instruments.synthetic_moderator_file(sts=True)
+    try:
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            src = instruments.sts_source_chain(path, dmode=dmode).components[0]
+    finally:
+        os.remove(path)
+    _, out, _ = O.run_chain(build_chain([src], binder=HostBinder()), 4000,
+                            seed=3, record=True)
+    r = np.hypot(out[:, 0] - src.cylx, out[:, 2] - src.cylz)
+    np.testing.assert_allclose(r, src.MRadius0, rtol=1e-12)
+    assert np.abs(out[:, 1]).max() <= 0.015 + 1e-12
+    assert out[:, 1].max() > 0.014 and out[:, 1].min() < -0.014
