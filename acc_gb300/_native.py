@@ -41,6 +41,7 @@ OP_BEAMSTOP = 14
 OP_HMS = 15
 OP_GUIDE_TAPERING = 16
 OP_SNS_SOURCE = 17
+OP_NEUTRON_STORAGE = 18
 
 SHAPE_SPHERE, SHAPE_CYLINDER, SHAPE_BOX = 1, 2, 3
 CSG_PRIMITIVE, CSG_DIFFERENCE, CSG_UNION, CSG_INTERSECTION = 0, 1, 2, 3

@@ -61,6 +61,11 @@ struct PhiloxStream {
     ++c2;
   }
 
+  // the neutron's index (the counter's low words)
+  __device__ __forceinline__ uint64_t index() const {
+    return (uint64_t)c0 | ((uint64_t)c1 << 32);
+  }
+
   // float32-exact uniform u * 2^-24 in [0, 1)
   __device__ __forceinline__ float next() {
     if (left == 0) refill();
@@ -79,8 +84,11 @@ struct PhiloxStream {
 struct InjectedStream {
   const float* p;
   int n, i, bad;
-  __device__ __forceinline__ InjectedStream(const float* ptr, int count)
-      : p(ptr), n(count), i(0), bad(0) {}
+  uint64_t idx;  // the neutron's index
+  __device__ __forceinline__ InjectedStream(const float* ptr, int count,
+                                            uint64_t index)
+      : p(ptr), n(count), i(0), bad(0), idx(index) {}
+  __device__ __forceinline__ uint64_t index() const { return idx; }
   __device__ __forceinline__ float next() {
     if (i < n) return p[i++];
     bad = 1;

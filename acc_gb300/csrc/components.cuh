@@ -71,6 +71,37 @@ __device__ __forceinline__ void source_simple(Neutron<R>& n, Rng& rng,
   n.p = pmul * solidangle;
 }
 
+// ==================================================== stored neutrons
+// NeutronFromStorage.propagate (acc/components/sources/
+// neutronfromstorage.py:68-82): neutron i is stored neutron i mod N
+// (table: N x 10 [x y z vx vy vz sx sy t p], float64; ftable its float
+// copy).
+template <typename R>
+__device__ __forceinline__ void storage_source(Neutron<R>& n, uint64_t index,
+                                               const mcv_component& c) {
+  const uint64_t N = c.table_len / 10;
+  const uint64_t row = (index % N) * 10;
+  double v[10];
+  if constexpr (sizeof(R) == 4) {
+#pragma unroll
+    for (int k = 0; k < 10; ++k) v[k] = __ldg(&c.ftable[row + k]);
+  } else {
+    const double* d = static_cast<const double*>(c.table);
+#pragma unroll
+    for (int k = 0; k < 10; ++k) v[k] = __ldg(&d[row + k]);
+  }
+  n.x = R(v[0]);
+  n.y = R(v[1]);
+  n.z = R(v[2]);
+  n.vx = R(v[3]);
+  n.vy = R(v[4]);
+  n.vz = R(v[5]);
+  n.sx = R(v[6]);
+  n.sy = R(v[7]);
+  n.t.set(R(v[8]));
+  n.p = R(v[9]);
+}
+
 // ================================================== SNS moderator source
 // SNS_source (acc/components/sources/SNS_source.py:20-207): E and the
 // emission time from the moderator's cumulative tables (the host computes

@@ -99,6 +99,14 @@ int validate_component(const mcv_component& c, int k, mcv_status* st) {
         return MCV_EINVAL;
       }
       break;
+    case MCV_OP_NEUTRON_STORAGE:
+      if (!c.table || !c.ftable || c.table_len < 10 || c.table_len % 10) {
+        set_msg(st, MCV_EINVAL,
+                "component %s%lld: stored neutrons need an N x 10 table", "",
+                (long long)k);
+        return MCV_EINVAL;
+      }
+      break;
     case MCV_OP_SNS_SOURCE: {
       const int nE = c.ip[1], nt = c.ip[2];
       const bool ok = c.table && nE >= 3 && nt >= 3 &&
@@ -214,7 +222,7 @@ bool is_exotic(const mcv_chain* ch) {
   for (int k = 0; k < ch->ncomp; ++k) {
     const int op = ch->comp[k].opcode;
     if (op == MCV_OP_HMS || op == MCV_OP_SNS_SOURCE ||
-        op == MCV_OP_GUIDE_TAPERING)
+        op == MCV_OP_GUIDE_TAPERING || op == MCV_OP_NEUTRON_STORAGE)
       return true;
   }
   return false;

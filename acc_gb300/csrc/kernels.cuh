@@ -82,6 +82,12 @@ __device__ __forceinline__ int run_component(Neutron<R>& n, Rng& rng,
       source_simple<R>(n, rng, c);
       if constexpr (sizeof(R) == 4) n.p *= weight_up<R>(ch);
       return 0;
+    case MCV_OP_NEUTRON_STORAGE:
+      if constexpr (kX) {
+        storage_source<R>(n, rng.index(), c);
+        if constexpr (sizeof(R) == 4) n.p *= weight_up<R>(ch);
+      }
+      return 0;
     case MCV_OP_SNS_SOURCE:
       if constexpr (kX) {
         sns_source<R>(n, rng, c);
@@ -243,7 +249,7 @@ __global__ void __launch_bounds__(kMaxThreads)
     zero_neutron(nt);
     int last;
     if constexpr (MODE == 2) {
-      InjectedStream rng(uni + i * (uint64_t)stride, stride);
+      InjectedStream rng(uni + i * (uint64_t)stride, stride, first + i);
       last = run_chain_one<R, kX>(nt, rng, ch, k);
       k.overrun += rng.overrun();
     } else {
@@ -542,7 +548,10 @@ __global__ void __launch_bounds__(kMaxThreads)
     nt.p = s[9] * weight_up<R>(ch);
     for (int c = 0; c < ch.ncomp; ++c) {
       const mcv_component& cp = ch.comp[c];
-      if (cp.opcode != MCV_OP_SOURCE_SIMPLE && !(nt.p > 0)) break;
+      const bool source = cp.opcode == MCV_OP_SOURCE_SIMPLE ||
+                          cp.opcode == MCV_OP_SNS_SOURCE ||
+                          cp.opcode == MCV_OP_NEUTRON_STORAGE;
+      if (!source && !(nt.p > 0)) break;
       if (c > 0) apply_transform<R>(nt, ch, c);
       PhiloxStream rng(seed, first + i, (uint32_t)(c + 1));
       NoTrack trk;

@@ -249,6 +249,38 @@ def sts_source_chain(filename=None, Emin=5., Emax=20., dmode=1.0):
     return ins
 
 
+def stored_neutrons(n=10007, seed=11):
+    """n seeded neutrons (x y z vx vy vz sx sy t p rows) leaving z=0 within
+    +-2 cm at about 2000 m/s along z, 1 ms, weights in [1e-4, 1e-3]."""
+    rng = np.random.default_rng(seed)
+    a = np.zeros((n, 10))
+    a[:, 0:2] = rng.uniform(-0.02, 0.02, (n, 2))
+    a[:, 3:5] = rng.normal(0.0, 10.0, (n, 2))
+    a[:, 5] = rng.uniform(1500.0, 2500.0, n)
+    a[:, 8] = 1e-3
+    a[:, 9] = rng.uniform(1e-4, 1e-3, n)
+    return a
+
+
+def storage_chain(neutrons=None):
+    """Stored neutrons (stored_neutrons() by default) replayed through a
+    1 cm isotropic sphere 1 m downstream onto a 4pi theta x tof shell
+    (NeutronFromStorage, neutronfromstorage.py:42-82)."""
+    from .components.sources.neutronfromstorage import NeutronFromStorage
+    if neutrons is None:
+        neutrons = stored_neutrons()
+    ins = instrument("storage_chain")
+    sample = factory(Sphere(0.01), IsotropicKernel(25.0, 25.0))
+    mon = ThetaTOF_monitor_4Pi("theta_tof", radius=3.0, ntheta=180, ntof=200,
+                               tofmin=0.0, tofmax=0.01,
+                               filename="theta_tof.h5")
+    ins.append(NeutronFromStorage("src", neutrons=neutrons),
+               position=(0, 0, 0))
+    ins.append(sample("sample"), position=(0, 0, 1.0))
+    ins.append(mon, position=(0, 0, 1.0))
+    return ins
+
+
 def elliptic_segments(nseg=100, w_in=0.05, w_mid=0.08, w_out=0.04,
                       h_in=0.05, h_mid=0.07, h_out=0.04):
     """(h1, h2, w1, w2) of `nseg` equal segments approximating a guide whose

@@ -73,7 +73,8 @@ enum {
   MCV_OP_HMS = 15,              /* acc/components/samples/homogeneous_multiple_scatterer.py */
   MCV_OP_GUIDE_TAPERING = 16,   /* acc/components/optics/guide_tapering.py  */
   MCV_OP_SNS_SOURCE = 17,       /* acc/components/sources/SNS_source.py     */
-  MCV_OP_COUNT = 18
+  MCV_OP_NEUTRON_STORAGE = 18,  /* acc/components/sources/neutronfromstorage.py */
+  MCV_OP_COUNT = 19
 };
 
 /* ---- shapes of the homogeneous scatterer (acc/geometry/arrow_intersect.py)
@@ -158,6 +159,9 @@ enum {
  *   dp: 9 tanMOa 10 cylx 11 cylz 12 cylphi1 13 cylphi2 14 MRadius0
  *       15 MOffangle (rad): the face point lies on the cylindrical
  *       moderator (square ports) or on the tilted disk
+ * NEUTRON_STORAGE (neutronfromstorage.py:42-82): neutron i of a run is
+ *   stored neutron i mod N; table: N x 10 float64 neutrons (table_len =
+ *   10 N), ftable its float32 copy
  * SLIT / BEAMSTOP (slit.py:20-108, beamstop.py:18-112)
  *                                dp: xmin xmax ymin ymax radius^2 cut
  *

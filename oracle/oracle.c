@@ -1781,6 +1781,13 @@ static void run_component(neutron_t* n, rng_t* rng, const mcv_component* c,
     case MCV_OP_ARM: break;
     case MCV_OP_SOURCE_SIMPLE: source_simple(n, rng, c); break;
     case MCV_OP_SNS_SOURCE: sns_source(n, rng, c); break;
+    case MCV_OP_NEUTRON_STORAGE: {
+      /* NeutronFromStorage.propagate (neutronfromstorage.py:68-82) */
+      uint64_t N = c->table_len / 10;
+      uint64_t idx = (uint64_t)rng->ctr[0] | ((uint64_t)rng->ctr[1] << 32);
+      memcpy(n, (const double*)c->table + (idx % N) * 10, sizeof *n);
+      break;
+    }
     case MCV_OP_GUIDE: st->bounce_overflow += guide(n, c, NULL); break;
     case MCV_OP_GUIDE_TAPERING:
       st->bounce_overflow += guide_tapering(n, c);
@@ -2002,7 +2009,10 @@ int oracle_process_buffer(const mcv_chain* chain, double* neutrons, uint64_t n,
       st.processed++;
       for (int k = 0; k < nc; ++k) {
         const mcv_component* c = &chain->comp[k];
-        if (c->opcode != MCV_OP_SOURCE_SIMPLE && !(nt.p > 0)) break;
+        int source = c->opcode == MCV_OP_SOURCE_SIMPLE ||
+                     c->opcode == MCV_OP_SNS_SOURCE ||
+                     c->opcode == MCV_OP_NEUTRON_STORAGE;
+        if (!source && !(nt.p > 0)) break;
         if (k > 0) apply_transform(&nt, chain->rot[k], chain->off[k]);
         rng_t rng;
         rng_init(&rng, seed, first + (uint64_t)ii, (uint32_t)(k + 1), NULL, 0);

@@ -59,6 +59,7 @@ BUILDERS = {
     "tapered_guide_chain": instruments.tapered_guide_chain,
     "sns_source_chain": _sns_source_chain,
     "sts_source_chain": _sts_source_chain,
+    "storage_chain": instruments.storage_chain,
 }
 
 

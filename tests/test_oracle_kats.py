@@ -296,3 +296,20 @@ def test_sts_source_face_points_on_the_moderator_cylinder(oracle_lib, dmode):
     np.testing.assert_allclose(r, src.MRadius0, rtol=1e-12)
     assert np.abs(out[:, 1]).max() <= 0.015 + 1e-12
     assert out[:, 1].max() > 0.014 and out[:, 1].min() < -0.014
+
+
+def test_stored_neutrons_replay_by_index(oracle_lib):
+    """NeutronFromStorage.propagate (neutronfromstorage.py:68-82): neutron
+    i of the run is stored neutron i mod N, past N too."""
+    from acc_gb300 import instruments
+    from acc_gb300.components.sources.neutronfromstorage import \
+        NeutronFromStorage
+    from acc_gb300.engine import build_chain
+    from acc_gb300.memory import HostBinder
+    from oracle import binding as O
+    stored = instruments.stored_neutrons(n=101)
+    ch = build_chain([NeutronFromStorage("src", neutrons=stored)],
+                     binder=HostBinder())
+    _, out, _ = O.run_chain(ch, 350, seed=1, first=7, record=True)
+    idx = (7 + np.arange(350)) % 101
+    np.testing.assert_array_equal(out, stored[idx])
