@@ -19,7 +19,7 @@ LIB = os.path.join(HERE, "libacc_gb300.so")
 SOURCES = ["engine.cu", "launch_fp32.cu", "launch_fp64.cu", "probe.cu",
            "noalloc.cu"]
 HEADERS = ["common.cuh", "components.cuh", "sample.cuh", "monitors.cuh",
-           "kernels.cuh"]
+           "kernels.cuh", "ms.cuh", "track.cuh"]
 # per-source extra flags: the FP64 kernels round every multiply and add
 # separately, like the CPU restatement they are checked against
 EXTRA_FLAGS = {"launch_fp64.cu": ["--fmad=false"]}

@@ -11,13 +11,15 @@ import ctypes
 import os
 import threading
 
-MCV_MAX_COMPONENTS = 16
-MCV_NPARAM = 40
+MCV_MAX_COMPONENTS = 32
+MCV_NPARAM = 24
 MCV_NIPARAM = 8
 MCV_MAX_INTERSECTIONS = 10
 MCV_MAX_BOUNCES = 100000
 MCV_MAX_VARIANTS = 1024
 MCV_MS_MAX_SCATTERED = 16
+MCV_EXPR_STACK = 8
+MCV_EXPR_MAX_OPS = 256
 MCV_NOALLOC_MAX_VARIANTS = 64
 
 MCV_OK, MCV_EINVAL, MCV_ECUDA, MCV_ECOUNT, MCV_EBOUNCE = 0, 1, 2, 3, 4
@@ -46,6 +48,7 @@ OP_NEUTRON_STORAGE = 18
 SHAPE_SPHERE, SHAPE_CYLINDER, SHAPE_BOX = 1, 2, 3
 CSG_PRIMITIVE, CSG_DIFFERENCE, CSG_UNION, CSG_INTERSECTION = 0, 1, 2, 3
 KERNEL_ISOTROPIC, KERNEL_POWDER, KERNEL_SQE_GRID = 1, 2, 3
+KERNEL_CONSTANT_QE, KERNEL_E_Q = 4, 5
 
 FLAG_IDENTITY_ROT = 1
 FLAG_AGGREGATE = 2

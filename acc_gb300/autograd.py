@@ -27,7 +27,6 @@ import torch
 from . import engine
 from .components.monitors.MonitorBase import MonitorBase
 from .components.ComponentBase import set_param
-from .instrument import calcTransformations
 from .memory import DeviceBinder
 
 _GUIDE_SLOT = {"guide_m": (8, 0), "guide_alpha": (7, 1), "guide_W": (9, 2)}
@@ -37,7 +36,7 @@ class GradRun:
     def __init__(self, instrument, loss_monitor, ncount, seed=1,
                  floattype="float64", params=None):
         self.ins = instrument
-        self.comps = list(instrument.components)
+        self.comps, off, rot, _ = engine.chain_parts(instrument)
         self.mon = loss_monitor
         if not isinstance(loss_monitor, MonitorBase):
             raise TypeError("loss_monitor must be a monitor of the instrument")
@@ -46,7 +45,6 @@ class GradRun:
         self.seed = int(seed)
         self.floattype = floattype
         self.params = dict(params or {})
-        off, rot = calcTransformations(instrument)
         self.binder = DeviceBinder()
         self.chain = engine.build_chain(self.comps, off, rot, self.binder)
 

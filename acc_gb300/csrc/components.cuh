@@ -203,9 +203,20 @@ static __device__ __noinline__ void sns_generate(const mcv_component& c,
     if (__ldg(&Es[mid]) < Eval) lo = mid + 1;
     else hi = mid;
   }
-  const int Eidxh = lo, Eidxl = lo - 1;
-  const double wl = (__ldg(&Es[Eidxh]) - Eval) /
-                    (__ldg(&Es[Eidxh]) - __ldg(&Es[Eidxl]));
+  // the reference's bracket Eidxh = lo, Eidxl = lo - 1 (:38-46), in
+  // bounds: index -1 wraps to the last energy as numba's indexing does
+  // (its weight wl is then 0 when Eval == Es[0]); an Eval above the last
+  // tabulated energy, where the reference reads one row past its table,
+  // takes the last row.
+  int Eidxh = lo, Eidxl = lo - 1;
+  double wl = 0.0;
+  if (lo >= nE) {
+    Eidxh = nE - 1;
+    Eidxl = nE - 1;
+  } else {
+    if (Eidxl < 0) Eidxl = nE - 1;
+    wl = (__ldg(&Es[Eidxh]) - Eval) / (__ldg(&Es[Eidxh]) - __ldg(&Es[Eidxl]));
+  }
   const SnsVec pt{Ptmat + (size_t)Eidxl * nt, Ptmat + (size_t)Eidxh * nt, wl};
   const double p0 = pt.at(tidx_start), p1 = pt.at(tidx_stop - 1);
   randp = p0 + randt * (p1 - p0);

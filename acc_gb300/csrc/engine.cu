@@ -168,7 +168,18 @@ int validate_component(const mcv_component& c, int k, mcv_status* st) {
                 (long long)k);
         return MCV_EINVAL;
       }
-      if (ker < MCV_KERNEL_ISOTROPIC || ker > MCV_KERNEL_SQE_GRID) {
+      if (ker == MCV_KERNEL_E_Q &&
+          (!c.table || !c.ftable || c.ip[4] < 1 ||
+           c.ip[4] > MCV_EXPR_MAX_OPS || c.ip[5] < 1 ||
+           c.ip[5] > MCV_EXPR_MAX_OPS || !(c.dp[12] >= 1) ||
+           !(c.dp[12] <= 1e6))) {
+        set_msg(st, MCV_EINVAL,
+                "component %s%lld: E(Q) kernel needs E(Q) and S(Q) programs "
+                "of 1..256 instructions and 1 <= max_iter <= 1e6",
+                "", (long long)k);
+        return MCV_EINVAL;
+      }
+      if (ker < MCV_KERNEL_ISOTROPIC || ker > MCV_KERNEL_E_Q) {
         set_msg(st, MCV_EINVAL, "component %s%lld: unknown scattering kernel",
                 "", (long long)k);
         return MCV_EINVAL;
@@ -187,7 +198,7 @@ int validate_chain(const mcv_chain* ch, mcv_status* st) {
     return MCV_EINVAL;
   }
   if (ch->ncomp < 1 || ch->ncomp > MCV_MAX_COMPONENTS) {
-    set_msg(st, MCV_EINVAL, "chain has %s%lld components (1..16 allowed)", "",
+    set_msg(st, MCV_EINVAL, "chain has %s%lld components (1..32 allowed)", "",
             (long long)ch->ncomp);
     return MCV_EINVAL;
   }
@@ -217,12 +228,16 @@ bool has_hms(const mcv_chain* ch) {
 }
 
 // The rarer components run in their own kernel instantiations (kX): the
-// SNS source, the tapered guide, the multiple scatterer.
+// SNS source, the tapered guide, the multiple scatterer, stored neutrons,
+// and samples with the constant-(Q, E) or E(Q) kernel.
 bool is_exotic(const mcv_chain* ch) {
   for (int k = 0; k < ch->ncomp; ++k) {
     const int op = ch->comp[k].opcode;
     if (op == MCV_OP_HMS || op == MCV_OP_SNS_SOURCE ||
         op == MCV_OP_GUIDE_TAPERING || op == MCV_OP_NEUTRON_STORAGE)
+      return true;
+    if (op == MCV_OP_HSS && (ch->comp[k].ip[1] == MCV_KERNEL_CONSTANT_QE ||
+                             ch->comp[k].ip[1] == MCV_KERNEL_E_Q))
       return true;
   }
   return false;

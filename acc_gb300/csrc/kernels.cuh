@@ -100,7 +100,7 @@ __device__ __forceinline__ int run_component(Neutron<R>& n, Rng& rng,
       if constexpr (kX) return guide_tapering<R>(n, c);
       return 0;
     case MCV_OP_HSS:
-      hss(n, rng, c, trk);
+      hss<kX>(n, rng, c, trk);
       return 0;
     case MCV_OP_PSD_MONITOR:
       psd_monitor<R>(n, c, tl, trk);
@@ -593,6 +593,31 @@ __global__ void intersect_kernel(const __grid_constant__ mcv_component c,
 // work items of `chunk` neutrons from a device counter (DevStatus::
 // work_next); item k belongs to the variant whose cumulative item range
 // holds k.  The block stages that variant's chain in shared memory once per
+// Copies into dst (a shared-memory mcv_chain) the parts of *src that its
+// first ncomp components use: the header, comp[0..ncomp) and the hop
+// transforms rot, off, frot, foff [0..ncomp).  The rest of dst is never
+// read.  Every region is a multiple of 4 bytes at a 4-byte offset.
+__device__ __forceinline__ void stage_chain(unsigned char* dst,
+                                            const mcv_chain* src) {
+  int nc = src->ncomp;
+  nc = nc < 0 ? 0 : (nc > MCV_MAX_COMPONENTS ? MCV_MAX_COMPONENTS : nc);
+  const size_t off[6] = {0, offsetof(mcv_chain, comp),
+                         offsetof(mcv_chain, rot), offsetof(mcv_chain, off),
+                         offsetof(mcv_chain, frot), offsetof(mcv_chain, foff)};
+  const size_t len[6] = {offsetof(mcv_chain, comp),
+                         nc * sizeof(mcv_component), nc * 9 * sizeof(double),
+                         nc * 3 * sizeof(double), nc * 9 * sizeof(float),
+                         nc * 3 * sizeof(float)};
+  const unsigned char* s = reinterpret_cast<const unsigned char*>(src);
+#pragma unroll
+  for (int r = 0; r < 6; ++r) {
+    const uint32_t* a = reinterpret_cast<const uint32_t*>(s + off[r]);
+    uint32_t* b = reinterpret_cast<uint32_t*>(dst + off[r]);
+    for (int i = threadIdx.x; i < (int)(len[r] / 4); i += blockDim.x)
+      b[i] = a[i];
+  }
+}
+
 // change of variant.  Neutron i of variant v draws from Philox (seeds[v], i).
 template <typename R>
 __global__ void __launch_bounds__(kMaxThreads)
@@ -635,11 +660,7 @@ __global__ void __launch_bounds__(kMaxThreads)
     const int v = s_var;
     if (it >= total) break;
     if (v != cur) {
-      const uint2* src = reinterpret_cast<const uint2*>(variants + v);
-      uint2* dst = reinterpret_cast<uint2*>(smem);
-      for (int i = threadIdx.x; i < (int)(sizeof(mcv_chain) / 8);
-           i += blockDim.x)
-        dst[i] = src[i];
+      stage_chain(smem, variants + v);
       cur = v;
       __syncthreads();
     }

@@ -205,7 +205,7 @@ __device__ __noinline__ int ms_interact_m1(const mcv_component& c,
   out[1].p *= prob;
   prop_dt(out[1], x / v);
   NoTrack trk;
-  hss_kernel<R>(out[1], rng, c, trk);
+  hss_kernel<R, true>(out[1], rng, c, trk);
   return 2;
 }
 

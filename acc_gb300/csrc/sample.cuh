@@ -687,6 +687,247 @@ __device__ __forceinline__ void sqe_scatter(Neutron<R>& n, Rng& rng,
   }
 }
 
+// Outgoing velocity of a (Q, E) transfer (constant_qe.py:38-67,
+// E_Q.py:64-92): vf cos(t) along the incident direction e1,
+// vf sin(t) cos(phi) along e2 = unit(n x e1), vf sin(t) sin(phi) along
+// e3 = e1 x e2, with n = z unless e1 lies within 0.1 of it (then x).
+template <typename R>
+__device__ __forceinline__ void qe_velocity(Neutron<R>& n, R vi, R vf,
+                                            R cost, R sint, R uphi) {
+  R sp, cp;
+  m_sincos_2pi(uphi, &sp, &cp);
+  R v2 = vf * sint * cp, v3 = vf * sint * sp, v1 = vf * cost;
+  R inv = R(1.0) / vi;
+  R e1x = n.vx * inv, e1y = n.vy * inv, e1z = n.vz * inv;
+  R nx, ny, nz;
+  if (m_fabs(e1x) > R(1e-1) || m_fabs(e1y) > R(1e-1)) { nx = 0; ny = 0; nz = 1; }
+  else { nx = 1; ny = 0; nz = 0; }
+  R e2x = ny * e1z - nz * e1y, e2y = nz * e1x - nx * e1z,
+    e2z = nx * e1y - ny * e1x;
+  R l2 = R(1.0) / m_sqrt(e2x * e2x + e2y * e2y + e2z * e2z);
+  e2x *= l2;
+  e2y *= l2;
+  e2z *= l2;
+  R e3x = e1y * e2z - e1z * e2y, e3y = e1z * e2x - e1x * e2z,
+    e3z = e1x * e2y - e1y * e2x;
+  n.vx = e1x * v1 + e2x * v2 + e3x * v3;
+  n.vy = e1y * v1 + e2y * v2 + e3y * v3;
+  n.vz = e1z * v1 + e2z * v2 + e3z * v3;
+}
+
+// constant_qe.S (acc/kernels/constant_qe.py:15-67): the fixed transfer
+// (Q, E) = (prm 10, prm 11), one draw for the azimuth.  A transfer the
+// neutron cannot make (E above Ei, |cos(theta)| > 1) leaves the
+// reference's velocity NaN; here it absorbs the neutron.  FP32 forms
+// sin^2(theta) from the factored (Q^2 - (ki-kf)^2)((ki+kf)^2 - Q^2) /
+// (2 ki kf)^2, which keeps its precision near 0 and 180 degrees.
+template <typename R, typename Rng>
+__device__ __forceinline__ void constant_qe_scatter(Neutron<R>& n, Rng& rng,
+                                                    const mcv_component& c) {
+  const R Q = prm<R>(c, 10), E = prm<R>(c, 11);
+  const R vi = m_sqrt(n.vx * n.vx + n.vy * n.vy + n.vz * n.vz);
+  const R Ei = vi * vi * R(kVS2E);
+  const R Ef = Ei - E;
+  const R uphi = rng.next();
+  if (!(Ef >= R(0))) {
+    n.p = R(-1);
+    return;
+  }
+  const R vf = m_sqrt(Ef) * R(kSE2V);
+  const R ki = R(kV2K) * vi, kf = R(kV2K) * vf;
+  const R cost = (ki * ki + kf * kf - Q * Q) / (2 * ki * kf);
+  R s2;
+  if constexpr (sizeof(R) == 4) {
+    const R Q2 = Q * Q, dk = ki - kf, sk = ki + kf;
+    s2 = (Q2 - dk * dk) * (sk * sk - Q2) / (4 * ki * ki * kf * kf);
+  } else {
+    s2 = 1.0 - cost * cost;
+  }
+  if (!(s2 >= R(0))) {
+    n.p = R(-1);
+    return;
+  }
+  qe_velocity<R>(n, vi, vf, cost, m_sqrt(s2), uphi);
+}
+
+// The E_Q kernel's E(Q) and S(Q) programs: postfix {opcode, argument}
+// pairs (MCV_EXPR_*) in the working precision (the FP32 kernels read the
+// float copy), run on a stack of MCV_EXPR_STACK values.  A malformed
+// program (stack under- or overflow, unknown opcode, not exactly one value
+// left) gives NaN and never reads or writes outside the stack.  POWI is
+// x**n by binary powering, MOD Python's float % (sign of the divisor).
+template <typename R>
+__device__ __forceinline__ R expr_unary(int op, R x) {
+  if constexpr (sizeof(R) == 4) {
+    switch (op) {
+      case MCV_EXPR_NEG: return -x;
+      case MCV_EXPR_EXP: return expf(x);
+      case MCV_EXPR_LOG: return logf(x);
+      case MCV_EXPR_LOG10: return log10f(x);
+      case MCV_EXPR_SQRT: return sqrtf(x);
+      case MCV_EXPR_SIN: return sinf(x);
+      case MCV_EXPR_COS: return cosf(x);
+      case MCV_EXPR_TAN: return tanf(x);
+      case MCV_EXPR_ASIN: return asinf(x);
+      case MCV_EXPR_ACOS: return acosf(x);
+      case MCV_EXPR_ATAN: return atanf(x);
+      case MCV_EXPR_SINH: return sinhf(x);
+      case MCV_EXPR_COSH: return coshf(x);
+      case MCV_EXPR_TANH: return tanhf(x);
+      case MCV_EXPR_ASINH: return asinhf(x);
+      case MCV_EXPR_ACOSH: return acoshf(x);
+      case MCV_EXPR_ATANH: return atanhf(x);
+      case MCV_EXPR_ERF: return erff(x);
+      case MCV_EXPR_ERFC: return erfcf(x);
+      case MCV_EXPR_FABS: return fabsf(x);
+      case MCV_EXPR_FLOOR: return floorf(x);
+      case MCV_EXPR_CEIL: return ceilf(x);
+      default: return __int_as_float(0x7fffffff);
+    }
+  } else {
+    switch (op) {
+      case MCV_EXPR_NEG: return -x;
+      case MCV_EXPR_EXP: return exp(x);
+      case MCV_EXPR_LOG: return log(x);
+      case MCV_EXPR_LOG10: return log10(x);
+      case MCV_EXPR_SQRT: return sqrt(x);
+      case MCV_EXPR_SIN: return sin(x);
+      case MCV_EXPR_COS: return cos(x);
+      case MCV_EXPR_TAN: return tan(x);
+      case MCV_EXPR_ASIN: return asin(x);
+      case MCV_EXPR_ACOS: return acos(x);
+      case MCV_EXPR_ATAN: return atan(x);
+      case MCV_EXPR_SINH: return sinh(x);
+      case MCV_EXPR_COSH: return cosh(x);
+      case MCV_EXPR_TANH: return tanh(x);
+      case MCV_EXPR_ASINH: return asinh(x);
+      case MCV_EXPR_ACOSH: return acosh(x);
+      case MCV_EXPR_ATANH: return atanh(x);
+      case MCV_EXPR_ERF: return erf(x);
+      case MCV_EXPR_ERFC: return erfc(x);
+      case MCV_EXPR_FABS: return fabs(x);
+      case MCV_EXPR_FLOOR: return floor(x);
+      case MCV_EXPR_CEIL: return ceil(x);
+      default: return __longlong_as_double(0x7ff8000000000000ll);
+    }
+  }
+}
+
+template <typename R>
+__device__ __forceinline__ R expr_binary(int op, R a, R b) {
+  switch (op) {
+    case MCV_EXPR_ADD: return a + b;
+    case MCV_EXPR_SUB: return a - b;
+    case MCV_EXPR_MUL: return a * b;
+    case MCV_EXPR_DIV: return a / b;
+    case MCV_EXPR_MIN: return b < a ? b : a;
+    case MCV_EXPR_MAX: return b > a ? b : a;
+    default: break;
+  }
+  if constexpr (sizeof(R) == 4) {
+    if (op == MCV_EXPR_POW) return powf(a, b);
+    if (op == MCV_EXPR_ATAN2) return atan2f(a, b);
+    R r = fmodf(a, b);
+    return (r != 0.f && ((r < 0.f) != (b < 0.f))) ? r + b : r;
+  } else {
+    if (op == MCV_EXPR_POW) return pow(a, b);
+    if (op == MCV_EXPR_ATAN2) return atan2(a, b);
+    R r = fmod(a, b);
+    return (r != 0.0 && ((r < 0.0) != (b < 0.0))) ? r + b : r;
+  }
+}
+
+template <typename R>
+__device__ __noinline__ R expr_eval(const R* __restrict__ prog, int nops,
+                                    R Q) {
+  R st[MCV_EXPR_STACK];
+  int sp = 0;
+  const R nan = R(0) / R(0);
+  for (int i = 0; i < nops; ++i) {
+    const int op = (int)__ldg(&prog[2 * i]);
+    const R arg = __ldg(&prog[2 * i + 1]);
+    if (op == MCV_EXPR_CONST || op == MCV_EXPR_Q) {
+      if (sp >= MCV_EXPR_STACK) return nan;
+      st[sp++] = op == MCV_EXPR_CONST ? arg : Q;
+      continue;
+    }
+    if (sp < 1) return nan;
+    const R x = st[sp - 1];
+    if (op >= MCV_EXPR_ADD && op <= MCV_EXPR_MOD && op != MCV_EXPR_NEG &&
+        op != MCV_EXPR_POWI) {
+      if (sp < 2) return nan;
+      st[sp - 2] = expr_binary<R>(op, st[sp - 2], x);
+      --sp;
+      continue;
+    }
+    if (op == MCV_EXPR_POWI) {
+      const int e = (int)arg;
+      unsigned m = e < 0 ? 0u - (unsigned)e : (unsigned)e;
+      R r = R(1), b = x;
+      while (m) {
+        if (m & 1u) r *= b;
+        m >>= 1;
+        if (m) b *= b;
+      }
+      st[sp - 1] = e < 0 ? R(1) / r : r;
+      continue;
+    }
+    st[sp - 1] = expr_unary<R>(op, x);
+  }
+  return sp == 1 ? st[0] : nan;
+}
+
+// The S of makeS (acc/kernels/E_Q.py:37-98): up to max_iter draws of Q
+// uniform on [Qmin, Qmax), each rejected while E(Q) exceeds Ei or the
+// transfer is kinematically closed (cos^2 > 1); none accepted -> p = 0.
+// Weight S(Q) (vf/vi) Q (Qmax-Qmin) / (2 ki kf) / tries.
+template <typename R, typename Rng>
+__device__ __forceinline__ void e_q_scatter(Neutron<R>& n, Rng& rng,
+                                            const mcv_component& c) {
+  const R Qmin = prm<R>(c, 10), Qmax = prm<R>(c, 11);
+  const int max_iter = (int)c.dp[12];
+  const int nE = c.ip[4], nS = c.ip[5];
+  const R* progE = sizeof(R) == 4 ? (const R*)c.ftable : (const R*)c.table;
+  const R* progS = progE + 2 * nE;
+  const R vi = m_sqrt(n.vx * n.vx + n.vy * n.vy + n.vz * n.vz);
+  const R Ei = vi * vi * R(kVS2E);
+  const R ki = R(kV2K) * vi;
+  R Q = 0, vf = 0, kf = 0, cost = 0, cost2 = 0;
+  int itr = 0;
+  bool found = false;
+  for (; itr < max_iter; ++itr) {
+    Q = rng.next() * (Qmax - Qmin);
+    Q += Qmin;
+    const R E = expr_eval<R>(progE, nE, Q);
+    const R Ef = Ei - E;
+    if (Ef < R(0)) continue;
+    vf = m_sqrt(Ef) * R(kSE2V);
+    kf = R(kV2K) * vf;
+    cost = (ki * ki + kf * kf - Q * Q) / (2 * ki * kf);
+    cost2 = cost * cost;
+    if (cost2 > R(1)) continue;
+    found = true;
+    break;
+  }
+  if (!found) {
+    n.p = R(0);
+    return;
+  }
+  R s2;
+  if constexpr (sizeof(R) == 4) {
+    const R Q2 = Q * Q, dk = ki - kf, sk = ki + kf;
+    s2 = (Q2 - dk * dk) * (sk * sk - Q2) / (4 * ki * ki * kf * kf);
+    s2 = s2 > R(0) ? s2 : R(0);
+  } else {
+    s2 = 1.0 - cost2;
+  }
+  const R uphi = rng.next();
+  qe_velocity<R>(n, vi, vf, cost, m_sqrt(s2), uphi);
+  const R S = expr_eval<R>(progS, nS, Q);
+  const R prob_f = S * (vf / vi) * Q * (Qmax - Qmin) / (kf * ki) / 2;
+  n.p *= prob_f / R(itr + 1);
+}
+
 template <typename R>
 __device__ __forceinline__ R hss_sigma(const Neutron<R>& n,
                                        const mcv_component& c) {
@@ -702,7 +943,9 @@ __device__ __forceinline__ R hss_mu(const Neutron<R>& n,
   return prm<R>(c, 8) / v * 2200;
 }
 
-template <typename R, typename Rng, typename Trk>
+// kX: the constant-(Q, E) and E(Q) kernels are compiled into the
+// instantiations for the rarer components only.
+template <typename R, bool kX = false, typename Rng, typename Trk>
 __device__ __forceinline__ void hss_kernel(Neutron<R>& n, Rng& rng,
                                            const mcv_component& c, Trk& trk) {
   switch (c.ip[1]) {
@@ -718,6 +961,18 @@ __device__ __forceinline__ void hss_kernel(Neutron<R>& n, Rng& rng,
       n.p *= prm<R>(c, 9);
       trk.sigma_factor(prm<R>(c, 9));
       sqe_scatter<R>(n, rng, c, trk);
+      break;
+    case MCV_KERNEL_CONSTANT_QE:
+      if constexpr (kX) {
+        n.p *= prm<R>(c, 9);  // kernels/__init__.py:85
+        constant_qe_scatter<R>(n, rng, c);
+      }
+      break;
+    case MCV_KERNEL_E_Q:
+      if constexpr (kX) {
+        n.p *= prm<R>(c, 9);  // kernels/__init__.py:103
+        e_q_scatter<R>(n, rng, c);
+      }
       break;
     default:
       break;
@@ -746,7 +1001,7 @@ __device__ __forceinline__ void track_atten(const Neutron<R>& n,
 // HomogeneousSingleScatterer.propagate
 // (acc/components/samples/homogeneous_single_scatterer.py:62-100), FP64:
 // the reference's sequence.
-template <typename Rng, typename Trk>
+template <bool kX, typename Rng, typename Trk>
 __device__ __forceinline__ void hss(Neutron<double>& n, Rng& rng,
                                     const mcv_component& c, Trk& trk) {
   double x = n.x, y = n.y, z = n.z, vx = n.vx, vy = n.vy, vz = n.vz;
@@ -767,7 +1022,7 @@ __device__ __forceinline__ void hss(Neutron<double>& n, Rng& rng,
   double atten = exp(-(mu + sigma) * dist);
   n.p *= fulllen * atten;
   track_atten<double>(n, c, dist, trk);
-  hss_kernel<double>(n, rng, c, trk);
+  hss_kernel<double, kX>(n, rng, c, trk);
   if (n.p <= 0) return;
   h = intersect_shape<double>(c, n.x, n.y, n.z, n.vx, n.vy, n.vz);
   double dt3 = total_time_in_shape<double>(h);
@@ -787,7 +1042,7 @@ __device__ __forceinline__ void hss(Neutron<double>& n, Rng& rng,
 // "now" is formed as a difference of tau values.  In exact arithmetic this
 // is the reference's sequence; in float it avoids cancelling metre-scale
 // flight times against centimetre-scale chords.
-template <typename Rng, typename Trk>
+template <bool kX, typename Rng, typename Trk>
 __device__ __forceinline__ void hss(Neutron<float>& n, Rng& rng,
                                     const mcv_component& c, Trk& trk) {
   float vx = n.vx, vy = n.vy, vz = n.vz;
@@ -845,7 +1100,7 @@ __device__ __forceinline__ void hss(Neutron<float>& n, Rng& rng,
   float mu = hss_mu<float>(n, c);
   n.p *= fulllen * __expf(-(mu + sigma) * dist);
   track_atten<float>(n, c, dist, trk);
-  hss_kernel<float>(n, rng, c, trk);
+  hss_kernel<float, kX>(n, rng, c, trk);
   if (n.p <= 0.f) return;
   h = intersect_shape<float>(c, n.x, n.y, n.z, n.vx, n.vy, n.vz);
   float dt3 = total_time_in_shape<float>(h);

@@ -25,8 +25,11 @@ def build_chain(components, offsets=None, rotmats=None, binder=None):
         from .memory import DeviceBinder
         binder = DeviceBinder()
     ch = nat.mcv_chain()
-    # the chain holds raw pointers into memory the binder owns
+    # the chain holds raw pointers into memory that the binder and the
+    # components own (tallies, lookup tables): keep both alive with it, so
+    # that a chain built from a temporary instrument stays valid
     ch._binder = binder
+    ch._components = list(components)
     ch.ncomp = len(components)
     eye = np.eye(3)
     for i, comp in enumerate(components):
@@ -71,9 +74,32 @@ def weight_exp2(components):
     return max(-100, min(100, e))
 
 
-def chain_for_instrument(instrument, binder=None):
+def chain_parts(instrument):
+    """(components, offsets, rotmats, first) of the chain that runs an
+    instrument.  Arms ahead of the first other component are left out:
+    the reference runs them as no-ops on a neutron that no source has set
+    yet (its generated kernel calls every component in turn,
+    acc/run_script.py:58-80), while the engine ends a neutron once its
+    weight is not positive, which would end every neutron there.  Frames
+    are absolute, so leaving them out changes no transform of the others.
+    `first` is the instrument index of chain component 0."""
     offsets, rotmats = calcTransformations(instrument)
-    return build_chain(instrument.components, offsets, rotmats, binder)
+    comps = list(instrument.components)
+    k = 0
+    while k < len(comps) - 1 and getattr(comps[k], "opcode", None) == nat.OP_ARM:
+        k += 1
+    return comps[k:], offsets[k:], rotmats[k:], k
+
+
+def chain_for_instrument(instrument, binder=None):
+    """The chain of an instrument's components (chain_parts) with the frame
+    transforms between them.  chain.first_component is the instrument
+    index of chain component 0 (the engine's component indices, such as
+    replay's `last`, count from it)."""
+    comps, offsets, rotmats, k = chain_parts(instrument)
+    ch = build_chain(comps, offsets, rotmats, binder)
+    ch.first_component = k
+    return ch
 
 
 VARIANTS = {None: 0, "auto": 0, "thread": 1, "regen": 2,

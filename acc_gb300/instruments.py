@@ -6,6 +6,10 @@ guide_chain        disc source -> 10 m guide -> 5 m tapered guide ->
 sqe_hollow_cylinder  60 meV beam -> hollow cylinder with a gridded S(Q,E)
                    -> 3 m cylinder detector binned in I(Q,E)
 powder_banked      guide chain -> powder cylinder -> banked cylinder detector
+constant_qe_box    70 meV beam -> Al block with the constant-(Q, E) kernel ->
+                   I(Q, E) monitor
+e_q_box            70 meV beam -> Al block with an analytic E(Q) dispersion
+                   -> I(Q, E) monitor
 
 Numbers that the workload descriptions leave open are fixed here once
 (source distance, gaps between components, detector heights, number
@@ -20,16 +24,18 @@ import numpy as np
 from .components.monitors.cylinder_detectors import (BankedCylinder_detector,
                                                      CylinderIQE_detector)
 from .components.monitors.energy_monitor import Energy_monitor
+from .components.monitors.iqe_monitor import IQE_monitor
 from .components.monitors.psd_monitor import PSD_monitor
 from .components.monitors.psd_monitor_4pi import PSD_monitor_4Pi
 from .components.monitors.theta_tof_monitor_4pi import ThetaTOF_monitor_4Pi
 from .components.optics.guide import Guide
 from .components.samples.homogeneous_single_scatterer import factory
 from .components.sources.source_simple import Source_simple
-from .geometry import Cylinder, Difference, HollowCylinder, Sphere
+from .geometry import Block, Cylinder, Difference, HollowCylinder, Sphere
 from .instrument import instrument
-from .kernels import (IsotropicKernel, Peak, SimplePowderDiffractionKernel,
-                      SQEGridKernel, coefficient_from_cross_section)
+from .kernels import (ConstantQEKernel, E_Q_Kernel, IsotropicKernel, Peak,
+                      SimplePowderDiffractionKernel, SQEGridKernel,
+                      coefficient_from_cross_section)
 
 COATING = dict(R0=0.99, Qc=0.0219, alpha=3.0, m=3.0, W=0.003)
 
@@ -371,3 +377,257 @@ def sphere_variants(nvariants=64, seed=0, nmin=1e6, nmax=1e8, emin=20.0,
         src.propagate_params = tuple(sp)
         out.append(ins)
     return out, counts, seeds
+
+
+# fcc Al, a = 4.04 A, 4 atoms per cell (the sample of the reference's
+# constant-(Q, E) and E(Q) box tests); tabulated free-atom cross sections
+# absorption 0.231 b (2200 m/s), coherent 1.495 b, incoherent 0.0082 b
+AL_NUMBER_DENSITY = 4 / 4.04 ** 3
+AL_MU = coefficient_from_cross_section(AL_NUMBER_DENSITY, 0.231)
+AL_SIGMA = coefficient_from_cross_section(AL_NUMBER_DENSITY, 1.495 + 0.0082)
+
+
+def _al_box(name, kernel):
+    """The instrument of the reference's box tests
+    (tests/components/samples/acc_ss_test_instrument.py:6-33 with the
+    source and monitor of test_fccAl_E_Q_kernel.py:28-55): 1 x 1 cm source,
+    70 +- 0.1 meV, aimed at 8 x 8 mm 1 m away; 6 x 10 x 1 cm block
+    (width x height x thickness along the beam) 2 m downstream; I(Q, E)
+    monitor at the sample, Q 0-8 /A x 160, E -60..60 meV x 120, all
+    directions."""
+    ins = instrument(name)
+    src = Source_simple("src", radius=0.0, width=0.01, height=0.01, dist=1.0,
+                        xw=0.008, yh=0.008, E0=70.0, dE=0.1, Lambda0=0.0,
+                        dLambda=0.0)
+    HSS = factory(Block(0.06, 0.10, 0.01), kernel)
+    mon = IQE_monitor("iqe_monitor", Ei=70.0, Qmin=0.0, Qmax=8.0, nQ=160,
+                      Emin=-60.0, Emax=60.0, nE=120,
+                      min_angle_in_plane=0.0, max_angle_in_plane=359.0,
+                      min_angle_out_of_plane=-90.0,
+                      max_angle_out_of_plane=90.0)
+    ins.append(src, position=(0, 0, 0))
+    ins.append(HSS("sample"), position=(0, 0, 2.0))
+    ins.append(mon, position=(0, 0, 2.0))
+    return ins
+
+
+def constant_qe_box(Q=3.0, E=30.0):
+    """Al block scattering every neutron to Q = 3 /A, E = 30 meV
+    (sampleassemblies/Al-constantqekernel/Al-scatterer.xml:7-8)."""
+    return _al_box("constant_qe_box",
+                   ConstantQEKernel(Q, E, AL_MU, AL_SIGMA))
+
+
+def e_q_box(E_Q="30+20*sin(Q)", S_Q="1", Qmin=0.0, Qmax=10.0):
+    """Al block with the dispersion E = 30 + 20 sin(Q) meV, S = 1 over
+    Q 0-10 /A (sampleassemblies/Al-E_Q_kernel/Al-scatterer.xml:7-12)."""
+    return _al_box("e_q_box",
+                   E_Q_Kernel(E_Q, S_Q, Qmin, Qmax, AL_MU, AL_SIGMA))
+
+
+# ---------------------------------------------------------------- VERDI
+def ellipse_half_opening(z, a, b):
+    """Half opening of an ellipse with semi-minor axis a and semi-major
+    axis b, at distance z along the major axis from its vertex:
+    a sqrt(z/b (2 - z/b)) (acc/test/ellipse.py:148-162)."""
+    z = np.asarray(z, dtype=np.float64)
+    return a * np.sqrt(z / b * (2 - z / b))
+
+
+def shield_vertex(a, b, z_src, src_size, z_guide_start, z_guide_end,
+                  z_target, target_size):
+    """Where the ray from the source's lower edge to the guide exit's upper
+    edge crosses the ray from the guide entrance's upper edge to the
+    target's lower edge: the tip (x, z) of the shield that blocks the
+    direct line of sight of a single-wall elliptic mirror
+    (SingleWall.calc_shield_xz, acc/test/ellipse.py:37-54)."""
+    x_end = float(ellipse_half_opening(z_guide_end - z_src, a, b))
+    x_src = -src_size / 2.
+    k1 = (x_end - x_src) / (z_guide_end - z_src)
+    b1 = x_src - k1 * z_src
+    x_start = float(ellipse_half_opening(z_guide_start - z_src, a, b))
+    x_tgt = -target_size / 2.
+    k2 = (x_tgt - x_start) / (z_target - z_guide_start)
+    b2 = x_tgt - k2 * z_target
+    z = (b2 - b1) / (k1 - k2)
+    return k1 * z + b1, z
+
+
+def elliptic_guide_segments(z_center, z_start, z_exit, nseg, major, minor):
+    """(h1, h2, w1, w2) of `nseg` equal segments from z_start to z_exit of
+    an elliptic guide (both axes of the opening on the same ellipse,
+    centre at z_center), as the segment files of
+    acc/test/ellipse.py:101-145 list them; the tapered guide's loader then
+    drops the last one, as the reference's does."""
+    b, a = major / 2., minor / 2.
+    zs, step = np.linspace(z_start, z_exit, nseg, retstep=True,
+                           endpoint=False)
+    zs = zs - (z_center - b)
+    h1 = 2 * ellipse_half_opening(zs, a, b)
+    h2 = 2 * ellipse_half_opening(zs + step, a, b)
+    return h1, h2, h1.copy(), h2.copy()
+
+
+def verdi(moderator_file=None, guide_mvalue=6., sample_width=0.005,
+          sample_height=0.005, source_width=0.03, source_height=0.03,
+          secsource_size=0.02, xDivergence=2, yDivergence=2,
+          guide1_start=6.35, guide1_len=10.99 + 9.56,
+          ellipse1_major_axis_len=31.75, ellipse1_minor_axis_len=0.21,
+          guide2_start=35.05, guide2_len=2.44 + 1.01,
+          ellipse2_major_axis_len=40.0 - 31.75, ellipse2_minor_axis_len=0.1,
+          guide_n_segments=500, Emin=0.1, Emax=1000.):
+    """The VERDI instrument of tests/instruments/VERDI/VERDI_base.py:14-339
+    (the reference's largest acc instrument, timed in its walltime.txt):
+    SNS moderator -> two elliptic mirrors, each cut in two tapered guides of
+    499 segments with a two-plate shield between them -> secondary-source
+    slit -> sample mask, with wavelength, position-divergence and PSD
+    monitors along the way (26 components, 4 of them arms).
+
+    `moderator_file`: a moderator file in the SNS format; a synthetic one
+    of the reference file's size (141 energies x 160 times) when None."""
+    from .components.monitors.posdiv_monitor import PosDiv_monitor
+    from .components.monitors.wavelength_monitor import Wavelength_monitor
+    from .components.optics.arm import Arm
+    from .components.optics.beamstop import Beamstop
+    from .components.optics.guide_tapering import Guide as TaperedGuide
+    from .components.optics.slit import Slit
+    from .components.sources.SNS_source import SNS_source
+    if moderator_file is None:
+        moderator_file = synthetic_moderator_file(nE=141, nt=160)
+    # first mirror and its shield (VERDI_base.py:37-49)
+    a1, b1 = ellipse1_minor_axis_len / 2, ellipse1_major_axis_len / 2
+    shield1_x, shield1_z = shield_vertex(
+        a1, b1, 0., source_width, guide1_start, guide1_start + guide1_len,
+        ellipse1_major_axis_len, secsource_size)
+    guide11_len = shield1_z - guide1_start
+    guide12_len = guide1_len - guide11_len
+    focus = float(ellipse_half_opening(guide1_start, a1, b1)) * 2
+    focus_dist = guide1_start * .99
+    # second mirror, looked at backwards from the sample (:51-67)
+    a2, b2 = ellipse2_minor_axis_len / 2, ellipse2_major_axis_len / 2
+    z_gs = (ellipse1_major_axis_len + ellipse2_major_axis_len - guide2_start
+            - guide2_len)
+    shield2_x, shield2_z = shield_vertex(
+        a2, b2, 0., sample_width, z_gs, z_gs + guide2_len,
+        ellipse2_major_axis_len, secsource_size)
+    guide22_len = shield2_z - z_gs
+    guide21_len = guide2_len - guide22_len
+    guide21_start = ellipse1_major_axis_len + (ellipse2_major_axis_len
+                                               - z_gs - guide2_len)
+    # segment profiles (:69-93)
+    c1 = ellipse1_major_axis_len / 2.
+    g11 = elliptic_guide_segments(c1, guide1_start, guide1_start + guide11_len,
+                                  guide_n_segments, ellipse1_major_axis_len,
+                                  ellipse1_minor_axis_len)
+    g12 = elliptic_guide_segments(c1, guide1_start + guide11_len,
+                                  guide1_start + guide1_len, guide_n_segments,
+                                  ellipse1_major_axis_len,
+                                  ellipse1_minor_axis_len)
+    c2 = ellipse1_major_axis_len + ellipse2_major_axis_len / 2
+    g21 = elliptic_guide_segments(c2, guide21_start,
+                                  guide21_start + guide21_len,
+                                  guide_n_segments, ellipse2_major_axis_len,
+                                  ellipse2_minor_axis_len)
+    g22 = elliptic_guide_segments(c2, guide21_start + guide21_len,
+                                  guide21_start + guide2_len,
+                                  guide_n_segments, ellipse2_major_axis_len,
+                                  ellipse2_minor_axis_len)
+
+    def segs(g):  # the loader drops the last segment of a file
+        return tuple(v[:-1] for v in g)
+
+    m = guide_mvalue
+    ins = instrument("verdi")
+    origin = Arm("origin")
+    ins.append(origin, position=(0, 0, 0))
+    moderator = SNS_source("moderator", moderator_file, Emin, Emax,
+                           source_width, source_height, focus_dist, focus,
+                           focus, Anorm=0.0009)
+    ins.append(moderator, position=(0, 0, 0), relativeTo=origin)
+    mod_w, mod_h = source_width * 1.1, source_height * 1.1
+    ins.append(Wavelength_monitor("ModeratorSpectrumL", Lmin=0, Lmax=20,
+                                  nchan=100, xwidth=mod_w, yheight=mod_h,
+                                  filename="moderator_L.h5"),
+               position=(0, 0, 1e-5), relativeTo=moderator)
+    ins.append(PosDiv_monitor("ModeratorDivergence_xpos", maxdiv=xDivergence,
+                              ndiv=1000, npos=100, xwidth=mod_w,
+                              yheight=mod_h, filename="moderator_divXpos.h5"),
+               position=(0, 0, 2e-5), relativeTo=moderator)
+    ins.append(PosDiv_monitor("ModeratorDivergence_ypos", maxdiv=yDivergence,
+                              ndiv=1000, npos=100, xwidth=mod_w,
+                              yheight=mod_h, filename="moderator_divYpos.h5"),
+               position=(0, 0, 3e-5), orientation=(0, 0, 90),
+               relativeTo=moderator)
+    g1_1 = TaperedGuide("Guide1_1", l=guide11_len, mx=m, my=m,
+                        segments=segs(g11))
+    ins.append(g1_1, position=(0, 0, guide1_start), relativeTo=moderator)
+    ins.append(Beamstop("Shield1_1", xmin=-0.5, xmax=shield1_x, ymin=-0.5,
+                        ymax=0.5),
+               position=(0, 0, guide11_len + 1e-6), relativeTo=g1_1)
+    ins.append(Beamstop("Shield1_2", xmin=-0.5, xmax=0.5, ymin=-0.5,
+                        ymax=shield1_x),
+               position=(0, 0, guide11_len + 2e-6), relativeTo=g1_1)
+    ins.append(TaperedGuide("Guide1_2", l=guide12_len, mx=m, my=m,
+                            segments=segs(g12)),
+               position=(0, 0, guide11_len + 4e-6), relativeTo=g1_1)
+    sec = Arm("SecSource")
+    ins.append(sec, position=(0, 0, ellipse1_major_axis_len),
+               relativeTo=origin)
+    ins.append(PosDiv_monitor("secsrc_divxpos", maxdiv=xDivergence,
+                              ndiv=1000, npos=100, xwidth=0.15, yheight=0.15,
+                              filename="secsrc_divXpos.h5"),
+               position=(0, 0, 1e-7), relativeTo=sec)
+    ins.append(PosDiv_monitor("secsrc_divypos", maxdiv=yDivergence,
+                              ndiv=1000, npos=100, xwidth=0.15, yheight=0.15,
+                              filename="secsrc_divYpos.h5"),
+               position=(0, 0, 2e-7), orientation=(0, 0, 90), relativeTo=sec)
+    slit = Slit("SecSourceSlit", xmin=-0.01, xmax=0.013, ymin=-0.01,
+                ymax=0.013)
+    ins.append(slit, position=(0, 0, 1e-5), relativeTo=sec)
+    ins.append(Wavelength_monitor("secsrc_IL", Lmin=0, Lmax=20, nchan=100,
+                                  xwidth=0.026, yheight=0.026,
+                                  filename="secsrc_L.h5"),
+               position=(0, 0, 1e-6), relativeTo=slit)
+    g2_1 = TaperedGuide("Guide2_1", l=guide21_len, mx=m, my=m,
+                        segments=segs(g21))
+    ins.append(g2_1, position=(0.0016, 0.0016, guide21_start),
+               relativeTo=moderator)
+    ins.append(Beamstop("Shield2_1", xmin=-shield2_x, xmax=0.5, ymin=-0.5,
+                        ymax=0.5),
+               position=(0, 0, guide21_len + 1e-6), relativeTo=g2_1)
+    ins.append(Beamstop("Shield2_2", xmin=-0.5, xmax=0.5, ymin=-shield2_x,
+                        ymax=0.5),
+               position=(0, 0, guide21_len + 2e-6), relativeTo=g2_1)
+    ins.append(TaperedGuide("Guide2_2", l=guide22_len, mx=m, my=m,
+                            segments=segs(g22)),
+               position=(0, 0, guide21_len + 4e-6), relativeTo=g2_1)
+    sample = Arm("sampleMantid")
+    ins.append(sample, position=(0.001, 0.001, 40.0), relativeTo=origin)
+    ins.append(Wavelength_monitor("sample0_IL", Lmin=0, Lmax=20, nchan=100,
+                                  xwidth=sample_width, yheight=sample_height,
+                                  filename="sample0_L.h5"),
+               position=(0, 0, 0), relativeTo=sample)
+    pack = Arm("brilliancePack")
+    ins.append(pack, position=(0, 0, 0), relativeTo=sample)
+    ins.append(Slit("Mask", width=sample_width, height=sample_height),
+               position=(0, 0, 0), relativeTo=pack)
+    ins.append(PSD_monitor("imagePlate", nx=500, ny=500,
+                           xwidth=3 * sample_width,
+                           yheight=3 * sample_height, filename="sample_xy.h5"),
+               position=(0, 0, 1e-5), relativeTo=pack)
+    ins.append(Wavelength_monitor("sampleSpectrumL", Lmin=0, Lmax=20,
+                                  nchan=100, xwidth=sample_width,
+                                  yheight=sample_height, filename="sample_L.h5"),
+               position=(0, 0, 2e-5), relativeTo=pack)
+    ins.append(PosDiv_monitor("Divergence_xpos", maxdiv=xDivergence,
+                              ndiv=1000, npos=100, xwidth=sample_width,
+                              yheight=sample_height,
+                              filename="sample_divXpos.h5"),
+               position=(0, 0, 3e-5), relativeTo=pack)
+    ins.append(PosDiv_monitor("Divergence_ypos", maxdiv=yDivergence,
+                              ndiv=1000, npos=100, xwidth=sample_width,
+                              yheight=sample_height,
+                              filename="sample_divYpos.h5"),
+               position=(0, 0, 4e-5), orientation=(0, 0, 90),
+               relativeTo=pack)
+    return ins

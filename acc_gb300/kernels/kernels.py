@@ -131,3 +131,62 @@ class SQEGridKernel:
         c.table = p
         c.ftable = p
         c.table_len = self.S.size
+
+
+class ConstantQEKernel:
+    """constant_qe.S (acc/kernels/constant_qe.py:15-67) with p *= sigma
+    (acc/kernels/__init__.py:76-88): every scattered neutron takes the
+    momentum transfer Q (1/A) and the energy transfer E (meV), at a
+    uniform azimuth about its incident direction.  A neutron that cannot
+    make that transfer is absorbed."""
+    kind = nat.KERNEL_CONSTANT_QE
+
+    def __init__(self, Q, E, absorption_coefficient, scattering_coefficient):
+        self.Q, self.E = float(Q), float(E)
+        self.absorption_coefficient = float(absorption_coefficient)
+        self.scattering_coefficient = float(scattering_coefficient)
+
+    def pack(self, comp, c, binder, set_param):
+        set_param(c, 8, self.absorption_coefficient)
+        set_param(c, 9, self.scattering_coefficient)
+        set_param(c, 10, self.Q)
+        set_param(c, 11, self.E)
+
+
+class E_Q_Kernel:
+    """The makeS kernel of acc/kernels/E_Q.py:16-117 with p *= sigma
+    (acc/kernels/__init__.py:90-105): an analytic dispersion E(Q) and
+    intensity S(Q), both Python expressions in Q (1/A) with the names of
+    the math module ("^" is "**"), Q drawn on [Qmin, Qmax) with up to
+    max_iter tries.  The expressions are compiled to postfix programs on
+    the host (expression.compile_expression)."""
+    kind = nat.KERNEL_E_Q
+
+    def __init__(self, E_Q, S_Q, Qmin, Qmax, absorption_coefficient,
+                 scattering_coefficient, max_iter=100):
+        from .expression import compile_expression
+        self.E_Q, self.S_Q = str(E_Q), str(S_Q)
+        self.Qmin, self.Qmax = float(Qmin), float(Qmax)
+        self.max_iter = int(max_iter)
+        if self.max_iter < 1:
+            raise ValueError("max_iter must be >= 1")
+        self.absorption_coefficient = float(absorption_coefficient)
+        self.scattering_coefficient = float(scattering_coefficient)
+        self.E_prog = compile_expression(self.E_Q)
+        self.S_prog = compile_expression(self.S_Q)
+
+    def program(self):
+        """{opcode, argument} rows: the E(Q) program, then the S(Q) one."""
+        return np.concatenate([self.E_prog, self.S_prog])
+
+    def pack(self, comp, c, binder, set_param):
+        set_param(c, 8, self.absorption_coefficient)
+        set_param(c, 9, self.scattering_coefficient)
+        set_param(c, 10, self.Qmin)
+        set_param(c, 11, self.Qmax)
+        set_param(c, 12, float(self.max_iter))
+        c.ip[4], c.ip[5] = len(self.E_prog), len(self.S_prog)
+        flat = np.ascontiguousarray(self.program().reshape(-1))
+        c.table = binder.table(comp, "expr", flat, np.float64)
+        c.ftable = binder.table(comp, "expr_f32", flat, np.float32)
+        c.table_len = flat.size

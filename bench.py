@@ -61,6 +61,18 @@ WORKLOADS = {
         "powder_banked: the guide_chain guides -> powder cylinder r=0.5 cm "
         "h=4 cm, 50 peaks -> banked detector R=3 m, 8 banks x 128 tubes x "
         "256 pixels x 1000 tof bins (2.62e8 bins)"),
+    "constant_qe_box": (
+        "constant_qe_box: 1x1 cm source 70 meV -> Al block 6x10x1 cm, "
+        "constant (Q, E) = (3 /A, 30 meV) kernel -> I(Q,E) monitor 160x120"),
+    "e_q_box": (
+        "e_q_box: 1x1 cm source 70 meV -> Al block 6x10x1 cm, E(Q) kernel "
+        "E = 30 + 20 sin(Q), S = 1, Q 0-10 /A -> I(Q,E) monitor 160x120"),
+    "verdi": (
+        "verdi: the VERDI instrument (26 components): SNS moderator "
+        "(synthetic file, 141 E x 160 t, 0.1-1000 meV) -> 2 elliptic "
+        "mirrors as 4 tapered guides of 499 segments, m=6, with shields -> "
+        "secondary-source slit -> 5x5 mm sample mask; 11 wavelength, "
+        "position-divergence and PSD monitors"),
 }
 
 # Per-neutron counts of the FP32 path-regeneration kernel on this workload,
@@ -349,13 +361,11 @@ def grad_costs():
 # ---------------------------------------------------------- CPU baseline
 def cpu_oracle_rate(workload, seconds, seed, nthreads=0):
     """Neutrons/s of the CPU oracle on a bounded sample of the workload."""
-    from acc_gb300.engine import build_chain
-    from acc_gb300.instrument import calcTransformations
+    from acc_gb300.engine import chain_for_instrument
     from acc_gb300.memory import HostBinder
     from oracle import binding as O
     ins = build_instrument(workload)
-    off, rot = calcTransformations(ins)
-    ch = build_chain(ins.components, off, rot, HostBinder())
+    ch = chain_for_instrument(ins, HostBinder())
     nthreads = nthreads or os.cpu_count() or 1
     chunk = 1_000_000
     O.run_chain(ch, 100_000, seed=seed, nthreads=nthreads)  # warm
@@ -390,13 +400,11 @@ def reference_arm(a, rank, world):
     if rank != 0:
         return 0
     sample = max(2_000_000, int(a.ncount) // 5)
-    from acc_gb300.engine import build_chain
-    from acc_gb300.instrument import calcTransformations
+    from acc_gb300.engine import chain_for_instrument
     from acc_gb300.memory import HostBinder
     from oracle import binding as O
     ins = build_instrument(a.workload)
-    off, rot = calcTransformations(ins)
-    ch = build_chain(ins.components, off, rot, HostBinder())
+    ch = chain_for_instrument(ins, HostBinder())
     nthreads = os.cpu_count() or 1
     for w in range(a.warmup):
         O.run_chain(ch, sample, seed=a.seed, first=w * sample,

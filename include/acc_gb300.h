@@ -30,15 +30,18 @@
 extern "C" {
 #endif
 
-#define MCV_ABI_VERSION 2
+#define MCV_ABI_VERSION 3
 
-#define MCV_MAX_COMPONENTS 16
-#define MCV_NPARAM 40
+#define MCV_MAX_COMPONENTS 32
+#define MCV_NPARAM 24
 #define MCV_NIPARAM 8
 #define MCV_MAX_INTERSECTIONS 10  /* acc/geometry/arrow_intersect.py:16 */
 #define MCV_MAX_BOUNCES 100000    /* acc/components/optics/guide.py:17 */
 #define MCV_MS_MAX_SCATTERED 16   /* output neutrons per HMS event (the
                                      reference default is 10) */
+#define MCV_EXPR_STACK 8          /* evaluation stack of an E(Q) / S(Q)
+                                     program (E_Q kernel)              */
+#define MCV_EXPR_MAX_OPS 256      /* instructions per E(Q) / S(Q) program */
 
 /* ---- error codes ---------------------------------------------------- */
 enum {
@@ -96,7 +99,29 @@ enum {
 enum {
   MCV_KERNEL_ISOTROPIC = 1,   /* acc/kernels/isotropic.py:5-21, __init__.py:36-44 */
   MCV_KERNEL_POWDER = 2,      /* acc/kernels/powderdiffr.py                        */
-  MCV_KERNEL_SQE_GRID = 3     /* no reference counterpart (gridded S(Q,E) table)   */
+  MCV_KERNEL_SQE_GRID = 3,    /* no reference counterpart (gridded S(Q,E) table)   */
+  MCV_KERNEL_CONSTANT_QE = 4, /* acc/kernels/constant_qe.py:15-67, __init__.py:76-88 */
+  MCV_KERNEL_E_Q = 5          /* acc/kernels/E_Q.py:16-117, __init__.py:90-105     */
+};
+
+/* Instructions of the postfix programs that carry the E_Q kernel's E(Q)
+ * and S(Q) expressions (the reference compiles the expression strings
+ * into device functions, acc/kernels/E_Q.py:16-34; here the host compiles
+ * them into this form).  Each instruction is two table entries
+ * {opcode, argument}.  The argument is used by CONST (the value) and POWI
+ * (the integer exponent); the others ignore it. */
+enum {
+  MCV_EXPR_CONST = 1, MCV_EXPR_Q = 2,
+  MCV_EXPR_ADD = 3, MCV_EXPR_SUB = 4, MCV_EXPR_MUL = 5, MCV_EXPR_DIV = 6,
+  MCV_EXPR_POW = 7, MCV_EXPR_NEG = 8, MCV_EXPR_POWI = 9, MCV_EXPR_ATAN2 = 10,
+  MCV_EXPR_MIN = 11, MCV_EXPR_MAX = 12, MCV_EXPR_MOD = 13,
+  MCV_EXPR_EXP = 16, MCV_EXPR_LOG = 17, MCV_EXPR_LOG10 = 18,
+  MCV_EXPR_SQRT = 19, MCV_EXPR_SIN = 20, MCV_EXPR_COS = 21, MCV_EXPR_TAN = 22,
+  MCV_EXPR_ASIN = 23, MCV_EXPR_ACOS = 24, MCV_EXPR_ATAN = 25,
+  MCV_EXPR_SINH = 26, MCV_EXPR_COSH = 27, MCV_EXPR_TANH = 28,
+  MCV_EXPR_ASINH = 29, MCV_EXPR_ACOSH = 30, MCV_EXPR_ATANH = 31,
+  MCV_EXPR_ERF = 32, MCV_EXPR_ERFC = 33, MCV_EXPR_FABS = 34,
+  MCV_EXPR_FLOOR = 35, MCV_EXPR_CEIL = 36
 };
 
 /*
@@ -119,6 +144,12 @@ enum {
  *               float64, q_v ascending (powderdiffr.py:112-155)
  *       SQE_GRID: 10 Qmin 11 Qmax 12 Emin 13 Emax
  *               table: nQ x nE float32 S(Q,E), row-major in Q
+ *       CONSTANT_QE: 10 Q (1/A) 11 E (meV)
+ *       E_Q: 10 Qmin 11 Qmax (1/A) 12 max_iter (tries of the Q draw)
+ *               ip[4] = E(Q) instructions, ip[5] = S(Q) instructions
+ *               (each 1..MCV_EXPR_MAX_OPS); table (float64) and ftable
+ *               (float32): the E(Q) program then the S(Q) program,
+ *               {opcode, argument} per instruction (MCV_EXPR_*)
  * PSD_MONITOR (psd_monitor.py:66-83)          ip: nx ny;  dp: xmin xmax ymin ymax
  * PSD_MONITOR_4PI (psd_monitor_4pi.py:56-79)  ip: nphi ntheta; dp: radius
  * WAVELENGTH_MONITOR (wavelength_monitor.py:52-74)

@@ -79,6 +79,10 @@ def lib():
         L.oracle_source_one.argtypes = [ctypes.c_void_p, ctypes.c_void_p, c_double_p]
         L.oracle_hss_one.argtypes = [ctypes.c_void_p, ctypes.c_void_p,
                                      ctypes.c_int, c_double_p]
+        L.oracle_kernel_scatter_one.argtypes = [ctypes.c_void_p, c_double_p,
+                                                ctypes.c_uint64, ctypes.c_uint64]
+        L.oracle_expr_eval.restype = ctypes.c_double
+        L.oracle_expr_eval.argtypes = [c_double_p, ctypes.c_int, ctypes.c_double]
         L.oracle_apply_transform.argtypes = [c_double_p, c_double_p, c_double_p]
         L.oracle_sqe_lookup.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double]
         L.oracle_sqe_lookup.restype = ctypes.c_double
@@ -203,6 +207,20 @@ def hss_one(comp, neutron, uniforms):
     u = np.ascontiguousarray(uniforms, dtype=np.float32)
     lib().oracle_hss_one(ctypes.byref(comp), u.ctypes.data, u.size, _dp(st))
     return st
+
+
+def kernel_scatter_one(comp, neutron, seed=1, index=0):
+    """The HSS kernel's scatter (p *= sigma, then S) on one neutron."""
+    st = np.array(neutron, dtype=np.float64)
+    lib().oracle_kernel_scatter_one(ctypes.byref(comp), _dp(st), int(seed),
+                                    int(index))
+    return st
+
+
+def expr_eval(prog, Q):
+    """An E_Q kernel program ({opcode, argument} rows) at Q."""
+    p = np.ascontiguousarray(prog, dtype=np.float64).reshape(-1)
+    return lib().oracle_expr_eval(_dp(p), p.size // 2, float(Q))
 
 
 def sqe_lookup(comp, Q, E):

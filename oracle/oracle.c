@@ -346,8 +346,19 @@ static void sns_generate(const mcv_component* c, double randE, double randt,
                               Es[Eidx_stop], 1e-7);
   int idx1 = 0;
   while (idx1 < nE && Es[idx1] < Eval) idx1 += 1;
+  /* the reference's bracket (:38-46) kept in bounds: index -1 wraps to
+   * the last energy as numba's indexing does (weight 0 when Eval ==
+   * Es[0]); above the last tabulated energy, where the reference reads one
+   * row past its table, the last row */
   int Eidxh = idx1, Eidxl = idx1 - 1;
-  double wl = (Es[Eidxh] - Eval) / (Es[Eidxh] - Es[Eidxl]);
+  double wl = 0.0;
+  if (idx1 >= nE) {
+    Eidxh = nE - 1;
+    Eidxl = nE - 1;
+  } else {
+    if (Eidxl < 0) Eidxl = nE - 1;
+    wl = (Es[Eidxh] - Eval) / (Es[Eidxh] - Es[Eidxl]);
+  }
   snsvec_t pt = {Ptmat + (size_t)Eidxl * nt, Ptmat + (size_t)Eidxh * nt, wl};
   double p0 = snsvec_at(&pt, tidx_start), p1 = snsvec_at(&pt, tidx_stop - 1);
   randp = p0 + randt * (p1 - p0);
@@ -1275,6 +1286,169 @@ static void sqe_scatter(neutron_t* n, rng_t* rng, const mcv_component* c) {
   n->p *= prob_f;
 }
 
+/* Outgoing velocity of a (Q, E) transfer, shared by the constant-(Q, E)
+ * and E(Q) kernels (constant_qe.py:38-67, E_Q.py:64-92): v1 = vf cos(t)
+ * along the incident direction e1, v2 = vf sin(t) cos(phi) along
+ * e2 = unit(n x e1), v3 = vf sin(t) sin(phi) along e3 = e1 x e2, with
+ * n = z unless e1 lies within 0.1 of it (then x). */
+static void qe_velocity(neutron_t* n, double vf, double cost, double sint,
+                        double phi) {
+  double v2 = vf * sint * cos(phi), v3 = vf * sint * sin(phi);
+  double v1 = vf * cost;
+  double e1[3] = {n->vx, n->vy, n->vz}, e2[3], e3[3], nrm[3];
+  normalize3(e1);
+  if (fabs(e1[0]) > 1e-1 || fabs(e1[1]) > 1e-1) { nrm[0] = 0; nrm[1] = 0; nrm[2] = 1; }
+  else { nrm[0] = 1; nrm[1] = 0; nrm[2] = 0; }
+  cross3(nrm, e1, e2);
+  normalize3(e2);
+  cross3(e1, e2, e3);
+  n->vx = e1[0] * v1 + e2[0] * v2 + e3[0] * v3;
+  n->vy = e1[1] * v1 + e2[1] * v2 + e3[1] * v3;
+  n->vz = e1[2] * v1 + e2[2] * v2 + e3[2] * v3;
+}
+
+/* constant_qe.S (acc/kernels/constant_qe.py:15-67): scatter to the fixed
+ * (Q, E) = (dp[10], dp[11]) with one draw for the azimuth.  The reference
+ * has no guard for a transfer the neutron cannot make (E above Ei, or
+ * |cos(theta)| > 1), where its velocity turns NaN; here such a neutron is
+ * absorbed (p = -1), after the azimuth draw. */
+static void constant_qe_S(neutron_t* n, rng_t* rng, const mcv_component* c) {
+  double Q = c->dp[10], E = c->dp[11];
+  double vi = length3(n->vx, n->vy, n->vz);
+  double Ei = vi * vi * VS2E;
+  double Ef = Ei - E;
+  double phi = rng_uniform(rng) * 2.0 * M_PI;
+  if (!(Ef >= 0)) { n->p = -1; return; }
+  double vf = sqrt(Ef) * SE2V;
+  double ki = V2K * vi, kf = V2K * vf;
+  double cost = (ki * ki + kf * kf - Q * Q) / (2 * ki * kf);
+  double s2 = 1.0 - cost * cost;
+  if (!(s2 >= 0)) { n->p = -1; return; }
+  qe_velocity(n, vf, cost, sqrt(s2), phi);
+}
+
+/* E_Q kernel programs: postfix {opcode, argument} pairs (MCV_EXPR_*),
+ * run with a stack of MCV_EXPR_STACK values; a malformed program (stack
+ * under- or overflow, unknown opcode, not exactly one value left) gives
+ * NaN.  POWI is x**n by binary powering. */
+static double expr_powi(double x, int n) {
+  unsigned m = n < 0 ? 0u - (unsigned)n : (unsigned)n;
+  double r = 1.0, b = x;
+  while (m) {
+    if (m & 1u) r *= b;
+    m >>= 1;
+    if (m) b *= b;
+  }
+  return n < 0 ? 1.0 / r : r;
+}
+
+static double expr_mod(double a, double b) {
+  /* Python's float %: the remainder takes the sign of b */
+  double r = fmod(a, b);
+  if (r != 0 && ((r < 0) != (b < 0))) r += b;
+  return r;
+}
+
+double oracle_expr_eval(const double* prog, int nops, double Q) {
+  double st[MCV_EXPR_STACK];
+  int sp = 0;
+  for (int i = 0; i < nops; ++i) {
+    int op = (int)prog[2 * i];
+    double arg = prog[2 * i + 1];
+    if (op == MCV_EXPR_CONST || op == MCV_EXPR_Q) {
+      if (sp >= MCV_EXPR_STACK) return NAN;
+      st[sp++] = op == MCV_EXPR_CONST ? arg : Q;
+      continue;
+    }
+    if (sp < 1) return NAN;
+    double x = st[sp - 1], r;
+    if (op >= MCV_EXPR_ADD && op <= MCV_EXPR_MOD && op != MCV_EXPR_NEG &&
+        op != MCV_EXPR_POWI) {
+      if (sp < 2) return NAN;
+      double a = st[sp - 2], b = x;
+      switch (op) {
+        case MCV_EXPR_ADD: r = a + b; break;
+        case MCV_EXPR_SUB: r = a - b; break;
+        case MCV_EXPR_MUL: r = a * b; break;
+        case MCV_EXPR_DIV: r = a / b; break;
+        case MCV_EXPR_POW: r = pow(a, b); break;
+        case MCV_EXPR_ATAN2: r = atan2(a, b); break;
+        case MCV_EXPR_MIN: r = b < a ? b : a; break;
+        case MCV_EXPR_MAX: r = b > a ? b : a; break;
+        default: r = expr_mod(a, b); break;
+      }
+      st[sp - 2] = r;
+      --sp;
+      continue;
+    }
+    switch (op) {
+      case MCV_EXPR_NEG: r = -x; break;
+      case MCV_EXPR_POWI: r = expr_powi(x, (int)arg); break;
+      case MCV_EXPR_EXP: r = exp(x); break;
+      case MCV_EXPR_LOG: r = log(x); break;
+      case MCV_EXPR_LOG10: r = log10(x); break;
+      case MCV_EXPR_SQRT: r = sqrt(x); break;
+      case MCV_EXPR_SIN: r = sin(x); break;
+      case MCV_EXPR_COS: r = cos(x); break;
+      case MCV_EXPR_TAN: r = tan(x); break;
+      case MCV_EXPR_ASIN: r = asin(x); break;
+      case MCV_EXPR_ACOS: r = acos(x); break;
+      case MCV_EXPR_ATAN: r = atan(x); break;
+      case MCV_EXPR_SINH: r = sinh(x); break;
+      case MCV_EXPR_COSH: r = cosh(x); break;
+      case MCV_EXPR_TANH: r = tanh(x); break;
+      case MCV_EXPR_ASINH: r = asinh(x); break;
+      case MCV_EXPR_ACOSH: r = acosh(x); break;
+      case MCV_EXPR_ATANH: r = atanh(x); break;
+      case MCV_EXPR_ERF: r = erf(x); break;
+      case MCV_EXPR_ERFC: r = erfc(x); break;
+      case MCV_EXPR_FABS: r = fabs(x); break;
+      case MCV_EXPR_FLOOR: r = floor(x); break;
+      case MCV_EXPR_CEIL: r = ceil(x); break;
+      default: return NAN;
+    }
+    st[sp - 1] = r;
+  }
+  return sp == 1 ? st[0] : NAN;
+}
+
+/* The S of makeS (acc/kernels/E_Q.py:37-98): up to max_iter draws of
+ * Q uniform on [Qmin, Qmax), each rejected while E(Q) exceeds Ei or the
+ * transfer is kinematically closed (cos^2 > 1); none accepted -> p = 0.
+ * Weight S(Q) (vf/vi) Q (Qmax-Qmin) / (2 ki kf) / tries. */
+static void e_q_S(neutron_t* n, rng_t* rng, const mcv_component* c) {
+  double Qmin = c->dp[10], Qmax = c->dp[11];
+  int max_iter = (int)c->dp[12];
+  const double* progE = (const double*)c->table;
+  const double* progS = progE + 2 * c->ip[4];
+  double vi = length3(n->vx, n->vy, n->vz);
+  double Ei = vi * vi * VS2E;
+  double Q = 0, vf = 0, ki = 0, kf = 0, cost = 0, cost2 = 0;
+  int itr, found = 0;
+  for (itr = 0; itr < max_iter; ++itr) {
+    Q = rng_uniform(rng) * (Qmax - Qmin);
+    Q += Qmin;
+    double E = oracle_expr_eval(progE, c->ip[4], Q);
+    double Ef = Ei - E;
+    if (Ef < 0) continue;
+    vf = sqrt(Ef) * SE2V;
+    ki = V2K * vi;
+    kf = V2K * vf;
+    cost = (ki * ki + kf * kf - Q * Q) / (2 * ki * kf);
+    cost2 = cost * cost;
+    if (cost2 > 1) continue;
+    found = 1;
+    break;
+  }
+  if (!found) { n->p = 0; return; }
+  double sint = sqrt(1.0 - cost2);
+  double phi = rng_uniform(rng) * 2.0 * M_PI;
+  qe_velocity(n, vf, cost, sint, phi);
+  double S = oracle_expr_eval(progS, c->ip[5], Q);
+  double prob_f = S * (vf / vi) * Q * (Qmax - Qmin) / (kf * ki) / 2;
+  n->p *= prob_f / (itr + 1);
+}
+
 /* ---------------------------------------------------------------- HSS */
 static double hss_sigma(const neutron_t* n, const mcv_component* c) {
   if (c->ip[1] == MCV_KERNEL_POWDER) return powder_coeff(n, c);
@@ -1296,6 +1470,14 @@ static void kernel_scatter(neutron_t* n, rng_t* rng, const mcv_component* c) {
     case MCV_KERNEL_SQE_GRID:
       n->p *= c->dp[9];
       sqe_scatter(n, rng, c);
+      break;
+    case MCV_KERNEL_CONSTANT_QE:
+      n->p *= c->dp[9]; /* kernels/__init__.py:85 */
+      constant_qe_S(n, rng, c);
+      break;
+    case MCV_KERNEL_E_Q:
+      n->p *= c->dp[9]; /* kernels/__init__.py:103 */
+      e_q_S(n, rng, c);
       break;
     default:
       break;
@@ -2049,6 +2231,14 @@ void oracle_hss_one(const mcv_component* c, const float* u, int nu,
   rng_t rng;
   rng_init(&rng, 0, 0, 0, u, nu);
   hss((neutron_t*)st, &rng, c);
+}
+/* The HSS kernel's scatter (p *= sigma, then S) on one neutron state,
+ * uniforms from Philox (seed, index) stream 0. */
+void oracle_kernel_scatter_one(const mcv_component* c, double* st,
+                               uint64_t seed, uint64_t index) {
+  rng_t rng;
+  rng_init(&rng, seed, index, 0, NULL, 0);
+  kernel_scatter((neutron_t*)st, &rng, c);
 }
 void oracle_apply_transform(const double* rot, const double* off, double* st) {
   apply_transform((neutron_t*)st, rot, off);

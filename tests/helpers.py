@@ -3,8 +3,7 @@ and on the GPU engine with the same Philox stream, and compare."""
 
 import numpy as np
 
-from acc_gb300.engine import build_chain
-from acc_gb300.instrument import calcTransformations
+from acc_gb300.engine import chain_for_instrument
 from acc_gb300.memory import HostBinder
 from acc_gb300.stats import chi2_per_dof  # noqa: F401
 
@@ -15,8 +14,7 @@ def oracle_run(ins, ncount, seed=7, first=0, record=False, uniforms=None,
     stats, neutrons, last)."""
     from oracle import binding as O
     b = HostBinder()
-    off, rot = calcTransformations(ins)
-    ch = build_chain(ins.components, off, rot, b)
+    ch = chain_for_instrument(ins, b)
     stats, out, last = O.run_chain(ch, ncount, seed=seed, first=first,
                                    record=record, uniforms=uniforms,
                                    nthreads=nthreads)

@@ -38,7 +38,7 @@ def test_struct_layout_matches(engine_lib, oracle_lib):
     assert oracle_lib.oracle_sizeof_chain() == ctypes.sizeof(nat.mcv_chain)
     assert oracle_lib.oracle_sizeof_component() == \
         ctypes.sizeof(nat.mcv_component)
-    assert engine_lib.mcv_abi_version() == 2
+    assert engine_lib.mcv_abi_version() == 3
 
 
 def _bad_chain():
@@ -94,6 +94,41 @@ def test_hss_validation(engine_lib):
     rc = engine_lib.mcv_run_chain(None, ctypes.byref(ch), 1, 0, 1, 32, None,
                                   None, ctypes.byref(st))
     assert rc == nat.MCV_EINVAL and b"shape" in st.message
+
+
+def test_e_q_kernel_validation(engine_lib):
+    """The E(Q) kernel needs both programs (1..MCV_EXPR_MAX_OPS
+    instructions) and 1 <= max_iter <= 1e6; a kernel kind past E_Q is
+    unknown."""
+    from acc_gb300.components.samples.homogeneous_single_scatterer import \
+        factory
+    from acc_gb300.engine import build_chain
+    from acc_gb300.geometry import Block
+    from acc_gb300.kernels import E_Q_Kernel
+    from acc_gb300.memory import HostBinder
+    H = factory(Block(0.01, 0.01, 0.01), E_Q_Kernel("Q", "1", 0, 5, 1, 1))
+    st = nat.mcv_status()
+
+    def run(ch):
+        return engine_lib.mcv_run_chain(None, ctypes.byref(ch), 1, 0, 1, 32,
+                                        None, None, ctypes.byref(st))
+    for field, value in (("ip4", 0), ("ip4", nat.MCV_EXPR_MAX_OPS + 1),
+                         ("ip5", 0), ("dp12", 0.0), ("dp12", 2e6),
+                         ("table", None)):
+        ch = build_chain([H("s")], binder=HostBinder())
+        c = ch.comp[0]
+        if field == "ip4":
+            c.ip[4] = value
+        elif field == "ip5":
+            c.ip[5] = value
+        elif field == "dp12":
+            c.dp[12] = value
+        else:
+            c.table = value
+        assert run(ch) == nat.MCV_EINVAL and b"E(Q)" in st.message, field
+    ch = build_chain([H("s")], binder=HostBinder())
+    ch.comp[0].ip[1] = nat.KERNEL_E_Q + 1
+    assert run(ch) == nat.MCV_EINVAL and b"unknown scattering" in st.message
 
 
 def test_context_create(engine_lib):

@@ -1,0 +1,74 @@
+"""Constant-(Q, E) and E(Q) kernels on the GPU, both precisions, against
+the pins of the reference's kernel tests (tests/kernels/test_constant_qe.py:
+25-65: the transfer is Q = 3 /A, E = 30 meV to 7 decimals;
+tests/kernels/test_E_Q.py:15-34: every scattered neutron has E = E(Q)).
+
+The incident state of each neutron comes from the same chain cut after its
+source, replayed with the same seed: the source draws the first numbers of
+each neutron's stream, so both runs start from the same neutron.
+Tolerances: FP64 7 decimals (as the reference); FP32 1e-3 meV in E and
+1e-4 /A in Q, several float roundings of 70 meV and 3.7 km/s velocities.
+"""
+
+import numpy as np
+import pytest
+import torch
+
+from acc_gb300 import engine, instruments
+from acc_gb300.conversion import V2K, v2e
+
+pytestmark = pytest.mark.gpu
+
+TOL = {"float64": (1e-7, 1e-7), "float32": (1e-3, 1e-4)}
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _engine(engine_lib):
+    torch.cuda.init()
+    yield
+
+
+def _incident_and_scattered(ins_factory, n, seed, floattype):
+    ch = engine.chain_for_instrument(ins_factory())
+    out, last = engine.replay(ch, n, seed=seed, floattype=floattype)
+    src = engine.chain_for_instrument(ins_factory())
+    src.ncomp = 1
+    inc, _ = engine.replay(src, n, seed=seed, floattype=floattype)
+    return inc.cpu().numpy(), out.cpu().numpy(), last.cpu().numpy()
+
+
+def _transfer(inc, out):
+    vi, vf = inc[:, 3:6], out[:, 3:6]
+    E = v2e(np.linalg.norm(vi, axis=1)) - v2e(np.linalg.norm(vf, axis=1))
+    Q = V2K * np.linalg.norm(vi - vf, axis=1)
+    return Q, E
+
+
+@pytest.mark.parametrize("floattype", ["float64", "float32"])
+def test_constant_qe_transfer_on_gpu(floattype):
+    n = 20000
+    inc, out, last = _incident_and_scattered(instruments.constant_qe_box, n,
+                                             7, floattype)
+    alive = out[:, 9] > 0
+    assert alive.sum() == n  # every neutron hits the block and scatters
+    Q, E = _transfer(inc, out)
+    tE, tQ = TOL[floattype]
+    assert np.abs(E - 30.0).max() <= tE
+    assert np.abs(Q - 3.0).max() <= tQ
+
+
+@pytest.mark.parametrize("floattype", ["float64", "float32"])
+def test_e_q_dispersion_on_gpu(floattype):
+    E_Q = "5*sin(Q)**2+5"
+
+    def box():
+        return instruments.e_q_box(E_Q=E_Q, S_Q="1", Qmin=0.0, Qmax=15.0)
+
+    n = 20000
+    inc, out, _ = _incident_and_scattered(box, n, 9, floattype)
+    ok = out[:, 9] > 0
+    assert ok.sum() > 0.9 * n
+    Q, E = _transfer(inc[ok], out[ok])
+    want = 5 * np.sin(Q) ** 2 + 5
+    tE, _ = TOL[floattype]
+    assert np.abs(E - want).max() <= max(tE, 1e-7), np.abs(E - want).max()

@@ -92,7 +92,8 @@ def test_build_chain_limits():
     with pytest.raises(ValueError):
         build_chain([], binder=HostBinder())
     with pytest.raises(ValueError):
-        build_chain([Arm(f"a{i}") for i in range(17)], binder=HostBinder())
+        build_chain([Arm(f"a{i}") for i in range(nat.MCV_MAX_COMPONENTS + 1)],
+                    binder=HostBinder())
 
 
 def test_mcvine_alias_and_script_loading(tmp_path):
@@ -178,3 +179,57 @@ def test_weight_exp2_places_the_source_weight_near_2_64():
         assert ch.weight_exp2 == e
     # no source first: no scaling
     assert engine.weight_exp2([Arm("a")]) == 0
+
+
+def test_leading_arms_are_left_out_of_the_chain():
+    """An arm ahead of the source (as VERDI's origin) is not in the chain;
+    the transforms of the kept components are unchanged."""
+    from acc_gb300 import instruments as I
+    from acc_gb300.engine import chain_for_instrument, chain_parts
+    from acc_gb300.instrument import calcTransformations
+    ins = I.verdi(moderator_file=I.synthetic_moderator_file(nE=20, nt=20))
+    comps, off, rot, first = chain_parts(ins)
+    assert first == 1 and comps[0] is ins.components[1]
+    off_all, rot_all = calcTransformations(ins)
+    np.testing.assert_array_equal(off, off_all[1:])
+    np.testing.assert_array_equal(rot, rot_all[1:])
+    ch = chain_for_instrument(ins, HostBinder())
+    assert ch.ncomp == len(ins.components) - 1 == 25
+    assert ch.first_component == 1
+    assert ch.comp[0].opcode == nat.OP_SNS_SOURCE
+    # the FP32 weight scale comes from the source's nominal weight
+    assert ch.weight_exp2 != 0
+
+
+def test_verdi_mirror_geometry():
+    """The elliptic profile (acc/test/ellipse.py:101-162) is continuous from
+    segment to segment and the shield tip lies on both sight lines of
+    SingleWall.calc_shield_xz (:37-54)."""
+    from acc_gb300 import instruments as I
+    a, b = 0.105, 15.875
+    h1, h2, w1, w2 = I.elliptic_guide_segments(b, 6.35, 16.0, 500, 2 * b, 2 * a)
+    np.testing.assert_allclose(h2[:-1], h1[1:], rtol=1e-12)
+    np.testing.assert_array_equal(h1, w1)
+    np.testing.assert_allclose(h1[0], 2 * a * np.sqrt(6.35 / b * (2 - 6.35 / b)))
+    x, z = I.shield_vertex(a, b, 0., 0.03, 6.35, 26.9, 31.75, 0.02)
+    xe = I.ellipse_half_opening(26.9, a, b)
+    xs = I.ellipse_half_opening(6.35, a, b)
+    # on the line (0, -0.015) -> (26.9, xe) and on (6.35, xs) -> (31.75, -0.01)
+    np.testing.assert_allclose(x, -0.015 + (xe + 0.015) * z / 26.9, rtol=1e-12)
+    np.testing.assert_allclose(
+        x, xs + (-0.01 - xs) * (z - 6.35) / (31.75 - 6.35), rtol=1e-12)
+    assert 6.35 < z < 26.9
+
+
+def test_chain_keeps_its_tables_alive():
+    """A chain built from a temporary instrument holds the components whose
+    lookup tables its pointers refer to."""
+    import gc
+    import weakref
+    from acc_gb300 import instruments as I
+    from acc_gb300.engine import chain_for_instrument
+    ch = chain_for_instrument(I.tapered_guide_chain(), HostBinder())
+    guide = weakref.ref(ch._components[1])
+    gc.collect()
+    assert guide() is not None
+    assert ch.comp[1].table != 0

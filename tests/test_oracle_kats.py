@@ -272,6 +272,42 @@ def test_sns_source_draws_follow_the_moderator_spectrum(oracle_lib):
         assert 0.0 < t < 3000e-6
 
 
+def test_sns_energy_beyond_the_table_takes_the_last_time_row(oracle_lib):
+    """The reference brackets the drawn E with Es[idx1-1], Es[idx1] where
+    idx1 is the first energy not below E (SNS_source.py:38-46).  Its
+    zero_find can return an E past the last tabulated energy (it expands
+    the bracket beyond the table and extrapolates the last quadratic),
+    where idx1 = len(Es) and the reference reads a row past its table.  Here
+    that E takes the last row of P(t | E): t stays finite, inside the
+    tabulated window, and repeatable.  VERDI's 0.1-1000 meV window on the
+    synthetic file (energies 0.1 meV - 10 eV) draws such energies for
+    randE near 0: there EPmin = 0 lies below the cumulative probability at
+    the bisection's lower end Es[Eidx_start], the bracket expands past the
+    table and the extrapolated last quadratic crosses the target far out."""
+    from acc_gb300 import instruments
+    from acc_gb300.engine import build_chain
+    from acc_gb300.memory import HostBinder
+    from oracle import binding as O
+    path = instruments.synthetic_moderator_file(nE=141, nt=160)
+    try:
+        from acc_gb300.components.sources.SNS_source import SNS_source
+        import warnings
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            src = SNS_source("m", path, 0.1, 1000., 0.03, 0.03, 6.2, 0.1, 0.1)
+        comp = build_chain([src], binder=HostBinder()).comp[0]
+    finally:
+        os.remove(path)
+    beyond = 0
+    for u in np.linspace(0.0, 0.002, 400):
+        E, t = O.sns_generate(comp, u, 0.37)
+        assert np.isfinite(E) and np.isfinite(t)
+        assert 0.0 <= t <= 3000e-6
+        assert (E, t) == O.sns_generate(comp, u, 0.37)
+        beyond += E > 1e4  # meV: past the table's last energy (10 eV)
+    assert beyond > 0
+
+
 @pytest.mark.parametrize("dmode", [1.0, 0.0])
 def test_sts_source_face_points_on_the_moderator_cylinder(oracle_lib, dmode):
     """STS_source.propagate (STS_source.py:242-259): on a square port the
