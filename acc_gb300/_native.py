@@ -20,6 +20,8 @@ MCV_MAX_VARIANTS = 1024
 MCV_MS_MAX_SCATTERED = 16
 MCV_EXPR_STACK = 8
 MCV_EXPR_MAX_OPS = 256
+MCV_SNS_E_NODES = 4096
+MCV_SNS_T_NODES = 512
 MCV_NOALLOC_MAX_VARIANTS = 64
 
 MCV_OK, MCV_EINVAL, MCV_ECUDA, MCV_ECOUNT, MCV_EBOUNCE = 0, 1, 2, 3, 4

@@ -159,6 +159,121 @@ def init(Emin, Emax, datafile, sts_load=False):
     return out + (loaded[5],) if sts_load else out
 
 
+# ------------------------------------------------- FP32 sampling tables
+# The FP64 kernels invert the cumulative tables per neutron with the
+# reference's zero_find (SNS_source.py:77-96).  The FP32 kernels read
+# inverse tables instead, computed here once with the same zero_find:
+#   E(u) at SNS_E_NODES + 1 evenly spaced u, linearly interpolated;
+#   for every energy row r, t_r(u) at SNS_T_NODES + 1 evenly spaced u over
+#   the row's t window, and the row's probability mass in that window.
+# A neutron's t comes from the two rows that bracket its E, mixed with the
+# reference's weights wl, 1 - wl: the row is picked with probability
+# proportional to its weight times its mass and the uniform rescaled into
+# it, which samples the mixture the reference inverts.  Draws of u outside
+# [u_lo, u_hi], where zero_find's bracket leaves the table, go to the FP64
+# sampler, so the reference's values there are kept.
+SNS_E_NODES = nat.MCV_SNS_E_NODES
+SNS_T_NODES = nat.MCV_SNS_T_NODES
+ZERO_FIND_EXPAND_MAX, ZERO_FIND_BISECT_MAX = 64, 200
+
+
+def _quadfuncint(xdes, vecx, rows, vecy):
+    """quadfuncint (SNS_source.py:66-75) for arrays of xdes; vecy[rows]
+    gives each element's table (rows None: one table).  The index is the
+    first in [1, len) not below xdes, clamped to the last point; index -1
+    wraps to the last point (numba's indexing)."""
+    n = len(vecx)
+    idx = np.searchsorted(vecx[1:], xdes, side="left") + 1
+    idx = np.minimum(idx, n - 1)
+    i0 = idx - 2
+    i0 = np.where(i0 < 0, i0 + n, i0)
+    if rows is None:
+        y0, y1, y2 = vecy[i0], vecy[idx - 1], vecy[idx]
+    else:
+        y0, y1, y2 = vecy[rows, i0], vecy[rows, idx - 1], vecy[rows, idx]
+    x1, x2, x3 = vecx[i0], vecx[idx - 1], vecx[idx]
+    with np.errstate(all="ignore"):
+        t1 = ((xdes - x2) * (xdes - x3) * y0) / ((x1 - x2) * (x1 - x3))
+        t2 = ((xdes - x1) * (xdes - x3) * y1) / ((x2 - x1) * (x2 - x3))
+        t3 = ((xdes - x1) * (xdes - x2) * y2) / ((x3 - x1) * (x3 - x2))
+        val = t1 + t2 + t3
+    return np.where(vecx[idx] == xdes, y2, val)
+
+
+def zero_find(vecx, vecy, yval, xmin, xmax, tol, rows=None):
+    """zero_find (SNS_source.py:77-96) for an array of targets yval, with
+    its loops bounded as the kernels bound them (64 expansions, 200
+    bisections)."""
+    yval = np.asarray(yval, dtype=np.float64)
+    F = lambda x, sel: _quadfuncint(  # noqa: E731
+        x, vecx, None if rows is None else rows[sel], vecy) - yval[sel]
+    allsel = np.arange(yval.size)
+    xl = np.full(yval.shape, float(xmin))
+    with np.errstate(all="ignore"):
+        xh = np.power(10.0, np.log10(xmin) + yval * (np.log10(xmax)
+                                                     - np.log10(xmin)))
+        f = F(xl, allsel)
+        fmid = F(xh, allsel)
+        for _ in range(ZERO_FIND_EXPAND_MAX):
+            m = np.where(fmid * f >= 0.0)[0]
+            if m.size == 0:
+                break
+            xh[m] = xh[m] + (xh[m] - xl[m]) * 2.0
+            fmid[m] = F(xh[m], m)
+        dx = xh - xl
+        rtb = xl.copy()
+        act = np.where(np.abs(F(rtb, allsel)) > tol)[0]
+        for _ in range(ZERO_FIND_BISECT_MAX):
+            if act.size == 0:
+                break
+            dx[act] *= 0.5
+            xmid = rtb[act] + dx[act]
+            fm = F(xmid, act)
+            up = fm < 0
+            rtb[act[up]] = xmid[up]
+            act = act[np.abs(F(rtb[act], act)) > tol]
+    return rtb
+
+
+def fp32_tables(Es, Pvec, ts, Ptmat, EPmin, EPmax, Eidx, tidx):
+    """(ftable float32 array, u_lo, u_hi): the inverse tables the FP32
+    kernels sample (layout in include/acc_gb300.h, SNS_SOURCE)."""
+    Es = np.asarray(Es, dtype=np.float64)
+    ts = np.asarray(ts, dtype=np.float64)
+    Pvec = np.asarray(Pvec, dtype=np.float64)
+    Ptmat = np.asarray(Ptmat, dtype=np.float64)
+    nE = len(Es)
+    u = np.arange(SNS_E_NODES + 1) / SNS_E_NODES
+    randp = EPmin + u * (EPmax - EPmin)
+    xmin, xmax = Es[Eidx[0]], Es[Eidx[1]]
+    Einv = zero_find(Es, Pvec, randp, xmin, xmax, 1e-7)
+    # the regular range: zero_find's bracket starts with the target above
+    # the cumulative probability at xmin, and the nodes lie in [xmin, xmax]
+    # and increase (the table's cumulative column drops to 0 past the
+    # file's usable rows, so the top is found from the nodes themselves)
+    ok = (randp > Pvec[Eidx[0]] + 1e-7) & (Einv >= xmin) & (Einv <= xmax)
+    # the longest run of regular nodes, each not below the one before
+    link = ok[1:] & ok[:-1] & (np.diff(Einv) >= 0)
+    best, start, lo, hi = 0, 0, 1, 0
+    for kk in range(1, len(u) + 1):
+        if kk == len(u) or not link[kk - 1]:
+            if ok[start] and kk - start > best:
+                best, lo, hi = kk - start, start, kk - 1
+            start = kk
+    if best >= 2:
+        u_lo, u_hi = u[lo], u[hi]
+    else:
+        u_lo, u_hi = 1.0, 0.0  # every draw takes the FP64 sampler
+    t0, t1 = tidx[0], tidx[1] - 1
+    mass = Ptmat[:, t1] - Ptmat[:, t0]
+    ut = np.arange(SNS_T_NODES + 1) / SNS_T_NODES
+    rows = np.repeat(np.arange(nE), SNS_T_NODES + 1)
+    targ = (Ptmat[rows, t0] + np.tile(ut, nE) * mass[rows])
+    Tinv = zero_find(ts, Ptmat, targ, ts[t0], ts[t1], 1e-5, rows=rows)
+    ftab = np.concatenate([Einv, Es, np.maximum(mass, 0.0), Tinv])
+    return ftab.astype(np.float32), float(u_lo), float(u_hi)
+
+
 class SNS_source(SourceBase):
     opcode = nat.OP_SNS_SOURCE
 
@@ -211,6 +326,14 @@ class SNS_source(SourceBase):
         flat = np.concatenate([Es, Pvec, ts, np.asarray(Ptmat).reshape(-1)])
         c.table = binder.table(self, "moderator", flat, np.float64)
         c.table_len = flat.size
+        if getattr(self, "_fp32", None) is None:
+            self._fp32 = fp32_tables(Es, Pvec, ts, Ptmat, EPmin, EPmax,
+                                     (Eidx_start, Eidx_stop),
+                                     (tidx_start, tidx_stop))
+        ftab, u_lo, u_hi = self._fp32
+        c.ftable = binder.table(self, "moderator_f32", ftab, np.float32)
+        set_param(c, 16, u_lo)
+        set_param(c, 17, u_hi)
         self.pack_geometry(c)
 
     def pack_geometry(self, c):

@@ -105,9 +105,11 @@ __device__ __forceinline__ void storage_source(Neutron<R>& n, uint64_t index,
 // ================================================== SNS moderator source
 // SNS_source (acc/components/sources/SNS_source.py:20-207): E and the
 // emission time from the moderator's cumulative tables (the host computes
-// them as _SNS_source_utils.py:187-223 does), in FP64 in both precisions.
-// The two loops of zero_find, unbounded in the reference, stop after 64 /
-// 200 passes, as in the oracle.
+// them as _SNS_source_utils.py:187-223 does).  FP64 inverts them per
+// neutron with the reference's zero_find, whose two loops, unbounded in the
+// reference, stop after 64 / 200 passes, as in the oracle; FP32 reads
+// inverse tables the host builds with the same zero_find
+// (sns_generate_f32).
 constexpr int kSnsExpandMax = 64;
 constexpr int kSnsBisectMax = 200;
 
@@ -228,6 +230,59 @@ static __device__ __noinline__ void sns_generate(const mcv_component& c,
   *tout = tval * 1e-6;
 }
 
+// FP32 draw of E (meV) and t (s) from the host's inverse tables (ftable,
+// layout in the header): E by linear interpolation in u; t from one of the
+// two energy rows that bracket E, picked with probability proportional to
+// the reference's row weight (wl, 1 - wl) times the row's mass in the t
+// window, with the uniform rescaled into the pick, which samples the
+// mixture the reference inverts (SNS_source.py:38-52).  Returns false for
+// a u outside [u_lo, u_hi] or rows without mass: the caller then takes
+// the FP64 sampler.
+__device__ __forceinline__ bool sns_generate_f32(const mcv_component& c,
+                                                 float randE, float randt,
+                                                 double* Eout,
+                                                 double* tout) {
+  if (!(randE >= c.fp[16] && randE <= c.fp[17])) return false;
+  const int nE = c.ip[1];
+  const float* Einv = c.ftable;
+  const float* Es = Einv + (MCV_SNS_E_NODES + 1);
+  const float* mass = Es + nE;
+  const float* Tinv = mass + nE;
+  const float s = randE * float(MCV_SNS_E_NODES);
+  const int k = min((int)s, MCV_SNS_E_NODES - 1);
+  const float e0 = __ldg(&Einv[k]);
+  const float E = fmaf(s - float(k), __ldg(&Einv[k + 1]) - e0, e0);
+  int lo = 0, hi = nE;  // first row with !(Es < E)
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (__ldg(&Es[mid]) < E) lo = mid + 1;
+    else hi = mid;
+  }
+  int Eh = lo, El = lo - 1;
+  float wl = 0.f;
+  if (lo >= nE) {
+    Eh = nE - 1;
+    El = nE - 1;
+  } else {
+    if (El < 0) El = nE - 1;
+    wl = (__ldg(&Es[Eh]) - E) / (__ldg(&Es[Eh]) - __ldg(&Es[El]));
+  }
+  const float ml = wl * __ldg(&mass[El]), mh = (1.f - wl) * __ldg(&mass[Eh]);
+  if (!(ml + mh > 0.f)) return false;
+  const float pl = ml / (ml + mh);
+  const bool low = randt < pl;
+  const int row = low ? El : Eh;
+  const float ut = low ? randt / pl : (randt - pl) / (1.f - pl);
+  const float* T = Tinv + (size_t)row * (MCV_SNS_T_NODES + 1);
+  const float st = fminf(ut, 1.f) * float(MCV_SNS_T_NODES);
+  const int j = min((int)st, MCV_SNS_T_NODES - 1);
+  const float t0 = __ldg(&T[j]);
+  const float t = fmaf(st - float(j), __ldg(&T[j + 1]) - t0, t0);
+  *Eout = double(E) * 1000.0;
+  *tout = double(t) * 1e-6;
+  return true;
+}
+
 // SNS_source.propagate (:157-207)
 template <typename R, typename Rng>
 __device__ __forceinline__ void sns_source(Neutron<R>& n, Rng& rng,
@@ -280,7 +335,12 @@ __device__ __forceinline__ void sns_source(Neutron<R>& n, Rng& rng,
   const R theta = hdivmin + (hdivmax - hdivmin) * rand_theta;
   const R phi = vdivmin + (vdivmax - vdivmin) * rand_phi;
   double E, t;
-  sns_generate(c, randE, randt, &E, &t);
+  if constexpr (sizeof(R) == 4) {
+    if (!sns_generate_f32(c, float(randE), float(randt), &E, &t))
+      sns_generate(c, randE, randt, &E, &t);
+  } else {
+    sns_generate(c, randE, randt, &E, &t);
+  }
   const R v = R(kSE2V * sqrt(E));
   n.x = x;
   n.y = y;

@@ -42,6 +42,10 @@ extern "C" {
 #define MCV_EXPR_STACK 8          /* evaluation stack of an E(Q) / S(Q)
                                      program (E_Q kernel)              */
 #define MCV_EXPR_MAX_OPS 256      /* instructions per E(Q) / S(Q) program */
+#define MCV_SNS_E_NODES 4096      /* intervals of the SNS source's FP32
+                                     inverse table of E                */
+#define MCV_SNS_T_NODES 512       /* intervals of each energy row's FP32
+                                     inverse table of t                */
 
 /* ---- error codes ---------------------------------------------------- */
 enum {
@@ -185,7 +189,13 @@ enum {
  *       7 EPmax 8 prob
  *   table: float64 Es[nE] (eV), Pvec[nE], ts[nt] (us), Ptmat[nE][nt]
  *          (cumulative probabilities from the host's set-up)
- *   E and t are drawn in FP64 in both precisions (the tables are FP64).
+ *   The FP64 kernels invert these tables per neutron (zero_find).  The
+ *   FP32 kernels read ftable (float32): E_inv[MCV_SNS_E_NODES + 1] (eV at
+ *   evenly spaced u, the same zero_find run on the host), Es[nE],
+ *   mass[nE] (each row's probability in the t window), then
+ *   t_inv[nE][MCV_SNS_T_NODES + 1] (us, evenly spaced u over each row's
+ *   window); a draw of u outside [dp 16, dp 17] (u_lo, u_hi: where
+ *   zero_find's bracket leaves the table) takes the FP64 sampler.
  *   STS_source (STS_source.py:107-284): ip[7] bit 0 set, bit 1 = dmode;
  *   dp: 9 tanMOa 10 cylx 11 cylz 12 cylphi1 13 cylphi2 14 MRadius0
  *       15 MOffangle (rad): the face point lies on the cylindrical
@@ -201,7 +211,8 @@ enum {
  */
 /* mcv_component.flags */
 #define MCV_COMP_IDENTITY_ROT 1   /* rot of this hop is the identity         */
-#define MCV_COMP_AGGREGATE 2      /* monitors: warp-aggregate tally atomics  */
+#define MCV_COMP_AGGREGATE 2      /* monitors: always warp-aggregate tally
+                                     atomics (hot bins aggregate anyway) */
 
 typedef struct mcv_component {
   int32_t opcode;

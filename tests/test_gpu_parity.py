@@ -72,12 +72,16 @@ BUILDERS = {
 CHI2_BUILDERS = [k for k in BUILDERS if k not in ("constant_qe_box", "verdi")]
 # neutrons of the same-stream tests (VERDI: enough to reach its sample)
 SAME_STREAM_N = {"verdi": 200_000}
-# VERDI is a 40 m chain with ~2000 tapered-guide segments: float positions
-# there carry ~1e-6 m of rounding (a float's spacing at 10 m), about 3e-4
-# of its 5 mm sample, above this test's 1e-4 bound for most neutrons.  Its
-# FP32 check is test_verdi_fp32_chi2; FP64 runs the same-stream test at
-# 1e-12.
-FP32_SAME_STREAM = [k for k in BUILDERS if k != "verdi"]
+# Not held to the FP32 same-stream bounds (their FP32 check is chi^2; FP64
+# runs the same-stream test at 1e-12):
+#  * the SNS and STS sources: FP32 draws E and t from inverse tables, t by
+#    sampling the two-row mixture the reference inverts, so a neutron's t
+#    is a different (equally distributed) draw from its uniforms;
+#  * VERDI (an SNS source too) is a 40 m chain with ~2000 tapered-guide
+#    segments: float positions there carry ~1e-6 m of rounding (a float's
+#    spacing at 10 m), about 3e-4 of its 5 mm sample.
+FP32_SAME_STREAM = [k for k in BUILDERS if k not in
+                    ("sns_source_chain", "sts_source_chain", "verdi")]
 
 
 @pytest.fixture(scope="module", autouse=True)
