@@ -81,10 +81,10 @@ WORKLOADS = {
 # warp instructions issued, and the DRAM bytes of that launch (tally bins
 # touched; it does not grow with the neutron count).
 KERNEL_COUNTS = {
-    "guide_chain": {"fp32_flops_per_neutron": 189.82,
-                    "warp_inst_per_neutron": 36.31,
-                    "thread_inst_per_neutron": 847.8,
-                    "dram_bytes_per_launch": 130560,
+    "guide_chain": {"fp32_flops_per_neutron": 169.32,
+                    "warp_inst_per_neutron": 35.23,
+                    "thread_inst_per_neutron": 823.2,
+                    "dram_bytes_per_launch": 135936,
                     "captured_neutrons": 10_000_000},
 }
 
