@@ -17,7 +17,8 @@ MCV_NIPARAM = 8
 MCV_MAX_INTERSECTIONS = 10
 MCV_MAX_BOUNCES = 100000
 MCV_MAX_VARIANTS = 1024
-MCV_MS_MAX_SCATTERED = 16
+MCV_MS_MAX_SCATTERED = 48
+MCV_COMPOSITE_MAX = 16
 MCV_EXPR_STACK = 8
 MCV_EXPR_MAX_OPS = 256
 MCV_SNS_E_NODES = 4096
@@ -46,11 +47,12 @@ OP_HMS = 15
 OP_GUIDE_TAPERING = 16
 OP_SNS_SOURCE = 17
 OP_NEUTRON_STORAGE = 18
+OP_KERNEL_ELEMENT = 19
 
 SHAPE_SPHERE, SHAPE_CYLINDER, SHAPE_BOX = 1, 2, 3
 CSG_PRIMITIVE, CSG_DIFFERENCE, CSG_UNION, CSG_INTERSECTION = 0, 1, 2, 3
 KERNEL_ISOTROPIC, KERNEL_POWDER, KERNEL_SQE_GRID = 1, 2, 3
-KERNEL_CONSTANT_QE, KERNEL_E_Q = 4, 5
+KERNEL_CONSTANT_QE, KERNEL_E_Q, KERNEL_COMPOSITE, KERNEL_SANS2D = 4, 5, 6, 7
 
 FLAG_IDENTITY_ROT = 1
 FLAG_AGGREGATE = 2

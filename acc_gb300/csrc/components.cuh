@@ -242,7 +242,7 @@ __device__ __forceinline__ bool sns_generate_f32(const mcv_component& c,
                                                  float randE, float randt,
                                                  double* Eout,
                                                  double* tout) {
-  if (!(randE >= c.fp[16] && randE <= c.fp[17])) return false;
+  if (!c.ftable || !(randE >= c.fp[16] && randE <= c.fp[17])) return false;
   const int nE = c.ip[1];
   const float* Einv = c.ftable;
   const float* Es = Einv + (MCV_SNS_E_NODES + 1);

@@ -65,6 +65,91 @@ class DeviceGuard {
   int prev_ = 0, dev_ = 0;
 };
 
+// The parameters of one scattering kernel (an HSS / HMS component's, or a
+// composite kernel's element, whose kind may not be composite itself).
+int validate_kernel(const mcv_component& c, int ker, int64_t k,
+                    bool composite_ok, mcv_status* st) {
+  if (ker == MCV_KERNEL_POWDER &&
+      (!c.table || !c.ftable || c.ip[4] < 1 || c.dp[10] <= 0)) {
+    set_msg(st, MCV_EINVAL, "component %s%lld: powder kernel needs peaks", "",
+            (long long)k);
+    return MCV_EINVAL;
+  }
+  if (ker == MCV_KERNEL_SQE_GRID &&
+      (!c.ftable || c.ip[4] < 2 || c.ip[5] < 2)) {
+    set_msg(st, MCV_EINVAL,
+            "component %s%lld: S(Q,E) kernel needs a >= 2x2 table", "",
+            (long long)k);
+    return MCV_EINVAL;
+  }
+  if (ker == MCV_KERNEL_E_Q &&
+      (!c.table || !c.ftable || c.ip[4] < 1 || c.ip[4] > MCV_EXPR_MAX_OPS ||
+       c.ip[5] < 1 || c.ip[5] > MCV_EXPR_MAX_OPS || !(c.dp[12] >= 1) ||
+       !(c.dp[12] <= 1e6))) {
+    set_msg(st, MCV_EINVAL,
+            "component %s%lld: E(Q) kernel needs E(Q) and S(Q) programs of "
+            "1..256 instructions and 1 <= max_iter <= 1e6",
+            "", (long long)k);
+    return MCV_EINVAL;
+  }
+  if (ker == MCV_KERNEL_SANS2D &&
+      (!c.table || !c.ftable || c.ip[4] < 2 || c.ip[5] < 2 ||
+       !(c.dp[11] > c.dp[10]) || !(c.dp[13] > c.dp[12]))) {
+    set_msg(st, MCV_EINVAL,
+            "component %s%lld: SANS2D kernel needs a >= 2x2 S(Qx, Qy) grid "
+            "over increasing Q ranges", "", (long long)k);
+    return MCV_EINVAL;
+  }
+  if (ker == MCV_KERNEL_COMPOSITE &&
+      (!composite_ok || c.ip[4] < 1 || c.ip[4] > MCV_COMPOSITE_MAX)) {
+    set_msg(st, MCV_EINVAL,
+            "component %s%lld: a composite kernel holds 1..16 elements, none "
+            "of them composite", "", (long long)k);
+    return MCV_EINVAL;
+  }
+  if (ker < MCV_KERNEL_ISOTROPIC || ker > MCV_KERNEL_SANS2D) {
+    set_msg(st, MCV_EINVAL, "component %s%lld: unknown scattering kernel", "",
+            (long long)k);
+    return MCV_EINVAL;
+  }
+  return MCV_OK;
+}
+
+// A composite kernel at slot k: its N elements fill the next N slots,
+// each a kernel element of a non-composite kind with a positive weight
+// and running sums that increase to 1.
+int validate_composite(const mcv_chain* ch, int k, mcv_status* st) {
+  const int n = ch->comp[k].ip[4];
+  if (k + n >= ch->ncomp) {
+    set_msg(st, MCV_EINVAL,
+            "component %s%lld: a composite kernel's elements must follow it "
+            "in the chain", "", (long long)k);
+    return MCV_EINVAL;
+  }
+  double run = 0.0;
+  for (int i = 1; i <= n; ++i) {
+    const mcv_component& e = ch->comp[k + i];
+    const double w = e.dp[22], cum = e.dp[23];
+    if (e.opcode != MCV_OP_KERNEL_ELEMENT || !(w > 0) ||
+        !(fabs(cum - (run + w)) <= 1e-9) || !(cum <= 1.0 + 1e-9)) {
+      set_msg(st, MCV_EINVAL,
+              "component %s%lld: composite kernel element with a bad slot, "
+              "weight or running weight", "", (long long)(k + i));
+      return MCV_EINVAL;
+    }
+    run = cum;
+    int rc = validate_kernel(e, e.ip[1], k + i, false, st);
+    if (rc) return rc;
+  }
+  if (!(fabs(run - 1.0) <= 1e-9)) {
+    set_msg(st, MCV_EINVAL,
+            "component %s%lld: composite kernel weights must sum to 1", "",
+            (long long)k);
+    return MCV_EINVAL;
+  }
+  return MCV_OK;
+}
+
 int validate_component(const mcv_component& c, int k, mcv_status* st) {
   if (c.opcode < 0 || c.opcode >= MCV_OP_COUNT) {
     set_msg(st, MCV_EINVAL, "component %s%lld: unknown opcode", "",
@@ -136,13 +221,13 @@ int validate_component(const mcv_component& c, int k, mcv_status* st) {
       break;
     case MCV_OP_HSS:
     case MCV_OP_HMS: {
-      int op = c.ip[0], ker = c.ip[1];
+      int op = c.ip[0], ker = c.ip[1], rc;
       if (c.opcode == MCV_OP_HMS &&
           (c.ip[6] < 1 || c.ip[6] > MCV_MS_MAX_SCATTERED ||
            (c.ip[7] & 0xffff) > 64 || (c.ip[7] >> 16) > 64 || c.ip[7] < 0)) {
         set_msg(st, MCV_ECAPACITY,
                 "component %s%lld: multiple scatterer needs 1 <= "
-                "max_scattered_neutrons <= 16 and loop counts <= 64",
+                "max_scattered_neutrons <= 48 and loop counts <= 64",
                 "", (long long)k);
         return MCV_ECAPACITY;
       }
@@ -155,35 +240,8 @@ int validate_component(const mcv_component& c, int k, mcv_status* st) {
                 (long long)k);
         return MCV_EINVAL;
       }
-      if (ker == MCV_KERNEL_POWDER &&
-          (!c.table || !c.ftable || c.ip[4] < 1 || c.dp[10] <= 0)) {
-        set_msg(st, MCV_EINVAL, "component %s%lld: powder kernel needs peaks",
-                "", (long long)k);
-        return MCV_EINVAL;
-      }
-      if (ker == MCV_KERNEL_SQE_GRID &&
-          (!c.ftable || c.ip[4] < 2 || c.ip[5] < 2)) {
-        set_msg(st, MCV_EINVAL,
-                "component %s%lld: S(Q,E) kernel needs a >= 2x2 table", "",
-                (long long)k);
-        return MCV_EINVAL;
-      }
-      if (ker == MCV_KERNEL_E_Q &&
-          (!c.table || !c.ftable || c.ip[4] < 1 ||
-           c.ip[4] > MCV_EXPR_MAX_OPS || c.ip[5] < 1 ||
-           c.ip[5] > MCV_EXPR_MAX_OPS || !(c.dp[12] >= 1) ||
-           !(c.dp[12] <= 1e6))) {
-        set_msg(st, MCV_EINVAL,
-                "component %s%lld: E(Q) kernel needs E(Q) and S(Q) programs "
-                "of 1..256 instructions and 1 <= max_iter <= 1e6",
-                "", (long long)k);
-        return MCV_EINVAL;
-      }
-      if (ker < MCV_KERNEL_ISOTROPIC || ker > MCV_KERNEL_E_Q) {
-        set_msg(st, MCV_EINVAL, "component %s%lld: unknown scattering kernel",
-                "", (long long)k);
-        return MCV_EINVAL;
-      }
+      rc = validate_kernel(c, ker, k, true, st);
+      if (rc) return rc;
       break;
     }
     default:
@@ -211,7 +269,13 @@ int validate_chain(const mcv_chain* ch, mcv_status* st) {
   for (int k = 0; k < ch->ncomp; ++k) {
     int rc = validate_component(ch->comp[k], k, st);
     if (rc) return rc;
-    nhms += ch->comp[k].opcode == MCV_OP_HMS;
+    const mcv_component& c = ch->comp[k];
+    nhms += c.opcode == MCV_OP_HMS;
+    if ((c.opcode == MCV_OP_HSS || c.opcode == MCV_OP_HMS) &&
+        c.ip[1] == MCV_KERNEL_COMPOSITE) {
+      rc = validate_composite(ch, k, st);
+      if (rc) return rc;
+    }
   }
   if (nhms > 1) {
     set_msg(st, MCV_EINVAL, "a chain holds at most one multiple scatterer%s",
@@ -229,15 +293,18 @@ bool has_hms(const mcv_chain* ch) {
 
 // The rarer components run in their own kernel instantiations (kX): the
 // SNS source, the tapered guide, the multiple scatterer, stored neutrons,
-// and samples with the constant-(Q, E) or E(Q) kernel.
+// and samples with the constant-(Q, E), E(Q), composite or SANS2D kernel.
 bool is_exotic(const mcv_chain* ch) {
   for (int k = 0; k < ch->ncomp; ++k) {
     const int op = ch->comp[k].opcode;
     if (op == MCV_OP_HMS || op == MCV_OP_SNS_SOURCE ||
         op == MCV_OP_GUIDE_TAPERING || op == MCV_OP_NEUTRON_STORAGE)
       return true;
-    if (op == MCV_OP_HSS && (ch->comp[k].ip[1] == MCV_KERNEL_CONSTANT_QE ||
-                             ch->comp[k].ip[1] == MCV_KERNEL_E_Q))
+    if ((op == MCV_OP_HSS || op == MCV_OP_KERNEL_ELEMENT) &&
+        (ch->comp[k].ip[1] == MCV_KERNEL_CONSTANT_QE ||
+         ch->comp[k].ip[1] == MCV_KERNEL_E_Q ||
+         ch->comp[k].ip[1] == MCV_KERNEL_COMPOSITE ||
+         ch->comp[k].ip[1] == MCV_KERNEL_SANS2D))
       return true;
   }
   return false;

@@ -478,7 +478,7 @@ __device__ __forceinline__ void regen_body(const mcv_chain& ch, uint64_t n,
 }
 
 template <typename R, bool kX = false>
-__global__ void __launch_bounds__(kMaxThreads)
+__global__ void __launch_bounds__(kMaxThreads, 4)
     regen_kernel(const __grid_constant__ mcv_chain ch, uint64_t n,
                  uint64_t first, uint64_t seed, int tail_queue,
                  DevStatus* st) {

@@ -157,11 +157,42 @@ __device__ __noinline__ void ms_to_exiting(const mcv_component& c,
   prop_dt(n, t);
 }
 
+// FP32: an incident neutron arrives in the sample's frame up to metres
+// away, and propagating it from there to the shape in float leaves its
+// entry point ~1e-7 m off (a float's spacing at 1 m), beyond the on-border
+// tolerance of locate: the reference's next steps then see it outside (no
+// scattering) or inside.  So it is first moved along its own ray to just
+// outside the shape's bounding sphere; the first entry point, the hits and
+// the time of flight are those of the original ray.
+template <typename R>
+__device__ __forceinline__ R shape_bound(const mcv_component& c, int kind,
+                                         int base) {
+  const R a = prm<R>(c, base), b = prm<R>(c, base + 1),
+          d = prm<R>(c, base + 2);
+  if (kind == MCV_SHAPE_SPHERE) return a;
+  if (kind == MCV_SHAPE_CYLINDER) return m_sqrt(a * a + R(0.25) * b * b);
+  return R(0.5) * m_sqrt(a * a + b * b + d * d);
+}
+
+template <typename R>
+__device__ __forceinline__ void ms_approach(const mcv_component& c,
+                                            Neutron<R>& n) {
+  R rb = shape_bound<R>(c, c.ip[2], 0);
+  if (c.ip[0] != MCV_CSG_PRIMITIVE) {
+    const R rb2 = shape_bound<R>(c, c.ip[3], 4);
+    rb = rb2 > rb ? rb2 : rb;
+  }
+  const R v2 = n.vx * n.vx + n.vy * n.vy + n.vz * n.vz;
+  const R tc = -(n.x * n.vx + n.y * n.vy + n.z * n.vz) / v2;
+  const R tm = tc - R(1.01) * rb / m_sqrt(v2);
+  if (tm > R(0)) prop_dt(n, tm);
+}
+
 // _calc_atten_coeff (homogeneous_multiple_scatterer.py:67-71)
 template <typename R>
 __device__ __forceinline__ R ms_atten_coeff(const Neutron<R>& n,
                                             const mcv_component& c) {
-  return hss_sigma<R>(n, c) + hss_mu<R>(n, c);
+  return hss_sigma<R, true>(n, c) + hss_mu<R>(n, c);
 }
 
 // _propagate_to_next_exiting_surface_with_attenuation (:73-84)
@@ -192,7 +223,7 @@ __device__ __noinline__ int ms_interact_m1(const mcv_component& c,
   if (!(tof > R(0))) return 0;
   const R v = m_sqrt(vx * vx + vy * vy + vz * vz);
   const R distance = tof * v;
-  const R sigma = hss_sigma<R>(n, c);
+  const R sigma = hss_sigma<R, true>(n, c);
   const R mu = hss_mu<R>(n, c);
   const R transmission_prob = m_exp(-(mu + sigma) * distance);
   out[0] = n;
@@ -265,12 +296,14 @@ __device__ __noinline__ int ms_scatter(const mcv_component& c, Rng& rng,
   Neutron<R> sc[MCV_MS_MAX_SCATTERED];
   Neutron<R>* tbs = buf_a;
   Neutron<R>* tbs2 = buf_b;
-  if (ms_is_exiting(c, n0)) {
+  Neutron<R> n = n0;
+  if constexpr (sizeof(R) == 4) ms_approach(c, n);
+  if (ms_is_exiting(c, n)) {
     out[0] = n0;
     return 1;
   }
   int ntbs = 1, out_index = 0;
-  tbs[0] = n0;
+  tbs[0] = n;
   for (int iloop = 0; iloop < loops; ++iloop) {
     int s2 = 0;
     for (int i = 0; i < ntbs; ++i) {

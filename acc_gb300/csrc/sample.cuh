@@ -928,10 +928,25 @@ __device__ __forceinline__ void e_q_scatter(Neutron<R>& n, Rng& rng,
   n.p *= prob_f / R(itr + 1);
 }
 
-template <typename R>
+// The scattering coefficient: the kernel's constant sigma, the powder's
+// speed-dependent one, or a composite's: the sum over its elements (the
+// element slots follow the component, header: COMPOSITE), scaled by dp[10]
+// (1/N when averaged, composite.py:95-99), when an element's depends on the
+// speed; else dp[9] holds that sum.
+template <typename R, bool kX = false>
 __device__ __forceinline__ R hss_sigma(const Neutron<R>& n,
                                        const mcv_component& c) {
   if (c.ip[1] == MCV_KERNEL_POWDER) return powder_coeff<R>(n, c);
+  if constexpr (kX) {
+    if (c.ip[1] == MCV_KERNEL_COMPOSITE && (c.ip[5] & 1)) {
+      const mcv_component* e = &c + 1;
+      R s = R(0);
+      for (int i = 0; i < c.ip[4]; ++i)
+        s += e[i].ip[1] == MCV_KERNEL_POWDER ? powder_coeff<R>(n, e[i])
+                                             : prm<R>(e[i], 9);
+      return s * prm<R>(c, 10);
+    }
+  }
   return prm<R>(c, 9);
 }
 
@@ -943,11 +958,47 @@ __device__ __forceinline__ R hss_mu(const Neutron<R>& n,
   return prm<R>(c, 8) / v * 2200;
 }
 
-// kX: the constant-(Q, E) and E(Q) kernels are compiled into the
-// instantiations for the rarer components only.
+// SANS2D_ongrid's S (acc/kernels/SANS2D_ongrid.py:16-56): (Qx, Qy) drawn
+// uniformly over the grid's box; vx -= Qx K2V, vy -= Qy K2V and vz from
+// vi^2 - vx^2 vy^2 (the reference's expression: a product where
+// |v| = vi would need a sum; kept); p *= S bilinear on cells of width
+// (Qmax - Qmin) / n, indices clamped to [0, n-2].
+template <typename R, typename Rng>
+__device__ __forceinline__ void sans2d_scatter(Neutron<R>& n, Rng& rng,
+                                               const mcv_component& c) {
+  const R Qxmin = prm<R>(c, 10), Qxmax = prm<R>(c, 11),
+          Qymin = prm<R>(c, 12), Qymax = prm<R>(c, 13);
+  const int nx = c.ip[4], ny = c.ip[5];
+  const R vi = m_sqrt(n.vx * n.vx + n.vy * n.vy + n.vz * n.vz);
+  R Qx = rng.next() * (Qxmax - Qxmin);
+  Qx += Qxmin;
+  R Qy = rng.next() * (Qymax - Qymin);
+  Qy += Qymin;
+  n.vx -= Qx * R(kK2V);
+  n.vy -= Qy * R(kK2V);
+  n.vz = m_sqrt(vi * vi - n.vx * n.vx * n.vy * n.vy);
+  const R dQx = (Qxmax - Qxmin) / nx, dQy = (Qymax - Qymin) / ny;
+  int xi = (int)((Qx - Qxmin) / dQx), yi = (int)((Qy - Qymin) / dQy);
+  xi = xi < 0 ? 0 : (xi > nx - 2 ? nx - 2 : xi);
+  yi = yi < 0 ? 0 : (yi > ny - 2 ? ny - 2 : yi);
+  const R xf = (Qx - Qxmin) / dQx - xi, yf = (Qy - Qymin) / dQy - yi;
+  const R* S = sizeof(R) == 4 ? (const R*)c.ftable : (const R*)c.table;
+  const R f00 = __ldg(&S[xi * ny + yi]), f10 = __ldg(&S[(xi + 1) * ny + yi]);
+  const R f01 = __ldg(&S[xi * ny + yi + 1]),
+          f11 = __ldg(&S[(xi + 1) * ny + yi + 1]);
+  // bilinear_interp (SANS2D_ongrid.py:16-22)
+  const R a00 = f00, a10 = f10 - f00, a01 = f01 - f00,
+          a11 = f11 - f10 - f01 + f00;
+  n.p *= a00 + a10 * xf + a01 * yf + a11 * xf * yf;
+}
+
+// One kernel's scatter (p *= sigma, then its S).  kX: the constant-(Q, E)
+// and E(Q) kernels are compiled into the instantiations for the rarer
+// components only.
 template <typename R, bool kX = false, typename Rng, typename Trk>
-__device__ __forceinline__ void hss_kernel(Neutron<R>& n, Rng& rng,
-                                           const mcv_component& c, Trk& trk) {
+__device__ __forceinline__ void hss_kernel_leaf(Neutron<R>& n, Rng& rng,
+                                                const mcv_component& c,
+                                                Trk& trk) {
   switch (c.ip[1]) {
     case MCV_KERNEL_ISOTROPIC:
       n.p *= prm<R>(c, 9);  // kernels/__init__.py:42
@@ -974,9 +1025,43 @@ __device__ __forceinline__ void hss_kernel(Neutron<R>& n, Rng& rng,
         e_q_scatter<R>(n, rng, c);
       }
       break;
+    case MCV_KERNEL_SANS2D:
+      if constexpr (kX) {
+        n.p *= prm<R>(c, 9);  // kernels/__init__.py:119
+        sans2d_scatter<R>(n, rng, c);
+      }
+      break;
     default:
       break;
   }
+}
+
+// The composite kernel's scatter (composite.py:62-75, 101-104): one uniform
+// picks element i, the first whose running weight exceeds it (the last one
+// otherwise); the element scatters, and p /= its weight.
+template <typename R, typename Rng, typename Trk>
+__device__ __noinline__ void composite_scatter(Neutron<R>& n, Rng& rng,
+                                               const mcv_component& c,
+                                               Trk& trk) {
+  const R r = rng.next();
+  const mcv_component* e = &c + 1;
+  const int last = c.ip[4] - 1;
+  int i = 0;
+  while (i < last && !(r < prm<R>(e[i], 23))) ++i;
+  hss_kernel_leaf<R, true>(n, rng, e[i], trk);
+  n.p /= prm<R>(e[i], 22);
+}
+
+template <typename R, bool kX = false, typename Rng, typename Trk>
+__device__ __forceinline__ void hss_kernel(Neutron<R>& n, Rng& rng,
+                                           const mcv_component& c, Trk& trk) {
+  if constexpr (kX) {
+    if (c.ip[1] == MCV_KERNEL_COMPOSITE) {
+      composite_scatter<R>(n, rng, c, trk);
+      return;
+    }
+  }
+  hss_kernel_leaf<R, kX>(n, rng, c, trk);
 }
 
 // The weight factor exp(-(mu(v) + sigma(v)) L) seen by the tracker:
@@ -1017,7 +1102,7 @@ __device__ __forceinline__ void hss(Neutron<double>& n, Rng& rng,
   double v = sqrt(vx * vx + vy * vy + vz * vz);
   double dist = v * tin;
   double fulllen = v * T;
-  double sigma = hss_sigma<double>(n, c);
+  double sigma = hss_sigma<double, kX>(n, c);
   double mu = hss_mu<double>(n, c);
   double atten = exp(-(mu + sigma) * dist);
   n.p *= fulllen * atten;
@@ -1027,7 +1112,7 @@ __device__ __forceinline__ void hss(Neutron<double>& n, Rng& rng,
   h = intersect_shape<double>(c, n.x, n.y, n.z, n.vx, n.vy, n.vz);
   double dt3 = total_time_in_shape<double>(h);
   prop_dt(n, dt3);
-  sigma = hss_sigma<double>(n, c);
+  sigma = hss_sigma<double, kX>(n, c);
   mu = hss_mu<double>(n, c);
   // the reference uses the incident speed v here (line 98)
   double atten2 = exp(-(mu + sigma) * v * dt3);
@@ -1096,7 +1181,7 @@ __device__ __forceinline__ void hss(Neutron<float>& n, Rng& rng,
   n.t.add(tau_s);
   float v = sqrtf(v2);
   float dist = v * tin, fulllen = v * T;
-  float sigma = hss_sigma<float>(n, c);
+  float sigma = hss_sigma<float, kX>(n, c);
   float mu = hss_mu<float>(n, c);
   n.p *= fulllen * __expf(-(mu + sigma) * dist);
   track_atten<float>(n, c, dist, trk);
@@ -1105,7 +1190,7 @@ __device__ __forceinline__ void hss(Neutron<float>& n, Rng& rng,
   h = intersect_shape<float>(c, n.x, n.y, n.z, n.vx, n.vy, n.vz);
   float dt3 = total_time_in_shape<float>(h);
   prop_dt(n, dt3);
-  sigma = hss_sigma<float>(n, c);
+  sigma = hss_sigma<float, kX>(n, c);
   mu = hss_mu<float>(n, c);
   n.p *= __expf(-(mu + sigma) * v * dt3);
   track_atten<float>(n, c, v * dt3, trk);

@@ -16,11 +16,16 @@ from .instrument import calcTransformations
 
 def build_chain(components, offsets=None, rotmats=None, binder=None):
     """An mcv_chain for `components`, with the frame transforms between
-    consecutive components (identity when offsets/rotmats are None)."""
-    if not 1 <= len(components) <= nat.MCV_MAX_COMPONENTS:
+    consecutive components (identity when offsets/rotmats are None).  A
+    component with extra slots (a sample with a composite kernel) is
+    followed by them; they take the identity transform, and the next
+    component the transform from the component they follow."""
+    extra = [int(getattr(c, "extra_slots", lambda: 0)()) for c in components]
+    nslots = len(components) + sum(extra)
+    if not components or not 1 <= nslots <= nat.MCV_MAX_COMPONENTS:
         raise ValueError(
-            f"a chain holds 1..{nat.MCV_MAX_COMPONENTS} components, "
-            f"got {len(components)}")
+            f"a chain holds 1..{nat.MCV_MAX_COMPONENTS} components "
+            f"(composite kernel elements included), got {nslots}")
     if binder is None:
         from .memory import DeviceBinder
         binder = DeviceBinder()
@@ -30,26 +35,36 @@ def build_chain(components, offsets=None, rotmats=None, binder=None):
     # that a chain built from a temporary instrument stays valid
     ch._binder = binder
     ch._components = list(components)
-    ch.ncomp = len(components)
+    ch.ncomp = nslots
     eye = np.eye(3)
-    for i, comp in enumerate(components):
-        c = ch.comp[i]
-        comp.pack(c, binder)
-        if i == 0:
-            continue
-        if offsets is None:
-            off, rot = np.zeros(3), eye
-        else:
-            off = np.asarray(offsets[i - 1], dtype=float)
-            rot = np.asarray(rotmats[i - 1], dtype=float)
+
+    def transform(slot, off, rot):
         for k in range(9):
-            ch.rot[i][k] = float(rot.flat[k])
-            ch.frot[i][k] = float(rot.flat[k])
+            ch.rot[slot][k] = float(rot.flat[k])
+            ch.frot[slot][k] = float(rot.flat[k])
         for k in range(3):
-            ch.off[i][k] = float(off[k])
-            ch.foff[i][k] = float(off[k])
+            ch.off[slot][k] = float(off[k])
+            ch.foff[slot][k] = float(off[k])
         if np.array_equal(rot, eye):
-            c.flags |= nat.FLAG_IDENTITY_ROT
+            ch.comp[slot].flags |= nat.FLAG_IDENTITY_ROT
+
+    slot = 0
+    for i, comp in enumerate(components):
+        c = ch.comp[slot]
+        comp.pack(c, binder)
+        if slot > 0:
+            if offsets is None:
+                off, rot = np.zeros(3), eye
+            else:
+                off = np.asarray(offsets[i - 1], dtype=float)
+                rot = np.asarray(rotmats[i - 1], dtype=float)
+            transform(slot, off, rot)
+        if extra[i]:
+            slots = [ch.comp[slot + 1 + j] for j in range(extra[i])]
+            comp.pack_extra(c, slots, binder)
+            for j in range(extra[i]):
+                transform(slot + 1 + j, np.zeros(3), eye)
+        slot += 1 + extra[i]
     ch.weight_exp2 = weight_exp2(components)
     return ch
 

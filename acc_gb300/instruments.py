@@ -10,6 +10,11 @@ constant_qe_box    70 meV beam -> Al block with the constant-(Q, E) kernel ->
                    I(Q, E) monitor
 e_q_box            70 meV beam -> Al block with an analytic E(Q) dispersion
                    -> I(Q, E) monitor
+un_ms              500 meV beam -> UN cylinder, multiple scattering with a
+                   composite of 8 E(Q) kernels -> I(Q, E) monitor
+verdi              the VERDI instrument (SNS source, elliptic guides)
+sans2d_grid        10 A beam -> thin Al plate with S(Qx, Qy) on a 1475 x
+                   1100 grid -> PSD 10 m downstream
 
 Numbers that the workload descriptions leave open are fixed here once
 (source distance, gaps between components, detector heights, number
@@ -33,7 +38,8 @@ from .components.samples.homogeneous_single_scatterer import factory
 from .components.sources.source_simple import Source_simple
 from .geometry import Block, Cylinder, Difference, HollowCylinder, Sphere
 from .instrument import instrument
-from .kernels import (ConstantQEKernel, E_Q_Kernel, IsotropicKernel, Peak,
+from .kernels import (CompositeKernel, ConstantQEKernel, E_Q_Kernel,
+                      IsotropicKernel, Peak, SANS2D_ongrid_Kernel,
                       SimplePowderDiffractionKernel, SQEGridKernel,
                       coefficient_from_cross_section)
 
@@ -630,4 +636,112 @@ def verdi(moderator_file=None, guide_mvalue=6., sample_width=0.005,
                               filename="sample_divYpos.h5"),
                position=(0, 0, 4e-5), orientation=(0, 0, 90),
                relativeTo=pack)
+    return ins
+
+
+# ------------------------------------------------------------------- UN
+def un_kernel(n_levels=8, Qmax=35.0, mu=32.395, sigma=69.847, dE=50.0,
+              a=0.00276):
+    """The UN sample's kernel (tests/kernels/UN/UN-scatterer.xml): an
+    averaged composite of E(Q) kernels, level n at E = n dE (meV) with
+    S(Q) = (a Q^2)^n / n! exp(-a Q^2) (S = 1 for n = 0: the elastic line),
+    Q 0-35 /A, absorption 32.395 /m and scattering 69.847 /m each."""
+    elements = []
+    for k in range(n_levels):
+        if k == 0:
+            S_Q = "1"
+        elif k == 1:
+            S_Q = f"Q*Q*{a} * exp(-{a} * Q*Q)"
+        else:
+            S_Q = f"1./{math.factorial(k)} * ({a}*Q*Q)^{k} * exp(-{a} * Q*Q)"
+        elements.append(E_Q_Kernel(f"{k * dE:g}", S_Q, 0.0, Qmax, mu, sigma))
+    return CompositeKernel(elements, average=True)
+
+
+def un_ms(Ei=500.0, max_scattered_neutrons=33, max_ms_loops=1,
+          max_ms_loops_path1=5, kernel=None, multiple_scattering=True):
+    """The UN multiple-scattering benchmark
+    (tests/components/samples/UN_test_instrument.py, UN_HMS.py,
+    test_ms_UN.py): a 1 x 1 cm source aimed at 8 x 8 mm 1 m away, Ei = 500
+    meV +- 1%; the UN cylinder (radius 5.6419 mm, height 1 cm, axis
+    vertical) 1.1 m downstream, scattering through un_kernel() with up to
+    33 outputs per neutron (1 loop among re-entries, 5 on the first
+    passage); an I(Q, E) monitor at the sample, Q 0-30 /A x 150, E -100 to
+    400 meV x 100, 10-135 deg in plane, +-26 deg out of it.  `kernel`
+    replaces the sample's kernel; multiple_scattering=False scatters once
+    (the reference's UN_HSS.py)."""
+    from .components.samples.homogeneous_multiple_scatterer import \
+        factory as ms_factory
+    ins = instrument("un_ms")
+    src = Source_simple("src", radius=0.0, width=0.01, height=0.01, dist=1.0,
+                        xw=0.008, yh=0.008, E0=Ei, dE=0.01 * Ei, Lambda0=0.0,
+                        dLambda=0.0)
+    kernel = un_kernel() if kernel is None else kernel
+    if multiple_scattering:
+        HMS = ms_factory(Cylinder(0.0056419, 0.01), kernel,
+                         max_scattered_neutrons=max_scattered_neutrons,
+                         max_ms_loops=max_ms_loops,
+                         max_ms_loops_path1=max_ms_loops_path1)
+    else:  # the single-scattering variant (UN_HSS.py)
+        HMS = factory(Cylinder(0.0056419, 0.01), kernel)
+    mon = IQE_monitor("iqe_monitor", Ei=Ei, Qmin=0.0, Qmax=30.0, nQ=150,
+                      Emin=-100.0, Emax=400.0, nE=100,
+                      min_angle_in_plane=10.0, max_angle_in_plane=135.0,
+                      min_angle_out_of_plane=-26.0,
+                      max_angle_out_of_plane=26.0)
+    sample = HMS("sample")
+    ins.append(src, position=(0, 0, 0))
+    # the cylinder's axis is local z; orientation (90, 0, 0) turns it vertical
+    ins.append(sample, position=(0, 0, 1.1), orientation=(90, 0, 0))
+    ins.append(mon, position=(0, 0, 0), relativeTo=sample)
+    return ins
+
+
+def composite_box():
+    """The Al box of the reference's box tests (_al_box) with a composite
+    kernel of three kinds, weights 2 : 1 : 1: the E(Q) dispersion of
+    e_q_box, the constant (Q, E) = (2 /A, 15 meV) transfer and isotropic
+    elastic scattering, each with Al's coefficients."""
+    return _al_box("composite_box", CompositeKernel(
+        [E_Q_Kernel("30+20*sin(Q)", "1", 0.0, 10.0, AL_MU, AL_SIGMA),
+         ConstantQEKernel(2.0, 15.0, AL_MU, AL_SIGMA),
+         IsotropicKernel(AL_MU, AL_SIGMA)], weights=[2, 1, 1]))
+
+
+# ----------------------------------------------------------------- SANS
+def sans2d_image(nx=1475, ny=1100, Qx_max=0.0047176, Qy_max=0.0035176):
+    """The synthetic S(Qx, Qy) of the reference's SANS test data
+    (tests/components/samples/make_sans2d_data.py:5-31):
+    sin(3000 Q)^2 exp(-300 Q) at cell centres over +-Qx_max x +-Qy_max,
+    as an image indexed (y, x)."""
+    dQx, dQy = 2 * Qx_max / nx, 2 * Qy_max / ny
+    Qx = -Qx_max + dQx * (np.arange(nx) + 0.5)
+    Qy = -Qy_max + dQy * (np.arange(ny) + 0.5)
+    X, Y = np.meshgrid(Qx, Qy)
+    Q = np.sqrt(X * X + Y * Y)
+    return np.sin(Q * 3000) ** 2 * np.exp(-Q * 300)
+
+
+def sans2d_grid(image=None):
+    """The reference's SANS test instrument
+    (tests/components/samples/sans2d_grid_instrument.py:9-37,
+    sampleassemblies/sans2d): a 0.3 x 0.3 mm source aimed at a 0.3 x 0.3 mm
+    window 9.9 m away, 10 +- 0.65 A; a 3 x 3 cm Al plate 0.2 mm thick at
+    10 m, scattering through S(Qx, Qy) on a 1475 x 1100 grid over
+    +-0.0047 x +-0.0035 /A; a PSD 250 x 250 over +-7.5 cm 10 m further."""
+    if image is None:
+        image = sans2d_image()
+    ins = instrument("sans2d_grid")
+    src = Source_simple("source", radius=0.0, height=0.0003, width=0.0003,
+                        dist=9.9, xw=0.0003, yh=0.0003, E0=0.0, dE=0.0,
+                        Lambda0=10.0, dLambda=0.65)
+    ker = SANS2D_ongrid_Kernel(image, -0.0047176, 0.0047176, -0.0035176,
+                               0.0035176, AL_MU, AL_SIGMA)
+    HSS = factory(Block(0.03, 0.03, 0.0002), ker)
+    mon = PSD_monitor("Ixy", nx=250, ny=250, xmin=-0.075, xmax=0.075,
+                      ymin=-0.075, ymax=0.075, filename="Ixy.h5")
+    sample = HSS("sample")
+    ins.append(src, position=(0, 0, 0))
+    ins.append(sample, position=(0, 0, 10.0))
+    ins.append(mon, position=(0, 0, 10.0), relativeTo=sample)
     return ins

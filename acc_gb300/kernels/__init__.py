@@ -1,7 +1,9 @@
 """Scattering kernels of homogeneous scatterers (acc/kernels)."""
 
-from .kernels import (ConstantQEKernel, E_Q_Kernel,  # noqa: F401
+from .kernels import (CompositeKernel, ConstantQEKernel,  # noqa: F401
+                      E_Q_Kernel,
                       IsotropicKernel, Peak, PowderDiffraction,
-                      SimplePowderDiffractionKernel, SQEGridKernel,
+                      SANS2D_ongrid_Kernel, SimplePowderDiffractionKernel,
+                      SQEGridKernel,
                       coefficient_from_cross_section)
 from .expression import compile_expression  # noqa: F401

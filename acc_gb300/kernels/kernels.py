@@ -190,3 +190,95 @@ class E_Q_Kernel:
         c.table = binder.table(comp, "expr", flat, np.float64)
         c.ftable = binder.table(comp, "expr_f32", flat, np.float32)
         c.table_len = flat.size
+
+
+class CompositeKernel:
+    """The composite kernel of acc/kernels/composite.py:7-127 (rendered by
+    acc/kernels/__init__.py:24-34): `elements` (1..16 kernels, none of them
+    composite) with weights (each element's `weight`, 1 when it has none),
+    normalised to sum 1.  A scattering picks element i with probability
+    w_i, lets it scatter and divides p by w_i.  The scattering coefficient
+    is the sum of the elements' (divided by N when `average`), the
+    absorption coefficient their mean.  Its elements take the chain slots
+    after the sample (include/acc_gb300.h, COMPOSITE)."""
+    kind = nat.KERNEL_COMPOSITE
+
+    def __init__(self, elements, weights=None, average=False):
+        elements = list(elements)
+        if not 1 <= len(elements) <= nat.MCV_COMPOSITE_MAX:
+            raise ValueError(f"a composite kernel holds 1.."
+                             f"{nat.MCV_COMPOSITE_MAX} elements")
+        if any(isinstance(e, CompositeKernel) for e in elements):
+            raise ValueError("composite kernels do not nest")
+        if weights is None:
+            weights = [float(getattr(e, "weight", 1.0)) for e in elements]
+        weights = np.asarray(weights, dtype=np.float64)
+        if weights.shape != (len(elements),) or not np.all(weights > 0):
+            raise ValueError("one positive weight per element")
+        self.elements = elements
+        self.weights = weights / weights.sum()
+        self.average = bool(average)
+        self.n_slots = len(elements)
+
+    def pack(self, comp, c, binder, set_param):
+        c.ip[4] = len(self.elements)
+        # mu, sigma and the speed-dependence flag follow in pack_elements,
+        # once the elements' own slots are packed
+
+    def pack_elements(self, c, slots, binder, set_param):
+        n = len(self.elements)
+        scale = 1.0 / n if self.average else 1.0
+        cum, mu, sigma, speed = 0.0, 0.0, 0.0, False
+        for i, (e, w, cs) in enumerate(zip(self.elements, self.weights,
+                                           slots)):
+            cs.opcode = nat.OP_KERNEL_ELEMENT
+            cs.ip[1] = e.kind
+            # the element is the owner of its tables (one set per element)
+            e.pack(e, cs, binder, set_param)
+            cum = 1.0 if i == n - 1 else cum + float(w)
+            set_param(cs, 22, float(w))
+            set_param(cs, 23, cum)
+            mu += cs.dp[8]
+            if e.kind == nat.KERNEL_POWDER:
+                speed = True
+            else:
+                sigma += cs.dp[9]
+        set_param(c, 8, mu / n)
+        set_param(c, 9, sigma * scale)
+        set_param(c, 10, scale)
+        c.ip[5] = 1 if speed else 0
+
+
+class SANS2D_ongrid_Kernel:
+    """acc/kernels/SANS2D_ongrid.py:16-78 with p *= sigma
+    (acc/kernels/__init__.py:107-122): small-angle scattering from
+    S(Qx, Qy) on a grid.  `S_QxQy` is the reference's image, indexed
+    (y, x) (a .npy path or an array); the kernel stores its transpose.
+    (Qx, Qy) is drawn uniformly over the box and S interpolated bilinearly
+    on cells of width (Qmax - Qmin) / n."""
+    kind = nat.KERNEL_SANS2D
+
+    def __init__(self, S_QxQy, Qx_min, Qx_max, Qy_min, Qy_max,
+                 absorption_coefficient, scattering_coefficient):
+        if isinstance(S_QxQy, str):
+            S_QxQy = np.load(S_QxQy)
+        img = np.asarray(S_QxQy, dtype=np.float64)
+        if img.ndim != 2 or min(img.shape) < 2:
+            raise ValueError("S_QxQy must be a (ny >= 2, nx >= 2) image")
+        self.S_QxQy = img
+        self.S = np.ascontiguousarray(img.T)  # [nx][ny]
+        self.Qx_min, self.Qx_max = float(Qx_min), float(Qx_max)
+        self.Qy_min, self.Qy_max = float(Qy_min), float(Qy_max)
+        self.absorption_coefficient = float(absorption_coefficient)
+        self.scattering_coefficient = float(scattering_coefficient)
+
+    def pack(self, comp, c, binder, set_param):
+        set_param(c, 8, self.absorption_coefficient)
+        set_param(c, 9, self.scattering_coefficient)
+        for k, v in enumerate((self.Qx_min, self.Qx_max, self.Qy_min,
+                               self.Qy_max)):
+            set_param(c, 10 + k, v)
+        c.ip[4], c.ip[5] = self.S.shape
+        c.table = binder.table(comp, "sans2d", self.S, np.float64)
+        c.ftable = binder.table(comp, "sans2d_f32", self.S, np.float32)
+        c.table_len = self.S.size

@@ -67,6 +67,18 @@ WORKLOADS = {
     "e_q_box": (
         "e_q_box: 1x1 cm source 70 meV -> Al block 6x10x1 cm, E(Q) kernel "
         "E = 30 + 20 sin(Q), S = 1, Q 0-10 /A -> I(Q,E) monitor 160x120"),
+    "un_ms": (
+        "un_ms: 1x1 cm source 500 meV -> UN cylinder r=5.64 mm h=1 cm, "
+        "multiple scattering (<= 33 outputs per neutron) through a "
+        "composite of 8 E(Q) kernels -> I(Q,E) monitor 150x100"),
+    "composite_box": (
+        "composite_box: 70 meV -> Al block 6x10x1 cm, composite kernel "
+        "(E(Q), constant (Q, E), isotropic; weights 2:1:1) -> I(Q,E) "
+        "160x120"),
+    "sans2d_grid": (
+        "sans2d_grid: 0.3x0.3 mm source, 10 +- 0.65 A -> Al plate 3x3 cm "
+        "x 0.2 mm with S(Qx,Qy) on a 1475x1100 grid -> PSD 250x250 at "
+        "10 m"),
     "verdi": (
         "verdi: the VERDI instrument (26 components): SNS moderator "
         "(synthetic file, 141 E x 160 t, 0.1-1000 meV) -> 2 elliptic "

@@ -37,8 +37,10 @@ extern "C" {
 #define MCV_NIPARAM 8
 #define MCV_MAX_INTERSECTIONS 10  /* acc/geometry/arrow_intersect.py:16 */
 #define MCV_MAX_BOUNCES 100000    /* acc/components/optics/guide.py:17 */
-#define MCV_MS_MAX_SCATTERED 16   /* output neutrons per HMS event (the
-                                     reference default is 10) */
+#define MCV_MS_MAX_SCATTERED 48   /* output neutrons per HMS event (the
+                                     reference default is 10, its UN
+                                     sample uses 33) */
+#define MCV_COMPOSITE_MAX 16      /* elements of a composite kernel */
 #define MCV_EXPR_STACK 8          /* evaluation stack of an E(Q) / S(Q)
                                      program (E_Q kernel)              */
 #define MCV_EXPR_MAX_OPS 256      /* instructions per E(Q) / S(Q) program */
@@ -81,7 +83,9 @@ enum {
   MCV_OP_GUIDE_TAPERING = 16,   /* acc/components/optics/guide_tapering.py  */
   MCV_OP_SNS_SOURCE = 17,       /* acc/components/sources/SNS_source.py     */
   MCV_OP_NEUTRON_STORAGE = 18,  /* acc/components/sources/neutronfromstorage.py */
-  MCV_OP_COUNT = 19
+  MCV_OP_KERNEL_ELEMENT = 19,   /* an element of a composite kernel
+                                   (acc/kernels/composite.py): not run */
+  MCV_OP_COUNT = 20
 };
 
 /* ---- shapes of the homogeneous scatterer (acc/geometry/arrow_intersect.py)
@@ -105,7 +109,9 @@ enum {
   MCV_KERNEL_POWDER = 2,      /* acc/kernels/powderdiffr.py                        */
   MCV_KERNEL_SQE_GRID = 3,    /* no reference counterpart (gridded S(Q,E) table)   */
   MCV_KERNEL_CONSTANT_QE = 4, /* acc/kernels/constant_qe.py:15-67, __init__.py:76-88 */
-  MCV_KERNEL_E_Q = 5          /* acc/kernels/E_Q.py:16-117, __init__.py:90-105     */
+  MCV_KERNEL_E_Q = 5,         /* acc/kernels/E_Q.py:16-117, __init__.py:90-105     */
+  MCV_KERNEL_COMPOSITE = 6,   /* acc/kernels/composite.py:7-127, __init__.py:24-34 */
+  MCV_KERNEL_SANS2D = 7       /* acc/kernels/SANS2D_ongrid.py:16-78, __init__.py:107-122 */
 };
 
 /* Instructions of the postfix programs that carry the E_Q kernel's E(Q)
@@ -154,6 +160,22 @@ enum {
  *               (each 1..MCV_EXPR_MAX_OPS); table (float64) and ftable
  *               (float32): the E(Q) program then the S(Q) program,
  *               {opcode, argument} per instruction (MCV_EXPR_*)
+ *       SANS2D: 10 Qx_min 11 Qx_max 12 Qy_min 13 Qy_max (1/A)
+ *               ip[4] = nx, ip[5] = ny (each >= 2); table (float64) and
+ *               ftable (float32): S[nx][ny], x-major (the transpose of
+ *               the reference's (y, x) image)
+ *       COMPOSITE: ip[4] = N elements (1..MCV_COMPOSITE_MAX), in the N
+ *               chain slots right after this component, each an
+ *               MCV_OP_KERNEL_ELEMENT whose ip[1] is its kernel kind (not
+ *               COMPOSITE), slots 8.. that kind's parameters as above and
+ *               dp[22] its weight w (the weights sum to 1), dp[23] the
+ *               running sum of the weights up to and including it.
+ *               ip[5] bit 0: an element's scattering coefficient depends
+ *               on the speed (powder), so sigma is summed per neutron;
+ *               else dp[9] holds it.  dp[8] = mean of the elements' mu,
+ *               dp[9] = sum of their sigma, / N when averaged.  One
+ *               uniform picks element i (the first whose running sum
+ *               exceeds it), which scatters, then p /= w.
  * PSD_MONITOR (psd_monitor.py:66-83)          ip: nx ny;  dp: xmin xmax ymin ymax
  * PSD_MONITOR_4PI (psd_monitor_4pi.py:56-79)  ip: nphi ntheta; dp: radius
  * WAVELENGTH_MONITOR (wavelength_monitor.py:52-74)

@@ -1449,9 +1449,49 @@ static void e_q_S(neutron_t* n, rng_t* rng, const mcv_component* c) {
   n->p *= prob_f / (itr + 1);
 }
 
+/* SANS2D_ongrid's S (acc/kernels/SANS2D_ongrid.py:16-56): (Qx, Qy)
+ * uniform over the grid's box; vx -= Qx K2V, vy -= Qy K2V, vz from
+ * vi^2 - vx^2 vy^2 (the reference's product, kept); p *= S bilinear on
+ * cells of width (Qmax - Qmin) / n, indices clamped to [0, n-2];
+ * S[nx][ny] x-major */
+static void sans2d_S(neutron_t* n, rng_t* rng, const mcv_component* c) {
+  double Qxmin = c->dp[10], Qxmax = c->dp[11], Qymin = c->dp[12],
+         Qymax = c->dp[13];
+  int nx = c->ip[4], ny = c->ip[5];
+  const double* S = (const double*)c->table;
+  double vi = length3(n->vx, n->vy, n->vz);
+  double Qx = rng_uniform(rng) * (Qxmax - Qxmin);
+  Qx += Qxmin;
+  double Qy = rng_uniform(rng) * (Qymax - Qymin);
+  Qy += Qymin;
+  n->vx -= Qx * K2V;
+  n->vy -= Qy * K2V;
+  n->vz = sqrt(vi * vi - n->vx * n->vx * n->vy * n->vy);
+  double dQx = (Qxmax - Qxmin) / nx, dQy = (Qymax - Qymin) / ny;
+  int xi = (int)((Qx - Qxmin) / dQx), yi = (int)((Qy - Qymin) / dQy);
+  if (xi < 0) xi = 0;
+  if (xi > nx - 2) xi = nx - 2;
+  if (yi < 0) yi = 0;
+  if (yi > ny - 2) yi = ny - 2;
+  double xf = (Qx - Qxmin) / dQx - xi, yf = (Qy - Qymin) / dQy - yi;
+  double f00 = S[xi * ny + yi], f10 = S[(xi + 1) * ny + yi];
+  double f01 = S[xi * ny + yi + 1], f11 = S[(xi + 1) * ny + yi + 1];
+  n->p *= bilinear(xf, yf, f00, f01, f10, f11);
+}
+
 /* ---------------------------------------------------------------- HSS */
+/* the scattering coefficient; a composite's sums its elements' (the slots
+ * after the component), scaled by dp[10] (1/N when averaged,
+ * composite.py:95-99) */
 static double hss_sigma(const neutron_t* n, const mcv_component* c) {
   if (c->ip[1] == MCV_KERNEL_POWDER) return powder_coeff(n, c);
+  if (c->ip[1] == MCV_KERNEL_COMPOSITE && (c->ip[5] & 1)) {
+    const mcv_component* e = c + 1;
+    double s = 0.0;
+    for (int i = 0; i < c->ip[4]; ++i)
+      s += e[i].ip[1] == MCV_KERNEL_POWDER ? powder_coeff(n, &e[i]) : e[i].dp[9];
+    return s * c->dp[10];
+  }
   return c->dp[9];
 }
 
@@ -1459,6 +1499,18 @@ static double hss_sigma(const neutron_t* n, const mcv_component* c) {
  * acc/kernels/__init__.py:10-22, 36-44): p *= sigma for the kernels with a
  * constant scattering coefficient, then the kernel's S */
 static void kernel_scatter(neutron_t* n, rng_t* rng, const mcv_component* c) {
+  if (c->ip[1] == MCV_KERNEL_COMPOSITE) {
+    /* composite.py:62-75, 101-104: one uniform picks the first element
+     * whose running weight exceeds it (else the last); the element
+     * scatters; p /= its weight */
+    double r = rng_uniform(rng);
+    const mcv_component* e = c + 1;
+    int i = 0, last = c->ip[4] - 1;
+    while (i < last && !(r < e[i].dp[23])) ++i;
+    kernel_scatter(n, rng, &e[i]);
+    n->p /= e[i].dp[22];
+    return;
+  }
   switch (c->ip[1]) {
     case MCV_KERNEL_ISOTROPIC:
       n->p *= c->dp[9]; /* kernels/__init__.py:42 */
@@ -1478,6 +1530,10 @@ static void kernel_scatter(neutron_t* n, rng_t* rng, const mcv_component* c) {
     case MCV_KERNEL_E_Q:
       n->p *= c->dp[9]; /* kernels/__init__.py:103 */
       e_q_S(n, rng, c);
+      break;
+    case MCV_KERNEL_SANS2D:
+      n->p *= c->dp[9]; /* kernels/__init__.py:119 */
+      sans2d_S(n, rng, c);
       break;
     default:
       break;

@@ -98,7 +98,7 @@ def test_hss_validation(engine_lib):
 
 def test_e_q_kernel_validation(engine_lib):
     """The E(Q) kernel needs both programs (1..MCV_EXPR_MAX_OPS
-    instructions) and 1 <= max_iter <= 1e6; a kernel kind past E_Q is
+    instructions) and 1 <= max_iter <= 1e6; a kernel kind past SANS2D is
     unknown."""
     from acc_gb300.components.samples.homogeneous_single_scatterer import \
         factory
@@ -127,8 +127,41 @@ def test_e_q_kernel_validation(engine_lib):
             c.table = value
         assert run(ch) == nat.MCV_EINVAL and b"E(Q)" in st.message, field
     ch = build_chain([H("s")], binder=HostBinder())
-    ch.comp[0].ip[1] = nat.KERNEL_E_Q + 1
+    ch.comp[0].ip[1] = nat.KERNEL_SANS2D + 1
     assert run(ch) == nat.MCV_EINVAL and b"unknown scattering" in st.message
+
+
+def test_composite_kernel_validation(engine_lib):
+    """A composite kernel's elements fill the slots after it, each a kernel
+    element (not composite) with a positive weight, running weights that
+    reach 1."""
+    from acc_gb300.components.samples.homogeneous_single_scatterer import \
+        factory
+    from acc_gb300.engine import build_chain
+    from acc_gb300.geometry import Block
+    from acc_gb300.kernels import CompositeKernel, IsotropicKernel
+    from acc_gb300.memory import HostBinder
+    kern = CompositeKernel([IsotropicKernel(1, 2), IsotropicKernel(3, 4)])
+    H = factory(Block(0.01, 0.01, 0.01), kern)
+    st = nat.mcv_status()
+
+    def run(ch):
+        return engine_lib.mcv_run_chain(None, ctypes.byref(ch), 1, 0, 1, 32,
+                                        None, None, ctypes.byref(st))
+    ch = build_chain([H("s")], binder=HostBinder())
+    assert run(ch) == nat.MCV_EINVAL and b"context" in st.message  # valid
+    ch = build_chain([H("s")], binder=HostBinder())
+    ch.ncomp = 2  # the second element is cut off
+    assert run(ch) == nat.MCV_EINVAL and b"follow" in st.message
+    ch = build_chain([H("s")], binder=HostBinder())
+    ch.comp[2].dp[23] = 0.9  # running weight short of 1
+    assert run(ch) == nat.MCV_EINVAL and b"running weight" in st.message
+    ch = build_chain([H("s")], binder=HostBinder())
+    ch.comp[1].ip[1] = nat.KERNEL_COMPOSITE  # nested
+    assert run(ch) == nat.MCV_EINVAL and b"composite" in st.message
+    ch = build_chain([H("s")], binder=HostBinder())
+    ch.comp[2].opcode = nat.OP_ARM
+    assert run(ch) == nat.MCV_EINVAL and b"bad slot" in st.message
 
 
 def test_context_create(engine_lib):

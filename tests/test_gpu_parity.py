@@ -26,6 +26,7 @@ import pytest
 import torch
 
 from acc_gb300 import engine, instruments
+from acc_gb300.memory import HostBinder
 from acc_gb300.components.samples.homogeneous_single_scatterer import factory
 from acc_gb300.geometry import Cylinder, Difference, Sphere
 from acc_gb300.kernels import IsotropicKernel
@@ -62,6 +63,8 @@ BUILDERS = {
     "storage_chain": instruments.storage_chain,
     "constant_qe_box": instruments.constant_qe_box,
     "e_q_box": instruments.e_q_box,
+    "composite_box": instruments.composite_box,
+    "sans2d_grid": instruments.sans2d_grid,
     "verdi": instruments.verdi,
 }
 # every scattered neutron of the constant-(Q, E) box lands in one or two
@@ -135,8 +138,9 @@ def test_fp32_same_stream_within_1e4(name):
     _, _, o_out, o_last = oracle_run(BUILDERS[name](), n, seed=seed,
                                      record=True)
     err = rel_err(g_out, o_out).max(axis=1)
-    # the last chain component (leading arms are not in the chain)
-    nlast = len(engine.chain_parts(BUILDERS[name]())[0]) - 1
+    # the last chain slot (leading arms are not in the chain; a composite
+    # kernel's elements are)
+    nlast = engine.chain_for_instrument(BUILDERS[name](), HostBinder()).ncomp - 1
     o_alive = (o_last == nlast) & (o_out[:, 9] > 1e-30)
     g_alive = (g_last == nlast) & (g_out[:, 9] > 1e-30)
     cmp = o_alive | g_alive
@@ -369,3 +373,35 @@ def test_verdi_fp32_chi2():
         limit = 1.1 if dof >= 2000 else 1.1 + 3 * np.sqrt(2.0 / dof)
         assert c2 <= limit, (gc.name, c2, dof, limit)
     assert checked >= 6
+
+
+def test_un_multiple_scattering_fp64_matches_oracle():
+    """The UN benchmark (a composite of 8 E(Q) kernels under the multiple
+    scatterer, up to 33 outputs a neutron): FP64 kernel and oracle on the
+    same stream give identical bin counts and sums within 1e-12."""
+    n, seed = 50_000, 5
+    ins = instruments.un_ms()
+    st = engine.run_instrument(ins, n, seed=seed, floattype="float64")
+    assert st.processed == n
+    ot, _, _, _ = oracle_run(instruments.un_ms(), n, seed=seed)
+    (gc, g), = gpu_tallies(ins).items()
+    (oc, o), = ot.items()
+    np.testing.assert_array_equal(g[0], o[0])
+    np.testing.assert_allclose(g[1], o[1], rtol=1e-12, atol=1e-300)
+    np.testing.assert_allclose(g[2], o[2], rtol=1e-12, atol=1e-300)
+    assert g[0].sum() > 0.2 * n
+
+
+def test_un_multiple_scattering_fp32_chi2():
+    """FP32 UN against the FP64 oracle on independent streams, the bound
+    of test_fp32_independent_stream_chi2."""
+    n = 1_000_000
+    ins = instruments.un_ms()
+    engine.run_instrument(ins, n, seed=101, floattype="float32")
+    ot, _, _, _ = oracle_run(instruments.un_ms(), n, seed=202)
+    (_, g), = gpu_tallies(ins).items()
+    (_, o), = ot.items()
+    c2, dof = chi2_per_dof(g.reshape(3, -1), o.reshape(3, -1))
+    assert dof > 200
+    bound = 1.1 if dof >= 2000 else 1.1 + 3 * np.sqrt(2 / dof)
+    assert c2 <= bound, (c2, dof)

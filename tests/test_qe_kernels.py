@@ -14,6 +14,7 @@ import math
 import numpy as np
 import pytest
 
+from acc_gb300 import _native as nat
 from acc_gb300.components.samples.homogeneous_single_scatterer import factory
 from acc_gb300.conversion import V2K, e2v, v2e
 from acc_gb300.geometry import Block
@@ -170,3 +171,89 @@ def test_malformed_program_gives_nan(oracle_lib):
     assert math.isnan(O.expr_eval(np.array([[2, 0]] * 9 + [[3, 0]] * 8), 1.0))
     assert math.isnan(O.expr_eval(np.array([[2, 0], [99, 0]]), 1.0))
     assert math.isnan(O.expr_eval(np.array([[2, 0], [2, 0]]), 1.0))
+
+
+def test_composite_picks_elements_by_weight(oracle_lib):
+    """composite.py:62-75, 101-104: one uniform picks element i with
+    probability w_i (weights 1 and 3, normalised), the element scatters
+    (p *= its sigma, then its S) and p /= w_i.  Two constant-(Q, E)
+    elements tell which one scattered by the energy transfer."""
+    from acc_gb300.engine import build_chain
+    from acc_gb300.kernels import CompositeKernel
+    k1 = ConstantQEKernel(2.0, 10.0, 0.0, 5.0)
+    k2 = ConstantQEKernel(3.0, 20.0, 0.0, 7.0)
+    H = factory(Block(0.06, 0.10, 0.01), CompositeKernel([k1, k2], [1, 3]))
+    ch = build_chain([H("s")], binder=HostBinder())
+    assert ch.ncomp == 3 and ch.comp[0].ip[4] == 2
+    assert [ch.comp[i].opcode for i in (1, 2)] == [nat.OP_KERNEL_ELEMENT] * 2
+    np.testing.assert_allclose([ch.comp[1].dp[22], ch.comp[2].dp[22]],
+                               [0.25, 0.75])
+    assert ch.comp[2].dp[23] == 1.0
+    assert ch.comp[0].dp[9] == 12.0  # sigma: the sum (not averaged)
+    n0 = np.r_[0, 0, 0, 0, 0, e2v(60.0), 0, 0, 0, 1.0]
+    first = 0
+    N = 2000
+    for seed in range(N):
+        n1 = O.kernel_scatter_one(ch.comp[0], n0, seed=seed + 1, index=seed)
+        q, e = _transfer(n0, n1)
+        if abs(e - 10.0) < 1e-6:
+            first += 1
+            assert abs(q - 2.0) < 1e-6 and n1[9] == pytest.approx(5.0 / 0.25)
+        else:
+            assert abs(e - 20.0) < 1e-6 and abs(q - 3.0) < 1e-6
+            assert n1[9] == pytest.approx(7.0 / 0.75)
+    assert abs(first / N - 0.25) < 4 * np.sqrt(0.25 * 0.75 / N)
+
+
+def test_un_kernel_packs_the_reference_sample(oracle_lib):
+    """tests/kernels/UN/UN-scatterer.xml: 8 E(Q) levels averaged; sigma
+    and mu of the composite are then those of one level."""
+    from acc_gb300 import instruments
+    from acc_gb300.engine import chain_for_instrument
+    ch = chain_for_instrument(instruments.un_ms(), HostBinder())
+    c = ch.comp[1]
+    assert c.opcode == nat.OP_HMS and c.ip[1] == nat.KERNEL_COMPOSITE
+    assert c.ip[4] == 8 and c.ip[6] == 33
+    np.testing.assert_allclose([c.dp[8], c.dp[9], c.dp[10]],
+                               [32.395, 69.847, 0.125])
+    # level 3: E = 150 meV, S = (a Q^2)^3 / 3! exp(-a Q^2)
+    from acc_gb300.kernels.expression import evaluate
+    k3 = instruments.un_kernel().elements[3]
+    a = 0.00276
+    for Q in (1.0, 7.5, 20.0):
+        assert evaluate(k3.E_prog, Q) == 150.0
+        want = (a * Q * Q) ** 3 / 6 * math.exp(-a * Q * Q)
+        np.testing.assert_allclose(evaluate(k3.S_prog, Q), want, rtol=1e-14)
+
+
+def test_sans2d_transfer_and_weight(oracle_lib):
+    """SANS2D_ongrid.S (acc/kernels/SANS2D_ongrid.py:24-56): the drawn
+    (Qx, Qy) comes back from the velocity change as (vi - vf) V2K in x and
+    y; vz = sqrt(vi^2 - vx^2 vy^2) (the reference's expression); p = sigma
+    times S bilinear on cells of width (Qmax - Qmin) / n, indices clamped
+    to [0, n-2]; the image is indexed (y, x)."""
+    from acc_gb300.kernels import SANS2D_ongrid_Kernel
+    rng = np.random.default_rng(3)
+    img = rng.random((7, 9))  # (ny, nx)
+    qx0, qx1, qy0, qy1 = -0.01, 0.02, -0.005, 0.004
+    sigma = 3.0
+    comp = _comp(SANS2D_ongrid_Kernel(img, qx0, qx1, qy0, qy1, 0.0, sigma))
+    v0 = np.array([1.5, -0.7, 400.0])
+    n0 = np.r_[0, 0, 0, v0, 0, 0, 0, 1.0]
+    S = img.T
+    nx, ny = S.shape
+    for seed in range(1, 200):
+        n1 = O.kernel_scatter_one(comp, n0, seed=seed)
+        Qx = (v0[0] - n1[3]) * V2K
+        Qy = (v0[1] - n1[4]) * V2K
+        assert qx0 <= Qx < qx1 and qy0 <= Qy < qy1
+        vi2 = v0 @ v0
+        np.testing.assert_allclose(n1[5], math.sqrt(vi2 - n1[3] ** 2 * n1[4] ** 2),
+                                   rtol=1e-14)
+        dx, dy = (qx1 - qx0) / nx, (qy1 - qy0) / ny
+        xi = min(max(int((Qx - qx0) / dx), 0), nx - 2)
+        yi = min(max(int((Qy - qy0) / dy), 0), ny - 2)
+        fx, fy = (Qx - qx0) / dx - xi, (Qy - qy0) / dy - yi
+        s = (S[xi, yi] * (1 - fx) * (1 - fy) + S[xi + 1, yi] * fx * (1 - fy)
+             + S[xi, yi + 1] * (1 - fx) * fy + S[xi + 1, yi + 1] * fx * fy)
+        np.testing.assert_allclose(n1[9], sigma * s, rtol=1e-9)
