@@ -53,6 +53,7 @@ SHAPE_SPHERE, SHAPE_CYLINDER, SHAPE_BOX = 1, 2, 3
 CSG_PRIMITIVE, CSG_DIFFERENCE, CSG_UNION, CSG_INTERSECTION = 0, 1, 2, 3
 KERNEL_ISOTROPIC, KERNEL_POWDER, KERNEL_SQE_GRID = 1, 2, 3
 KERNEL_CONSTANT_QE, KERNEL_E_Q, KERNEL_COMPOSITE, KERNEL_SANS2D = 4, 5, 6, 7
+KERNEL_DGSSXRES = 8
 
 FLAG_IDENTITY_ROT = 1
 FLAG_AGGREGATE = 2

@@ -107,7 +107,12 @@ int validate_kernel(const mcv_component& c, int ker, int64_t k,
             "of them composite", "", (long long)k);
     return MCV_EINVAL;
   }
-  if (ker < MCV_KERNEL_ISOTROPIC || ker > MCV_KERNEL_SANS2D) {
+  if (ker == MCV_KERNEL_DGSSXRES && !(c.dp[20] >= 0)) {
+    set_msg(st, MCV_EINVAL, "component %s%lld: DGSSXRes kernel needs dtof >= 0",
+            "", (long long)k);
+    return MCV_EINVAL;
+  }
+  if (ker < MCV_KERNEL_ISOTROPIC || ker > MCV_KERNEL_DGSSXRES) {
     set_msg(st, MCV_EINVAL, "component %s%lld: unknown scattering kernel", "",
             (long long)k);
     return MCV_EINVAL;
@@ -293,7 +298,8 @@ bool has_hms(const mcv_chain* ch) {
 
 // The rarer components run in their own kernel instantiations (kX): the
 // SNS source, the tapered guide, the multiple scatterer, stored neutrons,
-// and samples with the constant-(Q, E), E(Q), composite or SANS2D kernel.
+// and samples with the constant-(Q, E), E(Q), composite, SANS2D or
+// DGSSXRes kernel.
 bool is_exotic(const mcv_chain* ch) {
   for (int k = 0; k < ch->ncomp; ++k) {
     const int op = ch->comp[k].opcode;
@@ -304,7 +310,8 @@ bool is_exotic(const mcv_chain* ch) {
         (ch->comp[k].ip[1] == MCV_KERNEL_CONSTANT_QE ||
          ch->comp[k].ip[1] == MCV_KERNEL_E_Q ||
          ch->comp[k].ip[1] == MCV_KERNEL_COMPOSITE ||
-         ch->comp[k].ip[1] == MCV_KERNEL_SANS2D))
+         ch->comp[k].ip[1] == MCV_KERNEL_SANS2D ||
+         ch->comp[k].ip[1] == MCV_KERNEL_DGSSXRES))
       return true;
   }
   return false;

@@ -992,6 +992,69 @@ __device__ __forceinline__ void sans2d_scatter(Neutron<R>& n, Rng& rng,
   n.p *= a00 + a10 * xf + a01 * yf + a11 * xf * yf;
 }
 
+// DGSSXResKernel.scatter (acc/kernels/DGSSXResKernel.py:19-98): towards
+// a target disc of the given radius (choose_direction: uniform in cos(theta)
+// over the cone, a rotation about an axis built with the reference's
+// in-place vec3.cross, whose later components read the ones it already
+// replaced, then about the target direction by phi), arriving at a time of
+// flight uniform in tof_target +- dtof / 2.
+// p *= solid angle / 4 pi * dtof * (2 Ef / tof) * vf / vi.  The flight time
+// tof - t is formed in double in both precisions (times near 1 s apart by
+// milliseconds).
+template <typename R, typename Rng>
+__device__ __forceinline__ void dgssxres_scatter(Neutron<R>& n, Rng& rng,
+                                                 const mcv_component& c) {
+  const R tx = prm<R>(c, 15) - n.x, ty = prm<R>(c, 16) - n.y,
+          tz = prm<R>(c, 17) - n.z;
+  const R rad = prm<R>(c, 18);
+  const R l2 = tx * tx + ty * ty + tz * tz;
+  R cmax = m_sqrt(l2 / (rad * rad + l2));
+  if (rad < R(0)) cmax = -cmax;
+  R solid, theta;
+  if constexpr (sizeof(R) == 4) {
+    // the cone of a small target has cos(theta) within ~1e-5 of 1, where
+    // 1 - r and acos(r) lose most of float's digits: form 1 - cos(theta_max)
+    // as sin^2 / (1 + cos) and theta as 2 asin(sqrt((1 - r) / 2))
+    const R omc = rad < R(0) ? R(1) - cmax
+                             : (rad * rad / (rad * rad + l2)) / (R(1) + cmax);
+    solid = R(2 * kPi) * omc;
+    const R om = rng.next() * omc;  // 1 - r
+    theta = R(2) * asinf(m_sqrt(R(0.5) * om));
+  } else {
+    solid = R(2 * kPi) * (R(1) - cmax);
+    R r = rng.next();
+    r = r * (cmax - R(1)) + R(1);
+    theta = acos(r);
+  }
+  const R phi = rng.next() * R(2 * kPi);
+  R nx, ny, nz;
+  if (tx == R(0) && tz == R(0)) { nx = 1; ny = 0; nz = 0; }
+  else { nx = -tz; ny = 0; nz = tx; }
+  nx = ny * tz - nz * ty;
+  ny = nz * tx - nx * tz;
+  nz = nx * ty - ny * tx;
+  R dx = tx, dy = ty, dz = tz;
+  rotate3<R>(dx, dy, dz, nx, ny, nz, theta, R(1e-7));
+  rotate3<R>(dx, dy, dz, tx, ty, tz, phi, R(1e-7));
+  const R inv = R(1) / m_sqrt(dx * dx + dy * dy + dz * dz);
+  const double u = rng.next();
+  const double tof_t = c.dp[19], dtof = c.dp[20];
+  const double tmin = tof_t - 0.5 * dtof, tmax = tof_t + 0.5 * dtof;
+  const double tof = u * (tmax - tmin) + tmin;
+  double tn;
+  if constexpr (sizeof(R) == 4) tn = n.t.dval();
+  else tn = n.t.val();
+  const R vf = R(double(m_sqrt(l2)) / (tof - tn));
+  const R Ef = vf * vf * R(kVS2E);
+  const R dEdt = R(2) * Ef / R(tof);
+  const R prob = solid / R(4 * kPi) * R(dtof) * dEdt;
+  const R vi = m_sqrt(n.vx * n.vx + n.vy * n.vy + n.vz * n.vz);
+  n.vx = dx * inv * vf;
+  n.vy = dy * inv * vf;
+  n.vz = dz * inv * vf;
+  n.p *= prob * (vf / vi);
+}
+
 // One kernel's scatter (p *= sigma, then its S).  kX: the constant-(Q, E)
 // and E(Q) kernels are compiled into the instantiations for the rarer
 // components only.
@@ -1029,6 +1092,12 @@ __device__ __forceinline__ void hss_kernel_leaf(Neutron<R>& n, Rng& rng,
       if constexpr (kX) {
         n.p *= prm<R>(c, 9);  // kernels/__init__.py:119
         sans2d_scatter<R>(n, rng, c);
+      }
+      break;
+    case MCV_KERNEL_DGSSXRES:
+      if constexpr (kX) {
+        n.p *= prm<R>(c, 9);  // kernels/__init__.py:138
+        dgssxres_scatter<R>(n, rng, c);
       }
       break;
     default:

@@ -38,7 +38,8 @@ from .components.samples.homogeneous_single_scatterer import factory
 from .components.sources.source_simple import Source_simple
 from .geometry import Block, Cylinder, Difference, HollowCylinder, Sphere
 from .instrument import instrument
-from .kernels import (CompositeKernel, ConstantQEKernel, E_Q_Kernel,
+from .kernels import (CompositeKernel, ConstantQEKernel, DGSSXResKernel,
+                      E_Q_Kernel,
                       IsotropicKernel, Peak, SANS2D_ongrid_Kernel,
                       SimplePowderDiffractionKernel, SQEGridKernel,
                       coefficient_from_cross_section)
@@ -744,4 +745,27 @@ def sans2d_grid(image=None):
     ins.append(src, position=(0, 0, 0))
     ins.append(sample, position=(0, 0, 10.0))
     ins.append(mon, position=(0, 0, 10.0), relativeTo=sample)
+    return ins
+
+
+def dgssxres_box(target=(3.0, 0.0, 0.0), radius=0.025, tof=0.003,
+                 dtof=1e-5):
+    """The Al box of the reference's box tests (_al_box's source and
+    sample) with the DGSSXRes kernel (sampleassemblies/Al-DGSSXResKernel:
+    a target 3 m to the side; here a 2.5 cm target radius and a 10 us
+    window around 3 ms, which the kernel test uses), and a 4pi theta x tof
+    shell of radius 3 m around the sample, binned 180 x 200 over 0-180 deg
+    x tof +- 10 us."""
+    ins = instrument("dgssxres_box")
+    src = Source_simple("src", radius=0.0, width=0.01, height=0.01, dist=1.0,
+                        xw=0.008, yh=0.008, E0=70.0, dE=0.1, Lambda0=0.0,
+                        dLambda=0.0)
+    HSS = factory(Block(0.06, 0.10, 0.01),
+                  DGSSXResKernel(target, radius, tof, dtof, AL_MU, AL_SIGMA))
+    mon = ThetaTOF_monitor_4Pi("theta_tof", radius=3.0, ntheta=180, ntof=200,
+                               tofmin=tof - 1e-5, tofmax=tof + 1e-5,
+                               filename="theta_tof.h5")
+    ins.append(src, position=(0, 0, 0))
+    ins.append(HSS("sample"), position=(0, 0, 2.0))
+    ins.append(mon, position=(0, 0, 2.0))
     return ins

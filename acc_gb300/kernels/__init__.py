@@ -1,7 +1,7 @@
 """Scattering kernels of homogeneous scatterers (acc/kernels)."""
 
 from .kernels import (CompositeKernel, ConstantQEKernel,  # noqa: F401
-                      E_Q_Kernel,
+                      DGSSXResKernel, E_Q_Kernel,
                       IsotropicKernel, Peak, PowderDiffraction,
                       SANS2D_ongrid_Kernel, SimplePowderDiffractionKernel,
                       SQEGridKernel,

@@ -282,3 +282,31 @@ class SANS2D_ongrid_Kernel:
         c.table = binder.table(comp, "sans2d", self.S, np.float64)
         c.ftable = binder.table(comp, "sans2d_f32", self.S, np.float32)
         c.table_len = self.S.size
+
+
+class DGSSXResKernel:
+    """acc/kernels/DGSSXResKernel.py:19-98 with p *= sigma
+    (acc/kernels/__init__.py:124-146): every neutron scatters towards a
+    target disc of `target_radius` (m) at `target_position` (m, the
+    sample's frame), arriving at a time of flight uniform in
+    tof_at_target +- dtof / 2 (s) -- the resolution kernel of a
+    single-crystal direct-geometry spectrometer."""
+    kind = nat.KERNEL_DGSSXRES
+
+    def __init__(self, target_position, target_radius, tof_at_target, dtof,
+                 absorption_coefficient, scattering_coefficient):
+        self.target_position = tuple(float(v) for v in target_position)
+        self.target_radius = float(target_radius)
+        self.tof_at_target = float(tof_at_target)
+        self.dtof = float(dtof)
+        self.absorption_coefficient = float(absorption_coefficient)
+        self.scattering_coefficient = float(scattering_coefficient)
+
+    def pack(self, comp, c, binder, set_param):
+        set_param(c, 8, self.absorption_coefficient)
+        set_param(c, 9, self.scattering_coefficient)
+        for k, v in enumerate(self.target_position):
+            set_param(c, 15 + k, v)
+        set_param(c, 18, self.target_radius)
+        set_param(c, 19, self.tof_at_target)
+        set_param(c, 20, self.dtof)

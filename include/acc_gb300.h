@@ -111,7 +111,8 @@ enum {
   MCV_KERNEL_CONSTANT_QE = 4, /* acc/kernels/constant_qe.py:15-67, __init__.py:76-88 */
   MCV_KERNEL_E_Q = 5,         /* acc/kernels/E_Q.py:16-117, __init__.py:90-105     */
   MCV_KERNEL_COMPOSITE = 6,   /* acc/kernels/composite.py:7-127, __init__.py:24-34 */
-  MCV_KERNEL_SANS2D = 7       /* acc/kernels/SANS2D_ongrid.py:16-78, __init__.py:107-122 */
+  MCV_KERNEL_SANS2D = 7,      /* acc/kernels/SANS2D_ongrid.py:16-78, __init__.py:107-122 */
+  MCV_KERNEL_DGSSXRES = 8     /* acc/kernels/DGSSXResKernel.py:19-98, __init__.py:124-146 */
 };
 
 /* Instructions of the postfix programs that carry the E_Q kernel's E(Q)
@@ -164,6 +165,9 @@ enum {
  *               ip[4] = nx, ip[5] = ny (each >= 2); table (float64) and
  *               ftable (float32): S[nx][ny], x-major (the transpose of
  *               the reference's (y, x) image)
+ *       DGSSXRES: 15-17 target position (m, the sample's frame),
+ *               18 target radius (m), 19 time of flight at the target
+ *               (s), 20 dtof (s)
  *       COMPOSITE: ip[4] = N elements (1..MCV_COMPOSITE_MAX), in the N
  *               chain slots right after this component, each an
  *               MCV_OP_KERNEL_ELEMENT whose ip[1] is its kernel kind (not

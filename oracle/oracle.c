@@ -1479,6 +1479,46 @@ static void sans2d_S(neutron_t* n, rng_t* rng, const mcv_component* c) {
   n->p *= bilinear(xf, yf, f00, f01, f10, f11);
 }
 
+/* DGSSXResKernel.scatter (acc/kernels/DGSSXResKernel.py:19-98): towards a
+ * target disc (choose_direction :19-58, with the reference's in-place
+ * vec3.cross whose later components read the ones it already replaced),
+ * arriving at a time of flight uniform in tof_target +- dtof / 2;
+ * p *= solid angle / 4 pi * dtof * (2 Ef / tof) * vf / vi */
+static void dgssxres_S(neutron_t* n, rng_t* rng, const mcv_component* c) {
+  double td[3] = {c->dp[15] - n->x, c->dp[16] - n->y, c->dp[17] - n->z};
+  double rad = c->dp[18], tof_t = c->dp[19], dtof = c->dp[20];
+  double l2 = td[0] * td[0] + td[1] * td[1] + td[2] * td[2];
+  double cmax = sqrt(l2 / (rad * rad + l2));
+  if (rad < 0.0) cmax *= -1.0;
+  double solid = 2.0 * M_PI * (1.0 - cmax);
+  double r = rng_uniform(rng);
+  r = r * (cmax - 1.0) + 1.0;
+  double theta = acos(r);
+  double phi = rng_uniform(rng) * 2.0 * M_PI;
+  double nm[3];
+  if (td[0] == 0.0 && td[2] == 0.0) { nm[0] = 1; nm[1] = 0; nm[2] = 0; }
+  else { nm[0] = -td[2]; nm[1] = 0; nm[2] = td[0]; }
+  nm[0] = nm[1] * td[2] - nm[2] * td[1];
+  nm[1] = nm[2] * td[0] - nm[0] * td[2];
+  nm[2] = nm[0] * td[1] - nm[1] * td[0];
+  double d[3] = {td[0], td[1], td[2]};
+  oracle_rotate(d, nm, theta, 1e-7);
+  oracle_rotate(d, td, phi, 1e-7);
+  normalize3(d);
+  double u = rng_uniform(rng);
+  double tmin = tof_t - 0.5 * dtof, tmax = tof_t + 0.5 * dtof;
+  double tof = u * (tmax - tmin) + tmin;
+  double vf = sqrt(l2) / (tof - n->t);
+  double Ef = vf * vf * VS2E;
+  double dEdt = 2.0 * Ef / tof;
+  double prob = solid / 4.0 / M_PI * dtof * dEdt;
+  double vi = length3(n->vx, n->vy, n->vz);
+  n->vx = d[0] * vf;
+  n->vy = d[1] * vf;
+  n->vz = d[2] * vf;
+  n->p *= prob * (vf / vi);
+}
+
 /* ---------------------------------------------------------------- HSS */
 /* the scattering coefficient; a composite's sums its elements' (the slots
  * after the component), scaled by dp[10] (1/N when averaged,
@@ -1534,6 +1574,10 @@ static void kernel_scatter(neutron_t* n, rng_t* rng, const mcv_component* c) {
     case MCV_KERNEL_SANS2D:
       n->p *= c->dp[9]; /* kernels/__init__.py:119 */
       sans2d_S(n, rng, c);
+      break;
+    case MCV_KERNEL_DGSSXRES:
+      n->p *= c->dp[9]; /* kernels/__init__.py:138 */
+      dgssxres_S(n, rng, c);
       break;
     default:
       break;

@@ -98,7 +98,7 @@ def test_hss_validation(engine_lib):
 
 def test_e_q_kernel_validation(engine_lib):
     """The E(Q) kernel needs both programs (1..MCV_EXPR_MAX_OPS
-    instructions) and 1 <= max_iter <= 1e6; a kernel kind past SANS2D is
+    instructions) and 1 <= max_iter <= 1e6; a kernel kind past DGSSXRES is
     unknown."""
     from acc_gb300.components.samples.homogeneous_single_scatterer import \
         factory
@@ -127,7 +127,7 @@ def test_e_q_kernel_validation(engine_lib):
             c.table = value
         assert run(ch) == nat.MCV_EINVAL and b"E(Q)" in st.message, field
     ch = build_chain([H("s")], binder=HostBinder())
-    ch.comp[0].ip[1] = nat.KERNEL_SANS2D + 1
+    ch.comp[0].ip[1] = nat.KERNEL_DGSSXRES + 1
     assert run(ch) == nat.MCV_EINVAL and b"unknown scattering" in st.message
 
 

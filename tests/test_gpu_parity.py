@@ -65,6 +65,7 @@ BUILDERS = {
     "e_q_box": instruments.e_q_box,
     "composite_box": instruments.composite_box,
     "sans2d_grid": instruments.sans2d_grid,
+    "dgssxres_box": instruments.dgssxres_box,
     "verdi": instruments.verdi,
 }
 # every scattered neutron of the constant-(Q, E) box lands in one or two
@@ -83,8 +84,13 @@ SAME_STREAM_N = {"verdi": 200_000}
 #  * VERDI (an SNS source too) is a 40 m chain with ~2000 tapered-guide
 #    segments: float positions there carry ~1e-6 m of rounding (a float's
 #    spacing at 10 m), about 3e-4 of its 5 mm sample.
+#  * the DGSSXRes kernel: the reference's vec3.rotate skips the turn about
+#    the target direction when the vector lies within 1e-7 of it, a test at
+#    float resolution, so FP32 and FP64 decide it differently for the 0.3%
+#    of draws with theta below 4.5e-4 rad (0.25 relative at the shell).
 FP32_SAME_STREAM = [k for k in BUILDERS if k not in
-                    ("sns_source_chain", "sts_source_chain", "verdi")]
+                    ("sns_source_chain", "sts_source_chain", "verdi",
+                     "dgssxres_box")]
 
 
 @pytest.fixture(scope="module", autouse=True)

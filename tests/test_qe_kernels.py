@@ -257,3 +257,31 @@ def test_sans2d_transfer_and_weight(oracle_lib):
         s = (S[xi, yi] * (1 - fx) * (1 - fy) + S[xi + 1, yi] * fx * (1 - fy)
              + S[xi, yi + 1] * (1 - fx) * fy + S[xi + 1, yi + 1] * fx * fy)
         np.testing.assert_allclose(n1[9], sigma * s, rtol=1e-9)
+
+
+def test_dgssxres_kernel_reference_case(oracle_lib):
+    """tests/kernels/test_DGSSXRes.py:23-66: a 3000 m/s neutron along z at
+    t = 1 s scattering towards a target 3 m along x (radius 0.025 m), to
+    arrive at 1.001 s +- 5 us: elastic within 0.5 meV, Q = 6.74 /A within
+    1%.  Also: the direction lies in the target's cone, and the weight is
+    sigma * solid angle / 4 pi * dtof * (2 Ef / tof) * vf / vi."""
+    from acc_gb300.kernels import DGSSXResKernel
+    sigma = 2.0
+    comp = _comp(DGSSXResKernel((3.0, 0.0, 0.0), 0.025, 1.001, 1e-5, 0.0,
+                                sigma))
+    n0 = np.r_[0, 0, 0, 0, 0, 3000.0, 0, 0, 1.0, 1.0]
+    cmax = math.sqrt(9.0 / (0.025 ** 2 + 9.0))
+    for seed in range(1, 101):
+        n1 = O.kernel_scatter_one(comp, n0, seed=seed)
+        q, e = _transfer(n0, n1)
+        np.testing.assert_allclose(e, 0.0, atol=0.5)
+        np.testing.assert_allclose(q, 6.74, rtol=1e-2)
+        vf = n1[3:6]
+        vfl = np.linalg.norm(vf)
+        assert vf[0] / vfl >= cmax - 1e-9  # inside the cone towards +x
+        tof = 3.0 / vfl + 1.0
+        assert abs(tof - 1.001) <= 5e-6 * (1 + 1e-9)
+        Ef = v2e(vfl)
+        want = sigma * 2 * math.pi * (1 - cmax) / (4 * math.pi) * 1e-5 \
+            * (2 * Ef / tof) * vfl / 3000.0
+        np.testing.assert_allclose(n1[9], want, rtol=1e-9)
