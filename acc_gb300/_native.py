@@ -19,6 +19,8 @@ MCV_MAX_BOUNCES = 100000
 MCV_MAX_VARIANTS = 1024
 MCV_MS_MAX_SCATTERED = 48
 MCV_COMPOSITE_MAX = 16
+MCV_ANYSHAPE_MAX_FACES = 99
+MCV_ANYSHAPE_MAX_VERTICES = 16
 MCV_EXPR_STACK = 8
 MCV_EXPR_MAX_OPS = 256
 MCV_SNS_E_NODES = 4096
@@ -48,6 +50,7 @@ OP_GUIDE_TAPERING = 16
 OP_SNS_SOURCE = 17
 OP_NEUTRON_STORAGE = 18
 OP_KERNEL_ELEMENT = 19
+OP_GUIDE_ANYSHAPE = 20
 
 SHAPE_SPHERE, SHAPE_CYLINDER, SHAPE_BOX = 1, 2, 3
 CSG_PRIMITIVE, CSG_DIFFERENCE, CSG_UNION, CSG_INTERSECTION = 0, 1, 2, 3

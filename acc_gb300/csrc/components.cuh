@@ -698,6 +698,100 @@ __device__ __forceinline__ int guide_tapering(Neutron<R>& n,
   return overflow;
 }
 
+// ============================================================ mesh guide
+// inside_convex_polygon (acc/components/optics/geometry2d.py:12-33): the
+// point is on one side of every edge (cross products of one sign); an
+// edge it lies on (|cross| < 1e-14) is skipped.
+template <typename R>
+__device__ __forceinline__ bool inside_convex_polygon(R px, R py,
+                                                      const R* poly, int nv) {
+  R ax = __ldg(&poly[0]), ay = __ldg(&poly[1]);
+  R prev = (__ldg(&poly[2]) - ax) * (py - ay) - (__ldg(&poly[3]) - ay) * (px - ax);
+  bool prev_side = prev <= R(0);
+  for (int k = 1; k < nv; ++k) {
+    const int k2 = k + 1 < nv ? k + 1 : 0;
+    ax = __ldg(&poly[2 * k]);
+    ay = __ldg(&poly[2 * k + 1]);
+    const R sign = (__ldg(&poly[2 * k2]) - ax) * (py - ay) -
+                   (__ldg(&poly[2 * k2 + 1]) - ay) * (px - ax);
+    if (m_fabs(sign) < R(1e-14)) continue;
+    const bool side = sign <= R(0);
+    if (m_fabs(prev) < R(1e-14)) {
+      prev_side = side;
+      continue;
+    }
+    if (prev_side != side) return false;
+  }
+  return true;
+}
+
+// Guide_anyshape._propagate (acc/components/optics/guide_anyshape.py:
+// 96-158): each pass takes, among the faces whose plane the neutron reaches
+// at t > 0, the nearest hit that lies inside the face's polygon (the
+// reference sorts every positive hit time and takes the first inside one:
+// the same face, ties aside), moves there less 1e-14 of the way, and
+// reflects off the face with the supermirror reflectivity; none -> the
+// neutron has left the guide, where it stays (no propagation to the exit).
+// Returns 1 when MCV_ANYSHAPE_MAX_BOUNCES passes did not let it out.
+template <typename R>
+__device__ __forceinline__ int guide_anyshape(Neutron<R>& n,
+                                              const mcv_component& c) {
+  const int nf = c.ip[0], nv = c.ip[1], stride = 12 + 2 * nv;
+  const R* F = sizeof(R) == 4 ? (const R*)c.ftable : (const R*)c.table;
+  const R R0 = prm<R>(c, 0), Qc = prm<R>(c, 1), alpha = prm<R>(c, 2),
+          m = prm<R>(c, 3), W = prm<R>(c, 4);
+  // FP32: the reference backs a hit off by 1e-14 of its flight so that
+  // the next pass does not find the same face again; in float that is
+  // below resolution, so the face just left is skipped instead (a
+  // reflection from a plane moves away from it: in exact arithmetic it
+  // cannot be next).  FP64 keeps the reference's sequence.
+  int last = -1;
+  for (int nb = 0; nb < MCV_ANYSHAPE_MAX_BOUNCES; ++nb) {
+    R best = R(0);
+    int bi = -1;
+    for (int f = 0; f < nf; ++f) {
+      if (sizeof(R) == 4 && f == last) continue;
+      const R* g = F + (size_t)f * stride;
+      const R cx = __ldg(&g[0]), cy = __ldg(&g[1]), cz = __ldg(&g[2]);
+      const R nx = __ldg(&g[9]), ny = __ldg(&g[10]), nz = __ldg(&g[11]);
+      // intersect_plane (:22-29)
+      const R dist = (cx - n.x) * nx + (cy - n.y) * ny + (cz - n.z) * nz;
+      const R vn = n.vx * nx + n.vy * ny + n.vz * nz;
+      const R t = dist / vn;
+      if (!(t > R(0)) || (bi >= 0 && !(t < best))) continue;
+      const R qx = n.x + n.vx * t - cx, qy = n.y + n.vy * t - cy,
+              qz = n.z + n.vz * t - cz;
+      const R u = qx * __ldg(&g[3]) + qy * __ldg(&g[4]) + qz * __ldg(&g[5]);
+      const R w = qx * __ldg(&g[6]) + qy * __ldg(&g[7]) + qz * __ldg(&g[8]);
+      if (inside_convex_polygon<R>(u, w, g + 12, nv)) {
+        best = t;
+        bi = f;
+      }
+    }
+    if (bi < 0) return 0;
+    const R* g = F + (size_t)bi * stride;
+    const R nx = __ldg(&g[9]), ny = __ldg(&g[10]), nz = __ldg(&g[11]);
+    const R t = best - best * R(1e-14);
+    const R vq = -(n.vx * nx + n.vy * ny + n.vz * nz) * R(2);
+    const R Rf = reflectivity(m_fabs(vq) * R(kV2K), R0, Qc, alpha, m, W);
+    if (!(n.p * Rf > R(0))) {
+      // absorb (acc/neutron.py:27-28) before the move is written back
+      n.p = R(-1);
+      return 0;
+    }
+    n.p *= Rf;
+    n.x += n.vx * t;
+    n.y += n.vy * t;
+    n.z += n.vz * t;
+    n.t.add(t);
+    n.vx += nx * vq;
+    n.vy += ny * vq;
+    n.vz += nz * vq;
+    last = bi;
+  }
+  return 1;
+}
+
 // Slit / Beamstop (acc/components/optics/slit.py:71-108,
 // beamstop.py:75-112); dp = {xmin, xmax, ymin, ymax, radius^2, cut}
 // (`up`: the chain's FP32 weight scale, which the cut is compared in)

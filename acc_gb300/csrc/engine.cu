@@ -214,6 +214,18 @@ int validate_component(const mcv_component& c, int k, mcv_status* st) {
       }
       break;
     }
+    case MCV_OP_GUIDE_ANYSHAPE: {
+      const int nf = c.ip[0], nv = c.ip[1];
+      if (nf < 1 || nf > MCV_ANYSHAPE_MAX_FACES || nv < 3 ||
+          nv > MCV_ANYSHAPE_MAX_VERTICES || !c.table || !c.ftable ||
+          c.table_len < (uint64_t)nf * (12 + 2 * nv)) {
+        set_msg(st, MCV_EINVAL,
+                "component %s%lld: mesh guide needs 1..99 faces of 3..16 "
+                "vertices and its face table", "", (long long)k);
+        return MCV_EINVAL;
+      }
+      break;
+    }
     case MCV_OP_GUIDE_TAPERING:
       if (c.ip[0] < 1 || !c.table || !c.ftable ||
           c.table_len < (uint64_t)10 * c.ip[0] || !(c.dp[0] > 0)) {
@@ -297,14 +309,15 @@ bool has_hms(const mcv_chain* ch) {
 }
 
 // The rarer components run in their own kernel instantiations (kX): the
-// SNS source, the tapered guide, the multiple scatterer, stored neutrons,
-// and samples with the constant-(Q, E), E(Q), composite, SANS2D or
-// DGSSXRes kernel.
+// SNS source, the tapered and mesh guides, the multiple scatterer, stored
+// neutrons, and samples with the constant-(Q, E), E(Q), composite, SANS2D
+// or DGSSXRes kernel.
 bool is_exotic(const mcv_chain* ch) {
   for (int k = 0; k < ch->ncomp; ++k) {
     const int op = ch->comp[k].opcode;
     if (op == MCV_OP_HMS || op == MCV_OP_SNS_SOURCE ||
-        op == MCV_OP_GUIDE_TAPERING || op == MCV_OP_NEUTRON_STORAGE)
+        op == MCV_OP_GUIDE_TAPERING || op == MCV_OP_NEUTRON_STORAGE ||
+        op == MCV_OP_GUIDE_ANYSHAPE)
       return true;
     if ((op == MCV_OP_HSS || op == MCV_OP_KERNEL_ELEMENT) &&
         (ch->comp[k].ip[1] == MCV_KERNEL_CONSTANT_QE ||

@@ -99,6 +99,9 @@ __device__ __forceinline__ int run_component(Neutron<R>& n, Rng& rng,
     case MCV_OP_GUIDE_TAPERING:
       if constexpr (kX) return guide_tapering<R>(n, c);
       return 0;
+    case MCV_OP_GUIDE_ANYSHAPE:
+      if constexpr (kX) return guide_anyshape<R>(n, c);
+      return 0;
     case MCV_OP_HSS:
       hss<kX>(n, rng, c, trk);
       return 0;

@@ -769,3 +769,42 @@ def dgssxres_box(target=(3.0, 0.0, 0.0), radius=0.025, tof=0.003,
     ins.append(HSS("sample"), position=(0, 0, 2.0))
     ins.append(mon, position=(0, 0, 2.0))
     return ins
+
+
+# ------------------------------------------------------------ mesh guide
+def anyshape_guide_chain(w1=0.035, h1=0.035, w2=0.035, h2=0.035, l=10.0,
+                         mesh_file=None):
+    """The reference's mesh-guide test instrument
+    (tests/components/optics/guide_anyshape_example1_instrument.py with
+    acc/test/instrument_factory.py): a 3 x 3 cm source (10 +- 9.5 A) aimed
+    at 3.5 x 3.5 cm 0.9 m away; a guide of l = 10 m read from an OFF mesh
+    (a w1 x h1 -> w2 x h2 channel written to `mesh_file`, a temporary file
+    when None) 1 m downstream, coating R0 0.99, Qc 0.0219, alpha 6.07,
+    m 3, W 0.003; 1 m after its exit a PSD (250 x 250 over 10 x 10 cm) and
+    position-divergence monitors in x and y (250 x 250)."""
+    import tempfile
+    from .components.monitors.posdiv_monitor import PosDiv_monitor
+    from .components.optics.guide_anyshape import (Guide_anyshape,
+                                                   box_guide_mesh, write_off)
+    if mesh_file is None:
+        fd, mesh_file = tempfile.mkstemp(suffix=".off", prefix="guide_")
+        os.close(fd)
+    write_off(mesh_file, *box_guide_mesh(w1, h1, w2, h2, l))
+    ins = instrument("anyshape_guide_chain")
+    src = Source_simple("source", radius=0.0, width=0.03, height=0.03,
+                        dist=0.9, xw=0.035, yh=0.035, Lambda0=10.0,
+                        dLambda=9.5)
+    guide = Guide_anyshape("guide", R0=0.99, Qc=0.0219, alpha=6.07, m=3,
+                           W=0.003, geometry=mesh_file)
+    z = 2 * 1.0 + l
+    ins.append(src, position=(0, 0, 0))
+    ins.append(guide, position=(0, 0, 1.0))
+    ins.append(PSD_monitor("Ixy", nx=250, ny=250, xwidth=0.1, yheight=0.1,
+                           filename="Ixy.h5"), position=(0, 0, z))
+    ins.append(PosDiv_monitor("Ixdivx", npos=250, ndiv=250, xwidth=0.1,
+                              yheight=0.1, filename="Ixdivx.h5"),
+               position=(0, 0, z))
+    ins.append(PosDiv_monitor("Ixdivy", npos=250, ndiv=250, xwidth=0.1,
+                              yheight=0.1, filename="Ixdivy.h5"),
+               position=(0, 0, z), orientation=(0, 0, 90))
+    return ins

@@ -79,6 +79,10 @@ WORKLOADS = {
         "sans2d_grid: 0.3x0.3 mm source, 10 +- 0.65 A -> Al plate 3x3 cm "
         "x 0.2 mm with S(Qx,Qy) on a 1475x1100 grid -> PSD 250x250 at "
         "10 m"),
+    "anyshape_guide_chain": (
+        "anyshape_guide_chain: 3x3 cm source, 10 +- 9.5 A -> 10 m guide "
+        "from an OFF mesh (4 faces, 3.5x3.5 cm), m=3 -> PSD 250x250 + "
+        "position-divergence x and y 250x250"),
     "verdi": (
         "verdi: the VERDI instrument (26 components): SNS moderator "
         "(synthetic file, 141 E x 160 t, 0.1-1000 meV) -> 2 elliptic "

@@ -41,6 +41,9 @@ extern "C" {
                                      reference default is 10, its UN
                                      sample uses 33) */
 #define MCV_COMPOSITE_MAX 16      /* elements of a composite kernel */
+#define MCV_ANYSHAPE_MAX_FACES 99 /* guide_anyshape.py:18-19, 240  */
+#define MCV_ANYSHAPE_MAX_VERTICES 16
+#define MCV_ANYSHAPE_MAX_BOUNCES 1000 /* guide_anyshape.py:18            */
 #define MCV_EXPR_STACK 8          /* evaluation stack of an E(Q) / S(Q)
                                      program (E_Q kernel)              */
 #define MCV_EXPR_MAX_OPS 256      /* instructions per E(Q) / S(Q) program */
@@ -85,7 +88,8 @@ enum {
   MCV_OP_NEUTRON_STORAGE = 18,  /* acc/components/sources/neutronfromstorage.py */
   MCV_OP_KERNEL_ELEMENT = 19,   /* an element of a composite kernel
                                    (acc/kernels/composite.py): not run */
-  MCV_OP_COUNT = 20
+  MCV_OP_GUIDE_ANYSHAPE = 20,   /* acc/components/optics/guide_anyshape.py */
+  MCV_OP_COUNT = 21
 };
 
 /* ---- shapes of the homogeneous scatterer (acc/geometry/arrow_intersect.py)
@@ -229,6 +233,13 @@ enum {
  * NEUTRON_STORAGE (neutronfromstorage.py:42-82): neutron i of a run is
  *   stored neutron i mod N; table: N x 10 float64 neutrons (table_len =
  *   10 N), ftable its float32 copy
+ * GUIDE_ANYSHAPE (guide_anyshape.py:96-249): a guide of flat convex
+ *   mirror faces (an OFF mesh), no propagation to z = 0 first
+ *   ip[0] = nfaces (1..MCV_ANYSHAPE_MAX_FACES), ip[1] = vertices a face
+ *   (3..MCV_ANYSHAPE_MAX_VERTICES); dp: 0 R0 1 Qc 2 alpha 3 m 4 W
+ *   table (float64) and ftable (float32): per face, 12 + 2 * nv values:
+ *   centre (3), in-plane unit vectors e0, e1 (3 each), normal e2 (3),
+ *   then the polygon's vertices in (e0, e1) coordinates (2 each)
  * SLIT / BEAMSTOP (slit.py:20-108, beamstop.py:18-112)
  *                                dp: xmin xmax ymin ymax radius^2 cut
  *

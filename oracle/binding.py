@@ -79,6 +79,7 @@ def lib():
         L.oracle_source_one.argtypes = [ctypes.c_void_p, ctypes.c_void_p, c_double_p]
         L.oracle_hss_one.argtypes = [ctypes.c_void_p, ctypes.c_void_p,
                                      ctypes.c_int, c_double_p]
+        L.oracle_anyshape_one.argtypes = [ctypes.c_void_p, c_double_p]
         L.oracle_kernel_scatter_one.argtypes = [ctypes.c_void_p, c_double_p,
                                                 ctypes.c_uint64, ctypes.c_uint64]
         L.oracle_expr_eval.restype = ctypes.c_double
@@ -207,6 +208,14 @@ def hss_one(comp, neutron, uniforms):
     u = np.ascontiguousarray(uniforms, dtype=np.float32)
     lib().oracle_hss_one(ctypes.byref(comp), u.ctypes.data, u.size, _dp(st))
     return st
+
+
+def anyshape_one(comp, neutron):
+    """The mesh guide (Guide_anyshape) on one neutron state; returns
+    (state, 1 if the bounce limit was reached)."""
+    st = np.array(neutron, dtype=np.float64)
+    over = lib().oracle_anyshape_one(ctypes.byref(comp), _dp(st))
+    return st, over
 
 
 def kernel_scatter_one(comp, neutron, seed=1, index=0):

@@ -538,6 +538,120 @@ static int guide(neutron_t* n, const mcv_component* c, int* nrefl) {
  * (acc/components/optics/guide_tapering.py:140-291): nseg equal segments,
  * each a tapered channel; table rows w1 w2 h1 h2 ww hh whalf hhalf lwhalf
  * lhhalf (float64, nseg each).  Returns 1 if a bounce loop ran out. */
+/* inside_convex_polygon (acc/components/optics/geometry2d.py:12-33) */
+static int inside_convex_polygon(double px, double py, const double* poly,
+                                 int nv) {
+  double prev = (poly[2] - poly[0]) * (py - poly[1]) -
+                (poly[3] - poly[1]) * (px - poly[0]);
+  int prev_side = prev <= 0;
+  for (int k = 1; k < nv; ++k) {
+    int k2 = (k + 1) % nv;
+    double ax = poly[2 * k], ay = poly[2 * k + 1];
+    double sign = (poly[2 * k2] - ax) * (py - ay) - (poly[2 * k2 + 1] - ay) * (px - ax);
+    if (fabs(sign) < 1e-14) continue;
+    int side = sign <= 0;
+    if (fabs(prev) < 1e-14) {
+      prev_side = side;
+      continue;
+    }
+    if (prev_side != side) return 0;
+  }
+  return 1;
+}
+
+/* insert_into_sorted_list_with_indexes (acc/geometry/_utils.py:35-65) */
+static int insert_sorted_idx(int index, double d, int* index_list, double* l,
+                             int N, int cap) {
+  if (N >= cap) return N;
+  if (N == 0) {
+    l[0] = d;
+    index_list[0] = index;
+    return 1;
+  }
+  int minidx = 0, maxidx = N - 1, idx;
+  while (minidx < maxidx - 1) {
+    int mid = (minidx + maxidx) / 2;
+    if (d > l[mid]) minidx = mid;
+    else maxidx = mid;
+  }
+  if (minidx == maxidx) {
+    idx = minidx;
+    if (d > l[idx]) idx += 1;
+  } else {
+    if (d >= l[maxidx]) idx = maxidx + 1;
+    else if (d <= l[minidx]) idx = minidx;
+    else idx = minidx + 1;
+  }
+  for (int i = N; i > idx; --i) {
+    l[i] = l[i - 1];
+    index_list[i] = index_list[i - 1];
+  }
+  l[idx] = d;
+  index_list[idx] = index;
+  return N + 1;
+}
+
+/* Guide_anyshape._propagate (acc/components/optics/guide_anyshape.py:
+ * 96-158), in the reference's order: every positive plane hit sorted, the
+ * first inside its face taken; the move is written back after the
+ * reflectivity (an absorbed neutron keeps its place).  Returns 1 when the
+ * bounce limit is reached. */
+static int guide_anyshape(neutron_t* n, const mcv_component* c) {
+  int nf = c->ip[0], nv = c->ip[1], stride = 12 + 2 * nv;
+  const double* F = (const double*)c->table;
+  double R0 = c->dp[0], Qc = c->dp[1], alpha = c->dp[2], m = c->dp[3],
+         W = c->dp[4];
+  double tl[MCV_ANYSHAPE_MAX_FACES];
+  int il[MCV_ANYSHAPE_MAX_FACES];
+  for (int nb = 0; nb < MCV_ANYSHAPE_MAX_BOUNCES; ++nb) {
+    int ninter = 0;
+    for (int f = 0; f < nf; ++f) {
+      const double* g = F + (size_t)f * stride;
+      double dist = (g[0] - n->x) * g[9] + (g[1] - n->y) * g[10] +
+                    (g[2] - n->z) * g[11];
+      double vn = n->vx * g[9] + n->vy * g[10] + n->vz * g[11];
+      double t = dist / vn;
+      if (t > 0) ninter = insert_sorted_idx(f, t, il, tl, ninter, nf);
+    }
+    if (!ninter) return 0;
+    int found = -1;
+    double t = 0;
+    for (int k = 0; k < ninter; ++k) {
+      const double* g = F + (size_t)il[k] * stride;
+      t = tl[k];
+      double qx = n->vx * t + n->x - g[0], qy = n->vy * t + n->y - g[1],
+             qz = n->vz * t + n->z - g[2];
+      double u = qx * g[3] + qy * g[4] + qz * g[5];
+      double w = qx * g[6] + qy * g[7] + qz * g[8];
+      if (inside_convex_polygon(u, w, g + 12, nv)) {
+        found = il[k];
+        break;
+      }
+    }
+    if (found < 0) return 0;
+    const double* g = F + (size_t)found * stride;
+    t -= t * 1e-14;
+    double x = n->x + n->vx * t, y = n->y + n->vy * t, z = n->z + n->vz * t;
+    double tt = n->t + t;
+    double vq = -(n->vx * g[9] + n->vy * g[10] + n->vz * g[11]) * 2;
+    double R = oracle_reflectivity(fabs(vq) * V2K, R0, Qc, alpha, m, W);
+    double prob = n->p * R;
+    if (prob <= 0) {
+      n->p = -1;
+      return 0;
+    }
+    n->vx += g[9] * vq;
+    n->vy += g[10] * vq;
+    n->vz += g[11] * vq;
+    n->x = x;
+    n->y = y;
+    n->z = z;
+    n->t = tt;
+    n->p = prob;
+  }
+  return 1;
+}
+
 static int guide_tapering(neutron_t* n, const mcv_component* c) {
   const int nseg = c->ip[0];
   const double* d = (const double*)c->table;
@@ -2074,6 +2188,9 @@ static void run_component(neutron_t* n, rng_t* rng, const mcv_component* c,
     case MCV_OP_GUIDE_TAPERING:
       st->bounce_overflow += guide_tapering(n, c);
       break;
+    case MCV_OP_GUIDE_ANYSHAPE:
+      st->bounce_overflow += guide_anyshape(n, c);
+      break;
     case MCV_OP_HSS: hss(n, rng, c); break;
     case MCV_OP_PSD_MONITOR: psd_monitor(n, c, tl); break;
     case MCV_OP_PSD_MONITOR_4PI: psd_monitor_4pi(n, c, tl); break;
@@ -2339,6 +2456,10 @@ void oracle_kernel_scatter_one(const mcv_component* c, double* st,
   rng_t rng;
   rng_init(&rng, seed, index, 0, NULL, 0);
   kernel_scatter((neutron_t*)st, &rng, c);
+}
+/* The mesh guide on one neutron state; returns 1 at the bounce limit. */
+int oracle_anyshape_one(const mcv_component* c, double* st) {
+  return guide_anyshape((neutron_t*)st, c);
 }
 void oracle_apply_transform(const double* rot, const double* off, double* st) {
   apply_transform((neutron_t*)st, rot, off);

@@ -66,6 +66,8 @@ BUILDERS = {
     "composite_box": instruments.composite_box,
     "sans2d_grid": instruments.sans2d_grid,
     "dgssxres_box": instruments.dgssxres_box,
+    "anyshape_guide_chain": lambda: instruments.anyshape_guide_chain(
+        w2=0.04, h2=0.04),
     "verdi": instruments.verdi,
 }
 # every scattered neutron of the constant-(Q, E) box lands in one or two
@@ -88,9 +90,14 @@ SAME_STREAM_N = {"verdi": 200_000}
 #    the target direction when the vector lies within 1e-7 of it, a test at
 #    float resolution, so FP32 and FP64 decide it differently for the 0.3%
 #    of draws with theta below 4.5e-4 rad (0.25 relative at the shell).
+#  * the mesh guide: whether a neutron reflected into a corner of the mesh
+#    leaves through it (the neighbouring face's plane found at t <= 0)
+#    turns on rounding, and float rounds differently from the reference's
+#    double for 0.5% of the neutrons (FP32 skips the face it just left
+#    where the reference backs off 1e-14, which is below float resolution).
 FP32_SAME_STREAM = [k for k in BUILDERS if k not in
                     ("sns_source_chain", "sts_source_chain", "verdi",
-                     "dgssxres_box")]
+                     "dgssxres_box", "anyshape_guide_chain")]
 
 
 @pytest.fixture(scope="module", autouse=True)
