@@ -148,3 +148,41 @@ class Guide_anyshape(ComponentBase):
         c.table = binder.table(self, "faces", self.table, np.float64)
         c.ftable = binder.table(self, "faces_f32", self.table, np.float32)
         c.table_len = self.table.size
+
+
+GRAVITY = 9.80665  # m/s^2 (guide_anyshape_gravity.py:219)
+
+
+class Guide_anyshape_gravity(Guide_anyshape):
+    """Guide_anyshape with gravity (acc/components/optics/
+    guide_anyshape_gravity.py): trajectories between reflections are
+    parabolas under `gravity`, the acceleration in the guide's own frame
+    (by default -9.80665 m/s^2 along y; an instrument sets it from the
+    guide's orientation, as the reference's orientation setter does:
+    rotation . (0, -9.80665, 0)).  Past its last reflection a neutron short
+    of the mesh's largest z is carried to that plane."""
+
+    def __init__(self, name, xwidth=0, yheight=0, zdepth=0, center=False,
+                 R0=0.99, Qc=0.0219, alpha=3, m=2, W=0.003, geometry="",
+                 gravity=(0.0, -GRAVITY, 0.0), **kwargs):
+        super().__init__(name, xwidth, yheight, zdepth, center, R0, Qc,
+                         alpha, m, W, geometry)
+        if len(self.propagate_params[3]) > 50:
+            import warnings
+            warnings.warn("with more than 50 faces the reference's list of "
+                          "plane hits (100 entries) can overflow, which the "
+                          "kernels do not reproduce")
+        self.z_max = float(np.max(self.propagate_params[0][:, :, 2]))
+        self.gravity = np.asarray(gravity, dtype=np.float64)
+
+    def orient(self, rotation):
+        """Set gravity from the guide's rotation in the instrument."""
+        self.gravity = np.asarray(rotation, dtype=np.float64) @ \
+            np.array([0.0, -GRAVITY, 0.0])
+
+    def pack(self, c, binder):
+        super().pack(c, binder)
+        c.ip[2] = 1
+        for k, v in enumerate(self.gravity):
+            set_param(c, 5 + k, float(v))
+        set_param(c, 8, self.z_max)

@@ -792,6 +792,122 @@ __device__ __forceinline__ int guide_anyshape(Neutron<R>& n,
   return 1;
 }
 
+// The gravity form (acc/components/optics/guide_anyshape_gravity.py:
+// 25-182): a face plane is reached where n.(r + v t + g t^2 / 2 - c) = 0
+// (intersect_plane: both roots of the quadratic, the linear root when
+// |g.n| / 2 < 1e-10); each pass takes the earliest root t > 0 at or past
+// 1e-10 s whose point lies inside its face (no back-off), moves along the
+// parabola (propagate_with_gravity: v' = v + g t, r' = r + (v + v') t / 2)
+// and reflects.  An absorbed neutron keeps the hit's position and time.
+// Past the last reflection a neutron short of z_max is carried to the
+// plane z = z_max without advancing its time, taking the first root when
+// it is positive and also when only the second one is (the reference's
+// choice, kept).  FP32: on the face just left a root below 1e-6 s is the
+// neutron's own position again (float rounding on the face), so it is
+// skipped there; a genuine return onto the same face takes milliseconds.
+template <typename R>
+__device__ __forceinline__ void gravity_roots(R px, R py, R pz, R vx, R vy,
+                                              R vz, R gx, R gy, R gz, R cx,
+                                              R cy, R cz, R nx, R ny, R nz,
+                                              R& t0, R& t1) {
+  const R A = (gx * nx + gy * ny + gz * nz) / R(2);
+  const R B = vx * nx + vy * ny + vz * nz;
+  const R C = (px * nx + py * ny + pz * nz) - (cx * nx + cy * ny + cz * nz);
+  if (m_fabs(A) < R(1e-10)) {
+    t0 = -C / B;
+    t1 = R(-1);
+    return;
+  }
+  const R d = B * B - R(4) * A * C;
+  if (d < R(0)) {
+    t0 = t1 = R(-1);
+    return;
+  }
+  const R s = m_sqrt(d);
+  t0 = (-B - s) / R(2) / A;
+  t1 = (-B + s) / R(2) / A;
+}
+
+template <typename R>
+__device__ __forceinline__ int guide_anyshape_gravity(Neutron<R>& n,
+                                                      const mcv_component& c) {
+  const int nf = c.ip[0], nv = c.ip[1], stride = 12 + 2 * nv;
+  const R* F = sizeof(R) == 4 ? (const R*)c.ftable : (const R*)c.table;
+  const R R0 = prm<R>(c, 0), Qc = prm<R>(c, 1), alpha = prm<R>(c, 2),
+          m = prm<R>(c, 3), W = prm<R>(c, 4);
+  const R gx = prm<R>(c, 5), gy = prm<R>(c, 6), gz = prm<R>(c, 7);
+  int last = -1, overflow = 1;
+  for (int nb = 0; nb < MCV_ANYSHAPE_MAX_BOUNCES; ++nb) {
+    R best = R(0);
+    int bi = -1;
+    for (int f = 0; f < nf; ++f) {
+      const R* g = F + (size_t)f * stride;
+      const R cx = __ldg(&g[0]), cy = __ldg(&g[1]), cz = __ldg(&g[2]);
+      R t[2];
+      gravity_roots<R>(n.x, n.y, n.z, n.vx, n.vy, n.vz, gx, gy, gz, cx, cy, cz,
+                       __ldg(&g[9]), __ldg(&g[10]), __ldg(&g[11]), t[0], t[1]);
+      const R tmin = (sizeof(R) == 4 && f == last) ? R(1e-6) : R(1e-10);
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        const R tk = t[k];
+        if (!(tk > R(0)) || tk < tmin || (bi >= 0 && !(tk < best))) continue;
+        const R wx = n.vx + gx * tk, wy = n.vy + gy * tk, wz = n.vz + gz * tk;
+        const R qx = n.x + (n.vx + wx) * (R(0.5) * tk) - cx,
+                qy = n.y + (n.vy + wy) * (R(0.5) * tk) - cy,
+                qz = n.z + (n.vz + wz) * (R(0.5) * tk) - cz;
+        const R u = qx * __ldg(&g[3]) + qy * __ldg(&g[4]) + qz * __ldg(&g[5]);
+        const R w = qx * __ldg(&g[6]) + qy * __ldg(&g[7]) + qz * __ldg(&g[8]);
+        if (inside_convex_polygon<R>(u, w, g + 12, nv)) {
+          best = tk;
+          bi = f;
+        }
+      }
+    }
+    if (bi < 0) {
+      overflow = 0;
+      break;
+    }
+    const R* g = F + (size_t)bi * stride;
+    const R nx = __ldg(&g[9]), ny = __ldg(&g[10]), nz = __ldg(&g[11]);
+    const R t = best;
+    const R wx = n.vx + gx * t, wy = n.vy + gy * t, wz = n.vz + gz * t;
+    n.x = n.x + (n.vx + wx) * (R(0.5) * t);
+    n.y = n.y + (n.vy + wy) * (R(0.5) * t);
+    n.z = n.z + (n.vz + wz) * (R(0.5) * t);
+    n.vx = wx;
+    n.vy = wy;
+    n.vz = wz;
+    n.t.add(t);
+    const R vq = -(wx * nx + wy * ny + wz * nz) * R(2);
+    const R Rf = reflectivity(m_fabs(vq) * R(kV2K), R0, Qc, alpha, m, W);
+    if (!(n.p * Rf > R(0))) {
+      n.p = R(-1);  // absorb (acc/neutron.py:27-28)
+      return 0;
+    }
+    n.p *= Rf;
+    n.vx += nx * vq;
+    n.vy += ny * vq;
+    n.vz += nz * vq;
+    last = bi;
+  }
+  const R zmax = prm<R>(c, 8);
+  if (n.z < zmax) {
+    R t0, t1;
+    gravity_roots<R>(n.x, n.y, n.z, n.vx, n.vy, n.vz, gx, gy, gz, R(0), R(0),
+                     zmax, R(0), R(0), R(1), t0, t1);
+    if (!(t0 > R(0)) && !(t1 > R(0))) return overflow;
+    const R t = t0;  // also when only t1 > 0 (the reference's choice)
+    const R wx = n.vx + gx * t, wy = n.vy + gy * t, wz = n.vz + gz * t;
+    n.x = n.x + (n.vx + wx) * (R(0.5) * t);
+    n.y = n.y + (n.vy + wy) * (R(0.5) * t);
+    n.z = n.z + (n.vz + wz) * (R(0.5) * t);
+    n.vx = wx;
+    n.vy = wy;
+    n.vz = wz;
+  }
+  return overflow;
+}
+
 // Slit / Beamstop (acc/components/optics/slit.py:71-108,
 // beamstop.py:75-112); dp = {xmin, xmax, ymin, ymax, radius^2, cut}
 // (`up`: the chain's FP32 weight scale, which the cut is compared in)

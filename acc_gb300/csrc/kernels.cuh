@@ -100,7 +100,10 @@ __device__ __forceinline__ int run_component(Neutron<R>& n, Rng& rng,
       if constexpr (kX) return guide_tapering<R>(n, c);
       return 0;
     case MCV_OP_GUIDE_ANYSHAPE:
-      if constexpr (kX) return guide_anyshape<R>(n, c);
+      if constexpr (kX) {
+        if (c.ip[2] & 1) return guide_anyshape_gravity<R>(n, c);
+        return guide_anyshape<R>(n, c);
+      }
       return 0;
     case MCV_OP_HSS:
       hss<kX>(n, rng, c, trk);

@@ -100,6 +100,11 @@ def chain_parts(instrument):
     `first` is the instrument index of chain component 0."""
     offsets, rotmats = calcTransformations(instrument)
     comps = list(instrument.components)
+    for comp in comps:
+        # components whose physics depends on their orientation in the
+        # instrument (gravity in the guide's frame)
+        if hasattr(comp, "orient"):
+            comp.orient(instrument.geometer.rotation(comp))
     k = 0
     while k < len(comps) - 1 and getattr(comps[k], "opcode", None) == nat.OP_ARM:
         k += 1

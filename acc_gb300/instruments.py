@@ -773,7 +773,7 @@ def dgssxres_box(target=(3.0, 0.0, 0.0), radius=0.025, tof=0.003,
 
 # ------------------------------------------------------------ mesh guide
 def anyshape_guide_chain(w1=0.035, h1=0.035, w2=0.035, h2=0.035, l=10.0,
-                         mesh_file=None):
+                         mesh_file=None, gravity=False):
     """The reference's mesh-guide test instrument
     (tests/components/optics/guide_anyshape_example1_instrument.py with
     acc/test/instrument_factory.py): a 3 x 3 cm source (10 +- 9.5 A) aimed
@@ -781,10 +781,12 @@ def anyshape_guide_chain(w1=0.035, h1=0.035, w2=0.035, h2=0.035, l=10.0,
     (a w1 x h1 -> w2 x h2 channel written to `mesh_file`, a temporary file
     when None) 1 m downstream, coating R0 0.99, Qc 0.0219, alpha 6.07,
     m 3, W 0.003; 1 m after its exit a PSD (250 x 250 over 10 x 10 cm) and
-    position-divergence monitors in x and y (250 x 250)."""
+    position-divergence monitors in x and y (250 x 250).  `gravity`: the
+    guide_anyshape_gravity form, g along -y."""
     import tempfile
     from .components.monitors.posdiv_monitor import PosDiv_monitor
     from .components.optics.guide_anyshape import (Guide_anyshape,
+                                                   Guide_anyshape_gravity,
                                                    box_guide_mesh, write_off)
     if mesh_file is None:
         fd, mesh_file = tempfile.mkstemp(suffix=".off", prefix="guide_")
@@ -794,8 +796,9 @@ def anyshape_guide_chain(w1=0.035, h1=0.035, w2=0.035, h2=0.035, l=10.0,
     src = Source_simple("source", radius=0.0, width=0.03, height=0.03,
                         dist=0.9, xw=0.035, yh=0.035, Lambda0=10.0,
                         dLambda=9.5)
-    guide = Guide_anyshape("guide", R0=0.99, Qc=0.0219, alpha=6.07, m=3,
-                           W=0.003, geometry=mesh_file)
+    G = Guide_anyshape_gravity if gravity else Guide_anyshape
+    guide = G("guide", R0=0.99, Qc=0.0219, alpha=6.07, m=3, W=0.003,
+              geometry=mesh_file)
     z = 2 * 1.0 + l
     ins.append(src, position=(0, 0, 0))
     ins.append(guide, position=(0, 0, 1.0))

@@ -88,7 +88,8 @@ enum {
   MCV_OP_NEUTRON_STORAGE = 18,  /* acc/components/sources/neutronfromstorage.py */
   MCV_OP_KERNEL_ELEMENT = 19,   /* an element of a composite kernel
                                    (acc/kernels/composite.py): not run */
-  MCV_OP_GUIDE_ANYSHAPE = 20,   /* acc/components/optics/guide_anyshape.py */
+  MCV_OP_GUIDE_ANYSHAPE = 20,   /* acc/components/optics/guide_anyshape.py,
+                                   guide_anyshape_gravity.py */
   MCV_OP_COUNT = 21
 };
 
@@ -240,6 +241,9 @@ enum {
  *   table (float64) and ftable (float32): per face, 12 + 2 * nv values:
  *   centre (3), in-plane unit vectors e0, e1 (3 each), normal e2 (3),
  *   then the polygon's vertices in (e0, e1) coordinates (2 each)
+ *   ip[2] bit 0: with gravity (guide_anyshape_gravity.py:25-182):
+ *   dp 5-7 the gravitational acceleration in the guide's frame (m/s^2),
+ *   dp 8 z_max (the mesh's largest z)
  * SLIT / BEAMSTOP (slit.py:20-108, beamstop.py:18-112)
  *                                dp: xmin xmax ymin ymax radius^2 cut
  *

@@ -601,8 +601,8 @@ static int guide_anyshape(neutron_t* n, const mcv_component* c) {
   const double* F = (const double*)c->table;
   double R0 = c->dp[0], Qc = c->dp[1], alpha = c->dp[2], m = c->dp[3],
          W = c->dp[4];
-  double tl[MCV_ANYSHAPE_MAX_FACES];
-  int il[MCV_ANYSHAPE_MAX_FACES];
+  double tl[MCV_ANYSHAPE_MAX_FACES + 1];
+  int il[MCV_ANYSHAPE_MAX_FACES + 1];
   for (int nb = 0; nb < MCV_ANYSHAPE_MAX_BOUNCES; ++nb) {
     int ninter = 0;
     for (int f = 0; f < nf; ++f) {
@@ -611,7 +611,8 @@ static int guide_anyshape(neutron_t* n, const mcv_component* c) {
                     (g[2] - n->z) * g[11];
       double vn = n->vx * g[9] + n->vy * g[10] + n->vz * g[11];
       double t = dist / vn;
-      if (t > 0) ninter = insert_sorted_idx(f, t, il, tl, ninter, nf);
+      if (t > 0)
+        ninter = insert_sorted_idx(f, t, il, tl, ninter, MCV_ANYSHAPE_MAX_FACES + 1);
     }
     if (!ninter) return 0;
     int found = -1;
@@ -650,6 +651,108 @@ static int guide_anyshape(neutron_t* n, const mcv_component* c) {
     n->p = prob;
   }
   return 1;
+}
+
+/* intersect_plane of guide_anyshape_gravity.py:25-41: the roots of
+ * A t^2 + B t + C = 0, A = g.n / 2, B = v.n, C = r.n - c.n */
+static void gravity_roots(const double* r, const double* v, const double* g,
+                          const double* c, const double* nrm, double* out) {
+  double A = (g[0] * nrm[0] + g[1] * nrm[1] + g[2] * nrm[2]) / 2;
+  double B = v[0] * nrm[0] + v[1] * nrm[1] + v[2] * nrm[2];
+  double C = (r[0] * nrm[0] + r[1] * nrm[1] + r[2] * nrm[2]) -
+             (c[0] * nrm[0] + c[1] * nrm[1] + c[2] * nrm[2]);
+  if (fabs(A) < 1e-10) {
+    out[0] = -C / B;
+    out[1] = -1;
+    return;
+  }
+  double d = B * B - 4 * A * C;
+  if (d < 0) {
+    out[0] = out[1] = -1;
+    return;
+  }
+  double s = sqrt(d);
+  out[0] = (-B - s) / 2 / A;
+  out[1] = (-B + s) / 2 / A;
+}
+
+/* propagate_with_gravity (:43-55) */
+static void gravity_move(const double* r, const double* v, const double* g,
+                         double t, double* r2, double* v2) {
+  double tmp[3];
+  for (int k = 0; k < 3; ++k) v2[k] = v[k] + g[k] * t;
+  for (int k = 0; k < 3; ++k) tmp[k] = (v[k] + v2[k]) * (0.5 * t);
+  for (int k = 0; k < 3; ++k) r2[k] = r[k] + tmp[k];
+}
+
+/* Guide_anyshape_gravity._propagate (:57-182), in the reference's order:
+ * both positive roots of every face sorted, the first at or past 1e-10 s
+ * inside its face taken; then the carry to z = z_max (without advancing
+ * the time; the first root also when only the second is positive, as the
+ * reference has it) */
+static int guide_anyshape_gravity(neutron_t* n, const mcv_component* c) {
+  int nf = c->ip[0], nv = c->ip[1], stride = 12 + 2 * nv;
+  const double* F = (const double*)c->table;
+  double R0 = c->dp[0], Qc = c->dp[1], alpha = c->dp[2], m = c->dp[3],
+         W = c->dp[4];
+  double g[3] = {c->dp[5], c->dp[6], c->dp[7]}, zmax = c->dp[8];
+  double tl[MCV_ANYSHAPE_MAX_FACES + 1];
+  int il[MCV_ANYSHAPE_MAX_FACES + 1];
+  int overflow = 1;
+  for (int nb = 0; nb < MCV_ANYSHAPE_MAX_BOUNCES; ++nb) {
+    double r[3] = {n->x, n->y, n->z}, v[3] = {n->vx, n->vy, n->vz};
+    int ninter = 0;
+    for (int f = 0; f < nf; ++f) {
+      const double* gf = F + (size_t)f * stride;
+      double roots[2];
+      gravity_roots(r, v, g, gf, gf + 9, roots);
+      /* the reference's list holds 100 entries (max_numfaces, :240); a
+       * root that finds it full is dropped */
+      if (roots[0] > 0)
+        ninter = insert_sorted_idx(f, roots[0], il, tl, ninter, MCV_ANYSHAPE_MAX_FACES + 1);
+      if (roots[1] > 0)
+        ninter = insert_sorted_idx(f, roots[1], il, tl, ninter, MCV_ANYSHAPE_MAX_FACES + 1);
+    }
+    if (!ninter) { overflow = 0; break; }
+    int found = -1;
+    double t = 0, r2[3], v2[3];
+    for (int k = 0; k < ninter; ++k) {
+      const double* gf = F + (size_t)il[k] * stride;
+      t = tl[k];
+      gravity_move(r, v, g, t, r2, v2);
+      if (t < 1e-10) continue;
+      double q[3] = {r2[0] - gf[0], r2[1] - gf[1], r2[2] - gf[2]};
+      double u = q[0] * gf[3] + q[1] * gf[4] + q[2] * gf[5];
+      double w = q[0] * gf[6] + q[1] * gf[7] + q[2] * gf[8];
+      if (inside_convex_polygon(u, w, gf + 12, nv)) { found = il[k]; break; }
+    }
+    if (found < 0) { overflow = 0; break; }
+    const double* gf = F + (size_t)found * stride;
+    n->t += t;
+    n->x = r2[0]; n->y = r2[1]; n->z = r2[2];
+    n->vx = v2[0]; n->vy = v2[1]; n->vz = v2[2];
+    double vq = -(v2[0] * gf[9] + v2[1] * gf[10] + v2[2] * gf[11]) * 2;
+    double R = oracle_reflectivity(fabs(vq) * V2K, R0, Qc, alpha, m, W);
+    double prob = n->p * R;
+    if (prob <= 0) { n->p = -1; return 0; }
+    n->vx += gf[9] * vq;
+    n->vy += gf[10] * vq;
+    n->vz += gf[11] * vq;
+    n->p = prob;
+  }
+  if (n->z < zmax) {
+    double r[3] = {n->x, n->y, n->z}, v[3] = {n->vx, n->vy, n->vz};
+    double cz[3] = {0, 0, zmax}, nz[3] = {0, 0, 1}, roots[2], r2[3], v2[3];
+    gravity_roots(r, v, g, cz, nz, roots);
+    double t;
+    if (roots[0] > 0) t = roots[0];
+    else if (roots[1] > 0) t = roots[0];
+    else return overflow;
+    gravity_move(r, v, g, t, r2, v2);
+    n->x = r2[0]; n->y = r2[1]; n->z = r2[2];
+    n->vx = v2[0]; n->vy = v2[1]; n->vz = v2[2];
+  }
+  return overflow;
 }
 
 static int guide_tapering(neutron_t* n, const mcv_component* c) {
@@ -2189,7 +2292,8 @@ static void run_component(neutron_t* n, rng_t* rng, const mcv_component* c,
       st->bounce_overflow += guide_tapering(n, c);
       break;
     case MCV_OP_GUIDE_ANYSHAPE:
-      st->bounce_overflow += guide_anyshape(n, c);
+      st->bounce_overflow += (c->ip[2] & 1) ? guide_anyshape_gravity(n, c)
+                                            : guide_anyshape(n, c);
       break;
     case MCV_OP_HSS: hss(n, rng, c); break;
     case MCV_OP_PSD_MONITOR: psd_monitor(n, c, tl); break;
@@ -2459,7 +2563,8 @@ void oracle_kernel_scatter_one(const mcv_component* c, double* st,
 }
 /* The mesh guide on one neutron state; returns 1 at the bounce limit. */
 int oracle_anyshape_one(const mcv_component* c, double* st) {
-  return guide_anyshape((neutron_t*)st, c);
+  return (c->ip[2] & 1) ? guide_anyshape_gravity((neutron_t*)st, c)
+                        : guide_anyshape((neutron_t*)st, c);
 }
 void oracle_apply_transform(const double* rot, const double* off, double* st) {
   apply_transform((neutron_t*)st, rot, off);

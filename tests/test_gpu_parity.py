@@ -68,6 +68,8 @@ BUILDERS = {
     "dgssxres_box": instruments.dgssxres_box,
     "anyshape_guide_chain": lambda: instruments.anyshape_guide_chain(
         w2=0.04, h2=0.04),
+    "anyshape_gravity_chain": lambda: instruments.anyshape_guide_chain(
+        gravity=True),
     "verdi": instruments.verdi,
 }
 # every scattered neutron of the constant-(Q, E) box lands in one or two
@@ -97,7 +99,8 @@ SAME_STREAM_N = {"verdi": 200_000}
 #    where the reference backs off 1e-14, which is below float resolution).
 FP32_SAME_STREAM = [k for k in BUILDERS if k not in
                     ("sns_source_chain", "sts_source_chain", "verdi",
-                     "dgssxres_box", "anyshape_guide_chain")]
+                     "dgssxres_box", "anyshape_guide_chain",
+                     "anyshape_gravity_chain")]
 
 
 @pytest.fixture(scope="module", autouse=True)

@@ -141,3 +141,51 @@ def test_box_mesh_equals_the_plain_guide(oracle_lib, tmp_path, w2):
     else:
         same = np.all(np.isclose(pa, pb, rtol=1e-9, atol=1e-12), axis=1)
         assert (~same).mean() < 5e-3, (~same).sum()
+
+
+def test_gravity_one_face(oracle_lib, tmp_path):
+    """guide_anyshape_gravity.py with g = -9.8 m/s^2 along y: a neutron
+    0.01 m above the y = 0 face, falling at 1 m/s and moving 2000 m/s
+    along z, reaches it at t = 0.009552841750957684 s (the reference's
+    test_intersect, tests/components/optics/test_guide_anyshape_gravity.py
+    :12-27), reflects with R0 and is then carried along its parabola to
+    the mesh's largest z (1 m) without advancing its time."""
+    from acc_gb300.components.optics.guide_anyshape import \
+        Guide_anyshape_gravity
+    from oracle import binding as O
+    path = str(tmp_path / "face.off")
+    write_off(path, np.array([[-1, 0, -1], [-1, 0, 1], [1, 0, 1],
+                              [1, 0, -1]], dtype=float), [[0, 1, 2, 3]])
+    g = Guide_anyshape_gravity("g", geometry=path, gravity=(0, -9.8, 0))
+    comp = build_chain([g], binder=HostBinder()).comp[0]
+    st, over = O.anyshape_one(comp, [0, 0.01, -20, 0, -1, 2000, 0, 0, 0, 1])
+    t_hit = 0.009552841750957684
+    assert over == 0
+    np.testing.assert_allclose(st[8], t_hit, rtol=1e-12)
+    z_hit = -20 + 2000 * t_hit
+    vy = 1 + 9.8 * t_hit  # reflected
+    dt = (1 - z_hit) / 2000
+    np.testing.assert_allclose(
+        st, [0, vy * dt - 4.9 * dt * dt, 1, 0, vy - 9.8 * dt, 2000, 0, 0,
+             t_hit, 0.99], rtol=1e-9, atol=1e-13)
+
+
+def test_gravity_falls_back_onto_the_same_face(oracle_lib, tmp_path):
+    """Under gravity a neutron can hit the face it has just left: a slow
+    neutron bouncing along a long floor makes several reflections off the
+    one face, each at the parabola's apex spacing 2 vy / g."""
+    from acc_gb300.components.optics.guide_anyshape import \
+        Guide_anyshape_gravity
+    from oracle import binding as O
+    path = str(tmp_path / "floor.off")
+    write_off(path, np.array([[-1, 0, 0], [-1, 0, 10], [1, 0, 10],
+                              [1, 0, 0]], dtype=float), [[0, 1, 2, 3]])
+    g = Guide_anyshape_gravity("g", geometry=path, gravity=(0, -9.8, 0))
+    comp = build_chain([g], binder=HostBinder()).comp[0]
+    # starts on the floor plane's level going up 0.5 m/s, 10 m/s along z
+    st, over = O.anyshape_one(comp, [0, 1e-9, 0.0, 0, 0.5, 10.0, 0, 0, 0, 1])
+    period = 2 * 0.5 / 9.8
+    nref = int(10 / 10 / period)  # reflections within the 10 m floor
+    assert nref == 9
+    np.testing.assert_allclose(st[8], nref * period, rtol=1e-6)
+    np.testing.assert_allclose(st[9], 0.99 ** nref, rtol=1e-9)
