@@ -233,3 +233,20 @@ def test_chain_keeps_its_tables_alive():
     gc.collect()
     assert guide() is not None
     assert ch.comp[1].table != 0
+
+
+def test_isotropic_box_and_guide_aliases():
+    """IsotropicBox (isotropic_box.py) is the single scatterer on a box with
+    the isotropic kernel; guide_baseline / numpy_guide / oo_guide name the
+    straight guide."""
+    from acc_gb300.components.optics import guide, guide_baseline, \
+        numpy_guide, oo_guide
+    from acc_gb300.components.samples.isotropic_box import IsotropicBox
+    ch = build_chain([IsotropicBox("b", 0.02, 0.03, 0.004, 10.0, 20.0)],
+                     binder=HostBinder())
+    c = ch.comp[0]
+    assert c.opcode == nat.OP_HSS and c.ip[1] == nat.KERNEL_ISOTROPIC
+    assert c.ip[2] == nat.SHAPE_BOX
+    assert [c.dp[k] for k in (0, 1, 2, 8, 9)] == [0.02, 0.03, 0.004, 10.0, 20.0]
+    assert guide_baseline.Guide is numpy_guide.Guide is oo_guide.Guide is \
+        guide.Guide
