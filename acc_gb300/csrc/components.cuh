@@ -574,8 +574,9 @@ __device__ __forceinline__ int guide_tapering(Neutron<R>& n,
                                               const mcv_component& c) {
   const int nseg = c.ip[0];
   const R* d = taper_table<R>(c);
-  const R *w1 = d, *h1 = d + 2 * nseg, *ww = d + 4 * nseg, *hh = d + 5 * nseg,
-          *whalf = d + 6 * nseg, *hhalf = d + 7 * nseg;
+  const R *w1 = d, *w2 = d + nseg, *h1 = d + 2 * nseg, *h2 = d + 3 * nseg,
+          *ww = d + 4 * nseg, *hh = d + 5 * nseg, *whalf = d + 6 * nseg,
+          *hhalf = d + 7 * nseg;
   const R l_seg = prm<R>(c, 0), R0 = prm<R>(c, 1), Qcx = prm<R>(c, 2),
           Qcy = prm<R>(c, 3), alphax = prm<R>(c, 4), alphay = prm<R>(c, 5),
           mx = prm<R>(c, 6), my = prm<R>(c, 7), W = prm<R>(c, 8);
@@ -613,6 +614,17 @@ __device__ __forceinline__ int guide_tapering(Neutron<R>& n,
     }
     x -= (edge + R(0.5) * w1s);
     const R hadj = edge + (R(0.5) * w1s) - R(0.5) * w1s;
+    if constexpr (sizeof(R) == 4) {
+      // inside at the entrance and at the exit plane: a straight flight
+      // between two points inside the (planar) walls crosses none of them,
+      // so the bounce loop would leave at once; go to the next segment
+      const R tex = (zr + l_seg - z) / vz;
+      if (m_fabs(fmaf(vx, tex, x)) < R(0.5) * __ldg(&w2[seg]) &&
+          m_fabs(fmaf(vy, tex, y)) < R(0.5) * __ldg(&h2[seg])) {
+        x += hadj;
+        continue;
+      }
+    }
     int nb;
     for (nb = 0; nb < MCV_MAX_BOUNCES; ++nb) {
       const R av = l_seg * vx, bv = wws * vz, ah = l_seg * vy, bh = hhs * vz;
