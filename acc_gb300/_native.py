@@ -51,6 +51,7 @@ OP_SNS_SOURCE = 17
 OP_NEUTRON_STORAGE = 18
 OP_KERNEL_ELEMENT = 19
 OP_GUIDE_ANYSHAPE = 20
+OP_NEUTRON_TO_STORAGE = 21
 
 SHAPE_SPHERE, SHAPE_CYLINDER, SHAPE_BOX = 1, 2, 3
 CSG_PRIMITIVE, CSG_DIFFERENCE, CSG_UNION, CSG_INTERSECTION = 0, 1, 2, 3

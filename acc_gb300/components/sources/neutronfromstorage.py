@@ -12,15 +12,12 @@ category = 'sources'
 
 def load_neutrons(path):
     """An (N, 10) float64 array [x y z vx vy vz sx sy t p] from `path`: a
-    NumPy .npy file.  The mcni storage format (.mcv) is read by mcni's
-    neutron_storage, which this package does not include."""
+    neutron storage file (.mcv, read as neutronfromstorage.py:58-61 reads
+    it) or a NumPy .npy array."""
     if str(path).endswith(".npy"):
-        a = np.load(path)
-    else:
-        raise RuntimeError(
-            f"{path}: neutron storage files (.mcv) are read by mcni, which "
-            "is not installed; store the neutrons as an (N, 10) .npy array")
-    return a
+        return np.load(path)
+    from ...neutron_storage import load
+    return load(path)
 
 
 class NeutronFromStorage(SourceBase):
@@ -28,8 +25,9 @@ class NeutronFromStorage(SourceBase):
     requires_neutron_index_in_processing = True
 
     def __init__(self, name, path=None, neutrons=None):
-        """`path`: an (N, 10) .npy file of neutrons; or `neutrons`, the
-        array itself (x y z vx vy vz sx sy t p per row)."""
+        """`path`: a neutron storage file (.mcv) or an (N, 10) .npy array;
+        or `neutrons`, the array itself (x y z vx vy vz sx sy t p a
+        row)."""
         self.name = name
         if neutrons is None:
             neutrons = load_neutrons(path)

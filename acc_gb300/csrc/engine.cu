@@ -189,6 +189,14 @@ int validate_component(const mcv_component& c, int k, mcv_status* st) {
         return MCV_EINVAL;
       }
       break;
+    case MCV_OP_NEUTRON_TO_STORAGE:
+      if (!c.tally || c.table_len < 1) {
+        set_msg(st, MCV_EINVAL,
+                "component %s%lld: neutron storage needs a buffer of >= 1 "
+                "rows", "", (long long)k);
+        return MCV_EINVAL;
+      }
+      break;
     case MCV_OP_NEUTRON_STORAGE:
       if (!c.table || !c.ftable || c.table_len < 10 || c.table_len % 10) {
         set_msg(st, MCV_EINVAL,
@@ -310,14 +318,14 @@ bool has_hms(const mcv_chain* ch) {
 
 // The rarer components run in their own kernel instantiations (kX): the
 // SNS source, the tapered and mesh guides, the multiple scatterer, stored
-// neutrons, and samples with the constant-(Q, E), E(Q), composite, SANS2D
+// neutrons in or out, and samples with the constant-(Q, E), E(Q), composite, SANS2D
 // or DGSSXRes kernel.
 bool is_exotic(const mcv_chain* ch) {
   for (int k = 0; k < ch->ncomp; ++k) {
     const int op = ch->comp[k].opcode;
     if (op == MCV_OP_HMS || op == MCV_OP_SNS_SOURCE ||
         op == MCV_OP_GUIDE_TAPERING || op == MCV_OP_NEUTRON_STORAGE ||
-        op == MCV_OP_GUIDE_ANYSHAPE)
+        op == MCV_OP_GUIDE_ANYSHAPE || op == MCV_OP_NEUTRON_TO_STORAGE)
       return true;
     if ((op == MCV_OP_HSS || op == MCV_OP_KERNEL_ELEMENT) &&
         (ch->comp[k].ip[1] == MCV_KERNEL_CONSTANT_QE ||

@@ -88,6 +88,9 @@ __device__ __forceinline__ int run_component(Neutron<R>& n, Rng& rng,
         if constexpr (sizeof(R) == 4) n.p *= weight_up<R>(ch);
       }
       return 0;
+    case MCV_OP_NEUTRON_TO_STORAGE:
+      if constexpr (kX) neutron_to_storage<R>(n, rng.index(), c, tl.down);
+      return 0;
     case MCV_OP_SNS_SOURCE:
       if constexpr (kX) {
         sns_source<R>(n, rng, c);

@@ -4,6 +4,8 @@
 // "inside" tests so that a NaN coordinate is never binned.
 #pragma once
 
+#include <cooperative_groups.h>
+
 #include "common.cuh"
 #include "sample.cuh"
 #include "track.cuh"
@@ -245,6 +247,40 @@ __device__ __forceinline__ void banked(Neutron<R>& n, const mcv_component& c,
   int it = bin_of(tt, tmin, tmax, ntof);
   uint64_t bin = (((uint64_t)b * ntube + tube) * npix + pix) * ntof + it;
   trk.tally(tl, bin, n.p);
+}
+
+// Save the neutron as it reaches the component (the NeutronToStorage
+// monitor of mcvine, which acc/test/instrument_factory.py:104-113 places
+// before and after a component): one row of 11 64-bit words -- the
+// neutron's index, then x y z vx vy vz sx sy t p in float64 -- at a slot
+// that the lanes arriving together reserve with one atomic on word 0.
+// Slots past the capacity (table_len rows) are counted but not written.
+// `wdown` undoes the FP32 kernels' weight scale.
+template <typename R>
+__device__ __forceinline__ void neutron_to_storage(const Neutron<R>& n,
+                                                   uint64_t index,
+                                                   const mcv_component& c,
+                                                   double wdown) {
+  namespace cg = cooperative_groups;
+  auto* words = reinterpret_cast<unsigned long long*>(c.tally);
+  cg::coalesced_group g = cg::coalesced_threads();
+  unsigned long long base = 0;
+  if (g.thread_rank() == 0) base = atomicAdd(words, (unsigned long long)g.size());
+  base = g.shfl(base, 0);
+  const unsigned long long slot = base + g.thread_rank();
+  if (slot >= c.table_len) return;
+  double* row = c.tally + 1 + 11 * slot;
+  words[1 + 11 * slot] = index;
+  row[1] = (double)n.x;
+  row[2] = (double)n.y;
+  row[3] = (double)n.z;
+  row[4] = (double)n.vx;
+  row[5] = (double)n.vy;
+  row[6] = (double)n.vz;
+  row[7] = (double)n.sx;
+  row[8] = (double)n.sy;
+  row[9] = n.t.dval();
+  row[10] = (double)n.p * wdown;
 }
 
 }  // namespace mcv

@@ -15,6 +15,8 @@ un_ms              500 meV beam -> UN cylinder, multiple scattering with a
 verdi              the VERDI instrument (SNS source, elliptic guides)
 sans2d_grid        10 A beam -> thin Al plate with S(Qx, Qy) on a 1475 x
                    1100 grid -> PSD 10 m downstream
+saved_guide_chain  guide_chain saving the neutrons at the guide exit (.mcv);
+                   guide_exit_replay replays them onto the same monitors
 
 Numbers that the workload descriptions leave open are fixed here once
 (source distance, gaps between components, detector heights, number
@@ -291,6 +293,32 @@ def storage_chain(neutrons=None):
                position=(0, 0, 0))
     ins.append(sample("sample"), position=(0, 0, 1.0))
     ins.append(mon, position=(0, 0, 1.0))
+    return ins
+
+
+def saved_guide_chain(path="after_guide2.mcv", capacity=None):
+    """guide_chain with a NeutronToStorage at the guide's exit plane, where
+    the reference's instrument factory saves `after_<component>.mcv`
+    (acc/test/instrument_factory.py:109-113)."""
+    from .components.monitors.neutron_to_storage import NeutronToStorage
+    return guide_chain(extra=[NeutronToStorage("after_guide2", path=path,
+                                               capacity=capacity)])
+
+
+def guide_exit_replay(neutrons):
+    """Neutrons saved at the guide exit (saved_guide_chain; a .mcv path or
+    an (N, 10) array) replayed onto guide_chain's PSD and energy monitors,
+    in the same frame."""
+    from .components.sources.neutronfromstorage import NeutronFromStorage
+    src = (NeutronFromStorage("src", path=neutrons)
+           if isinstance(neutrons, (str, os.PathLike))
+           else NeutronFromStorage("src", neutrons=neutrons))
+    ref = guide_chain()
+    psd, emon = ref.components[3], ref.components[4]
+    ins = instrument("guide_exit_replay")
+    ins.append(src, position=(0, 0, 0))
+    ins.append(psd, position=(0, 0, 0))
+    ins.append(emon, position=(0, 0, 0))
     return ins
 
 

@@ -32,6 +32,18 @@ class DeviceBinder:
             comp._device_tally = t
         return t.data_ptr()
 
+    def buffer(self, comp, key, n):
+        """A zeroed float64 device buffer of `n` values, kept on `comp` (a
+        component's output that is not a histogram); reused while its size
+        holds."""
+        import torch
+        cache = comp.__dict__.setdefault("_device_buffers", {})
+        t = cache.get(key)
+        if t is None or t.numel() != n or t.device != self.device:
+            t = torch.zeros(int(n), dtype=torch.float64, device=self.device)
+            cache[key] = t
+        return t.data_ptr()
+
     def table(self, comp, key, array, dtype):
         import torch
         cache = comp.__dict__.setdefault("_device_tables", {})
@@ -50,7 +62,16 @@ class HostBinder:
 
     def __init__(self):
         self.tallies = {}
+        self.buffers = {}
         self._tables = {}
+
+    def buffer(self, comp, key, n):
+        k = (id(comp), key)
+        a = self.buffers.get(k)
+        if a is None or a.size != n:
+            a = np.zeros(int(n))
+            self.buffers[k] = a
+        return a.ctypes.data
 
     def tally(self, comp, nbins):
         a = self.tallies.get(id(comp))

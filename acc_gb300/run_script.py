@@ -42,6 +42,9 @@ def run(script, workdir, ncount, overwrite_datafiles=True, ntotalthreads=None,
         if not isinstance(comp, ComponentBase):
             raise AssertionError(f"{comp} is not a mcvine.acc component")
     _write_description(instrument, compiled)
+    for comp in instrument.components:
+        if hasattr(comp, "expect_neutrons"):
+            comp.expect_neutrons(ncount)
     chain = engine.chain_for_instrument(instrument)
     tpb = threads_per_block or config.threads_per_block
     st = engine.run_chain(chain, ncount, seed=seed, floattype=floattype,
@@ -102,7 +105,8 @@ def _jsonable(x):
 def saveMonitorOutputs(instrument, scale_factor=1.0):
     from .components.monitors.MonitorBase import MonitorBase
     for comp in instrument.components:
-        if isinstance(comp, MonitorBase):
+        if isinstance(comp, MonitorBase) or getattr(comp, "saves_neutrons",
+                                                    False):
             comp.save(scale_factor=scale_factor)
 
 

@@ -90,7 +90,10 @@ enum {
                                    (acc/kernels/composite.py): not run */
   MCV_OP_GUIDE_ANYSHAPE = 20,   /* acc/components/optics/guide_anyshape.py,
                                    guide_anyshape_gravity.py */
-  MCV_OP_COUNT = 21
+  MCV_OP_NEUTRON_TO_STORAGE = 21, /* mcvine's NeutronToStorage monitor, as
+                                   acc/test/instrument_factory.py:104-113
+                                   places it: saves the neutrons that reach it */
+  MCV_OP_COUNT = 22
 };
 
 /* ---- shapes of the homogeneous scatterer (acc/geometry/arrow_intersect.py)
@@ -246,6 +249,13 @@ enum {
  *   dp 8 z_max (the mesh's largest z)
  * SLIT / BEAMSTOP (slit.py:20-108, beamstop.py:18-112)
  *                                dp: xmin xmax ymin ymax radius^2 cut
+ * NEUTRON_TO_STORAGE: every neutron that reaches it is saved, unchanged
+ *   and in the component's frame, into `tally`, read as 64-bit words:
+ *   word 0 counts the neutrons that reached it (also past the capacity),
+ *   then table_len (the capacity, >= 1) rows of 11 words: the neutron's
+ *   index in the run (uint64), then x y z vx vy vz sx sy t p (float64; the
+ *   FP32 kernels store p without their 2^weight_exp2 scale).  Rows are
+ *   written in no fixed order; the host sorts them by index.
  *
  * Every monitor tallies into `tally`: float64 [3][n0][n1] holding
  * (N, sum p, sum p^2) per bin, the `out` array of psd_monitor.py:61-65.

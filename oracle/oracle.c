@@ -2287,6 +2287,19 @@ static void run_component(neutron_t* n, rng_t* rng, const mcv_component* c,
       memcpy(n, (const double*)c->table + (idx % N) * 10, sizeof *n);
       break;
     }
+    case MCV_OP_NEUTRON_TO_STORAGE: {
+      /* mcvine's NeutronToStorage (placed by
+         acc/test/instrument_factory.py:104-113): the neutron as it arrives,
+         in this component's frame, one row [index, 10 values] a neutron */
+      uint64_t* words = (uint64_t*)c->tally;
+      uint64_t slot = __atomic_fetch_add(&words[0], 1, __ATOMIC_RELAXED);
+      if (slot < c->table_len) {
+        words[1 + 11 * slot] =
+            (uint64_t)rng->ctr[0] | ((uint64_t)rng->ctr[1] << 32);
+        memcpy(c->tally + 2 + 11 * slot, n, 10 * sizeof(double));
+      }
+      break;
+    }
     case MCV_OP_GUIDE: st->bounce_overflow += guide(n, c, NULL); break;
     case MCV_OP_GUIDE_TAPERING:
       st->bounce_overflow += guide_tapering(n, c);
