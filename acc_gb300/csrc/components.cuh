@@ -614,13 +614,22 @@ __device__ __forceinline__ int guide_tapering(Neutron<R>& n,
     }
     x -= (edge + R(0.5) * w1s);
     const R hadj = edge + (R(0.5) * w1s) - R(0.5) * w1s;
-    if constexpr (sizeof(R) == 4) {
-      // inside at the entrance and at the exit plane: a straight flight
-      // between two points inside the (planar) walls crosses none of them,
-      // so the bounce loop would leave at once; go to the next segment
+    if (vz > R(0)) {
+      // inside at the entrance and at the exit plane: a straight forward
+      // flight between two points inside the (planar) walls crosses none
+      // of them, so the bounce loop would leave at once without moving
+      // the neutron; go to the next segment with the same state
       const R tex = (zr + l_seg - z) / vz;
-      if (m_fabs(fmaf(vx, tex, x)) < R(0.5) * __ldg(&w2[seg]) &&
-          m_fabs(fmaf(vy, tex, y)) < R(0.5) * __ldg(&h2[seg])) {
+      R xe, ye;
+      if constexpr (sizeof(R) == 4) {
+        xe = fmaf(vx, tex, x);
+        ye = fmaf(vy, tex, y);
+      } else {
+        xe = x + vx * tex;
+        ye = y + vy * tex;
+      }
+      if (m_fabs(xe) < R(0.5) * __ldg(&w2[seg]) &&
+          m_fabs(ye) < R(0.5) * __ldg(&h2[seg])) {
         x += hadj;
         continue;
       }
