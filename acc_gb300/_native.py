@@ -25,6 +25,7 @@ MCV_EXPR_STACK = 8
 MCV_EXPR_MAX_OPS = 256
 MCV_SNS_E_NODES = 4096
 MCV_SNS_T_NODES = 512
+MCV_SNS_TAIL_MAX = 65536
 MCV_NOALLOC_MAX_VARIANTS = 64
 
 MCV_OK, MCV_EINVAL, MCV_ECUDA, MCV_ECOUNT, MCV_EBOUNCE = 0, 1, 2, 3, 4

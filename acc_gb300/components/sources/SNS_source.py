@@ -235,9 +235,17 @@ def zero_find(vecx, vecy, yval, xmin, xmax, tol, rows=None):
     return rtb
 
 
+# an FP32 kernel's uniform is k * 2^-24, k < 2^24 (PhiloxStream::next)
+UNIFORM_STEPS = 1 << 24
+# at most this many tail energies (float32) a source
+SNS_TAIL_MAX = nat.MCV_SNS_TAIL_MAX
+
+
 def fp32_tables(Es, Pvec, ts, Ptmat, EPmin, EPmax, Eidx, tidx):
-    """(ftable float32 array, u_lo, u_hi): the inverse tables the FP32
-    kernels sample (layout in include/acc_gb300.h, SNS_SOURCE)."""
+    """(ftable float32 array, u_lo, u_hi, n_lo, n_hi): the inverse tables
+    the FP32 kernels sample (layout in include/acc_gb300.h, SNS_SOURCE);
+    n_lo and n_hi count the tail energies of the draws below u_lo and
+    above u_hi."""
     Es = np.asarray(Es, dtype=np.float64)
     ts = np.asarray(ts, dtype=np.float64)
     Pvec = np.asarray(Pvec, dtype=np.float64)
@@ -270,8 +278,21 @@ def fp32_tables(Es, Pvec, ts, Ptmat, EPmin, EPmax, Eidx, tidx):
     rows = np.repeat(np.arange(nE), SNS_T_NODES + 1)
     targ = (Ptmat[rows, t0] + np.tile(ut, nE) * mass[rows])
     Tinv = zero_find(ts, Ptmat, targ, ts[t0], ts[t1], 1e-5, rows=rows)
-    ftab = np.concatenate([Einv, Es, np.maximum(mass, 0.0), Tinv])
-    return ftab.astype(np.float32), float(u_lo), float(u_hi)
+    # the draws outside [u_lo, u_hi]: an FP32 uniform is k * 2^-24, so
+    # each such draw is one of a few thousand k, whose energies zero_find
+    # gives here once (the kernels index them by k instead of running the
+    # FP64 sampler); none when there are too many
+    lo_k = np.arange(int(np.ceil(u_lo * UNIFORM_STEPS)), dtype=np.float64)
+    first_hi = int(np.floor(u_hi * UNIFORM_STEPS)) + 1
+    hi_k = np.arange(first_hi, UNIFORM_STEPS, dtype=np.float64)
+    if len(lo_k) + len(hi_k) > SNS_TAIL_MAX:
+        lo_k, hi_k = lo_k[:0], hi_k[:0]
+    uk = np.concatenate([lo_k, hi_k]) / UNIFORM_STEPS
+    Etail = zero_find(Es, Pvec, EPmin + uk * (EPmax - EPmin), xmin, xmax,
+                      1e-7) if len(uk) else uk
+    ftab = np.concatenate([Einv, Es, np.maximum(mass, 0.0), Tinv, Etail])
+    return (ftab.astype(np.float32), float(u_lo), float(u_hi), len(lo_k),
+            len(hi_k))
 
 
 class SNS_source(SourceBase):
@@ -330,10 +351,12 @@ class SNS_source(SourceBase):
             self._fp32 = fp32_tables(Es, Pvec, ts, Ptmat, EPmin, EPmax,
                                      (Eidx_start, Eidx_stop),
                                      (tidx_start, tidx_stop))
-        ftab, u_lo, u_hi = self._fp32
+        ftab, u_lo, u_hi, n_lo, n_hi = self._fp32
         c.ftable = binder.table(self, "moderator_f32", ftab, np.float32)
         set_param(c, 16, u_lo)
         set_param(c, 17, u_hi)
+        set_param(c, 18, n_lo)
+        set_param(c, 19, n_hi)
         self.pack_geometry(c)
 
     def pack_geometry(self, c):

@@ -242,16 +242,32 @@ __device__ __forceinline__ bool sns_generate_f32(const mcv_component& c,
                                                  float randE, float randt,
                                                  double* Eout,
                                                  double* tout) {
-  if (!c.ftable || !(randE >= c.fp[16] && randE <= c.fp[17])) return false;
+  if (!c.ftable) return false;
   const int nE = c.ip[1];
   const float* Einv = c.ftable;
   const float* Es = Einv + (MCV_SNS_E_NODES + 1);
   const float* mass = Es + nE;
   const float* Tinv = mass + nE;
-  const float s = randE * float(MCV_SNS_E_NODES);
-  const int k = min((int)s, MCV_SNS_E_NODES - 1);
-  const float e0 = __ldg(&Einv[k]);
-  const float E = fmaf(s - float(k), __ldg(&Einv[k + 1]) - e0, e0);
+  float E;
+  if (randE >= c.fp[16] && randE <= c.fp[17]) {
+    const float s = randE * float(MCV_SNS_E_NODES);
+    const int k = min((int)s, MCV_SNS_E_NODES - 1);
+    const float e0 = __ldg(&Einv[k]);
+    E = fmaf(s - float(k), __ldg(&Einv[k + 1]) - e0, e0);
+  } else {
+    // outside the regular range: the draw is u = k 2^-24, and the host
+    // tabulated zero_find's energy for each such k
+    const float* Etail = Tinv + (size_t)nE * (MCV_SNS_T_NODES + 1);
+    const int k = (int)(randE * 16777216.f);
+    const int nlo = (int)c.fp[18], nhi = (int)c.fp[19];
+    if (k < nlo) {
+      E = __ldg(&Etail[k]);
+    } else if (k >= (1 << 24) - nhi && k < (1 << 24)) {
+      E = __ldg(&Etail[nlo + k - ((1 << 24) - nhi)]);
+    } else {
+      return false;
+    }
+  }
   int lo = 0, hi = nE;  // first row with !(Es < E)
   while (lo < hi) {
     const int mid = (lo + hi) >> 1;

@@ -212,11 +212,16 @@ int validate_component(const mcv_component& c, int k, mcv_status* st) {
                                          (uint64_t)nE * nt &&
                       c.ip[3] >= 1 && c.ip[3] < nE && c.ip[4] >= 1 &&
                       c.ip[4] < nE && c.ip[5] >= 0 && c.ip[6] >= 1 &&
-                      c.ip[6] <= nt && c.ip[5] < c.ip[6] && c.dp[5] > 0;
+                      c.ip[6] <= nt && c.ip[5] < c.ip[6] && c.dp[5] > 0 &&
+                      c.dp[18] >= 0 && c.dp[19] >= 0 &&
+                      c.dp[18] + c.dp[19] <= MCV_SNS_TAIL_MAX &&
+                      c.dp[18] == floor(c.dp[18]) &&
+                      c.dp[19] == floor(c.dp[19]);
       if (!ok) {
         set_msg(st, MCV_EINVAL,
                 "component %s%lld: SNS source needs its E / t tables "
-                "(>= 3 points each) and index ranges inside them",
+                "(>= 3 points each), index ranges inside them and at most "
+                "MCV_SNS_TAIL_MAX tail energies",
                 "", (long long)k);
         return MCV_EINVAL;
       }
@@ -369,13 +374,31 @@ void launch_shape(const mcv_ctx* ctx, Occ occupancy, uint64_t n,
   *threads = t;
 }
 
+// kX chains whose time goes into sample kernels or the multiple
+// scatterer (and not into a tapered or mesh guide's loops): these run the
+// kDense instantiation (FP32, Philox mode), measured faster for them and
+// slower for the guide-heavy chains.
+bool dense_kx_chain(const mcv_chain* ch) {
+  bool samples = false;
+  for (int k = 0; k < ch->ncomp; ++k) {
+    const mcv_component& c = ch->comp[k];
+    if (c.opcode == MCV_OP_GUIDE_TAPERING || c.opcode == MCV_OP_GUIDE_ANYSHAPE)
+      return false;
+    if (c.opcode == MCV_OP_HMS) samples = true;
+    if (c.opcode == MCV_OP_HSS && c.ip[1] != MCV_KERNEL_ISOTROPIC &&
+        c.ip[1] != MCV_KERNEL_POWDER && c.ip[1] != MCV_KERNEL_SQE_GRID)
+      samples = true;
+  }
+  return samples;
+}
+
 template <typename R>
 int launch_chain(mcv_ctx* ctx, int mode, const mcv_chain* chain,
                  uint64_t ncount, uint64_t first, uint64_t seed,
                  const float* uni, int stride, double* out_n, int* out_last,
                  const mcv_launch* launch, cudaStream_t s) {
   int blocks, threads;
-  const bool x = is_exotic(chain);
+  const int x = is_exotic(chain) ? (dense_kx_chain(chain) ? 2 : 1) : 0;
   launch_shape(
       ctx,
       [mode, x](int t) { return Launchers<R>::occupancy_chain(mode, x, t); },

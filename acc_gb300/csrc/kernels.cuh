@@ -244,8 +244,12 @@ constexpr int kMaxThreads = 256;
 
 // MODE 0: Philox; 1: Philox + record; 2: injected uniforms + record.
 // kX: the instantiation with the rarer components (run_component).
-template <typename R, int MODE, bool kX = false>
-__global__ void __launch_bounds__(kMaxThreads)
+// kDense: the same kX code held to 4 blocks of 256 threads an SM (64
+// registers, some spills), which pays for chains whose time goes into
+// sample kernels and the multiple scatterer (latency-bound at 3 blocks)
+// and loses for the long guide loops; the host picks (dense_kx_chain).
+template <typename R, int MODE, bool kX = false, bool kDense = false>
+__global__ void __launch_bounds__(kMaxThreads, kDense ? 4 : 0)
     chain_kernel(const __grid_constant__ mcv_chain ch, uint64_t n,
                  uint64_t first, uint64_t seed, const float* __restrict__ uni,
                  int stride, double* __restrict__ out_n,
@@ -697,9 +701,11 @@ namespace mcv {
 // Host-side launchers of the kernels above for one working precision.
 template <typename R>
 struct Launchers {
-  // x: the chain holds one of the rarer components (kX instantiations)
-  static int occupancy_chain(int mode, bool x, int threads);
-  static void chain(int mode, bool x, int blocks, int threads,
+  // x: 0 the common kernels; 1 the chain holds one of the rarer
+  // components (kX instantiations); 2 kX with 4 blocks an SM (kDense,
+  // FP32 mode 0; other modes and FP64 take 1)
+  static int occupancy_chain(int mode, int x, int threads);
+  static void chain(int mode, int x, int blocks, int threads,
                     cudaStream_t s, const mcv_chain& ch, uint64_t n,
                     uint64_t first, uint64_t seed, const float* uni,
                     int stride, double* out_n, int* out_last, DevStatus* st);
@@ -752,7 +758,11 @@ void powder_finalize(const double* px, const double* py, int npeaks,
 
 #ifdef MCV_DEFINE_LAUNCHERS
 template <typename R>
-int Launchers<R>::occupancy_chain(int mode, bool x, int threads) {
+int Launchers<R>::occupancy_chain(int mode, int x, int threads) {
+  if constexpr (sizeof(R) == 4) {
+    if (x == 2 && mode == 0)
+      return occupancy_of(chain_kernel<R, 0, true, true>, threads, 0);
+  }
   if (x) {
     if (mode == 0) return occupancy_of(chain_kernel<R, 0, true>, threads, 0);
     if (mode == 1) return occupancy_of(chain_kernel<R, 1, true>, threads, 0);
@@ -764,11 +774,18 @@ int Launchers<R>::occupancy_chain(int mode, bool x, int threads) {
 }
 
 template <typename R>
-void Launchers<R>::chain(int mode, bool x, int blocks, int threads,
+void Launchers<R>::chain(int mode, int x, int blocks, int threads,
                          cudaStream_t s, const mcv_chain& ch, uint64_t n,
                          uint64_t first, uint64_t seed, const float* uni,
                          int stride, double* out_n, int* out_last,
                          DevStatus* st) {
+  if constexpr (sizeof(R) == 4) {
+    if (x == 2 && mode == 0) {
+      chain_kernel<R, 0, true, true><<<blocks, threads, 0, s>>>(
+          ch, n, first, seed, uni, stride, out_n, out_last, st);
+      return;
+    }
+  }
 #define MCV_CHAIN_LAUNCH(M, X)                                              \
   chain_kernel<R, M, X><<<blocks, threads, 0, s>>>(ch, n, first, seed, uni, \
                                                    stride, out_n, out_last, \

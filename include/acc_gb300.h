@@ -51,6 +51,7 @@ extern "C" {
                                      inverse table of E                */
 #define MCV_SNS_T_NODES 512       /* intervals of each energy row's FP32
                                      inverse table of t                */
+#define MCV_SNS_TAIL_MAX 65536    /* SNS source: most FP32 tail energies */
 
 /* ---- error codes ---------------------------------------------------- */
 enum {
@@ -228,8 +229,12 @@ enum {
  *   evenly spaced u, the same zero_find run on the host), Es[nE],
  *   mass[nE] (each row's probability in the t window), then
  *   t_inv[nE][MCV_SNS_T_NODES + 1] (us, evenly spaced u over each row's
- *   window); a draw of u outside [dp 16, dp 17] (u_lo, u_hi: where
- *   zero_find's bracket leaves the table) takes the FP64 sampler.
+ *   window), then Etail[dp 18 + dp 19] (eV): a draw u = k 2^-24 below
+ *   dp 16 (u_lo: where zero_find's bracket leaves the table) takes
+ *   Etail[k] (k < dp 18), one above dp 17 (u_hi) Etail[dp 18 + k -
+ *   (2^24 - dp 19)], both zero_find's energies from the host; other draws
+ *   outside [u_lo, u_hi] take the FP64 sampler.  dp 18 + dp 19 <=
+ *   MCV_SNS_TAIL_MAX.
  *   STS_source (STS_source.py:107-284): ip[7] bit 0 set, bit 1 = dmode;
  *   dp: 9 tanMOa 10 cylx 11 cylz 12 cylphi1 13 cylphi2 14 MRadius0
  *       15 MOffangle (rad): the face point lies on the cylindrical

@@ -10,7 +10,8 @@ by the two-row mixture, follows the oracle's distribution at fixed E
 (Kolmogorov-Smirnov distance below 0.02 over 20000 draws each, about 2.8
 standard errors); the regular range is the whole unit interval for a
 window inside the table and starts above the draws whose bracket leaves
-the table (VERDI's 0.1-1000 meV)."""
+the table (VERDI's 0.1-1000 meV), whose energies the host tabulates per
+FP32 draw."""
 
 import os
 import warnings
@@ -37,7 +38,7 @@ def _source(path, Emin, Emax):
         warnings.simplefilter("ignore")
         src = SNS_source("m", path, Emin, Emax, 0.03, 0.03, 6.2, 0.1, 0.1)
     comp = build_chain([src], binder=HostBinder()).comp[0]
-    ftab, u_lo, u_hi = src._fp32
+    ftab, u_lo, u_hi, _, _ = src._fp32
     return src, comp, ftab.astype(np.float64), u_lo, u_hi
 
 
@@ -47,7 +48,8 @@ def _lookup(ftab, nE, randE, randt):
     Einv = ftab[:NE + 1]
     Es = ftab[NE + 1:NE + 1 + nE]
     mass = ftab[NE + 1 + nE:NE + 1 + 2 * nE]
-    Tinv = ftab[NE + 1 + 2 * nE:].reshape(nE, NT + 1)
+    Tinv = ftab[NE + 1 + 2 * nE:NE + 1 + 2 * nE + nE * (NT + 1)].reshape(
+        nE, NT + 1)
     s = randE * NE
     k = min(int(s), NE - 1)
     E = Einv[k] + (s - k) * (Einv[k + 1] - Einv[k])
@@ -80,7 +82,7 @@ def test_energy_table_follows_zero_find(oracle_lib, moderator):
 def test_regular_range_excludes_the_wandering_draws(oracle_lib, moderator):
     """VERDI's window: below u_lo the reference's bracket expands past the
     table (energies far above it, test_oracle_kats.py); the FP32 kernels
-    send those draws to the FP64 sampler.  Above u_lo the table holds."""
+    look those draws up by k (tail table).  Above u_lo the table holds."""
     from oracle import binding as O
     src, comp, ftab, u_lo, u_hi = _source(moderator, 0.1, 1000.0)
     assert 0.0 < u_lo < 0.01 and u_hi == 1.0
@@ -91,6 +93,25 @@ def test_regular_range_excludes_the_wandering_draws(oracle_lib, moderator):
         E_tab, _ = _lookup(ftab, comp.ip[1], u, 0.5)
         E_ref, _ = O.sns_generate(comp, u, 0.5)
         assert abs(E_tab - E_ref) <= 2e-4 * E_ref, (u, E_tab, E_ref)
+
+
+def test_tail_energies_are_zero_finds_at_each_draw(oracle_lib, moderator):
+    """Below u_lo every FP32 draw u = k 2^-24 has its own tail entry,
+    zero_find's energy at that u (float32-rounded)."""
+    from oracle import binding as O
+    src, comp, ftab, u_lo, u_hi = _source(moderator, 0.1, 1000.0)
+    _, _, _, n_lo, n_hi = src._fp32
+    assert n_lo == int(np.ceil(u_lo * 2 ** 24)) > 0 and n_hi == 0
+    assert (comp.dp[18], comp.dp[19]) == (n_lo, n_hi)
+    nE, NE, NT = comp.ip[1], nat.MCV_SNS_E_NODES, nat.MCV_SNS_T_NODES
+    tail = ftab[NE + 1 + 2 * nE + nE * (NT + 1):]
+    assert len(tail) == n_lo
+    for k in list(range(0, n_lo, 997)) + [n_lo - 1]:
+        E_ref, _ = O.sns_generate(comp, k / 2 ** 24, 0.5)
+        assert abs(tail[k] * 1000.0 - E_ref) <= 1e-6 * E_ref, (k, E_ref)
+    # a window inside the table needs no tail
+    src2, comp2, _, _, _ = _source(moderator, 5.0, 20.0)
+    assert src2._fp32[3:] == (0, 0) and comp2.dp[18] == comp2.dp[19] == 0
 
 
 @pytest.mark.parametrize("randE", [0.05, 0.3, 0.62, 0.97])
