@@ -250,3 +250,42 @@ def test_isotropic_box_and_guide_aliases():
     assert [c.dp[k] for k in (0, 1, 2, 8, 9)] == [0.02, 0.03, 0.004, 10.0, 20.0]
     assert guide_baseline.Guide is numpy_guide.Guide is oo_guide.Guide is \
         guide.Guide
+
+
+# every component module of the reference's acc/components that an
+# instrument script imports, with the name it takes from it
+REFERENCE_COMPONENTS = [
+    ("monitors.iqe_monitor", "IQE_monitor"),
+    ("monitors.posdiv_monitor", "PosDiv_monitor"),
+    ("monitors.psd_monitor", "PSD_monitor"),
+    ("monitors.psd_monitor_4pi", "PSD_monitor_4Pi"),
+    ("monitors.wavelength_monitor", "Wavelength_monitor"),
+    ("optics.arm", "Arm"),
+    ("optics.beamstop", "Beamstop"),
+    ("optics.guide", "Guide"),
+    ("optics.guide_anyshape", "Guide_anyshape"),
+    ("optics.guide_anyshape_gravity", "Guide_anyshape_gravity"),
+    ("optics.guide_baseline", "Guide"),
+    ("optics.guide_tapering", "Guide"),
+    ("optics.numpy_guide", "Guide"),
+    ("optics.oo_guide", "Guide"),
+    ("optics.slit", "Slit"),
+    ("samples.homogeneous_multiple_scatterer", "factory"),
+    ("samples.homogeneous_single_scatterer", "factory"),
+    ("samples.isotropic_box", "IsotropicBox"),
+    ("sources.SNS_source", "SNS_source"),
+    ("sources.STS_source", "STS_source"),
+    ("sources.neutronfromstorage", "NeutronFromStorage"),
+    ("sources.source_simple", "Source_simple"),
+]
+
+
+@pytest.mark.parametrize("module,name", REFERENCE_COMPONENTS)
+def test_reference_component_paths_import(module, name):
+    import importlib
+    from acc_gb300 import compat
+    compat.install_mcvine_alias(force=True)
+    m = importlib.import_module("mcvine.acc.components." + module)
+    assert callable(getattr(m, name))
+    assert getattr(m, "category", module.split(".")[0]) == \
+        module.split(".")[0]
