@@ -183,3 +183,37 @@ def test_gpu_save_then_replay_reproduces_the_monitors(tmp_path):
         np.testing.assert_array_equal(a.out[0], b.out[0])
         np.testing.assert_allclose(a.out[1:], b.out[1:], rtol=1e-12,
                                    atol=0)
+
+
+def _ms_saved(capacity):
+    """The multiple-scattering test instrument with its outputs saved at
+    the 4pi monitor's position: several rows share an incident neutron's
+    index."""
+    from acc_gb300.instruments import ms_hollow_cylinder
+    ins = ms_hollow_cylinder()
+    ins.append(NeutronToStorage("after_sample", capacity=capacity),
+               position=(0, 0, 2.0))
+    return ins
+
+
+def test_oracle_saves_every_output_of_a_multiple_scatterer():
+    (idx, saved, reached), _, _, _ = _oracle_saved(_ms_saved(200000), 5000)
+    assert reached == len(saved) > 5000
+    counts = np.bincount(idx.astype(np.int64))
+    assert counts.max() > 1  # fan-out: rows share an index
+    assert np.all(np.diff(idx.astype(np.int64)) >= 0)
+
+
+@pytest.mark.gpu
+def test_gpu_multiple_scatterer_outputs_match_the_oracle():
+    """FP64: the same rows (index, then values) as the oracle, to 1e-12."""
+    from acc_gb300 import engine
+    from helpers import rel_err
+    n = 20000
+    (oidx, osaved, oreached), _, _, _ = _oracle_saved(_ms_saved(500000), n)
+    ins = _ms_saved(500000)
+    engine.run_instrument(ins, n, seed=5, floattype="float64")
+    idx, saved, reached = ins.components[-1].stored()
+    assert reached == oreached == len(saved)
+    np.testing.assert_array_equal(idx, oidx)
+    assert rel_err(saved, osaved).max() < 1e-12
