@@ -217,3 +217,27 @@ def test_gpu_multiple_scatterer_outputs_match_the_oracle():
     assert reached == oreached == len(saved)
     np.testing.assert_array_equal(idx, oidx)
     assert rel_err(saved, osaved).max() < 1e-12
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("floattype", ["float64", "float32"])
+def test_gpu_buffered_process_saves_its_input(floattype):
+    """ComponentBase.process (the buffered mode) on a NeutronToStorage:
+    it passes the neutrons through and saves each under its index."""
+    from acc_gb300 import engine
+    from acc_gb300.components import ComponentBase as CB
+    from acc_gb300.instruments import stored_neutrons
+    a = stored_neutrons(n=3001)
+    st = NeutronToStorage("st", capacity=4000)
+    old = CB.ComponentBase._floattype
+    CB.change_floattype(floattype)
+    try:
+        out = st.process(a)
+    finally:
+        CB.change_floattype(old)
+    idx, saved, reached = st.stored()
+    assert reached == len(saved) == len(a)
+    np.testing.assert_array_equal(idx, np.arange(len(a)))
+    tol = 1e-15 if floattype == "float64" else 1e-6
+    np.testing.assert_allclose(saved, a, rtol=tol, atol=tol * 1e-3)
+    np.testing.assert_allclose(out, a, rtol=tol, atol=tol * 1e-3)
