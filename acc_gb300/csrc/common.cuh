@@ -189,6 +189,15 @@ __device__ __forceinline__ const double* chain_off<double>(const mcv_chain& ch,
 // ------------------------------------------------------------ math
 __device__ __forceinline__ float m_sqrt(float x) { return sqrtf(x); }
 __device__ __forceinline__ double m_sqrt(double x) { return sqrt(x); }
+// square root of a uniform: the reference applies math.sqrt to the float32
+// that xoroshiro128p_uniform_float32 returns (the disc sources,
+// source_simple.py:139, SNS_source.py:177, STS_source.py:257), which Numba
+// types and evaluates as a float32 square root (correctly rounded); the
+// FP64 kernels take the same float32 root of the same 24-bit uniform
+__device__ __forceinline__ float m_sqrt_uniform(float u) { return sqrtf(u); }
+__device__ __forceinline__ double m_sqrt_uniform(double u) {
+  return double(__fsqrt_rn(float(u)));
+}
 __device__ __forceinline__ float m_rsqrt(float x) { return rsqrtf(x); }
 __device__ __forceinline__ double m_rsqrt(double x) { return 1.0 / sqrt(x); }
 __device__ __forceinline__ float m_exp(float x) { return __expf(x); }

@@ -32,7 +32,7 @@ __device__ __forceinline__ void source_simple(Neutron<R>& n, Rng& rng,
     x = width * (r1 - R(0.5));
     y = height * (r2 - R(0.5));
   } else {
-    R r = m_sqrt(r2) * radius, s, co;
+    R r = m_sqrt_uniform(r2) * radius, s, co;
     m_sincos_2pi(r1, &s, &co);
     x = r * co;
     y = r * s;
@@ -329,7 +329,7 @@ __device__ __forceinline__ void sns_source(Neutron<R>& n, Rng& rng,
     } else {
       R s, co;
       m_sincos_2pi(randx, &s, &co);
-      const R r = m_sqrt(randy) * radius;
+      const R r = m_sqrt_uniform(randy) * radius;
       x = r * co;
       y = r * s;
       z = tanMOa * x;
@@ -340,7 +340,7 @@ __device__ __forceinline__ void sns_source(Neutron<R>& n, Rng& rng,
   } else {
     R s, co;
     m_sincos_2pi(randx, &s, &co);
-    const R r = m_sqrt(randy) * radius;
+    const R r = m_sqrt_uniform(randy) * radius;
     x = r * co;
     y = r * s;
   }

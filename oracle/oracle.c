@@ -231,7 +231,8 @@ static void source_simple(neutron_t* n, rng_t* rng, const mcv_component* c) {
     y = height * (r2 - 0.5);
   } else {
     double chi = 2 * M_PI * r1;
-    double r = sqrt(r2) * radius;
+    /* math.sqrt of a float32 uniform: a float32 root under Numba */
+    double r = (double)sqrtf((float)r2) * radius;
     x = r * cos(chi);
     y = r * sin(chi);
   }
@@ -394,7 +395,8 @@ static void sns_source(neutron_t* n, rng_t* rng, const mcv_component* c) {
         x = cylx + MR * sin(ang);
       }
     } else {
-      double chi = 2.0 * M_PI * randx, r = sqrt(randy) * radius;
+      double chi = 2.0 * M_PI * randx,
+           r = (double)sqrtf((float)randy) * radius;
       x = r * cos(chi);
       y = r * sin(chi);
       z = tanMOa * x;
@@ -403,7 +405,8 @@ static void sns_source(neutron_t* n, rng_t* rng, const mcv_component* c) {
     x = xwidth * (randx - 0.5);
     y = yheight * (randy - 0.5);
   } else {
-    double chi = 2 * M_PI * randx, r = sqrt(randy) * radius;
+    double chi = 2 * M_PI * randx,
+           r = (double)sqrtf((float)randy) * radius;
     x = r * cos(chi);
     y = r * sin(chi);
   }
