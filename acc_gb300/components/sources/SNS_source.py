@@ -9,6 +9,7 @@ for every energy, P(t) are integrated from quadratic interpolants
 (mcv_component layout: include/acc_gb300.h, SNS_SOURCE).
 """
 
+import gzip
 import math
 import warnings
 
@@ -50,9 +51,11 @@ def sns_source_load(filename, xcol=0, ycol=2, sts=False):
     blank line; section 2 holds one block per energy of rows (t in us, E,
     brightness, error), blocks separated by blank lines, '#' lines are
     comments.  Returns (E, I(E), veclen, t, I[E][t]), and the STS
-    parameters first when `sts` (the file then opens with section 0)."""
+    parameters first when `sts` (the file then opens with section 0).  A
+    name ending in .gz is read through gzip."""
     params = None
-    with open(filename, "rt") as stream:
+    opener = gzip.open if str(filename).endswith(".gz") else open
+    with opener(filename, "rt") as stream:
         if sts:
             params = sts_params_load(stream)
         first_block = []
@@ -239,6 +242,9 @@ def zero_find(vecx, vecy, yval, xmin, xmax, tol, rows=None):
 UNIFORM_STEPS = 1 << 24
 # at most this many tail energies (float32) a source
 SNS_TAIL_MAX = nat.MCV_SNS_TAIL_MAX
+# largest relative error of the FP32 energy table's linear interpolation at
+# an interval's midpoint; coarser end intervals take per-draw tail energies
+SNS_INTERP_TOL = 2e-5
 
 
 def fp32_tables(Es, Pvec, ts, Ptmat, EPmin, EPmax, Eidx, tidx):
@@ -269,6 +275,21 @@ def fp32_tables(Es, Pvec, ts, Ptmat, EPmin, EPmax, Eidx, tidx):
                 best, lo, hi = kk - start, start, kk - 1
             start = kk
     if best >= 2:
+        # intervals at the ends of the range whose linear interpolation
+        # misses zero_find's energy at their midpoint by more than
+        # SNS_INTERP_TOL (the inverse spectrum bends sharply at its ends,
+        # e.g. VERDI's 0.1 meV lower limit) go to the per-draw tail table
+        # while it has room
+        um = (u[lo:hi] + u[lo + 1:hi + 1]) / 2
+        Em = zero_find(Es, Pvec, EPmin + um * (EPmax - EPmin), xmin, xmax,
+                       1e-7)
+        bad = (np.abs((Einv[lo:hi] + Einv[lo + 1:hi + 1]) / 2 - Em)
+               > SNS_INTERP_TOL * np.abs(Em))
+        room = SNS_TAIL_MAX // (UNIFORM_STEPS // SNS_E_NODES) - 1
+        while room > 0 and hi - lo > 2 and bad[0]:
+            lo, bad, room = lo + 1, bad[1:], room - 1
+        while room > 0 and hi - lo > 2 and bad[-1]:
+            hi, bad, room = hi - 1, bad[:-1], room - 1
         u_lo, u_hi = u[lo], u[hi]
     else:
         u_lo, u_hi = 1.0, 0.0  # every draw takes the FP64 sampler
@@ -282,11 +303,13 @@ def fp32_tables(Es, Pvec, ts, Ptmat, EPmin, EPmax, Eidx, tidx):
     # each such draw is one of a few thousand k, whose energies zero_find
     # gives here once (the kernels index them by k instead of running the
     # FP64 sampler); none when there are too many
-    lo_k = np.arange(int(np.ceil(u_lo * UNIFORM_STEPS)), dtype=np.float64)
+    n_lo = int(np.ceil(u_lo * UNIFORM_STEPS))
     first_hi = int(np.floor(u_hi * UNIFORM_STEPS)) + 1
-    hi_k = np.arange(first_hi, UNIFORM_STEPS, dtype=np.float64)
-    if len(lo_k) + len(hi_k) > SNS_TAIL_MAX:
-        lo_k, hi_k = lo_k[:0], hi_k[:0]
+    n_hi = max(0, UNIFORM_STEPS - first_hi)
+    if n_lo + n_hi > SNS_TAIL_MAX:
+        n_lo = n_hi = 0
+    lo_k = np.arange(n_lo, dtype=np.float64)
+    hi_k = np.arange(first_hi, first_hi + n_hi, dtype=np.float64)
     uk = np.concatenate([lo_k, hi_k]) / UNIFORM_STEPS
     Etail = zero_find(Es, Pvec, EPmin + uk * (EPmax - EPmin), xmin, xmax,
                       1e-7) if len(uk) else uk

@@ -48,6 +48,24 @@ from .kernels import (CompositeKernel, ConstantQEKernel, DGSSXResKernel,
 
 COATING = dict(R0=0.99, Qc=0.0219, alpha=3.0, m=3.0, W=0.003)
 
+# the moderator files of the reference's tests
+# (tests/components/sources), shipped gzip-compressed in acc_gb300/data
+DATA = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data")
+SNS_MODERATOR = "source_rot2_cdr_cyl_3x3_20190417.dat"
+STS_MODERATOR = "BL20-CY-123D-STS-Min-2G-source_mctal-195_sp.dat"
+
+
+def shipped_moderator(name):
+    """Path of a moderator file shipped with the package (SNS_MODERATOR:
+    the SNS moderator VERDI reads, VERDI_base.py:17; STS_MODERATOR: the
+    cylindrical STS moderator of test_STS_source.py)."""
+    path = os.path.join(DATA, name + ".gz")
+    if not os.path.exists(path):
+        raise FileNotFoundError(
+            f"{path} is missing: acc_gb300/data/copy_moderators.py copies "
+            "it from the mcvine/acc source tree")
+    return path
+
 
 def sphere_theta_tof(ntheta=180, ntof=200):
     """Disc source (r = 5 cm) aimed at a 1 x 1 cm target 5 m away, E uniform
@@ -224,13 +242,14 @@ def synthetic_moderator_file(path=None, nE=60, nt=50, sts=False):
 
 def sns_source_chain(filename=None, Emin=5., Emax=20.):
     """An SNS moderator source (3 x 3 cm face, energies Emin-Emax meV from
-    `filename`, a synthetic moderator file when None) aimed at a 3 x 3 cm
+    `filename`) aimed at a 3 x 3 cm
     window 5 m away, where a PSD (100 x 100 over +-3 cm) and an energy
     monitor (100 bins over 0-25 meV) sit: the reference's SNS source test
-    set-up (tests/components/sources/test_SNS_source.py:12-15)."""
+    set-up (tests/components/sources/test_SNS_source.py:12-15), on the
+    reference's SNS moderator file when `filename` is None."""
     from .components.sources.SNS_source import SNS_source
     if filename is None:
-        filename = synthetic_moderator_file()
+        filename = shipped_moderator(SNS_MODERATOR)
     ins = instrument("sns_source_chain")
     src = SNS_source("src", filename, Emin, Emax, 0.03, 0.03, 5., .03, .03)
     psd = PSD_monitor("psd", xmin=-0.03, xmax=0.03, ymin=-0.03, ymax=0.03,
@@ -246,10 +265,11 @@ def sns_source_chain(filename=None, Emin=5., Emax=20.):
 
 def sts_source_chain(filename=None, Emin=5., Emax=20., dmode=1.0):
     """An STS moderator source (the sns_source_chain set-up on the
-    cylindrical moderator of a synthetic STS file)."""
+    cylindrical moderator of an STS file; the reference's STS file when
+    `filename` is None)."""
     from .components.sources.SNS_source import STS_source
     if filename is None:
-        filename = synthetic_moderator_file(sts=True)
+        filename = shipped_moderator(STS_MODERATOR)
     ins = instrument("sts_source_chain")
     src = STS_source("src", filename, Emin, Emax, 0.03, 0.03, 5., .03, .03,
                      dmode=dmode)
@@ -518,8 +538,8 @@ def verdi(moderator_file=None, guide_mvalue=6., sample_width=0.005,
     slit -> sample mask, with wavelength, position-divergence and PSD
     monitors along the way (26 components, 4 of them arms).
 
-    `moderator_file`: a moderator file in the SNS format; a synthetic one
-    of the reference file's size (141 energies x 160 times) when None."""
+    `moderator_file`: a moderator file in the SNS format; VERDI's own
+    (source_rot2_cdr_cyl_3x3_20190417.dat, VERDI_base.py:17) when None."""
     from .components.monitors.posdiv_monitor import PosDiv_monitor
     from .components.monitors.wavelength_monitor import Wavelength_monitor
     from .components.optics.arm import Arm
@@ -528,7 +548,7 @@ def verdi(moderator_file=None, guide_mvalue=6., sample_width=0.005,
     from .components.optics.slit import Slit
     from .components.sources.SNS_source import SNS_source
     if moderator_file is None:
-        moderator_file = synthetic_moderator_file(nE=141, nt=160)
+        moderator_file = shipped_moderator(SNS_MODERATOR)
     # first mirror and its shield (VERDI_base.py:37-49)
     a1, b1 = ellipse1_minor_axis_len / 2, ellipse1_major_axis_len / 2
     shield1_x, shield1_z = shield_vertex(

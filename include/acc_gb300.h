@@ -230,11 +230,14 @@ enum {
  *   mass[nE] (each row's probability in the t window), then
  *   t_inv[nE][MCV_SNS_T_NODES + 1] (us, evenly spaced u over each row's
  *   window), then Etail[dp 18 + dp 19] (eV): a draw u = k 2^-24 below
- *   dp 16 (u_lo: where zero_find's bracket leaves the table) takes
- *   Etail[k] (k < dp 18), one above dp 17 (u_hi) Etail[dp 18 + k -
- *   (2^24 - dp 19)], both zero_find's energies from the host; other draws
- *   outside [u_lo, u_hi] take the FP64 sampler.  dp 18 + dp 19 <=
- *   MCV_SNS_TAIL_MAX.
+ *   dp 16 (u_lo: where zero_find's bracket leaves the table, or where the
+ *   linear interpolation of E_inv would be coarse) takes Etail[k]
+ *   (k < dp 18), one above dp 17 (u_hi) Etail[dp 18 + k - (2^24 -
+ *   dp 19)], both zero_find's energies from the host; other draws outside
+ *   [u_lo, u_hi] take the FP64 sampler.  dp 18 + dp 19 <=
+ *   MCV_SNS_TAIL_MAX.  ftable must hold (MCV_SNS_E_NODES + 1) + 2 nE +
+ *   nE (MCV_SNS_T_NODES + 1) + dp 18 + dp 19 floats: the library has no
+ *   length for it and cannot check it.
  *   STS_source (STS_source.py:107-284): ip[7] bit 0 set, bit 1 = dmode;
  *   dp: 9 tanMOa 10 cylx 11 cylz 12 cylphi1 13 cylphi2 14 MRadius0
  *       15 MOffangle (rad): the face point lies on the cylindrical

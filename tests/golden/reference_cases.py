@@ -40,6 +40,18 @@ AL_PEAKS = [dict(q=1.9200, F_squared=0.0, multiplicity=12,
                  intrinsic_line_width=0, DebyeWaller_factor=0)]
 AL_XS = dict(coh=4 * 1.495, inc=4 * 0.0082, abs=4 * 0.231)
 
+# the reference's moderator files (tests/components/sources), shipped
+# gzip-compressed in acc_gb300/data
+SNS_FILE = "source_rot2_cdr_cyl_3x3_20190417.dat"
+STS_FILE = "BL20-CY-123D-STS-Min-2G-source_mctal-195_sp.dat"
+
+
+def moderator_path(name):
+    """The package's copy of a reference moderator file."""
+    from acc_gb300.instruments import shipped_moderator
+    return shipped_moderator(name)
+
+
 GUIDE_COATING = dict(R0=0.99, Qc=0.0219, alpha=3.0, m=3.0, W=0.003)
 
 CASES = {
@@ -103,6 +115,27 @@ CASES = {
         kind="hss", n=256, nu=4, inputs=("along_z", 0.012, 0.012, 60.0),
         shape=("sphere", 0.01),
         kernel=dict(kind="constant_qe", Q=3.0, E=30.0, mu=2.0, sigma=8.0)),
+    # SNS / STS moderator sources (acc/components/sources/SNS_source.py,
+    # STS_source.py) on the reference's moderator files: the arguments of
+    # tests/components/sources/test_SNS_source.py:12 and
+    # test_STS_source.py:28, VERDI's energy window (VERDI_base.py:32), and
+    # a disc face
+    "sns_source_test": dict(
+        kind="sns_source", n=256, nu=6, file=SNS_FILE,
+        kw=dict(Emin=5, Emax=20, xwidth=0.03, yheight=0.03, dist=5,
+                focus_xw=.03, focus_yh=.03)),
+    "sns_source_verdi_window": dict(
+        kind="sns_source", n=256, nu=6, file=SNS_FILE,
+        kw=dict(Emin=0.1, Emax=1000., xwidth=0.03, yheight=0.03, dist=6.35,
+                focus_xw=0.04, focus_yh=0.04)),
+    "sns_source_disc": dict(
+        kind="sns_source", n=256, nu=6, file=SNS_FILE,
+        kw=dict(Emin=3, Emax=60, xwidth=0, yheight=0, dist=2.0,
+                focus_xw=0.02, focus_yh=0.05, radius=0.02)),
+    "sts_source_test": dict(
+        kind="sts_source", n=256, nu=6, file=STS_FILE,
+        kw=dict(Emin=3, Emax=82, xwidth=0.03, yheight=0.03, dist=2.5,
+                focus_xw=.03, focus_yh=.03)),
     # monitors (acc/components/monitors)
     "psd_monitor": dict(
         kind="psd_monitor", n=256, nu=1, inputs="plane",
@@ -222,6 +255,14 @@ def build_product(name):
     if kind == "source":
         from acc_gb300.components.sources.source_simple import Source_simple
         return Source_simple(name, **case["kw"])
+    if kind in ("sns_source", "sts_source"):
+        import warnings
+        from acc_gb300.components.sources.SNS_source import (SNS_source,
+                                                             STS_source)
+        cls = SNS_source if kind == "sns_source" else STS_source
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            return cls(name, moderator_path(case["file"]), **case["kw"])
     if kind == "guide":
         from acc_gb300.components.optics.guide import Guide
         return Guide(name, **case["kw"])

@@ -93,7 +93,47 @@ def sample_inputs(builder):
     return transform(source_output(builder), rot[0], off[0]), ins
 
 
+def powder_inputs():
+    """N neutrons crossing config 5's powder cylinder (local frame: axis z,
+    radius 5 mm, height 4 cm) along x, E 5-100 meV."""
+    from acc_gb300.conversion import SE2V
+    rng = np.random.default_rng(17)
+    a = np.zeros((N, 10))
+    a[:, 0] = -0.02
+    a[:, 1] = rng.uniform(-0.0055, 0.0055, N)
+    a[:, 2] = rng.uniform(-0.021, 0.021, N)
+    v = SE2V * np.sqrt(rng.uniform(5.0, 100.0, N))
+    d = np.stack([np.ones(N), rng.normal(0, 0.01, N), rng.normal(0, 0.01, N)],
+                 1)
+    a[:, 3:6] = v[:, None] * d / np.linalg.norm(d, axis=1, keepdims=True)
+    a[:, 8] = 0.01
+    a[:, 9] = 1.0
+    return a
+
+
+def banked_inputs():
+    """N neutrons leaving the sample position in all directions with a
+    tof of 1-15 ms, for the banked detector."""
+    from acc_gb300.conversion import SE2V
+    rng = np.random.default_rng(18)
+    a = np.zeros((N, 10))
+    a[:, :3] = rng.normal(0, 0.003, (N, 3))
+    d = rng.normal(0, 1, (N, 3))
+    v = SE2V * np.sqrt(rng.uniform(5.0, 100.0, N))
+    a[:, 3:6] = v[:, None] * d / np.linalg.norm(d, axis=1, keepdims=True)
+    a[:, 8] = rng.uniform(1e-3, 1.5e-2, N)
+    a[:, 9] = 1.0
+    return a
+
+
+def _powder_comp(k):
+    return instruments.powder_banked(ntubes=16, npixels=16, ntof=50) \
+        .components[k]
+
+
 CASES = {
+    "hss_cylinder_powder": (lambda: _powder_comp(5), powder_inputs),
+    "banked_detector": (lambda: _powder_comp(6), banked_inputs),
     "source_disc": (lambda: instruments.guide_chain().components[0],
                     lambda: np.zeros((N, 10))),
     "guide_straight": (lambda: instruments.guide_chain().components[1],

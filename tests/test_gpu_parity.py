@@ -4,6 +4,15 @@ Tolerances (stated per test):
  * FP64 kernels, same Philox stream or injected uniforms: every slot of
    every neutron within 1e-12 relative (denominator floored at the slot's
    RMS over the batch), identical exit component, identical bin counts.
+   The powder chains (CHORD_CONDITIONED) hold the weight of at most 1e-3
+   of their neutrons (at least two) to 1e-6 instead, and their bin sums to
+   1e-12 in 99% of the populated bins and 1e-8 in the rest: a neutron that
+   grazes the 5 mm powder cylinder has a chord 2 sqrt(k)/a whose
+   discriminant k = b^2 - a c cancels, so the last-bit differences between
+   the host's and the device's sin/cos/exp upstream (the source's sin/cos
+   of its disc angle, the guides' tanh) grow into the path length, and
+   the weight is p L exp(-mu L).  Each component on its own holds 1e-12
+   (test_gpu_components.py, test_reference_paths.py).
  * FP32 kernels against the FP64 oracle on the same stream, whole chain:
    of the neutrons that leave the chain alive with a weight above 1e-30 (in
    either run), at most 1e-3 beyond 1e-4 relative, and at most 1e-4 of them
@@ -34,26 +43,55 @@ from helpers import chi2_per_dof, gpu_tallies, oracle_run, rel_err
 
 pytestmark = pytest.mark.gpu
 
-_MODERATOR = []
-
-
 def _sns_source_chain():
-    # one synthetic moderator file for the session
-    if not _MODERATOR:
-        _MODERATOR.append(instruments.synthetic_moderator_file())
-        _MODERATOR.append(instruments.synthetic_moderator_file(sts=True))
-    return instruments.sns_source_chain(_MODERATOR[0])
+    """The reference's SNS source test set-up on its moderator file
+    (tests/components/sources/test_SNS_source.py:12)."""
+    return instruments.sns_source_chain()
 
 
 def _sts_source_chain():
+    """The same on the reference's STS moderator file."""
     import warnings
-    _sns_source_chain()
     with warnings.catch_warnings():
         warnings.simplefilter("ignore")
-        return instruments.sts_source_chain(_MODERATOR[1])
+        return instruments.sts_source_chain()
+
+
+def _powder_banked_small():
+    """Config 5's forward chain (guide chain -> powder cylinder -> banked
+    detector) with a coarser detector: 8 banks x 4 tubes x 8 pixels x 25
+    tof bins."""
+    return instruments.powder_banked(ntubes=4, npixels=8, ntof=25)
+
+
+def _powder_direct():
+    """Config 5's powder cylinder and banked detector (8 banks x 2 tubes x
+    4 pixels x 25 tof bins) fed straight by a disc source 1 m upstream
+    (E 5-100 meV), so that most neutrons reach the sample."""
+    import acc_gb300
+    from acc_gb300.components.sources.source_simple import Source_simple
+    from acc_gb300.components.monitors.cylinder_detectors import \
+        BankedCylinder_detector
+    from acc_gb300.geometry import Cylinder
+    from acc_gb300.kernels import SimplePowderDiffractionKernel
+    ker = SimplePowderDiffractionKernel(instruments.powder_peaks(), 66.4,
+                                        absorption_cross_section=0.23,
+                                        coherent_cross_section=1.5)
+    HSS = factory(Cylinder(0.005, 0.04), ker)
+    ins = acc_gb300.instrument()
+    ins.append(Source_simple("src", radius=0.005, dist=1.0, xw=0.008,
+                             yh=0.03, E0=52.5, dE=47.5), position=(0, 0, 0))
+    ins.append(HSS("sample"), position=(0, 0, 1.0), orientation=(90, 0, 0))
+    ins.append(BankedCylinder_detector(
+        "banked", radius=3.0, height=1.0, nbanks=8, ntubes=2, npixels=4,
+        bank_angle0=10.0, bank_width=15.0, bank_gap=5.0, tofmin=0.0,
+        tofmax=0.02, ntof=25, filename="banked.h5"), position=(0, 0, 1.0))
+    return ins
 
 
 BUILDERS = {
+    "powder_banked": _powder_banked_small,
+    "powder_direct": _powder_direct,
     "sphere_theta_tof": instruments.sphere_theta_tof,
     "guide_chain": instruments.guide_chain,
     "sqe_hollow_cylinder": instruments.sqe_hollow_cylinder,
@@ -77,9 +115,15 @@ BUILDERS = {
 # neutron in test_gpu_qe_kernels.py)
 # and VERDI's sample monitors see 0.7% of the neutrons over up to 250000
 # bins (test_verdi_fp32_chi2 below)
-CHI2_BUILDERS = [k for k in BUILDERS if k not in ("constant_qe_box", "verdi")]
-# neutrons of the same-stream tests (VERDI: enough to reach its sample)
-SAME_STREAM_N = {"verdi": 200_000}
+# the powder chain through the guides detects 6e-4 of its neutrons: its
+# detector is chi^2-tested on powder_direct (its guides and monitors are
+# guide_chain's)
+CHI2_BUILDERS = [k for k in BUILDERS
+                 if k not in ("constant_qe_box", "verdi", "powder_banked")]
+CHI2_N = {"powder_direct": 10_000_000}
+# neutrons of the same-stream tests (VERDI and the powder chain: enough to
+# reach their samples)
+SAME_STREAM_N = {"verdi": 200_000, "powder_banked": 200_000}
 # Not held to the FP32 same-stream bounds (their FP32 check is chi^2; FP64
 # runs the same-stream test at 1e-12):
 #  * the SNS and STS sources: FP32 draws E and t from inverse tables, t by
@@ -97,10 +141,15 @@ SAME_STREAM_N = {"verdi": 200_000}
 #    turns on rounding, and float rounds differently from the reference's
 #    double for 0.5% of the neutrons (FP32 skips the face it just left
 #    where the reference backs off 1e-14, which is below float resolution).
+#  * the powder chain through the guides: a 16.5 m flight leaves float
+#    positions ~1e-6 m off, against a 5 mm sample whose grazing chords
+#    amplify it (its FP32 check is powder_direct's, same stream and chi^2).
 FP32_SAME_STREAM = [k for k in BUILDERS if k not in
                     ("sns_source_chain", "sts_source_chain", "verdi",
                      "dgssxres_box", "anyshape_guide_chain",
-                     "anyshape_gravity_chain")]
+                     "anyshape_gravity_chain", "powder_banked")]
+# chains whose weights are conditioned by grazing chords (module docstring)
+CHORD_CONDITIONED = ("powder_banked", "powder_direct")
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -126,6 +175,11 @@ def test_fp64_same_stream_matches_oracle(name):
     assert stats["processed"] == n
     np.testing.assert_array_equal(g_last, o_last)
     err = rel_err(g_out, o_out)
+    if name in CHORD_CONDITIONED:
+        w = err[:, 9]
+        assert (w > 1e-12).sum() <= max(2, 1e-3 * n), (name, np.sort(w)[-5:])
+        assert w.max() <= 1e-6, (name, w.max())
+        err = err[:, :9]
     assert err.max() <= 1e-12, (name, err.max(), np.unravel_index(
         err.argmax(), err.shape))
 
@@ -142,8 +196,15 @@ def test_fp64_histograms_match_oracle(name):
     for (gc, g), (oc, o) in zip(gt.items(), ot.items()):
         assert gc.name == oc.name
         np.testing.assert_array_equal(g[0], o[0])
-        np.testing.assert_allclose(g[1], o[1], rtol=1e-12, atol=1e-300)
-        np.testing.assert_allclose(g[2], o[2], rtol=1e-12, atol=1e-300)
+        if name in CHORD_CONDITIONED:
+            for k in (1, 2):
+                pop = o[0] > 0
+                rel = np.abs(g[k] - o[k])[pop] / np.abs(o[k])[pop]
+                assert (rel > 1e-12).mean() <= 0.01, (gc.name, k)
+                assert rel.max() <= 1e-8, (gc.name, k, rel.max())
+        else:
+            np.testing.assert_allclose(g[1], o[1], rtol=1e-12, atol=1e-300)
+            np.testing.assert_allclose(g[2], o[2], rtol=1e-12, atol=1e-300)
         assert g[0].sum() > 0
 
 
@@ -177,7 +238,7 @@ def test_fp32_same_stream_within_1e4(name):
 
 @pytest.mark.parametrize("name", CHI2_BUILDERS)
 def test_fp32_independent_stream_chi2(name):
-    n = 1_000_000
+    n = CHI2_N.get(name, 1_000_000)
     ins = BUILDERS[name]()
     engine.run_instrument(ins, n, seed=101, floattype="float32")
     gt = gpu_tallies(ins)

@@ -310,22 +310,19 @@ def test_sns_energy_beyond_the_table_takes_the_last_time_row(oracle_lib):
 
 @pytest.mark.parametrize("dmode", [1.0, 0.0])
 def test_sts_source_face_points_on_the_moderator_cylinder(oracle_lib, dmode):
-    """STS_source.propagate (STS_source.py:242-259): on a square port the
-    emission point lies on the cylindrical moderator of radius MRadius
-    around (cylx, cylz), for the flat-projection (dmode 1) and the
-    flat-area (dmode 0) distributions; y spans the port height."""
+    """STS_source.propagate (STS_source.py:242-259) on the reference's STS
+    moderator file: on a square port the emission point lies on the
+    cylindrical moderator of radius MRadius around (cylx, cylz), for the
+    flat-projection (dmode 1) and the flat-area (dmode 0) distributions; y
+    spans the port height."""
     import warnings
     from acc_gb300 import instruments
     from acc_gb300.engine import build_chain
     from acc_gb300.memory import HostBinder
     from oracle import binding as O
-    path = instruments.synthetic_moderator_file(sts=True)
-    try:
-        with warnings.catch_warnings():
-            warnings.simplefilter("ignore")
-            src = instruments.sts_source_chain(path, dmode=dmode).components[0]
-    finally:
-        os.remove(path)
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        src = instruments.sts_source_chain(dmode=dmode).components[0]
     _, out, _ = O.run_chain(build_chain([src], binder=HostBinder()), 4000,
                             seed=3, record=True)
     r = np.hypot(out[:, 0] - src.cylx, out[:, 2] - src.cylz)
@@ -349,3 +346,36 @@ def test_stored_neutrons_replay_by_index(oracle_lib):
     _, out, _ = O.run_chain(ch, 350, seed=1, first=7, record=True)
     idx = (7 + np.arange(350)) % 101
     np.testing.assert_array_equal(out, stored[idx])
+
+
+def test_load_sts_source_file():
+    """test_load_sts_source (tests/components/sources/test_STS_source.py
+    :12-25) on the reference's STS moderator file: seven parameters
+    [700, 15, 0.04105, 5.5, 0.03, 0.03, 0], and energy tables two entries
+    longer than the veclen the loader reports, one pulse shape per energy
+    over the time vector."""
+    from acc_gb300 import instruments
+    from acc_gb300.components.sources.SNS_source import sns_source_load
+    path = instruments.shipped_moderator(instruments.STS_MODERATOR)
+    x, y, xylen, tvec, mat, params = sns_source_load(path, sts=True)
+    assert len(x) == xylen + 2
+    assert len(y) == xylen + 2
+    assert mat.shape[0] == xylen + 2
+    assert mat.shape[1] == len(tvec)
+    assert len(params) == 7
+    np.testing.assert_array_equal(
+        params, np.array([700.0, 15.0, 0.04105, 5.5, 0.03, 0.03, 0.0]))
+
+
+def test_load_sns_source_file():
+    """The SNS moderator file VERDI reads (VERDI_base.py:17): 141 energies
+    from 1e-5 eV, one pulse shape of 160 times per energy, the spectrum
+    positive on the tabulated range the loader keeps."""
+    from acc_gb300 import instruments
+    from acc_gb300.components.sources.SNS_source import sns_source_load
+    path = instruments.shipped_moderator(instruments.SNS_MODERATOR)
+    x, y, xylen, tvec, mat = sns_source_load(path)
+    assert mat.shape == (len(x), len(tvec)) == (141, 160)
+    assert x[0] == 1e-5 and len(x) == xylen + 2
+    assert np.all(np.diff(x) > 0) and np.all(np.diff(tvec) > 0)
+    assert (y[:xylen] > 0).all()
