@@ -16,13 +16,15 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libacc_gb300.so")
 
-SOURCES = ["engine.cu", "launch_fp32.cu", "launch_fp64.cu", "probe.cu",
-           "noalloc.cu"]
+SOURCES = ["engine.cu", "launch_fp32.cu", "launch_fp64.cu",
+           "launch_fp64_fma.cu", "probe.cu", "noalloc.cu"]
 HEADERS = ["common.cuh", "components.cuh", "sample.cuh", "monitors.cuh",
            "kernels.cuh", "ms.cuh", "track.cuh"]
 # per-source extra flags: the FP64 kernels round every multiply and add
-# separately, like the CPU restatement they are checked against
-EXTRA_FLAGS = {"launch_fp64.cu": ["--fmad=false"]}
+# separately, like the CPU restatement they are checked against; the
+# contracted FP64 chain kernel lives in a namespace of its own
+EXTRA_FLAGS = {"launch_fp64.cu": ["--fmad=false"],
+               "launch_fp64_fma.cu": ["-Dmcv=mcv_fma"]}
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # FP32 code paths are written for approximate division and square root;

@@ -27,6 +27,7 @@ MCV_SNS_E_NODES = 4096
 MCV_SNS_T_NODES = 512
 MCV_SNS_TAIL_MAX = 65536
 MCV_NOALLOC_MAX_VARIANTS = 64
+MCV_VARIANT_FP64_FMA = 4
 
 MCV_OK, MCV_EINVAL, MCV_ECUDA, MCV_ECOUNT, MCV_EBOUNCE = 0, 1, 2, 3, 4
 MCV_ENONFINITE, MCV_EBIN, MCV_ENODEV, MCV_ECAPACITY = 5, 6, 7, 8

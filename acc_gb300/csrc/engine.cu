@@ -11,6 +11,12 @@
 extern template struct mcv::Launchers<float>;
 extern template struct mcv::Launchers<double>;
 
+// launch_fp64_fma.cu: the FP64 chain kernel with contracted multiply-adds
+int mcv_fp64_fma_occupancy(int x, int threads);
+void mcv_fp64_fma_chain(int x, int blocks, int threads, cudaStream_t s,
+                        const mcv_chain& ch, uint64_t n, uint64_t first,
+                        uint64_t seed, void* status);
+
 // =================================================================== host
 using namespace mcv;
 
@@ -670,6 +676,14 @@ int mcv_run_chain(mcv_ctx* ctx, const mcv_chain* chain, uint64_t ncount,
       launch_chain<float>(ctx, 0, chain, ncount, first, seed, nullptr, 0,
                           nullptr, nullptr, launch, s);
     }
+  } else if (launch && launch->variant == MCV_VARIANT_FP64_FMA) {
+    int blocks, threads;
+    const int x = is_exotic(chain) ? 1 : 0;
+    launch_shape(
+        ctx, [x](int t) { return mcv_fp64_fma_occupancy(x, t); }, ncount,
+        launch, &blocks, &threads);
+    mcv_fp64_fma_chain(x, blocks, threads, s, *chain, ncount, first, seed,
+                       ctx->d_status);
   } else {
     launch_chain<double>(ctx, 0, chain, ncount, first, seed, nullptr, 0,
                          nullptr, nullptr, launch, s);

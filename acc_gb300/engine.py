@@ -123,7 +123,7 @@ def chain_for_instrument(instrument, binder=None):
 
 
 VARIANTS = {None: 0, "auto": 0, "thread": 1, "regen": 2,
-            "regen_noqueue": 3}
+            "regen_noqueue": 3, "fp64_fma": nat.MCV_VARIANT_FP64_FMA}
 
 
 def _launch(threads_per_block=None, blocks=None, variant=None):
@@ -144,8 +144,9 @@ def run_chain(chain, ncount, seed=None, floattype=None, first=0,
               threads_per_block=None, blocks=None, sync=True, device=None,
               variant=None):
     """mcv_run_chain: ncount neutrons through the fused chain kernel
-    (variant None/"auto", "thread" or "regen" for FP32).  Returns the
-    mcv_status (sync=True) or None."""
+    (variant None/"auto", "thread" or "regen" for FP32; "fp64_fma" for the
+    FP64 kernel with contracted multiply-adds).  Returns the mcv_status
+    (sync=True) or None."""
     ctx = nat.context(device)
     st = nat.mcv_status() if sync else None
     L = _launch(threads_per_block, blocks, variant)

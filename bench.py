@@ -47,8 +47,8 @@ WORKLOADS = {
         "sqe_hollow_cylinder: 60 meV 1x1 cm beam -> hollow cylinder with "
         "200x200 S(Q,E) -> 3 m cylinder I(Q,E) 100x100"),
     "sns_source_chain": (
-        "sns_source_chain: SNS moderator source (synthetic moderator file, "
-        "5-20 meV, 3x3 cm) -> PSD 100x100 + energy 100 bins at 5 m"),
+        "sns_source_chain: SNS moderator source (the reference's moderator "
+        "file, 5-20 meV, 3x3 cm) -> PSD 100x100 + energy 100 bins at 5 m"),
     "tapered_guide_chain": (
         "tapered_guide_chain: 3x3 cm source, 10 +- 9.5 A -> 10.99 m "
         "segmented tapered guide (100 elliptic segments, m=6) -> "
@@ -85,7 +85,7 @@ WORKLOADS = {
         "position-divergence x and y 250x250"),
     "verdi": (
         "verdi: the VERDI instrument (26 components): SNS moderator "
-        "(synthetic file, 141 E x 160 t, 0.1-1000 meV) -> 2 elliptic "
+        "(source_rot2_cdr_cyl_3x3_20190417.dat, 0.1-1000 meV) -> 2 elliptic "
         "mirrors as 4 tapered guides of 499 segments, m=6, with shields -> "
         "secondary-source slit -> 5x5 mm sample mask; 11 wavelength, "
         "position-divergence and PSD monitors"),
@@ -376,7 +376,8 @@ def grad_costs():
 
 # ---------------------------------------------------------- CPU baseline
 def cpu_oracle_rate(workload, seconds, seed, nthreads=0):
-    """Neutrons/s of the CPU oracle on a bounded sample of the workload."""
+    """Neutrons/s of the CPU oracle's timed-baseline build on a bounded
+    sample of the workload."""
     from acc_gb300.engine import chain_for_instrument
     from acc_gb300.memory import HostBinder
     from oracle import binding as O
@@ -384,10 +385,11 @@ def cpu_oracle_rate(workload, seconds, seed, nthreads=0):
     ch = chain_for_instrument(ins, HostBinder())
     nthreads = nthreads or os.cpu_count() or 1
     chunk = 1_000_000
-    O.run_chain(ch, 100_000, seed=seed, nthreads=nthreads)  # warm
+    O.run_chain(ch, 100_000, seed=seed, nthreads=nthreads, timing=True)
     done, t0 = 0, time.perf_counter()
     while True:
-        O.run_chain(ch, chunk, seed=seed, first=done, nthreads=nthreads)
+        O.run_chain(ch, chunk, seed=seed, first=done, nthreads=nthreads,
+                    timing=True)
         done += chunk
         el = time.perf_counter() - t0
         if el >= seconds:
@@ -413,23 +415,27 @@ def cpu_model():
 
 # ------------------------------------------------------------- arms
 def reference_arm(a, rank, world):
+    """The reference's CPU path (its restatement: the oracle's timed build)
+    on all host cores: each step is the GPU arm's step, --ncount neutrons
+    of the same workload."""
     if rank != 0:
         return 0
-    sample = max(2_000_000, int(a.ncount) // 5)
+    sample = int(a.ncount)
     from acc_gb300.engine import chain_for_instrument
     from acc_gb300.memory import HostBinder
     from oracle import binding as O
+    from oracle import build as OB
     ins = build_instrument(a.workload)
     ch = chain_for_instrument(ins, HostBinder())
     nthreads = os.cpu_count() or 1
     for w in range(a.warmup):
         O.run_chain(ch, sample, seed=a.seed, first=w * sample,
-                    nthreads=nthreads)
+                    nthreads=nthreads, timing=True)
     t = []
     for k in range(a.steps):
         t0 = time.perf_counter()
         O.run_chain(ch, sample, seed=a.seed, first=(a.warmup + k) * sample,
-                    nthreads=nthreads)
+                    nthreads=nthreads, timing=True)
         t.append(time.perf_counter() - t0)
     value = sample * a.steps / sum(t)
     line = {
@@ -442,11 +448,12 @@ def reference_arm(a, rank, world):
                    "neutrons_per_step": sample},
         "cpu_baseline": {
             "value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
-            "sample": f"{sample} neutrons per step of the same workload, "
-                      f"CPU FP64 restatement of the reference chain "
-                      f"(mcvine/acc is Python+Numba; its CPU engine "
-                      f"mcvine-core is not installable offline); "
-                      f"host {cpu_model()}"},
+            "sample": f"{sample} neutrons per step of the same workload "
+                      f"(the GPU arm's step), CPU FP64 restatement of the "
+                      f"reference chain (mcvine/acc is Python+Numba; its "
+                      f"CPU engine mcvine-core is not installable offline) "
+                      f"built {OB.describe(timing=True)}, {nthreads} "
+                      f"threads; host {cpu_model()}"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -475,11 +482,18 @@ def ours_arm(a, rank, world, local_rank):
     ms32 = time_chain(chain32, ncount, a.steps, a.warmup, "float32", a.seed,
                       0, world, rank, flush)
     t32 = max_over_ranks(sum(ms32) / 1e3, world)
-    # FP64 plain (the clock samples span both timed regions)
+    # FP64 plain (the clock samples span the three timed regions): the
+    # kernel with contracted multiply-adds, and the one that rounds every
+    # multiply and add separately (the oracle-parity build)
+    ins64f = build_instrument(a.workload)
+    chain64f = engine.chain_for_instrument(ins64f)
+    ms64f = time_chain(chain64f, ncount, a.steps, a.warmup, "float64",
+                       a.seed + 1, 0, world, rank, flush, variant="fp64_fma")
     ms64 = time_chain(chain64, ncount, a.steps, a.warmup, "float64",
                       a.seed + 1, 0, world, rank, flush)
     clk = clocks.stop()
     t64 = max_over_ranks(sum(ms64) / 1e3, world)
+    t64f = max_over_ranks(sum(ms64f) / 1e3, world)
     # the FP32 kernel without path regeneration, for comparison
     ins_t = build_instrument(a.workload)
     ms_t = time_chain(engine.chain_for_instrument(ins_t), ncount, a.steps,
@@ -575,13 +589,15 @@ def ours_arm(a, rank, world, local_rank):
                            "during the timed region"}
     cpu = None
     if world == 1 and not a.no_cpu_baseline:
+        from oracle import build as OB
         rate, n, cores = cpu_oracle_rate(a.workload, a.cpu_seconds, a.seed)
         cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
                "sample": f"{n} neutrons of the same workload through the CPU "
-                         f"FP64 oracle (C, OpenMP, {cores} threads), "
-                         f"host {cpu_model()}"}
+                         f"FP64 oracle (C, OpenMP, {cores} threads, built "
+                         f"{OB.describe(timing=True)}), host {cpu_model()}"}
     value = world * ncount * a.steps / t32
     v64 = world * ncount * a.steps / t64
+    v64f = world * ncount * a.steps / t64f
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": a.steps, "warmup": a.warmup,
@@ -596,9 +612,19 @@ def ours_arm(a, rank, world, local_rank):
                          "the CUDA events",
                    "parallelism": f"{world} replica(s), disjoint neutron "
                                   "index ranges, one tally all-reduce"},
-        "fp64_plain": {"value": v64, "unit": UNIT,
-                       "ms_per_step": 1e3 * t64 / a.steps, "dtype": "f64"},
-        "fp32_over_fp64": value / v64,
+        "fp64_plain": {"value": v64f, "unit": UNIT,
+                       "ms_per_step": 1e3 * t64f / a.steps, "dtype": "f64",
+                       "build": "multiply-adds contracted "
+                                "(MCV_VARIANT_FP64_FMA)"},
+        "fp64_plain_no_fma": {"value": v64, "unit": UNIT,
+                              "ms_per_step": 1e3 * t64 / a.steps,
+                              "dtype": "f64",
+                              "build": "--fmad=false: every multiply and "
+                                       "add rounded, as the oracle"},
+        "fp32_over_fp64": value / v64f,
+        "fp32_over_fp64_basis": "fp64_plain (contracted, the faster FP64 "
+                                "kernel)",
+        "fp32_over_fp64_no_fma": value / v64,
         "fp32_one_neutron_per_thread": {
             "value": world * ncount * a.steps / t_thread, "unit": UNIT,
             "ms_per_step": 1e3 * t_thread / a.steps,

@@ -319,8 +319,16 @@ typedef struct mcv_launch {
                                guides advance one bounce per step; the
                                components after the last guide run from a
                                per-warp queue in shared memory), 3 path
-                               regeneration without that queue */
+                               regeneration without that queue.
+                               FP64 mcv_run_chain: 0 the kernel that rounds
+                               every multiply and add separately (agrees
+                               with the CPU restatement operation for
+                               operation), MCV_VARIANT_FP64_FMA the same
+                               kernel with contracted multiply-adds
+                               (faster) */
 } mcv_launch;
+
+#define MCV_VARIANT_FP64_FMA 4
 
 typedef struct mcv_status {
   int32_t code;

@@ -14,83 +14,97 @@ import numpy as np
 from . import build as _build
 
 _lib = None
+_timing_lib = None
 
 c_double_p = ctypes.POINTER(ctypes.c_double)
 
 
 def lib():
+    """The checker build (multiply-adds never contracted)."""
     global _lib
     if _lib is None:
-        path = _build.build()
-        L = ctypes.CDLL(path)
-        L.oracle_philox4x32_10.argtypes = [ctypes.POINTER(ctypes.c_uint32)] * 3
-        L.oracle_philox4x32_10.restype = None
-        for name in ("oracle_intersect_sphere",):
-            getattr(L, name).argtypes = [ctypes.c_double] * 7 + [c_double_p] * 2
-        L.oracle_intersect_cylinder.argtypes = [ctypes.c_double] * 8 + [c_double_p] * 2
-        L.oracle_intersect_box.argtypes = [ctypes.c_double] * 9 + [c_double_p] * 2
-        L.oracle_locate.argtypes = [ctypes.c_void_p] + [ctypes.c_double] * 3
-        L.oracle_locate.restype = ctypes.c_int
-        L.oracle_insert_sorted.argtypes = [ctypes.c_double, c_double_p,
-                                           ctypes.c_int, ctypes.c_int]
-        L.oracle_insert_sorted.restype = ctypes.c_int
-        L.oracle_intersect.argtypes = [ctypes.c_void_p] + [ctypes.c_double] * 6 + [c_double_p]
-        L.oracle_intersect.restype = ctypes.c_int
-        L.oracle_time_to_scatter.argtypes = [c_double_p, ctypes.c_int,
-                                             ctypes.c_double, c_double_p]
-        L.oracle_time_to_scatter.restype = None
-        L.oracle_total_time_in_shape.argtypes = [c_double_p, ctypes.c_int]
-        L.oracle_total_time_in_shape.restype = ctypes.c_double
-        L.oracle_time_to_enter.argtypes = [c_double_p, ctypes.c_int]
-        L.oracle_time_to_enter.restype = ctypes.c_double
-        L.oracle_rotate.argtypes = [c_double_p, c_double_p, ctypes.c_double,
-                                    ctypes.c_double]
-        L.oracle_rotate.restype = None
-        L.oracle_reflectivity.argtypes = [ctypes.c_double] * 6
-        L.oracle_reflectivity.restype = ctypes.c_double
-        L.oracle_propagate_out.argtypes = [ctypes.c_void_p, c_double_p]
-        L.oracle_tof_before_first_exit.argtypes = [ctypes.c_void_p, c_double_p]
-        L.oracle_tof_before_first_exit.restype = ctypes.c_double
-        L.oracle_propagate_to_next_incident_surface.argtypes = [ctypes.c_void_p, c_double_p]
-        L.oracle_propagate_to_next_incident_surface.restype = ctypes.c_int
-        L.oracle_propagate_to_next_exiting_surface.argtypes = [ctypes.c_void_p, c_double_p]
-        L.oracle_run_chain.argtypes = [
-            ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,
-            ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
-            ctypes.c_int, ctypes.POINTER(ctypes.c_uint64)]
-        L.oracle_run_chain.restype = ctypes.c_int
-        L.oracle_process_buffer.argtypes = [
-            ctypes.c_void_p, c_double_p, ctypes.c_uint64, ctypes.c_uint64,
-            ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(ctypes.c_uint64)]
-        L.oracle_process_buffer.restype = ctypes.c_int
-        L.oracle_guide_reflections.argtypes = [
-            ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,
-            ctypes.c_int, ctypes.c_void_p, ctypes.c_int]
-        L.oracle_guide_reflections.restype = ctypes.c_int
-        L.oracle_ms_step.argtypes = [
-            ctypes.c_void_p, ctypes.c_int, c_double_p, ctypes.c_uint64,
-            ctypes.c_uint64, ctypes.c_void_p, ctypes.c_int, c_double_p]
-        L.oracle_ms_step.restype = ctypes.c_int
-        L.oracle_sns_generate.argtypes = [
-            ctypes.c_void_p, ctypes.c_double, ctypes.c_double, c_double_p,
-            c_double_p]
-        L.oracle_guide_one.argtypes = [ctypes.c_void_p, c_double_p]
-        L.oracle_guide_one.restype = ctypes.c_int
-        L.oracle_source_one.argtypes = [ctypes.c_void_p, ctypes.c_void_p, c_double_p]
-        L.oracle_hss_one.argtypes = [ctypes.c_void_p, ctypes.c_void_p,
-                                     ctypes.c_int, c_double_p]
-        L.oracle_anyshape_one.argtypes = [ctypes.c_void_p, c_double_p]
-        L.oracle_kernel_scatter_one.argtypes = [ctypes.c_void_p, c_double_p,
-                                                ctypes.c_uint64, ctypes.c_uint64]
-        L.oracle_expr_eval.restype = ctypes.c_double
-        L.oracle_expr_eval.argtypes = [c_double_p, ctypes.c_int, ctypes.c_double]
-        L.oracle_apply_transform.argtypes = [c_double_p, c_double_p, c_double_p]
-        L.oracle_sqe_lookup.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double]
-        L.oracle_sqe_lookup.restype = ctypes.c_double
-        L.oracle_sizeof_chain.restype = ctypes.c_int
-        L.oracle_sizeof_component.restype = ctypes.c_int
-        _lib = L
+        _lib = _bind(ctypes.CDLL(_build.build()))
     return _lib
+
+
+def timing_lib():
+    """The timed-baseline build (-O3, contraction allowed): the same
+    functions, for bench.py's CPU legs."""
+    global _timing_lib
+    if _timing_lib is None:
+        _timing_lib = _bind(ctypes.CDLL(_build.build(timing=True)))
+    return _timing_lib
+
+
+def _bind(L):
+    """Declare the argument and return types of the oracle's entry points."""
+    L.oracle_philox4x32_10.argtypes = [ctypes.POINTER(ctypes.c_uint32)] * 3
+    L.oracle_philox4x32_10.restype = None
+    for name in ("oracle_intersect_sphere",):
+        getattr(L, name).argtypes = [ctypes.c_double] * 7 + [c_double_p] * 2
+    L.oracle_intersect_cylinder.argtypes = [ctypes.c_double] * 8 + [c_double_p] * 2
+    L.oracle_intersect_box.argtypes = [ctypes.c_double] * 9 + [c_double_p] * 2
+    L.oracle_locate.argtypes = [ctypes.c_void_p] + [ctypes.c_double] * 3
+    L.oracle_locate.restype = ctypes.c_int
+    L.oracle_insert_sorted.argtypes = [ctypes.c_double, c_double_p,
+                                       ctypes.c_int, ctypes.c_int]
+    L.oracle_insert_sorted.restype = ctypes.c_int
+    L.oracle_intersect.argtypes = [ctypes.c_void_p] + [ctypes.c_double] * 6 + [c_double_p]
+    L.oracle_intersect.restype = ctypes.c_int
+    L.oracle_time_to_scatter.argtypes = [c_double_p, ctypes.c_int,
+                                         ctypes.c_double, c_double_p]
+    L.oracle_time_to_scatter.restype = None
+    L.oracle_total_time_in_shape.argtypes = [c_double_p, ctypes.c_int]
+    L.oracle_total_time_in_shape.restype = ctypes.c_double
+    L.oracle_time_to_enter.argtypes = [c_double_p, ctypes.c_int]
+    L.oracle_time_to_enter.restype = ctypes.c_double
+    L.oracle_rotate.argtypes = [c_double_p, c_double_p, ctypes.c_double,
+                                ctypes.c_double]
+    L.oracle_rotate.restype = None
+    L.oracle_reflectivity.argtypes = [ctypes.c_double] * 6
+    L.oracle_reflectivity.restype = ctypes.c_double
+    L.oracle_propagate_out.argtypes = [ctypes.c_void_p, c_double_p]
+    L.oracle_tof_before_first_exit.argtypes = [ctypes.c_void_p, c_double_p]
+    L.oracle_tof_before_first_exit.restype = ctypes.c_double
+    L.oracle_propagate_to_next_incident_surface.argtypes = [ctypes.c_void_p, c_double_p]
+    L.oracle_propagate_to_next_incident_surface.restype = ctypes.c_int
+    L.oracle_propagate_to_next_exiting_surface.argtypes = [ctypes.c_void_p, c_double_p]
+    L.oracle_run_chain.argtypes = [
+        ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,
+        ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+        ctypes.c_int, ctypes.POINTER(ctypes.c_uint64)]
+    L.oracle_run_chain.restype = ctypes.c_int
+    L.oracle_process_buffer.argtypes = [
+        ctypes.c_void_p, c_double_p, ctypes.c_uint64, ctypes.c_uint64,
+        ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(ctypes.c_uint64)]
+    L.oracle_process_buffer.restype = ctypes.c_int
+    L.oracle_guide_reflections.argtypes = [
+        ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,
+        ctypes.c_int, ctypes.c_void_p, ctypes.c_int]
+    L.oracle_guide_reflections.restype = ctypes.c_int
+    L.oracle_ms_step.argtypes = [
+        ctypes.c_void_p, ctypes.c_int, c_double_p, ctypes.c_uint64,
+        ctypes.c_uint64, ctypes.c_void_p, ctypes.c_int, c_double_p]
+    L.oracle_ms_step.restype = ctypes.c_int
+    L.oracle_sns_generate.argtypes = [
+        ctypes.c_void_p, ctypes.c_double, ctypes.c_double, c_double_p,
+        c_double_p]
+    L.oracle_guide_one.argtypes = [ctypes.c_void_p, c_double_p]
+    L.oracle_guide_one.restype = ctypes.c_int
+    L.oracle_source_one.argtypes = [ctypes.c_void_p, ctypes.c_void_p, c_double_p]
+    L.oracle_hss_one.argtypes = [ctypes.c_void_p, ctypes.c_void_p,
+                                 ctypes.c_int, c_double_p]
+    L.oracle_anyshape_one.argtypes = [ctypes.c_void_p, c_double_p]
+    L.oracle_kernel_scatter_one.argtypes = [ctypes.c_void_p, c_double_p,
+                                            ctypes.c_uint64, ctypes.c_uint64]
+    L.oracle_expr_eval.restype = ctypes.c_double
+    L.oracle_expr_eval.argtypes = [c_double_p, ctypes.c_int, ctypes.c_double]
+    L.oracle_apply_transform.argtypes = [c_double_p, c_double_p, c_double_p]
+    L.oracle_sqe_lookup.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double]
+    L.oracle_sqe_lookup.restype = ctypes.c_double
+    L.oracle_sizeof_chain.restype = ctypes.c_int
+    L.oracle_sizeof_component.restype = ctypes.c_int
+    return L
 
 
 def _dp(a):
@@ -237,9 +251,10 @@ def sqe_lookup(comp, Q, E):
 
 
 def run_chain(chain, ncount, seed=1, first=0, uniforms=None, record=False,
-              nthreads=0):
-    """Run the chain on the CPU.  Tallies land in the host memory the chain's
-    components were bound to.  Returns (stats dict, neutrons, last)."""
+              nthreads=0, timing=False):
+    """Run the chain on the CPU (`timing`: on the timed-baseline build).
+    Tallies land in the host memory the chain's components were bound to.
+    Returns (stats dict, neutrons, last)."""
     stats = (ctypes.c_uint64 * 4)()
     out = np.zeros((ncount, 10)) if record else None
     last = np.zeros(ncount, dtype=np.int32) if record else None
@@ -248,7 +263,8 @@ def run_chain(chain, ncount, seed=1, first=0, uniforms=None, record=False,
         u = np.ascontiguousarray(uniforms, dtype=np.float32)
         assert u.ndim == 2 and u.shape[0] == ncount
         uptr, stride = u.ctypes.data, u.shape[1]
-    rc = lib().oracle_run_chain(
+    L = timing_lib() if timing else lib()
+    rc = L.oracle_run_chain(
         ctypes.byref(chain), int(ncount), int(first), int(seed), uptr, stride,
         out.ctypes.data if record else None,
         last.ctypes.data if record else None, int(nthreads), stats)

@@ -4,15 +4,15 @@ Tolerances (stated per test):
  * FP64 kernels, same Philox stream or injected uniforms: every slot of
    every neutron within 1e-12 relative (denominator floored at the slot's
    RMS over the batch), identical exit component, identical bin counts.
-   The powder chains (CHORD_CONDITIONED) hold the weight of at most 1e-3
-   of their neutrons (at least two) to 1e-6 instead, and their bin sums to
-   1e-12 in 99% of the populated bins and 1e-8 in the rest: a neutron that
-   grazes the 5 mm powder cylinder has a chord 2 sqrt(k)/a whose
-   discriminant k = b^2 - a c cancels, so the last-bit differences between
-   the host's and the device's sin/cos/exp upstream (the source's sin/cos
-   of its disc angle, the guides' tanh) grow into the path length, and
-   the weight is p L exp(-mu L).  Each component on its own holds 1e-12
-   (test_gpu_components.py, test_reference_paths.py).
+   The powder chains (CHORD_CONDITIONED) hold at most 1e-3 of their
+   neutrons (at least two) to 1e-6 instead, and their bin sums to 1e-9: a
+   neutron that grazes the 5 mm powder cylinder has a chord 2 sqrt(k)/a
+   whose discriminant k = b^2 - a c cancels, so the last-bit differences
+   between the host's and the device's sin/cos/exp upstream (the source's
+   sin/cos of its disc angle, the guides' tanh) grow into the path length,
+   which sets the weight p L exp(-mu L) and the scattering point.  Each
+   component on its own holds 1e-12 (test_gpu_components.py,
+   test_reference_paths.py).
  * FP32 kernels against the FP64 oracle on the same stream, whole chain:
    of the neutrons that leave the chain alive with a weight above 1e-30 (in
    either run), at most 1e-3 beyond 1e-4 relative, and at most 1e-4 of them
@@ -176,10 +176,10 @@ def test_fp64_same_stream_matches_oracle(name):
     np.testing.assert_array_equal(g_last, o_last)
     err = rel_err(g_out, o_out)
     if name in CHORD_CONDITIONED:
-        w = err[:, 9]
+        w = err.max(axis=1)
         assert (w > 1e-12).sum() <= max(2, 1e-3 * n), (name, np.sort(w)[-5:])
         assert w.max() <= 1e-6, (name, w.max())
-        err = err[:, :9]
+        return
     assert err.max() <= 1e-12, (name, err.max(), np.unravel_index(
         err.argmax(), err.shape))
 
@@ -197,11 +197,8 @@ def test_fp64_histograms_match_oracle(name):
         assert gc.name == oc.name
         np.testing.assert_array_equal(g[0], o[0])
         if name in CHORD_CONDITIONED:
-            for k in (1, 2):
-                pop = o[0] > 0
-                rel = np.abs(g[k] - o[k])[pop] / np.abs(o[k])[pop]
-                assert (rel > 1e-12).mean() <= 0.01, (gc.name, k)
-                assert rel.max() <= 1e-8, (gc.name, k, rel.max())
+            np.testing.assert_allclose(g[1], o[1], rtol=1e-9, atol=1e-300)
+            np.testing.assert_allclose(g[2], o[2], rtol=1e-9, atol=1e-300)
         else:
             np.testing.assert_allclose(g[1], o[1], rtol=1e-12, atol=1e-300)
             np.testing.assert_allclose(g[2], o[2], rtol=1e-12, atol=1e-300)
@@ -482,3 +479,27 @@ def test_un_multiple_scattering_fp32_chi2():
     assert dof > 200
     bound = 1.1 if dof >= 2000 else 1.1 + 3 * np.sqrt(2 / dof)
     assert c2 <= bound, (c2, dof)
+
+
+@pytest.mark.parametrize("name", ["guide_chain", "sphere_theta_tof",
+                                  "powder_direct"])
+def test_fp64_fma_variant_histograms(name):
+    """MCV_VARIANT_FP64_FMA (the FP64 chain kernel with contracted
+    multiply-adds) against the oracle on the same stream: contraction moves
+    the last bits of every path, so a coordinate within rounding of a bin
+    edge may change bins (at most 1e-5 of the entries) and bin sums agree
+    within 1e-9 relative where the counts agree."""
+    n, seed = 200000, 5
+    ins = BUILDERS[name]()
+    st = engine.run_instrument(ins, n, seed=seed, floattype="float64",
+                               variant="fp64_fma")
+    assert st.processed == n
+    gt = gpu_tallies(ins)
+    ot, _, _, _ = oracle_run(BUILDERS[name](), n, seed=seed)
+    for (gc, g), (oc, o) in zip(gt.items(), ot.items()):
+        moved = np.abs(g[0] - o[0]).sum() / 2
+        assert moved <= max(2, 1e-5 * o[0].sum()), (gc.name, moved)
+        same = (g[0] == o[0]) & (o[0] > 0)
+        rel = np.abs(g[1] - o[1])[same] / o[1][same]
+        assert (rel > 1e-9).mean() <= 1e-3, (gc.name, np.sort(rel)[-3:])
+        assert g[0].sum() > 0

@@ -199,6 +199,9 @@ def test_gpu_tail_draws_take_their_tail_energy(engine_lib, which,
     with warnings.catch_warnings():
         warnings.simplefilter("ignore")
         src = SNS_source("m", path, 0.1, 1000., 0.03, 0.03, 6.2, 0.1, 0.1)
+    ins = acc_gb300.instrument()
+    ins.append(src)
+    chain = engine.chain_for_instrument(ins)  # packs the FP32 tables
     ftab, u_lo, u_hi, n_lo, n_hi = src._fp32
     nE, NE, NT = len(src.propagate_params[9]), nat.MCV_SNS_E_NODES, \
         nat.MCV_SNS_T_NODES
@@ -210,10 +213,7 @@ def test_gpu_tail_draws_take_their_tail_energy(engine_lib, which,
     expect = [tail[k] if k < n_lo else tail[n_lo + k - first_hi] for k in ks]
     u = np.full((len(ks), 6), 0.5, np.float32)
     u[:, 4] = np.array(ks, np.float64) / 2 ** 24
-    ins = acc_gb300.instrument()
-    ins.append(src)
-    out, _ = engine.replay(engine.chain_for_instrument(ins), len(ks),
-                           uniforms=u, floattype="float32")
+    out, _ = engine.replay(chain, len(ks), uniforms=u, floattype="float32")
     out = out.cpu().numpy()
     E = VS2E * (out[:, 3:6] ** 2).sum(axis=1)
     np.testing.assert_allclose(E, np.array(expect) * 1000.0, rtol=1e-6)
