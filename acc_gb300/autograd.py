@@ -33,8 +33,20 @@ _GUIDE_SLOT = {"guide_m": (8, 0), "guide_alpha": (7, 1), "guide_W": (9, 2)}
 
 
 class GradRun:
+    """`shard` = (rank, world[, group]): this process runs the neutron block
+    sharding.shard_range(ncount, rank, world) and the histogram and the
+    gradients are summed over the ranks (torch.distributed all-reduce)."""
+
     def __init__(self, instrument, loss_monitor, ncount, seed=1,
-                 floattype="float64", params=None):
+                 floattype="float64", params=None, shard=None):
+        from .sharding import shard_range
+        self.shard = None
+        self.first, self.count = 0, int(ncount)
+        if shard is not None:
+            rank, world = int(shard[0]), int(shard[1])
+            group = shard[2] if len(shard) > 2 else None
+            self.shard = (rank, world, group)
+            self.first, self.count = shard_range(ncount, rank, world)
         self.ins = instrument
         self.comps, off, rot, _ = engine.chain_parts(instrument)
         self.mon = loss_monitor
@@ -99,9 +111,12 @@ class GradRun:
         self._apply(values)
         t = self.mon._device_tally
         t.zero_()
-        st = engine.run_chain(self.chain, self.ncount, seed=self.seed,
-                              floattype=self.floattype)
-        assert st.processed == self.ncount
+        st = engine.run_chain(self.chain, self.count, seed=self.seed,
+                              floattype=self.floattype, first=self.first)
+        assert st.processed == self.count
+        if self.shard is not None:
+            from .sharding import reduce_tallies
+            reduce_tallies([t], self.shard[2])
         n = self.mon.nbins()
         return t[n:2 * n].clone().reshape(self.mon.hist_shape)
 
@@ -125,9 +140,9 @@ class GradRun:
                 size = c.ip[4] * c.ip[5] if kind == "sqe_table" else c.ip[4]
                 dtable[k] = torch.zeros(size, dtype=torch.float64,
                                         device="cuda")
-        engine.backward(self.chain, self.ncount, {self.mon_index: dout},
+        engine.backward(self.chain, self.count, {self.mon_index: dout},
                         dparam, dtable, seed=self.seed,
-                        floattype=self.floattype)
+                        floattype=self.floattype, first=self.first)
         for name, (kind, target) in self.params.items():
             if kind in _GUIDE_SLOT:
                 j = _GUIDE_SLOT[kind][1]
@@ -144,6 +159,13 @@ class GradRun:
             elif kind == "powder_F2":
                 out[name] = dtable[self._index(target)] * torch.from_numpy(
                     self._powder_base).cuda()
+        if self.shard is not None:
+            from .sharding import reduce_gradients
+            out = {k: (v if isinstance(v, torch.Tensor) else
+                       torch.tensor(float(v), dtype=torch.float64,
+                                    device="cuda")).clone()
+                   for k, v in out.items()}
+            reduce_gradients(out, self.shard[2])
         return out
 
     def __call__(self, **values):

@@ -47,6 +47,8 @@ void set_msg(mcv_status* st, int code, const char* msg) {
 
 // Device address of the scratch on the current device; looked up on the
 // first call per device (the array's name is only a host-side stand-in).
+// The address belongs to the device's primary context; a cudaDeviceReset
+// would end it, and the header rules out calls after one.
 int scratch_on_current_device(unsigned char** out, mcv_status* st) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);

@@ -11,6 +11,9 @@
 // the estimator (the common-random-number derivative).
 #pragma once
 
+#include <cooperative_groups.h>
+#include <cooperative_groups/reduce.h>
+
 #include "common.cuh"
 
 namespace mcv {
@@ -43,39 +46,22 @@ __device__ __forceinline__ double weight_down(const mcv_chain& ch) {
 }
 
 // Warp-aggregated entry (MCV_COMP_AGGREGATE): the lanes that reach this
-// call together and hit the same bin of the same tally (__match_any_sync on
-// the bin's address) first add their count, p and p^2 in a tree inside the
-// warp, and one lane (the group's lowest) makes the three atomics.  Not
-// inlined, so that its registers do not weigh on the kernels that do not
-// take it.
+// call together (cooperative_groups::coalesced_threads) and hit the same
+// bin of the same tally (labeled_partition on the bin's address) first sum
+// their count, p and p^2 inside the warp, and the group's first lane makes
+// the three atomics.  Not inlined, so that its registers do not weigh on
+// the kernels that do not take it.
 static __device__ __noinline__ void tally_add_aggregated(double* a,
                                                          uint64_t nbins,
                                                          double p) {
-  const unsigned mask = __activemask();
-  const unsigned lane = threadIdx.x & 31u;
-  const unsigned peers =
-      __match_any_sync(mask, (unsigned long long)(uintptr_t)a);
-  const unsigned me = 1u << lane;
-  double s1 = p, s2 = p * p;
-  if (!__all_sync(mask, peers == me)) {
-    // tree over ranks within the group: rank r adds rank r + k while
-    // r is a multiple of 2k; the group's lowest lane ends with the sum
-    const int size = __popc(peers);
-    const int rank = __popc(peers & (me - 1u));
-    const int most = __reduce_max_sync(mask, (unsigned)size);
-    for (int k = 1; k < most; k <<= 1) {
-      const unsigned src = __fns(peers, lane, k + 1);
-      const unsigned from = src < 32u ? src : lane;
-      const double o1 = __shfl_sync(mask, s1, from);
-      const double o2 = __shfl_sync(mask, s2, from);
-      if ((rank & (2 * k - 1)) == 0 && rank + k < size) {
-        s1 += o1;
-        s2 += o2;
-      }
-    }
-    if (peers & (me - 1u)) return;  // not the group's lowest lane
-  }
-  atomicAdd(a, (double)__popc(peers));
+  namespace cg = cooperative_groups;
+  const cg::coalesced_group active = cg::coalesced_threads();
+  const cg::coalesced_group peers =
+      cg::labeled_partition(active, (unsigned long long)(uintptr_t)a);
+  const double s1 = cg::reduce(peers, p, cg::plus<double>());
+  const double s2 = cg::reduce(peers, p * p, cg::plus<double>());
+  if (peers.thread_rank() != 0) return;
+  atomicAdd(a, (double)peers.size());
   atomicAdd(a + nbins, s1);
   atomicAdd(a + 2 * nbins, s2);
 }
@@ -87,21 +73,21 @@ constexpr int kHotLanes = 4;
 // One entry (1, p, p^2) into bin `bin`: three FP64 atomics into the
 // L2-resident histogram.  The lanes that reach the call together first
 // check, with one shuffle and one vote, how many of them hit the bin of
-// the lowest lane; when kHotLanes or more do (a beam into a few bins, a
-// fixed (Q, E) transfer), the warp aggregates its entries before the
-// atomics.  Measured on GB300: always aggregating costs 15-35% on monitors
-// whose entries spread over many bins, and gains 3.8x on the
+// the group's first lane; when kHotLanes or more do (a beam into a few
+// bins, a fixed (Q, E) transfer), the warp aggregates its entries before
+// the atomics.  Measured on GB300: always aggregating costs 15-35% on
+// monitors whose entries spread over many bins, and gains 3.8x on the
 // constant-(Q, E) box, whose entries land in one or two bins.
 // MCV_COMP_AGGREGATE forces the aggregated path.
 __device__ __forceinline__ void tally_add(const Tally& t, uint64_t bin,
                                           double p) {
   if (!t.out) return;
+  namespace cg = cooperative_groups;
   double* a = t.out + bin;
-  const unsigned mask = __activemask();
-  const int first = __ffs(mask) - 1;
+  const cg::coalesced_group active = cg::coalesced_threads();
   const unsigned long long mine = (unsigned long long)(uintptr_t)a;
-  const unsigned long long lead = __shfl_sync(mask, mine, first);
-  const unsigned same = __ballot_sync(mask, mine == lead);
+  const unsigned long long lead = active.shfl(mine, 0);
+  const unsigned same = active.ballot(mine == lead);
   if (t.aggregate || __popc(same) >= kHotLanes) {
     tally_add_aggregated(a, t.nbins, p);
     return;

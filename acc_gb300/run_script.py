@@ -28,11 +28,20 @@ def _check_workdir(workdir, overwrite_datafiles):
 
 
 def run(script, workdir, ncount, overwrite_datafiles=True, ntotalthreads=None,
-        threads_per_block=None, seed=None, floattype=None, **kwds):
+        threads_per_block=None, **kwds):
     """Run the instrument defined by `script` for `ncount` neutrons and save
     every monitor into `workdir` scaled by 1/ncount (run_script.py:10-35,
-    210-223).  Returns the instrument."""
+    210-223).  Returns the instrument.
+
+    Every keyword in `kwds` goes to the script's instrument factory, as in
+    the reference.  The random seed and the float type come from
+    acc_gb300.config (rng_seed, floattype: the reference's acc/config.py);
+    the keywords `_acc_seed` and `_acc_floattype`, which no instrument
+    takes, override them for one run.  An existing `workdir` raises IOError
+    unless `overwrite_datafiles`."""
     from . import engine
+    seed = kwds.pop("_acc_seed", None)
+    floattype = kwds.pop("_acc_floattype", None)
     _check_workdir(workdir, overwrite_datafiles)
     os.makedirs(workdir)
     ncount = int(ncount)
@@ -164,16 +173,31 @@ def main(argv=None):
     ap.add_argument("--threads_per_block", type=int, default=512)
     ap.add_argument("--floattype", default=None)
     ap.add_argument("--additional-kargs", default=None,
-                    help="keyword arguments in a JSON file")
+                    help="additional keyword arguments in a YAML file (JSON "
+                         "where PyYAML is not installed)")
     a = ap.parse_args(argv)
     kwds = {}
     if a.additional_kargs:
-        with open(a.additional_kargs) as f:
-            kwds = json.load(f)
+        kwds = load_additional_kargs(a.additional_kargs)
+    if a.floattype:
+        kwds["_acc_floattype"] = a.floattype
     run(a.script, a.workdir, int(a.ncount),
         overwrite_datafiles=a.overwrite_datafiles,
         ntotalthreads=a.total_threads, threads_per_block=a.threads_per_block,
-        floattype=a.floattype, **kwds)
+        **kwds)
+
+
+def load_additional_kargs(path):
+    """The keyword file of --additional-kargs: YAML, as the reference reads
+    it (yaml.safe_load, run_script.py:345-346); JSON (a subset of YAML)
+    when PyYAML is not installed."""
+    with open(path) as f:
+        text = f.read()
+    try:
+        import yaml
+    except ImportError:
+        return json.loads(text) if text.strip() else {}
+    return yaml.safe_load(text) or {}
 
 
 if __name__ == "__main__":

@@ -204,23 +204,29 @@ def time_chain(chain, ncount, steps, warmup, floattype, seed, first0, world,
     import torch
     import torch.distributed as dist
     from acc_gb300 import engine
+    from acc_gb300.sharding import shard_range
+
+    def block(k):
+        # step k covers world * ncount neutrons; this rank's block of them
+        first, count = shard_range(world * ncount, rank, world)
+        assert count == ncount
+        return first0 + k * world * ncount + first
+
     stream = torch.cuda.current_stream()
     for w in range(warmup):
         engine.run_chain(chain, ncount, seed=seed, floattype=floattype,
-                         first=first0 + (w * world + rank) * ncount,
-                         sync=False, variant=variant)
+                         first=block(w), sync=False, variant=variant)
     engine.read_status(expected=warmup * ncount if warmup else 0)
     evs = [(torch.cuda.Event(enable_timing=True),
             torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
-    base = first0 + warmup * world * ncount
     for k in range(steps):
         flush.zero_()
         evs[k][0].record(stream)
         engine.run_chain(chain, ncount, seed=seed, floattype=floattype,
-                         first=base + (k * world + rank) * ncount, sync=False,
+                         first=block(warmup + k), sync=False,
                          variant=variant)
         evs[k][1].record(stream)
     torch.cuda.synchronize()

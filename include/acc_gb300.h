@@ -441,10 +441,14 @@ int mcv_graph_destroy(mcv_graph* graph);
  * and re-allocating a growing staging buffer.  Same arguments and results as
  * mcv_run_batched, but no context: the variant descriptions, counts, seeds,
  * counters and work-queue head live in one static device array of
- * MCV_NOALLOC_MAX_VARIANTS variants (about 0.7 MB, held by every GPU that
- * loads the library until the process exits); more variants are rejected
- * with MCV_ECAPACITY.  The first call on a device looks up the array's
- * device address, so make that first call before any stream capture.  The
+ * MCV_NOALLOC_MAX_VARIANTS variants (1,034,496 bytes: 64 chain
+ * descriptions of 16,144 bytes, their counts and seeds, and the counters;
+ * held by every GPU that loads the library until the process exits); more
+ * variants are rejected with MCV_ECAPACITY.  The first call on a device
+ * looks up the array's device address, so make that first call before any
+ * stream capture.  The address stays valid for the life of the device's
+ * primary context: after a cudaDeviceReset in the process, do not call this
+ * entry point again.  The
  * call itself zeroes the counters and the work-queue head in the array
  * before its launch; the tallies add to what they hold, as with
  * mcv_run_batched.  Every call shares the one array: calls that overlap on

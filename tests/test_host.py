@@ -235,12 +235,9 @@ def test_chain_keeps_its_tables_alive():
     assert ch.comp[1].table != 0
 
 
-def test_isotropic_box_and_guide_aliases():
+def test_isotropic_box():
     """IsotropicBox (isotropic_box.py) is the single scatterer on a box with
-    the isotropic kernel; guide_baseline / numpy_guide / oo_guide name the
-    straight guide."""
-    from acc_gb300.components.optics import guide, guide_baseline, \
-        numpy_guide, oo_guide
+    the isotropic kernel."""
     from acc_gb300.components.samples.isotropic_box import IsotropicBox
     ch = build_chain([IsotropicBox("b", 0.02, 0.03, 0.004, 10.0, 20.0)],
                      binder=HostBinder())
@@ -248,12 +245,12 @@ def test_isotropic_box_and_guide_aliases():
     assert c.opcode == nat.OP_HSS and c.ip[1] == nat.KERNEL_ISOTROPIC
     assert c.ip[2] == nat.SHAPE_BOX
     assert [c.dp[k] for k in (0, 1, 2, 8, 9)] == [0.02, 0.03, 0.004, 10.0, 20.0]
-    assert guide_baseline.Guide is numpy_guide.Guide is oo_guide.Guide is \
-        guide.Guide
 
 
 # every component module of the reference's acc/components that an
-# instrument script imports, with the name it takes from it
+# instrument script imports, with the name it takes from it (the earlier
+# guide implementations guide_baseline, numpy_guide and oo_guide, superseded
+# by guide.py in the reference, are not provided)
 REFERENCE_COMPONENTS = [
     ("monitors.iqe_monitor", "IQE_monitor"),
     ("monitors.posdiv_monitor", "PosDiv_monitor"),
@@ -265,10 +262,7 @@ REFERENCE_COMPONENTS = [
     ("optics.guide", "Guide"),
     ("optics.guide_anyshape", "Guide_anyshape"),
     ("optics.guide_anyshape_gravity", "Guide_anyshape_gravity"),
-    ("optics.guide_baseline", "Guide"),
     ("optics.guide_tapering", "Guide"),
-    ("optics.numpy_guide", "Guide"),
-    ("optics.oo_guide", "Guide"),
     ("optics.slit", "Slit"),
     ("samples.homogeneous_multiple_scatterer", "factory"),
     ("samples.homogeneous_single_scatterer", "factory"),
@@ -289,3 +283,35 @@ def test_reference_component_paths_import(module, name):
     assert callable(getattr(m, name))
     assert getattr(m, "category", module.split(".")[0]) == \
         module.split(".")[0]
+
+
+def test_run_keywords_reach_the_instrument(tmp_path):
+    """run_script.run passes every keyword to the instrument factory (the
+    reference's run_script.py:10-35, 297-328): `seed` and `floattype` are
+    instrument keywords like any other; the engine's own overrides are
+    `_acc_seed` / `_acc_floattype`."""
+    import inspect
+    from acc_gb300 import run_script
+    params = inspect.signature(run_script.run).parameters
+    assert "seed" not in params and "floattype" not in params
+    script = tmp_path / "ins.py"
+    script.write_text(
+        "import acc_gb300\n"
+        "from acc_gb300.components.optics.arm import Arm\n"
+        "def instrument(seed=0, floattype='x'):\n"
+        "    ins = acc_gb300.instrument()\n"
+        "    ins.append(Arm('a'))\n"
+        "    ins.got = (seed, floattype)\n"
+        "    return ins\n")
+    ins = run_script.loadInstrument(str(script), seed=5, floattype="y")
+    assert ins.got == (5, "y")
+
+
+def test_additional_kargs_file(tmp_path):
+    """--additional-kargs reads a YAML file (JSON when PyYAML is absent)."""
+    from acc_gb300 import run_script
+    f = tmp_path / "k.yml"
+    f.write_text('{"Ei": 60.0, "seed": 3}')
+    assert run_script.load_additional_kargs(str(f)) == {"Ei": 60.0, "seed": 3}
+    (tmp_path / "e.yml").write_text("")
+    assert run_script.load_additional_kargs(str(tmp_path / "e.yml")) == {}

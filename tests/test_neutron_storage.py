@@ -170,7 +170,7 @@ def test_gpu_save_then_replay_reproduces_the_monitors(tmp_path):
     script.write_text(
         "from acc_gb300.instruments import saved_guide_chain\n"
         "instrument = saved_guide_chain()\n")
-    ins = run_script.run(str(script), str(tmp_path / "out"), n, seed=3)
+    ins = run_script.run(str(script), str(tmp_path / "out"), n, _acc_seed=3)
     path = tmp_path / "out" / "after_guide2.mcv"
     saved = ns.load(path)
     st = ins.components[-1]

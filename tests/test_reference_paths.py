@@ -15,7 +15,11 @@ this package runs on the same inputs with the same uniforms injected:
   within 1e-5 relative, none beyond 1e-3 unless it crossed a branch
   (a neutron absorbed in one run and not in the other, at most 1%), and
   histogram counts within 1% of the entries moved between bins (float
-  rounding at a bin edge).
+  rounding at a bin edge).  The SNS and STS sources draw E and t in FP32
+  from inverse tables, t by sampling the two-row mixture the reference
+  inverts, so their E and t are other (equally distributed) draws from the
+  same uniforms: there the position and the flight direction are held to
+  the bound, and E and t to their distributions (test_gpu_parity.py).
 """
 
 import json
@@ -123,6 +127,13 @@ def test_gpu_fp32_matches_reference(name, engine_lib):
     _, _, ref, valid, hist = _case(name)
     out, got_hist = _gpu_run(name, "float32")
     ref, out = ref[valid], out[valid]
+    if RC.CASES[name]["kind"] in ("sns_source", "sts_source"):
+        def pos_dir(a):
+            d = a[:, 3:6] / np.linalg.norm(a[:, 3:6], axis=1, keepdims=True)
+            return np.concatenate([a[:, :3], d], axis=1)
+        err = rel_err(pos_dir(out), pos_dir(ref)).max(axis=1)
+        assert (err > 1e-5).mean() <= 0.005, (name, np.sort(err)[-5:])
+        return
     alive_r, alive_g = ref[:, 9] > 0, out[:, 9] > 0
     flipped = alive_r != alive_g
     assert flipped.mean() <= 0.01, (name, flipped.sum())
