@@ -28,6 +28,7 @@ MCV_SNS_T_NODES = 512
 MCV_SNS_TAIL_MAX = 65536
 MCV_NOALLOC_MAX_VARIANTS = 64
 MCV_VARIANT_FP64_FMA = 4
+MCV_SMEM_TALLY_MAX = 2048
 
 MCV_OK, MCV_EINVAL, MCV_ECUDA, MCV_ECOUNT, MCV_EBOUNCE = 0, 1, 2, 3, 4
 MCV_ENONFINITE, MCV_EBIN, MCV_ENODEV, MCV_ECAPACITY = 5, 6, 7, 8
@@ -63,6 +64,7 @@ KERNEL_DGSSXRES = 8
 
 FLAG_IDENTITY_ROT = 1
 FLAG_AGGREGATE = 2
+FLAG_SMEM_TALLY = 4
 FP32, FP64 = 32, 64
 
 

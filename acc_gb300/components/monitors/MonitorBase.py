@@ -42,6 +42,15 @@ class MonitorBase(ComponentBase):
     # warp-aggregated tally atomics (MCV_COMP_AGGREGATE); plain atomics
     # measured faster on GB300 for the bench workloads
     aggregate_tallies = False
+    # a per-block copy of the tally in shared memory in the FP32
+    # path-regeneration kernel (MCV_COMP_SMEM_TALLY): True, False, or None
+    # for monitors of at most SMEM_TALLY_AUTO_BINS bins.  Off by default:
+    # on the guide chain (2% of the neutrons reach the monitors) the
+    # 200-bin energy monitor's copy measured 1.9% slower on GB300 than its
+    # global atomics (shared-memory FP64 atomics, the zeroing and the flush
+    # cost more than the L2 atomics they save)
+    smem_tally = False
+    SMEM_TALLY_AUTO_BINS = 256
 
     def nbins(self):
         return int(np.prod(self.hist_shape))

@@ -77,6 +77,20 @@ struct PhiloxStream {
     --left;
     return __uint2float_rz(w) * 5.9604644775390625e-08f;
   }
+  // the stream after k more draws, without forming them: whole blocks
+  // move the counter, the rest come off a fresh block
+  __device__ __forceinline__ void skip(int k) {
+    if (k <= 0) return;
+    if (k > left) {
+      k -= left;
+      left = 0;
+      c2 += (uint32_t)(k / 5);
+      k %= 5;
+      if (k == 0) return;
+      refill();
+    }
+    for (; k > 0; --k) next();
+  }
   __device__ __forceinline__ int overrun() const { return 0; }
 };
 
@@ -93,6 +107,15 @@ struct InjectedStream {
     if (i < n) return p[i++];
     bad = 1;
     return 0.5f;
+  }
+  __device__ __forceinline__ void skip(int k) {
+    if (k <= 0) return;
+    if (k > n - i) {
+      bad = 1;
+      i = n;
+    } else {
+      i += k;
+    }
   }
   __device__ __forceinline__ int overrun() const { return bad; }
 };

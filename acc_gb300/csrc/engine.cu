@@ -286,6 +286,8 @@ int validate_component(const mcv_component& c, int k, mcv_status* st) {
   return MCV_OK;
 }
 
+bool host_is_monitor(const mcv_component& c);
+
 int validate_chain(const mcv_chain* ch, mcv_status* st) {
   if (!ch) {
     set_msg(st, MCV_EINVAL, "chain is NULL%s", "");
@@ -318,7 +320,35 @@ int validate_chain(const mcv_chain* ch, mcv_status* st) {
             "");
     return MCV_EINVAL;
   }
+  // shared-memory tallies: monitors only, each 3 nbins doubles inside the
+  // MCV_SMEM_TALLY_MAX area
+  for (int k = 0; k < ch->ncomp; ++k) {
+    const mcv_component& c = ch->comp[k];
+    if (!(c.flags & MCV_COMP_SMEM_TALLY)) continue;
+    const uint64_t m = 3 * comp_nbins(c);
+    if (!host_is_monitor(c) || m == 0 || c.ip[6] < 0 ||
+        (uint64_t)c.ip[6] + m > MCV_SMEM_TALLY_MAX) {
+      set_msg(st, MCV_EINVAL,
+              "component %s%lld: a shared-memory tally needs a monitor whose "
+              "3 nbins doubles fit at ip[6] in MCV_SMEM_TALLY_MAX",
+              "", (long long)k);
+      return MCV_EINVAL;
+    }
+  }
   return MCV_OK;
+}
+
+// doubles of the regeneration kernel's shared-memory tally area: up to the
+// end of the furthest MCV_COMP_SMEM_TALLY copy (validated above)
+int smem_tally_words(const mcv_chain* ch) {
+  int words = 0;
+  for (int k = 0; k < ch->ncomp; ++k) {
+    const mcv_component& c = ch->comp[k];
+    if (!(c.flags & MCV_COMP_SMEM_TALLY) || !c.tally) continue;
+    const int end = c.ip[6] + 3 * (int)comp_nbins(c);
+    if (end > words) words = end;
+  }
+  return words;
 }
 
 bool has_hms(const mcv_chain* ch) {
@@ -662,16 +692,18 @@ int mcv_run_chain(mcv_ctx* ctx, const mcv_chain* chain, uint64_t ncount,
     if (use_regen(chain, launch)) {
       int blocks, threads;
       const bool x = is_exotic(chain);
+      const int tw = smem_tally_words(chain);
       launch_shape(
           ctx,
-          [chain, launch, x](int t) {
+          [chain, launch, x, tw](int t) {
             return Launchers<float>::occupancy_regen(
-                t, regen_tail_bytes(chain, launch, t), x);
+                t, (size_t)tw * 8 + regen_tail_bytes(chain, launch, t), x);
           },
           ncount, launch, &blocks, &threads);
-      Launchers<float>::regen(blocks, threads,
-                              regen_tail_bytes(chain, launch, threads), x, s,
-                              *chain, ncount, first, seed, ctx->d_status);
+      Launchers<float>::regen(
+          blocks, threads, (size_t)tw * 8 + regen_tail_bytes(chain, launch,
+                                                             threads),
+          tw, x, s, *chain, ncount, first, seed, ctx->d_status);
     } else {
       launch_chain<float>(ctx, 0, chain, ncount, first, seed, nullptr, 0,
                           nullptr, nullptr, launch, s);

@@ -21,9 +21,11 @@
 namespace mcv {
 
 enum { kFlagIdentityRot = MCV_COMP_IDENTITY_ROT,
-       kFlagAggregate = MCV_COMP_AGGREGATE };
+       kFlagAggregate = MCV_COMP_AGGREGATE,
+       kFlagSmemTally = MCV_COMP_SMEM_TALLY };
 
-__device__ __forceinline__ uint64_t comp_nbins(const mcv_component& c) {
+__host__ __device__ __forceinline__ uint64_t comp_nbins(
+    const mcv_component& c) {
   switch (c.opcode) {
     case MCV_OP_PSD_MONITOR:
     case MCV_OP_PSD_MONITOR_4PI:
@@ -71,12 +73,16 @@ __device__ __forceinline__ void apply_transform(Neutron<R>& n,
 // tapered guide, multiple scatterer); the common kernels leave their code
 // out so that it weighs on neither their registers nor their instruction
 // stream (the host launches the kX kernels for such chains only).
+// `smt`: the block's shared-memory tally area (the regeneration kernel's;
+// NULL elsewhere), where monitors flagged MCV_COMP_SMEM_TALLY add.
 template <typename R, bool kX = false, typename Rng, typename Trk>
 __device__ __forceinline__ int run_component(Neutron<R>& n, Rng& rng,
                                              const mcv_component& c,
-                                             Trk& trk, const mcv_chain& ch) {
+                                             Trk& trk, const mcv_chain& ch,
+                                             double* smt = nullptr) {
   Tally tl{c.tally, comp_nbins(c), weight_down<R>(ch),
-           (c.flags & kFlagAggregate) != 0};
+           (c.flags & kFlagAggregate) != 0,
+           (smt && (c.flags & kFlagSmemTally)) ? smt + c.ip[6] : nullptr};
   switch (c.opcode) {
     case MCV_OP_SOURCE_SIMPLE:
       source_simple<R>(n, rng, c);
@@ -153,6 +159,27 @@ struct Counters {
   unsigned processed, overflow, nonfinite, overrun;
 };
 
+// The components after multiple scatterer `c` on one of its output
+// neutrons; returns the index of the last component reached.  Not
+// inlined: the scattering tree calls it from several places.
+template <typename R, bool kX, typename Rng>
+__device__ __noinline__ int ms_downstream(Neutron<R> m, Rng& rng,
+                                          const mcv_chain& ch, int c,
+                                          Counters& k) {
+  NoTrack trk;
+  int last = c;
+  for (int c2 = c + 1; c2 < ch.ncomp; ++c2) {
+    apply_transform<R>(m, ch, c2);
+    last = c2;
+    k.overflow += run_component<R, kX>(m, rng, ch.comp[c2], trk, ch);
+    if (!(m.p > 0)) {
+      if (m_isnan(m.p)) k.nonfinite++;
+      break;
+    }
+  }
+  return last;
+}
+
 // Whole chain on one neutron (the body of the generated
 // process_kernel_no_buffer, acc/run_script.py:182-196).  A neutron leaves
 // the chain after a component that leaves its weight not positive.
@@ -174,24 +201,21 @@ __device__ __forceinline__ int run_chain_one(Neutron<R>& n, Rng& rng,
     trk.begin_component(ch, c);
     if constexpr (kX && !std::decay_t<Trk>::kActive) {
       if (ch.comp[c].opcode == MCV_OP_HMS) {
-        // fan-out: the rest of the chain for every output neutron, in
-        // order, on the same stream (run_script.py:66-92, 245-260)
+        // fan-out: the rest of the chain for every output neutron, on the
+        // same stream (run_script.py:66-92, 245-260); outputs run it as
+        // they become final unless a later component draws random numbers
+        // (ms_downstream_draws), when they wait in `outs` for the whole
+        // tree as in the reference
+        const bool hold = ms_downstream_draws(ch, c);
         Neutron<R> outs[MCV_MS_MAX_SCATTERED];
-        const int nout =
-            ms_scatter<R>(ch.comp[c], rng, outs, n, weight_up<R>(ch));
-        for (int j = 0; j < nout; ++j) {
-          n = outs[j];
-          for (int c2 = c + 1; c2 < nc; ++c2) {
-            apply_transform<R>(n, ch, c2);
-            last = c2;
-            k.overflow +=
-                run_component<R, kX>(n, rng, ch.comp[c2], trk, ch);
-            if (!(n.p > 0)) {
-              if (m_isnan(n.p)) k.nonfinite++;
-              break;
-            }
-          }
-        }
+        int nout = 0;
+        auto emit = [&](const Neutron<R>& o) {
+          if (hold) outs[nout++] = o;
+          else last = ms_downstream<R, kX>(o, rng, ch, c, k);
+        };
+        ms_scatter<R>(ch.comp[c], rng, n, weight_up<R>(ch), emit);
+        for (int j = 0; j < nout; ++j)
+          last = ms_downstream<R, kX>(outs[j], rng, ch, c, k);
         alive = false;
         continue;
       }
@@ -355,12 +379,19 @@ __device__ __forceinline__ void tail_load(const uint32_t* q, int slot,
 // Every neutron is computed with the same functions, in the same order and
 // with its own Philox stream, as in chain_kernel, so results agree neutron
 // by neutron (up to the compiler's contraction choices).
+//
+// Shared memory: first `tally_words` doubles of monitor tallies
+// (MCV_COMP_SMEM_TALLY: zeroed here, added to the global tallies when the
+// block ends), then the tail queues.
 template <typename R, bool kX, typename Trk>
 __device__ __forceinline__ void regen_body(const mcv_chain& ch, uint64_t n,
                                            uint64_t first, uint64_t seed,
-                                           int tail_queue, DevStatus* st,
-                                           Trk& trk) {
-  extern __shared__ uint32_t tail_smem[];
+                                           int tail_queue, int tally_words,
+                                           DevStatus* st, Trk& trk) {
+  extern __shared__ __align__(16) uint32_t tail_smem[];
+  double* const smt = tally_words ? (double*)tail_smem : nullptr;
+  for (int i = threadIdx.x; i < tally_words; i += blockDim.x) smt[i] = 0.0;
+  if (tally_words) __syncthreads();
   constexpr unsigned kFull = 0xffffffffu;
   const unsigned lane = threadIdx.x & 31u;
   const unsigned below = (1u << lane) - 1u;
@@ -387,7 +418,8 @@ __device__ __forceinline__ void regen_body(const mcv_chain& ch, uint64_t n,
   // per slot: the neutron and its stream (kTailWords), then the tracker's
   // per-neutron state
   constexpr int kWords = kTailWords + Trk::kQueueWords;
-  uint32_t* q = tail_smem + (threadIdx.x >> 5) * (kWords * kTailCap);
+  uint32_t* q = tail_smem + 2 * tally_words +
+                (threadIdx.x >> 5) * (kWords * kTailCap);
   uint32_t* qt = q + kTailWords * kTailCap;
   int qhead = 0, qcount = 0;  // warp-uniform
   for (;;) {
@@ -436,7 +468,7 @@ __device__ __forceinline__ void regen_body(const mcv_chain& ch, uint64_t n,
         nb = 0;
         if (inside) continue;
       } else {
-        k.overflow += run_component<R, kX>(nt, rng, cp, trk, ch);
+        k.overflow += run_component<R, kX>(nt, rng, cp, trk, ch, smt);
       }
       if (!(nt.p > 0) || kc + 1 >= nc) {
         if (m_isnan(nt.p)) k.nonfinite++;
@@ -488,15 +520,29 @@ __device__ __forceinline__ void regen_body(const mcv_chain& ch, uint64_t n,
     }
   }
   flush_counters(k, st);
+  if (tally_words) {
+    // the block's shared-memory tallies into the global ones
+    __syncthreads();
+    for (int kc = 0; kc < nc; ++kc) {
+      const mcv_component& cp = ch.comp[kc];
+      if (!(cp.flags & kFlagSmemTally) || !cp.tally) continue;
+      const int m = 3 * (int)comp_nbins(cp);
+      const double* src = smt + cp.ip[6];
+      for (int i = threadIdx.x; i < m; i += blockDim.x) {
+        const double v = src[i];
+        if (v != 0.0) atomicAdd(cp.tally + i, v);
+      }
+    }
+  }
 }
 
 template <typename R, bool kX = false>
 __global__ void __launch_bounds__(kMaxThreads, 4)
     regen_kernel(const __grid_constant__ mcv_chain ch, uint64_t n,
                  uint64_t first, uint64_t seed, int tail_queue,
-                 DevStatus* st) {
+                 int tally_words, DevStatus* st) {
   NoTrack trk;
-  regen_body<R, kX>(ch, n, first, seed, tail_queue, st, trk);
+  regen_body<R, kX>(ch, n, first, seed, tail_queue, tally_words, st, trk);
 }
 
 // The backward replay with the regeneration kernel's structure: the same
@@ -509,7 +555,7 @@ __global__ void __launch_bounds__(kMaxThreads)
                       uint64_t first, uint64_t seed, double* powder_x,
                       double* powder_y, int tail_queue, DevStatus* st) {
   GradTrack<R> trk(g, ch, powder_x, powder_y);
-  regen_body<R, false>(ch, n, first, seed, tail_queue, st, trk);
+  regen_body<R, false>(ch, n, first, seed, tail_queue, 0, st, trk);
   trk.flush(ch);
 }
 
@@ -710,9 +756,10 @@ struct Launchers {
                     uint64_t first, uint64_t seed, const float* uni,
                     int stride, double* out_n, int* out_last, DevStatus* st);
   // smem: the tail queue's bytes (0 = no queue)
+  // smem: the tally area (tally_words doubles) and the tail queue
   static int occupancy_regen(int threads, size_t smem, bool x);
-  static void regen(int blocks, int threads, size_t smem, bool x,
-                    cudaStream_t s, const mcv_chain& ch, uint64_t n,
+  static void regen(int blocks, int threads, size_t smem, int tally_words,
+                    bool x, cudaStream_t s, const mcv_chain& ch, uint64_t n,
                     uint64_t first, uint64_t seed, DevStatus* st);
   static int occupancy_grad_regen(int threads, size_t smem);
   // dynamic shared memory above 48 KB must be allowed per kernel
@@ -809,15 +856,17 @@ int Launchers<R>::occupancy_regen(int threads, size_t smem, bool x) {
 }
 
 template <typename R>
-void Launchers<R>::regen(int blocks, int threads, size_t smem, bool x,
-                         cudaStream_t s, const mcv_chain& ch, uint64_t n,
-                         uint64_t first, uint64_t seed, DevStatus* st) {
+void Launchers<R>::regen(int blocks, int threads, size_t smem,
+                         int tally_words, bool x, cudaStream_t s,
+                         const mcv_chain& ch, uint64_t n, uint64_t first,
+                         uint64_t seed, DevStatus* st) {
+  const int queue = smem > (size_t)tally_words * 8 ? 1 : 0;
   if (x)
     regen_kernel<R, true><<<blocks, threads, smem, s>>>(
-        ch, n, first, seed, smem > 0 ? 1 : 0, st);
+        ch, n, first, seed, queue, tally_words, st);
   else
     regen_kernel<R, false><<<blocks, threads, smem, s>>>(
-        ch, n, first, seed, smem > 0 ? 1 : 0, st);
+        ch, n, first, seed, queue, tally_words, st);
 }
 
 template <typename R>

@@ -6,7 +6,8 @@
 // (transmitted and scattered branches, iterated max_ms_loops x
 // max_ms_loops_path1 times).  The work lists are per-thread arrays of
 // MCV_MS_MAX_SCATTERED neutrons, as the reference's are per-thread local
-// arrays; the caller runs the rest of the chain on each output.  The FP64
+// arrays; the outputs go to a callback as they become final, and the
+// caller runs the rest of the chain on each.  The FP64
 // forms follow the reference's operation order; FP32 takes its hit times
 // from the ray's closest approach (intersect_shape_from), and the event
 // probability cut is compared in the chain's weight scale.
@@ -240,29 +241,32 @@ __device__ __noinline__ int ms_interact_m1(const mcv_component& c,
   return 2;
 }
 
-// _interactM_path1 (:123-177): out holds max_scattered_neutrons
-template <typename R, typename Rng>
-__device__ __noinline__ int ms_path1(const mcv_component& c, Rng& rng,
-                                     Neutron<R>* out, const Neutron<R>& n0,
-                                     R min_prob) {
+// _interactM_path1 (:123-177), with its output neutrons handed to
+// `emit` in the reference's order instead of collected in a list: the
+// work lists are the only per-lane arrays, and they hold the neutrons
+// still inside the shape (one a level for the usual shapes).
+template <typename R, typename Rng, typename Emit>
+__device__ __noinline__ void ms_path1(const mcv_component& c, Rng& rng,
+                                         const Neutron<R>& n0, R min_prob,
+                                         Emit& emit) {
   const int max_sc = c.ip[6], loops1 = c.ip[7] >> 16;
+  if (n0.p < min_prob) return;
   Neutron<R> buf_a[MCV_MS_MAX_SCATTERED], buf_b[MCV_MS_MAX_SCATTERED];
-  Neutron<R> sc[2];
   Neutron<R>* tbs = buf_a;
   Neutron<R>* tbs2 = buf_b;
-  if (n0.p < min_prob) return 0;
   int ntbs = 1, out_index = 0;
   tbs[0] = n0;
   for (int iloop = 0; iloop < loops1; ++iloop) {
     int s2 = 0;
     for (int i = 0; i < ntbs; ++i) {
+      Neutron<R> sc[2];
       const int ns = ms_interact_m1(c, rng, sc, tbs[i]);
       for (int j = 0; j < ns; ++j) {
         const Neutron<R>& s1 = sc[j];
         if (s1.p < min_prob) continue;
         if (ms_locate<R>(c, s1.x, s1.y, s1.z) != kInside) {
-          out[out_index++] = s1;
-          if (out_index >= max_sc) return out_index;
+          emit(s1);
+          if (++out_index >= max_sc) return;
           continue;
         }
         tbs2[s2++] = s1;
@@ -278,53 +282,59 @@ __device__ __noinline__ int ms_path1(const mcv_component& c, Rng& rng,
   }
   for (int i = 0; i < ntbs; ++i) {
     if (out_index >= max_sc) break;
-    out[out_index++] = tbs[i];
+    emit(tbs[i]);
+    ++out_index;
   }
-  return out_index;
 }
 
-// _scatterM (:196-256): the output neutrons of one incident neutron.
+// _scatterM (:196-256): the output neutrons of one incident neutron, each
+// handed to `emit` as soon as it is final (in the reference's order).
 // `up`: the chain's FP32 weight scale (the probability cut is compared in
-// it).
-template <typename R, typename Rng>
-__device__ __noinline__ int ms_scatter(const mcv_component& c, Rng& rng,
-                                       Neutron<R>* out, const Neutron<R>& n0,
-                                       R up) {
+// it).  A _interactM_path1 call always runs to its end, so that the draws
+// match the reference's (which collects its outputs first): where the
+// reference stops reading them (a full work list, the output limit reached)
+// the outputs that follow are drawn and dropped.
+template <typename R, typename Rng, typename Emit>
+__device__ __noinline__ void ms_scatter(const mcv_component& c, Rng& rng,
+                                           const Neutron<R>& n0, R up,
+                                           Emit& emit) {
   const int max_sc = c.ip[6], loops = c.ip[7] & 0xffff;
   const R min_prob = prm<R>(c, 14) * up;
   Neutron<R> buf_a[MCV_MS_MAX_SCATTERED], buf_b[MCV_MS_MAX_SCATTERED];
-  Neutron<R> sc[MCV_MS_MAX_SCATTERED];
   Neutron<R>* tbs = buf_a;
   Neutron<R>* tbs2 = buf_b;
   Neutron<R> n = n0;
   if constexpr (sizeof(R) == 4) ms_approach(c, n);
   if (ms_is_exiting(c, n)) {
-    out[0] = n0;
-    return 1;
+    emit(n0);
+    return;
   }
   int ntbs = 1, out_index = 0;
   tbs[0] = n;
   for (int iloop = 0; iloop < loops; ++iloop) {
     int s2 = 0;
-    for (int i = 0; i < ntbs; ++i) {
-      const int ns1 = ms_path1<R>(c, rng, sc, tbs[i], min_prob);
-      for (int j = 0; j < ns1; ++j) {
-        Neutron<R>& s1 = sc[j];
-        if (s1.p < min_prob) continue;
-        if (!(m_sqrt(s1.vx * s1.vx + s1.vy * s1.vy + s1.vz * s1.vz) >
-              R(1.e-6)))
-          continue;  // is_moving (acc/neutron.py:39-42)
-        if (ms_locate<R>(c, s1.x, s1.y, s1.z) == kInside)
-          ms_exit_attenuated(c, s1);
-        if (ms_is_exiting(c, s1)) {
-          out[out_index++] = s1;
-          if (out_index >= max_sc) return out_index;
-          continue;
-        }
-        tbs2[s2++] = s1;
-        if (s2 >= max_sc) break;
+    bool full = false, done = false;
+    auto take = [&](const Neutron<R>& o) {
+      if (full || done) return;
+      Neutron<R> s1 = o;
+      if (s1.p < min_prob) return;
+      if (!(m_sqrt(s1.vx * s1.vx + s1.vy * s1.vy + s1.vz * s1.vz) >
+            R(1.e-6)))
+        return;  // is_moving (acc/neutron.py:39-42)
+      if (ms_locate<R>(c, s1.x, s1.y, s1.z) == kInside)
+        ms_exit_attenuated(c, s1);
+      if (ms_is_exiting(c, s1)) {
+        emit(s1);
+        if (++out_index >= max_sc) done = true;
+        return;
       }
-      if (s2 >= max_sc) break;
+      tbs2[s2++] = s1;
+      if (s2 >= max_sc) full = true;
+    };
+    for (int i = 0; i < ntbs; ++i) {
+      ms_path1<R>(c, rng, tbs[i], min_prob, take);
+      if (done) return;
+      if (full) break;
     }
     Neutron<R>* tmp = tbs2;
     tbs2 = tbs;
@@ -341,9 +351,25 @@ __device__ __noinline__ int ms_scatter(const mcv_component& c, Rng& rng,
     const R dist = m_sqrt(dx * dx + dy * dy + dz * dz);
     const R atten = ms_atten_coeff(m, c);
     m.p *= m_exp(-atten * dist);
-    out[out_index++] = m;
+    emit(m);
+    ++out_index;
   }
-  return out_index;
+}
+
+// Whether a component after the multiple scatterer draws random numbers
+// (a sample or a source): then the rest of the chain runs on the outputs
+// after the whole scattering tree, in order, as the reference's generated
+// kernel does (run_script.py:66-92); otherwise each output runs it as soon
+// as it is final, which gives the same tallies without holding the outputs.
+__device__ __forceinline__ bool ms_downstream_draws(const mcv_chain& ch,
+                                                    int c) {
+  for (int k = c + 1; k < ch.ncomp; ++k) {
+    const int op = ch.comp[k].opcode;
+    if (op == MCV_OP_HSS || op == MCV_OP_HMS || op == MCV_OP_SOURCE_SIMPLE ||
+        op == MCV_OP_SNS_SOURCE)
+      return true;
+  }
+  return false;
 }
 
 }  // namespace mcv

@@ -895,19 +895,44 @@ __device__ __forceinline__ void e_q_scatter(Neutron<R>& n, Rng& rng,
   R Q = 0, vf = 0, kf = 0, cost = 0, cost2 = 0;
   int itr = 0;
   bool found = false;
-  for (; itr < max_iter; ++itr) {
-    Q = rng.next() * (Qmax - Qmin);
-    Q += Qmin;
-    const R E = expr_eval<R>(progE, nE, Q);
+  if (c.dp[13] != 0.0) {
+    // E does not depend on Q (dp 13, set by the host): evaluated once.
+    // Every try draws its Q and tests the same arithmetic as below; when
+    // the neutron cannot lose E at all, every one of the max_iter tries
+    // fails, and their draws are skipped without being formed.
+    const R E = expr_eval<R>(progE, nE, Qmin);
     const R Ef = Ei - E;
-    if (Ef < R(0)) continue;
+    if (Ef < R(0)) {
+      rng.skip(max_iter);
+      n.p = R(0);
+      return;
+    }
     vf = m_sqrt(Ef) * R(kSE2V);
     kf = R(kV2K) * vf;
-    cost = (ki * ki + kf * kf - Q * Q) / (2 * ki * kf);
-    cost2 = cost * cost;
-    if (cost2 > R(1)) continue;
-    found = true;
-    break;
+    for (; itr < max_iter; ++itr) {
+      Q = rng.next() * (Qmax - Qmin);
+      Q += Qmin;
+      cost = (ki * ki + kf * kf - Q * Q) / (2 * ki * kf);
+      cost2 = cost * cost;
+      if (cost2 > R(1)) continue;
+      found = true;
+      break;
+    }
+  } else {
+    for (; itr < max_iter; ++itr) {
+      Q = rng.next() * (Qmax - Qmin);
+      Q += Qmin;
+      const R E = expr_eval<R>(progE, nE, Q);
+      const R Ef = Ei - E;
+      if (Ef < R(0)) continue;
+      vf = m_sqrt(Ef) * R(kSE2V);
+      kf = R(kV2K) * vf;
+      cost = (ki * ki + kf * kf - Q * Q) / (2 * ki * kf);
+      cost2 = cost * cost;
+      if (cost2 > R(1)) continue;
+      found = true;
+      break;
+    }
   }
   if (!found) {
     n.p = R(0);

@@ -49,9 +49,11 @@ def build_chain(components, offsets=None, rotmats=None, binder=None):
             ch.comp[slot].flags |= nat.FLAG_IDENTITY_ROT
 
     slot = 0
+    smem_words = 0
     for i, comp in enumerate(components):
         c = ch.comp[slot]
         comp.pack(c, binder)
+        smem_words = _smem_tally(comp, c, smem_words)
         if slot > 0:
             if offsets is None:
                 off, rot = np.zeros(3), eye
@@ -67,6 +69,27 @@ def build_chain(components, offsets=None, rotmats=None, binder=None):
         slot += 1 + extra[i]
     ch.weight_exp2 = weight_exp2(components)
     return ch
+
+
+def _smem_tally(comp, c, words):
+    """Give a monitor a shared-memory tally copy (MCV_COMP_SMEM_TALLY) at
+    offset `words` of the block's tally area when it asks for one
+    (smem_tally True) or is small (None and at most SMEM_TALLY_AUTO_BINS
+    bins) and it fits; returns the area's new size."""
+    want = getattr(comp, "smem_tally", False)
+    if want is False or not c.tally:
+        return words
+    nb = comp.nbins()
+    if want is None and nb > comp.SMEM_TALLY_AUTO_BINS:
+        return words
+    if words + 3 * nb > nat.MCV_SMEM_TALLY_MAX:
+        if want:
+            raise ValueError(f"{comp.name}: {nb} bins do not fit the "
+                             "shared-memory tally area")
+        return words
+    c.flags |= nat.FLAG_SMEM_TALLY
+    c.ip[6] = words
+    return words + 3 * nb
 
 
 # where the FP32 kernels place a source's nominal weight: 2^64 leaves 64

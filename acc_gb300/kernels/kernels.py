@@ -175,6 +175,11 @@ class E_Q_Kernel:
         self.E_prog = compile_expression(self.E_Q)
         self.S_prog = compile_expression(self.S_Q)
 
+    def E_depends_on_Q(self):
+        """Whether the E(Q) program reads Q."""
+        from .expression import Q_
+        return bool(np.any(np.asarray(self.E_prog)[:, 0] == Q_))
+
     def program(self):
         """{opcode, argument} rows: the E(Q) program, then the S(Q) one."""
         return np.concatenate([self.E_prog, self.S_prog])
@@ -185,6 +190,9 @@ class E_Q_Kernel:
         set_param(c, 10, self.Qmin)
         set_param(c, 11, self.Qmax)
         set_param(c, 12, float(self.max_iter))
+        # 1 when E(Q) does not read Q: the device evaluates it once per
+        # scatter instead of once per try (same values, same draws)
+        set_param(c, 13, 0.0 if self.E_depends_on_Q() else 1.0)
         c.ip[4], c.ip[5] = len(self.E_prog), len(self.S_prog)
         flat = np.ascontiguousarray(self.program().reshape(-1))
         c.table = binder.table(comp, "expr", flat, np.float64)

@@ -366,6 +366,45 @@ def grad_cost(name, ncount, params, reps=2):
     return out
 
 
+def powder_atomic_roofline(ncount=int(1e9), reps=3):
+    """Config 5's forward (guide chain -> powder cylinder -> banked detector
+    of 2.62e8 bins) in FP32: its rate, and its tally atomics against the
+    measured L2 atomic throughput (mcv_probe_atomic_rate: FP64 atomicAdd
+    into random bins of an array the size of the detector's tally).  Each
+    detected neutron makes three FP64 atomics (N, sum p, sum p^2)."""
+    import torch
+    from acc_gb300 import engine, instruments
+    ins = instruments.powder_banked()
+    chain = engine.chain_for_instrument(ins)
+    det = ins.components[-1]
+    nb = det.nbins()
+    engine.run_chain(chain, ncount, seed=7, floattype="float32", sync=False)
+    engine.read_status(expected=ncount)
+    det._device_tally.zero_()
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    a.record()
+    for r in range(reps):
+        engine.run_chain(chain, ncount, seed=7, floattype="float32",
+                         first=(r + 1) * ncount, sync=False)
+    b.record()
+    b.synchronize()
+    engine.read_status(expected=reps * ncount)
+    s = a.elapsed_time(b) / 1e3 / reps
+    detected = float(det._device_tally[:nb].sum()) / reps
+    peak = engine.probe_atomic_rate(3 * nb)
+    got = 3 * detected / s
+    return {"value": ncount / s, "unit": UNIT, "ms_per_launch": 1e3 * s,
+            "neutrons_per_launch": ncount, "detector_bins": nb,
+            "detected_per_launch": detected,
+            "roofline": {"bound": "l2_atomics", "achieved": got,
+                         "peak": peak, "unit": "FP64 atomics/s",
+                         "frac": got / peak,
+                         "per_unit": "3 FP64 atomics per detected neutron",
+                         "peak_source": "mcv_probe_atomic_rate over "
+                                        f"{3 * nb} doubles (random bins)"}}
+
+
 def grad_costs():
     from acc_gb300 import instruments
     sqe = grad_cost(
@@ -531,6 +570,7 @@ def ours_arm(a, rank, world, local_rank):
     if not a.no_batched:
         batched = batched_run(world, rank)
     grads = None if a.no_grad or rank != 0 else grad_costs()
+    powder = None if a.no_grad or rank != 0 else powder_atomic_roofline()
 
     if rank != 0:
         return 0
@@ -561,38 +601,42 @@ def ours_arm(a, rank, world, local_rank):
     counts = KERNEL_COUNTS.get(a.workload, {})
     fpn = counts.get("fp32_flops_per_neutron")
     achieved = fpn * ncount / mean_s / 1e12 if fpn else None
-    roofline = {
-        "bound": "compute",
+    fp32_pipe = {
         "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
         "frac": achieved / fp32_peak if achieved else None,
-        "traffic": counts.get("dram_bytes_per_launch"),
-        "kernel": "mcv::regen_kernel<float>",
+        "per_unit": f"{fpn} executed FP32 flops per neutron (ncu count)",
         "peak_source": "FP32 FMA peak measured in this run "
                        "(mcv_probe_fma_peak); the measured peak file has "
                        "HBM and bf16-tensor peaks only",
-        "per_unit": f"{fpn} executed FP32 flops per neutron (ncu count)",
+        "fp64_peak_tflops": fp64_peak,
+    }
+    # the binding limit: one warp instruction per cycle per SM sub-partition
+    # (4 per SM); divergence (SIMT efficiency) sets how many warp
+    # instructions a neutron costs.  The FP32 pipe is far from its peak
+    # (fp32_pipe): the kernel issues control flow, compares and loads
+    # between its multiply-adds.
+    wpn = counts.get("warp_inst_per_neutron")
+    sms = torch.cuda.get_device_properties(
+        torch.cuda.current_device()).multi_processor_count
+    mhz = (clk or {}).get("sm_mhz") or 2070.0
+    peak_issue = sms * 4 * mhz * 1e6
+    got = wpn * ncount / mean_s if wpn else None
+    roofline = {
+        "bound": "issue",
+        "achieved": got, "peak": peak_issue, "unit": "warp-inst/s",
+        "frac": got / peak_issue if got else None,
+        "traffic": counts.get("dram_bytes_per_launch"),
+        "kernel": "mcv::regen_kernel<float>",
+        "per_unit": f"{wpn} warp instructions per neutron (ncu count), "
+                    f"{counts.get('thread_inst_per_neutron')} thread "
+                    "instructions",
+        "peak_source": "SMs x 4 issue slots x median SM clock sampled "
+                       "during the timed region",
         "traffic_note": "DRAM bytes of one launch from ncu on a "
                         f"{counts.get('captured_neutrons')}-neutron launch: "
                         "the tally bins, independent of the neutron count",
-        "fp64_peak_tflops": fp64_peak,
+        "fp32_pipe": fp32_pipe,
     }
-    wpn = counts.get("warp_inst_per_neutron")
-    if wpn and clk and clk.get("sm_mhz"):
-        # the binding limit: one warp instruction per cycle per SM sub-
-        # partition (4 per SM); divergence (SIMT efficiency) sets how many
-        # warp instructions a neutron costs
-        sms = torch.cuda.get_device_properties(
-            torch.cuda.current_device()).multi_processor_count
-        peak_issue = sms * 4 * clk["sm_mhz"] * 1e6
-        got = wpn * ncount / mean_s
-        roofline["issue"] = {
-            "achieved": got, "peak": peak_issue, "unit": "warp-inst/s",
-            "frac": got / peak_issue,
-            "per_unit": f"{wpn} warp instructions per neutron (ncu count), "
-                        f"{counts.get('thread_inst_per_neutron')} thread "
-                        "instructions",
-            "peak_source": "SMs x 4 issue slots x median SM clock sampled "
-                           "during the timed region"}
     cpu = None
     if world == 1 and not a.no_cpu_baseline:
         from oracle import build as OB
@@ -637,6 +681,7 @@ def ours_arm(a, rank, world, local_rank):
             "note": "same FP32 kernel body without path regeneration"},
         "chi2_fp32_vs_fp64": chi2,
         "bwd_over_fwd": grads,
+        "powder_banked_forward": powder,
         "batched": batched,
         "e2e": e2e,
         "roofline": roofline,

@@ -166,6 +166,8 @@ enum {
  *               table: nQ x nE float32 S(Q,E), row-major in Q
  *       CONSTANT_QE: 10 Q (1/A) 11 E (meV)
  *       E_Q: 10 Qmin 11 Qmax (1/A) 12 max_iter (tries of the Q draw)
+ *               13: 1 when the E(Q) program does not read Q (it is then
+ *               evaluated once per scatter; the results are the same)
  *               ip[4] = E(Q) instructions, ip[5] = S(Q) instructions
  *               (each 1..MCV_EXPR_MAX_OPS); table (float64) and ftable
  *               (float32): the E(Q) program then the S(Q) program,
@@ -272,6 +274,16 @@ enum {
 #define MCV_COMP_IDENTITY_ROT 1   /* rot of this hop is the identity         */
 #define MCV_COMP_AGGREGATE 2      /* monitors: always warp-aggregate tally
                                      atomics (hot bins aggregate anyway) */
+#define MCV_COMP_SMEM_TALLY 4     /* monitors: the FP32 path-regeneration
+                                     kernel adds this monitor's entries into
+                                     a per-block copy of its tally in shared
+                                     memory and adds that copy to `tally`
+                                     when the block ends; ip[6] = the copy's
+                                     offset (doubles) in the block's tally
+                                     area, which holds the 3 nbins doubles
+                                     of every such monitor, at most
+                                     MCV_SMEM_TALLY_MAX doubles in all */
+#define MCV_SMEM_TALLY_MAX 2048
 
 typedef struct mcv_component {
   int32_t opcode;

@@ -503,3 +503,31 @@ def test_fp64_fma_variant_histograms(name):
         rel = np.abs(g[1] - o[1])[same] / o[1][same]
         assert (rel > 1e-9).mean() <= 1e-3, (gc.name, np.sort(rel)[-3:])
         assert g[0].sum() > 0
+
+
+def test_shared_memory_tallies_equal_global_ones():
+    """MCV_COMP_SMEM_TALLY (the FP32 regeneration kernel adds a small
+    monitor's entries into a per-block shared-memory copy, added to the
+    global tally at the block's end) gives the global-atomic histogram:
+    identical counts, sums within 1e-12 (only the order of additions
+    differs).  With smem_tally None the guide chain's 200-bin energy
+    monitor takes the copy; the 10000-bin PSD does not."""
+    from acc_gb300.memory import HostBinder
+    n, seed = 2_000_000, 8
+    out = []
+    for smem in (False, None):
+        ins = instruments.guide_chain()
+        for c in ins.components:
+            if hasattr(c, "smem_tally"):
+                c.smem_tally = smem
+        ch = engine.chain_for_instrument(ins)
+        flags = [ch.comp[k].flags & 4 for k in range(ch.ncomp)]
+        assert sum(1 for f in flags if f) == (0 if smem is False else 1)
+        engine.run_chain(ch, n, seed=seed, floattype="float32",
+                         variant="regen")
+        out.append([c.out.reshape(3, -1) for c in ins.components
+                    if hasattr(c, "smem_tally")])
+    for g, s in zip(*out):
+        np.testing.assert_array_equal(g[0], s[0])
+        np.testing.assert_allclose(g[1:], s[1:], rtol=1e-12, atol=1e-300)
+        assert g[0].sum() > 1000
