@@ -897,9 +897,9 @@ __device__ __forceinline__ void e_q_scatter(Neutron<R>& n, Rng& rng,
   bool found = false;
   if (c.dp[13] != 0.0) {
     // E does not depend on Q (dp 13, set by the host): evaluated once.
-    // Every try draws its Q and tests the same arithmetic as below; when
-    // the neutron cannot lose E at all, every one of the max_iter tries
-    // fails, and their draws are skipped without being formed.
+    // FP64: every try draws its Q and tests the same arithmetic as below;
+    // when the neutron cannot lose E at all, every one of the max_iter
+    // tries fails, and their draws are skipped without being formed.
     const R E = expr_eval<R>(progE, nE, Qmin);
     const R Ef = Ei - E;
     if (Ef < R(0)) {
@@ -909,7 +909,44 @@ __device__ __forceinline__ void e_q_scatter(Neutron<R>& n, Rng& rng,
     }
     vf = m_sqrt(Ef) * R(kSE2V);
     kf = R(kV2K) * vf;
-    for (; itr < max_iter; ++itr) {
+    if constexpr (sizeof(R) == 4) {
+      // FP32: the loop's outcome drawn directly.  A try accepts Q exactly
+      // when |ki - kf| <= Q <= ki + kf (cos^2 <= 1), an interval of
+      // [Qmin, Qmax) taken with probability a; the failed tries before
+      // the first success are geometric (P(>= k) = (1 - a)^k, drawn by
+      // inversion) and the accepted Q is uniform on the interval, so
+      // (tries, Q) has the reference's distribution from two draws
+      // instead of up to max_iter.  Near the threshold (Ef -> 0, a -> 0)
+      // the loop takes tens of tries, on some lanes of a warp only.
+      const R lo = m_fabs(ki - kf) > Qmin ? m_fabs(ki - kf) : Qmin;
+      const R hi = ki + kf < Qmax ? ki + kf : Qmax;
+      if (!(hi > lo)) {
+        n.p = R(0);
+        return;
+      }
+      const R a = (hi - lo) / (Qmax - Qmin);
+      int fails = 0;
+      if (a < R(1)) {
+        const R u = rng.next();
+        const float r = logf(1.f - u) / log1pf(-a);
+        if (!(r < float(max_iter))) {
+          n.p = R(0);
+          return;
+        }
+        fails = (int)r;
+      }
+      if (fails >= max_iter) {
+        n.p = R(0);
+        return;
+      }
+      itr = fails;
+      Q = lo + rng.next() * (hi - lo);
+      cost = (ki * ki + kf * kf - Q * Q) / (2 * ki * kf);
+      cost = cost > R(1) ? R(1) : (cost < R(-1) ? R(-1) : cost);
+      cost2 = cost * cost;
+      found = true;
+    }
+    for (; !found && itr < max_iter; ++itr) {
       Q = rng.next() * (Qmax - Qmin);
       Q += Qmin;
       cost = (ki * ki + kf * kf - Q * Q) / (2 * ki * kf);

@@ -72,3 +72,43 @@ def test_e_q_dispersion_on_gpu(floattype):
     want = 5 * np.sin(Q) ** 2 + 5
     tE, _ = TOL[floattype]
     assert np.abs(E - want).max() <= max(tE, 1e-7), np.abs(E - want).max()
+
+
+@pytest.mark.parametrize("E_Q", ["59.5", "50", "20"])
+def test_constant_e_near_threshold_fp32_chi2(E_Q):
+    """An E(Q) kernel whose E does not depend on Q: the FP32 kernels draw
+    the rejection loop's outcome directly (geometric tries, Q uniform on the
+    accepted interval), the FP64 ones run the loop as the reference does.
+    On the 70 meV box with Q drawn on [0, 35) /A, E = 59.5 meV accepts
+    13% of the draws (several tries, weight 1/tries), E = 50 meV 20% and
+    E = 20 meV 34%.  FP32 (GPU) against the FP64 oracle on independent
+    streams: chi^2/dof of the I(Q, E) monitor within 1.1 + 3 sqrt(2/dof),
+    and the total weight within 1%.  FP64 GPU equals the oracle bin for
+    bin (counts exact, sums 1e-12)."""
+    import sys
+    import os
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    from helpers import chi2_per_dof, gpu_tallies, oracle_run
+
+    def box():
+        return instruments.e_q_box(E_Q=E_Q, S_Q="1+0.1*Q", Qmin=0.0,
+                                   Qmax=35.0)
+
+    n = 1_000_000
+    ins = box()
+    engine.run_instrument(ins, n, seed=101, floattype="float32")
+    (_, g), = gpu_tallies(ins).items()
+    ot, _, _, _ = oracle_run(box(), n, seed=202)
+    (_, o), = ot.items()
+    g, o = g.reshape(3, -1), o.reshape(3, -1)
+    c2, dof = chi2_per_dof(g, o)
+    assert dof > 20
+    assert c2 <= 1.1 + 3 * np.sqrt(2 / dof), (c2, dof)
+    assert g[1].sum() == pytest.approx(o[1].sum(), rel=0.01)
+    ins = box()
+    engine.run_instrument(ins, 200_000, seed=5, floattype="float64")
+    (_, g), = gpu_tallies(ins).items()
+    ot, _, _, _ = oracle_run(box(), 200_000, seed=5)
+    (_, o), = ot.items()
+    np.testing.assert_array_equal(g[0], o[0])
+    np.testing.assert_allclose(g[1:], o[1:], rtol=1e-12, atol=1e-300)
