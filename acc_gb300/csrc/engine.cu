@@ -357,6 +357,38 @@ bool has_hms(const mcv_chain* ch) {
   return false;
 }
 
+// Chains whose multiple scatterer runs in the warp-synchronous tree kernel
+// (ms_chain_kernel): no component after it draws random numbers (the
+// outputs then run the rest of the chain as they become final), and the
+// launch does not ask for the thread kernel (variant 1).
+bool use_ms_kernel(const mcv_chain* ch, const mcv_launch* launch) {
+  if (launch && launch->variant == 1) return false;
+  int k = 0;
+  while (k < ch->ncomp && ch->comp[k].opcode != MCV_OP_HMS) ++k;
+  if (k == ch->ncomp) return false;
+  for (++k; k < ch->ncomp; ++k) {
+    const int op = ch->comp[k].opcode;
+    if (op == MCV_OP_HSS || op == MCV_OP_HMS || op == MCV_OP_SOURCE_SIMPLE ||
+        op == MCV_OP_SNS_SOURCE)
+      return false;
+  }
+  return true;
+}
+
+template <typename R>
+void launch_ms(mcv_ctx* ctx, const mcv_chain* chain, uint64_t ncount,
+               uint64_t first, uint64_t seed, const mcv_launch* launch,
+               cudaStream_t s) {
+  int blocks, threads;
+  // one warp handles a run of incident neutrons: the grid's warps each
+  // take at least 32
+  launch_shape(
+      ctx, [](int t) { return Launchers<R>::occupancy_ms(t); },
+      (ncount + 31) / 32 * 32, launch, &blocks, &threads);
+  Launchers<R>::ms(blocks, threads, s, *chain, ncount, first, seed,
+                   ctx->d_status);
+}
+
 // The rarer components run in their own kernel instantiations (kX): the
 // SNS source, the tapered and mesh guides, the multiple scatterer, stored
 // neutrons in or out, and samples with the constant-(Q, E), E(Q), composite, SANS2D
@@ -688,16 +720,24 @@ int mcv_run_chain(mcv_ctx* ctx, const mcv_chain* chain, uint64_t ncount,
   if (ncount == 0) return st ? mcv_ctx_status(ctx, stream, 0, st) : MCV_OK;
   DeviceGuard g(ctx->device);
   cudaStream_t s = (cudaStream_t)stream;
-  if (precision == MCV_FP32) {
+  if (use_ms_kernel(chain, launch) &&
+      !(launch && launch->variant == MCV_VARIANT_FP64_FMA)) {
+    if (precision == MCV_FP32)
+      launch_ms<float>(ctx, chain, ncount, first, seed, launch, s);
+    else
+      launch_ms<double>(ctx, chain, ncount, first, seed, launch, s);
+  } else if (precision == MCV_FP32) {
     if (use_regen(chain, launch)) {
       int blocks, threads;
       const bool x = is_exotic(chain);
-      const int tw = smem_tally_words(chain);
+      // the kX kernels take no shared-memory tally copies
+      const int tw = x ? 0 : smem_tally_words(chain);
       launch_shape(
           ctx,
           [chain, launch, x, tw](int t) {
             return Launchers<float>::occupancy_regen(
-                t, (size_t)tw * 8 + regen_tail_bytes(chain, launch, t), x);
+                t, (size_t)tw * 8 + regen_tail_bytes(chain, launch, t), tw,
+                x);
           },
           ncount, launch, &blocks, &threads);
       Launchers<float>::regen(

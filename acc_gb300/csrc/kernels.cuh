@@ -302,6 +302,267 @@ __global__ void __launch_bounds__(kMaxThreads, kDense ? 4 : 0)
   flush_counters(k, st);
 }
 
+// ---------------------------------------------------------------------------
+// Chains with a multiple scatterer: a warp-synchronous form of the
+// scattering tree.
+//
+// The thread kernel runs each incident neutron's tree (_scatterM ->
+// _interactM_path1 -> _interactM1, homogeneous_multiple_scatterer.py:86-256)
+// as nested loops on its own lane.  Lanes leave those loops at different
+// points (a transfer the neutron cannot make ends its tree early), the warp
+// executes the branches one after the other, and each lane's call frames
+// and work lists are read and written at different times: on the UN
+// benchmark 5 lanes of 32 were active and the per-lane stacks spilled
+// gigabytes to DRAM.  Here the same tree is a per-lane state machine: each
+// pass of a warp-uniform loop first advances every lane's bookkeeping to its
+// next _interactM1 call (or to the end of its tree, emitting the outputs on
+// the way), then makes that call on all lanes together and files its two
+// outputs.  A lane whose tree ends takes the next incident neutron.  Every
+// neutron goes through the same operations in the same order, with its own
+// Philox stream, as in the thread kernel, so results agree neutron by
+// neutron.  Used when no component after the scatterer draws random
+// numbers (the outputs then run the rest of the chain as they become
+// final, ms_downstream_draws).
+template <typename R>
+struct MsLane {
+  Neutron<R> tbs[2][MCV_MS_MAX_SCATTERED];   // _scatterM's work lists
+  Neutron<R> ptbs[2][MCV_MS_MAX_SCATTERED];  // _interactM_path1's lists
+  Neutron<R> sc[2];                          // one _interactM1's outputs
+  // _scatterM: list in use, loop, index, sizes, output count, final index
+  int ob, iloop, i, ntbs, s2, out_index, fi, ophase;  // ophase 0 loop, 1 final
+  bool full, done;
+  // _interactM_path1: active, list in use, loop, index, sizes, outputs,
+  // tail index; pphase 0 calls, 1 tail, 2 returned
+  bool p_active;
+  int pb, pl, pi, pntbs, ps2, pout, ptail, pphase;
+};
+
+// the consumer of _scatterM (:214-235) for one _interactM_path1 output
+template <typename R, typename Emit>
+__device__ __forceinline__ void ms_take(const mcv_component& c, MsLane<R>& S,
+                                        const Neutron<R>& o, R min_prob,
+                                        int max_sc, Emit& emit) {
+  if (S.full || S.done) return;
+  Neutron<R> s1 = o;
+  if (s1.p < min_prob) return;
+  if (!(m_sqrt(s1.vx * s1.vx + s1.vy * s1.vy + s1.vz * s1.vz) > R(1.e-6)))
+    return;  // is_moving (acc/neutron.py:39-42)
+  if (ms_locate<R>(c, s1.x, s1.y, s1.z) == kInside) ms_exit_attenuated(c, s1);
+  if (ms_is_exiting(c, s1)) {
+    emit(s1);
+    if (++S.out_index >= max_sc) S.done = true;
+    return;
+  }
+  S.tbs[S.ob ^ 1][S.s2++] = s1;
+  if (S.s2 >= max_sc) S.full = true;
+}
+
+// Start an incident neutron's tree; false when it is final at once (it
+// does not enter the shape: _scatterM emits it unchanged, :203-205).
+template <typename R, typename Emit>
+__device__ __forceinline__ bool ms_begin(const mcv_component& c, MsLane<R>& S,
+                                         const Neutron<R>& n0, Emit& emit) {
+  Neutron<R> n = n0;
+  if constexpr (sizeof(R) == 4) ms_approach(c, n);
+  if (ms_is_exiting(c, n)) {
+    emit(n0);
+    return false;
+  }
+  S.tbs[0][0] = n;
+  S.ob = 0;
+  S.ntbs = 1;
+  S.iloop = 0;
+  S.i = 0;
+  S.s2 = 0;
+  S.out_index = 0;
+  S.fi = 0;
+  S.full = S.done = false;
+  S.p_active = false;
+  S.ophase = (c.ip[7] & 0xffff) > 0 ? 0 : 1;
+  return true;
+}
+
+// Advance a lane's tree to its next _interactM1 call (true: the call is on
+// S.ptbs[S.pb][S.pi]) or to its end (false), emitting outputs on the way.
+template <typename R, typename Emit>
+__device__ __noinline__ bool ms_advance(const mcv_component& c, MsLane<R>& S,
+                                        R min_prob, Emit& emit) {
+  const int max_sc = c.ip[6], loops = c.ip[7] & 0xffff,
+            loops1 = c.ip[7] >> 16;
+  for (;;) {
+    if (S.p_active) {
+      if (S.pphase == 0) {
+        if (S.pi < S.pntbs) return true;
+        // the end of one _interactM_path1 loop (:163-167)
+        S.pb ^= 1;
+        S.pntbs = S.ps2;
+        S.ps2 = 0;
+        S.pi = 0;
+        if (S.pntbs == 0 || ++S.pl >= loops1) {
+          S.pphase = 1;
+          S.ptail = 0;
+        }
+        continue;
+      }
+      if (S.pphase == 1 && S.ptail < S.pntbs && S.pout < max_sc &&
+          !S.done) {
+        // the neutrons still inside after the loops (:168-174)
+        ms_take<R>(c, S, S.ptbs[S.pb][S.ptail], min_prob, max_sc, emit);
+        ++S.ptail;
+        ++S.pout;
+        continue;
+      }
+      // _interactM_path1 returned (:237-240)
+      S.p_active = false;
+      if (S.done) return false;
+      if (S.full) S.i = S.ntbs;
+      else ++S.i;
+      continue;
+    }
+    if (S.ophase == 0) {
+      if (S.i < S.ntbs) {
+        const Neutron<R>& m = S.tbs[S.ob][S.i];
+        if (m.p < min_prob) {  // _interactM_path1 returns at once (:130)
+          ++S.i;
+          continue;
+        }
+        S.ptbs[0][0] = m;
+        S.pb = 0;
+        S.pntbs = 1;
+        S.ps2 = 0;
+        S.pl = 0;
+        S.pi = 0;
+        S.pout = 0;
+        S.pphase = loops1 > 0 ? 0 : 1;
+        S.ptail = 0;
+        S.p_active = true;
+        continue;
+      }
+      // the end of one _scatterM loop (:241-245)
+      S.ob ^= 1;
+      S.ntbs = S.s2;
+      S.s2 = 0;
+      S.i = 0;
+      S.full = false;
+      if (S.ntbs == 0 || ++S.iloop >= loops) {
+        S.ophase = 1;
+        S.fi = 0;
+      }
+      continue;
+    }
+    // the neutrons still inside after the loops leave with attenuation
+    // (:246-255)
+    if (S.fi < S.ntbs && S.out_index < max_sc) {
+      Neutron<R> m = S.tbs[S.ob][S.fi];
+      const R x = m.x, y = m.y, z = m.z;
+      ms_propagate_out(c, m);
+      const R dx = m.x - x, dy = m.y - y, dz = m.z - z;
+      const R dist = m_sqrt(dx * dx + dy * dy + dz * dz);
+      const R atten = ms_atten_coeff(m, c);
+      m.p *= m_exp(-atten * dist);
+      emit(m);
+      ++S.out_index;
+      ++S.fi;
+      continue;
+    }
+    return false;
+  }
+}
+
+// File the outputs of the lane's _interactM1 call (:147-162)
+template <typename R, typename Emit>
+__device__ __noinline__ void ms_file(const mcv_component& c, MsLane<R>& S,
+                                     int ns, R min_prob, Emit& emit) {
+  const int max_sc = c.ip[6];
+  for (int j = 0; j < ns; ++j) {
+    const Neutron<R>& s1 = S.sc[j];
+    if (s1.p < min_prob) continue;
+    if (ms_locate<R>(c, s1.x, s1.y, s1.z) != kInside) {
+      ms_take<R>(c, S, s1, min_prob, max_sc, emit);
+      // the rest of the tree of a neutron that has all its outputs is not
+      // drawn: nothing after it reads the incident neutron's stream
+      if (++S.pout >= max_sc || S.done) {
+        S.pphase = 2;
+        return;
+      }
+      continue;
+    }
+    S.ptbs[S.pb ^ 1][S.ps2++] = s1;
+    if (S.ps2 >= max_sc) break;
+  }
+  if (S.ps2 >= max_sc) S.pi = S.pntbs;
+  else ++S.pi;
+}
+
+template <typename R>
+__global__ void __launch_bounds__(kMaxThreads, 4)
+    ms_chain_kernel(const __grid_constant__ mcv_chain ch, uint64_t n,
+                    uint64_t first, uint64_t seed, DevStatus* st) {
+  constexpr unsigned kFull = 0xffffffffu;
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned below = (1u << lane) - 1u;
+  const uint64_t warp = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint64_t nwarps = ((uint64_t)gridDim.x * blockDim.x) >> 5;
+  const uint64_t per = (n + nwarps - 1) / nwarps;
+  uint64_t next = warp * per;
+  const uint64_t end = next + per < n ? next + per : n;
+  int hms = 0;
+  while (ch.comp[hms].opcode != MCV_OP_HMS) ++hms;  // the host checked one
+  const mcv_component& c = ch.comp[hms];
+  const R min_prob = prm<R>(c, 14) * weight_up<R>(ch);
+  Counters k{0, 0, 0, 0};
+  MsLane<R> S;
+  PhiloxStream rng(seed, 0, 0u);
+  int state = 0;  // 0 idle, 1 in a tree, 2 no neutrons left
+  auto emit = [&](const Neutron<R>& o) {
+    ms_downstream<R, true>(o, rng, ch, hms, k);
+  };
+  for (;;) {
+    const unsigned idle = __ballot_sync(kFull, state == 0);
+    if (idle) {
+      if (state == 0) {
+        const uint64_t idx = next + (uint64_t)__popc(idle & below);
+        if (idx < end) {
+          Neutron<R> nt;
+          zero_neutron(nt);
+          rng = PhiloxStream(seed, first + idx, 0u);
+          NoTrack trk;
+          bool alive = true;
+          for (int c2 = 0; c2 < hms && alive; ++c2) {
+            if (c2 > 0) apply_transform<R>(nt, ch, c2);
+            k.overflow += run_component<R, true>(nt, rng, ch.comp[c2], trk,
+                                                 ch);
+            if (!(nt.p > 0)) {
+              if (m_isnan(nt.p)) k.nonfinite++;
+              alive = false;
+            }
+          }
+          k.processed++;
+          if (alive) {
+            if (hms > 0) apply_transform<R>(nt, ch, hms);
+            state = ms_begin<R>(c, S, nt, emit) ? 1 : 0;
+          }
+        } else {
+          state = 2;
+        }
+      }
+      next += (uint64_t)__popc(idle);
+      if (next > end) next = end;
+    }
+    if (__all_sync(kFull, state == 2)) break;
+    bool call = false;
+    if (state == 1) {
+      call = ms_advance<R>(c, S, min_prob, emit);
+      if (!call) state = 0;
+    }
+    if (call) {
+      const int ns = ms_interact_m1(c, rng, S.sc, S.ptbs[S.pb][S.pi]);
+      ms_file<R>(c, S, ns, min_prob, emit);
+    }
+  }
+  flush_counters(k, st);
+}
+
 // The tail queue of the FP32 regeneration kernel: per warp, a ring of
 // kTailCap neutrons that have left the chain's last guide alive, each with
 // its position in its Philox stream (20 words, stored word-major so that
@@ -380,18 +641,22 @@ __device__ __forceinline__ void tail_load(const uint32_t* q, int slot,
 // with its own Philox stream, as in chain_kernel, so results agree neutron
 // by neutron (up to the compiler's contraction choices).
 //
-// Shared memory: first `tally_words` doubles of monitor tallies
-// (MCV_COMP_SMEM_TALLY: zeroed here, added to the global tallies when the
-// block ends), then the tail queues.
-template <typename R, bool kX, typename Trk>
+// Shared memory: with kSmem, first `tally_words` doubles of monitor
+// tallies (MCV_COMP_SMEM_TALLY: zeroed here, added to the global tallies
+// when the block ends), then the tail queues.  Without it (the default
+// instantiation) the kernel carries none of that code.
+template <typename R, bool kX, typename Trk, bool kSmem = false>
 __device__ __forceinline__ void regen_body(const mcv_chain& ch, uint64_t n,
                                            uint64_t first, uint64_t seed,
                                            int tail_queue, int tally_words,
                                            DevStatus* st, Trk& trk) {
   extern __shared__ __align__(16) uint32_t tail_smem[];
-  double* const smt = tally_words ? (double*)tail_smem : nullptr;
-  for (int i = threadIdx.x; i < tally_words; i += blockDim.x) smt[i] = 0.0;
-  if (tally_words) __syncthreads();
+  if constexpr (!kSmem) tally_words = 0;
+  double* const smt = kSmem ? (double*)tail_smem : nullptr;
+  if constexpr (kSmem) {
+    for (int i = threadIdx.x; i < tally_words; i += blockDim.x) smt[i] = 0.0;
+    __syncthreads();
+  }
   constexpr unsigned kFull = 0xffffffffu;
   const unsigned lane = threadIdx.x & 31u;
   const unsigned below = (1u << lane) - 1u;
@@ -520,7 +785,7 @@ __device__ __forceinline__ void regen_body(const mcv_chain& ch, uint64_t n,
     }
   }
   flush_counters(k, st);
-  if (tally_words) {
+  if constexpr (kSmem) {
     // the block's shared-memory tallies into the global ones
     __syncthreads();
     for (int kc = 0; kc < nc; ++kc) {
@@ -536,13 +801,14 @@ __device__ __forceinline__ void regen_body(const mcv_chain& ch, uint64_t n,
   }
 }
 
-template <typename R, bool kX = false>
+template <typename R, bool kX = false, bool kSmem = false>
 __global__ void __launch_bounds__(kMaxThreads, 4)
     regen_kernel(const __grid_constant__ mcv_chain ch, uint64_t n,
                  uint64_t first, uint64_t seed, int tail_queue,
                  int tally_words, DevStatus* st) {
   NoTrack trk;
-  regen_body<R, kX>(ch, n, first, seed, tail_queue, tally_words, st, trk);
+  regen_body<R, kX, NoTrack, kSmem>(ch, n, first, seed, tail_queue,
+                                    tally_words, st, trk);
 }
 
 // The backward replay with the regeneration kernel's structure: the same
@@ -757,7 +1023,8 @@ struct Launchers {
                     int stride, double* out_n, int* out_last, DevStatus* st);
   // smem: the tail queue's bytes (0 = no queue)
   // smem: the tally area (tally_words doubles) and the tail queue
-  static int occupancy_regen(int threads, size_t smem, bool x);
+  static int occupancy_regen(int threads, size_t smem, int tally_words,
+                             bool x);
   static void regen(int blocks, int threads, size_t smem, int tally_words,
                     bool x, cudaStream_t s, const mcv_chain& ch, uint64_t n,
                     uint64_t first, uint64_t seed, DevStatus* st);
@@ -778,6 +1045,9 @@ struct Launchers {
   static void buffer(int blocks, int threads, bool x, cudaStream_t s,
                      const mcv_chain& ch, void* buf, uint64_t n,
                      uint64_t first, uint64_t seed, DevStatus* st);
+  static int occupancy_ms(int threads);
+  static void ms(int blocks, int threads, cudaStream_t s, const mcv_chain& ch,
+                 uint64_t n, uint64_t first, uint64_t seed, DevStatus* st);
   static int occupancy_batched(int threads, size_t smem);
   static void batched(int blocks, int threads, size_t smem, cudaStream_t s,
                       const mcv_chain* variants, int nvar,
@@ -849,10 +1119,14 @@ void Launchers<R>::chain(int mode, int x, int blocks, int threads,
 #undef MCV_CHAIN_LAUNCH
 }
 
+// kX chains take no shared-memory tally copies (tally_words is 0 there)
 template <typename R>
-int Launchers<R>::occupancy_regen(int threads, size_t smem, bool x) {
-  return x ? occupancy_of(regen_kernel<R, true>, threads, smem)
-           : occupancy_of(regen_kernel<R, false>, threads, smem);
+int Launchers<R>::occupancy_regen(int threads, size_t smem, int tally_words,
+                                  bool x) {
+  if (x) return occupancy_of(regen_kernel<R, true>, threads, smem);
+  return tally_words ? occupancy_of(regen_kernel<R, false, true>, threads,
+                                    smem)
+                     : occupancy_of(regen_kernel<R, false>, threads, smem);
 }
 
 template <typename R>
@@ -863,10 +1137,13 @@ void Launchers<R>::regen(int blocks, int threads, size_t smem,
   const int queue = smem > (size_t)tally_words * 8 ? 1 : 0;
   if (x)
     regen_kernel<R, true><<<blocks, threads, smem, s>>>(
+        ch, n, first, seed, queue, 0, st);
+  else if (tally_words)
+    regen_kernel<R, false, true><<<blocks, threads, smem, s>>>(
         ch, n, first, seed, queue, tally_words, st);
   else
     regen_kernel<R, false><<<blocks, threads, smem, s>>>(
-        ch, n, first, seed, queue, tally_words, st);
+        ch, n, first, seed, queue, 0, st);
 }
 
 template <typename R>
@@ -922,6 +1199,18 @@ void Launchers<R>::buffer(int blocks, int threads, bool x, cudaStream_t s,
   else
     buffer_kernel<R, false><<<blocks, threads, 0, s>>>(ch, (R*)buf, n,
                                                        first, seed, st);
+}
+
+template <typename R>
+int Launchers<R>::occupancy_ms(int threads) {
+  return occupancy_of(ms_chain_kernel<R>, threads, 0);
+}
+
+template <typename R>
+void Launchers<R>::ms(int blocks, int threads, cudaStream_t s,
+                      const mcv_chain& ch, uint64_t n, uint64_t first,
+                      uint64_t seed, DevStatus* st) {
+  ms_chain_kernel<R><<<blocks, threads, 0, s>>>(ch, n, first, seed, st);
 }
 
 template <typename R>

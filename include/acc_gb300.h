@@ -282,7 +282,9 @@ enum {
                                      offset (doubles) in the block's tally
                                      area, which holds the 3 nbins doubles
                                      of every such monitor, at most
-                                     MCV_SMEM_TALLY_MAX doubles in all */
+                                     MCV_SMEM_TALLY_MAX doubles in all (the
+                                     kernels of chains with the rarer
+                                     components tally it globally) */
 #define MCV_SMEM_TALLY_MAX 2048
 
 typedef struct mcv_component {
@@ -337,7 +339,15 @@ typedef struct mcv_launch {
                                with the CPU restatement operation for
                                operation), MCV_VARIANT_FP64_FMA the same
                                kernel with contracted multiply-adds
-                               (faster) */
+                               (faster).
+                               Chains with a multiple scatterer followed
+                               by no source or sample run, in either
+                               precision, the warp-synchronous tree kernel
+                               (each lane's scattering tree as a state
+                               machine, one _interactM1 call a pass on
+                               all lanes); variant 1 runs them one
+                               neutron per thread instead, with the same
+                               results. */
 } mcv_launch;
 
 #define MCV_VARIANT_FP64_FMA 4

@@ -428,6 +428,40 @@ def test_multiple_scattering_fp32_chi2():
     assert c2 <= bound, (c2, dof)
 
 
+MS_CHAINS = {"ms_hollow_cylinder": instruments.ms_hollow_cylinder,
+             "un_ms": instruments.un_ms}
+
+
+@pytest.mark.parametrize("floattype", ["float64", "float32"])
+@pytest.mark.parametrize("name", list(MS_CHAINS))
+def test_tree_kernel_equals_thread_kernel(name, floattype):
+    """The warp-synchronous scattering tree (ms_chain_kernel) makes the
+    thread kernel's _interactM1 calls in the same order on the same
+    stream.  FP64 (no contraction anywhere): identical counts, sums within
+    1e-12 (the order of the atomic additions differs).  FP32: the two
+    kernels inline the bookkeeping into different code and the compiler may
+    contract other multiply-adds, so at most 1e-5 of the entries move
+    between bins and sums agree within 1e-6."""
+    n = 200_000
+    a, b = MS_CHAINS[name](), MS_CHAINS[name]()
+    sa = engine.run_instrument(a, n, seed=23, floattype=floattype)
+    sb = engine.run_instrument(b, n, seed=23, floattype=floattype,
+                               variant="thread")
+    assert sa.processed == sb.processed == n
+    (_, ta), = gpu_tallies(a).items()
+    (_, tb), = gpu_tallies(b).items()
+    ta, tb = ta.reshape(3, -1), tb.reshape(3, -1)
+    assert ta[0].sum() > 0.2 * n
+    if floattype == "float64":
+        np.testing.assert_array_equal(ta[0], tb[0])
+        np.testing.assert_allclose(ta[1:], tb[1:], rtol=1e-12, atol=1e-300)
+    else:
+        assert abs(ta[0].sum() - tb[0].sum()) <= max(2, 1e-5 * ta[0].sum())
+        moved = np.abs(ta[0] - tb[0]).sum() / 2
+        assert moved <= max(2, 1e-5 * ta[0].sum()), moved
+        assert ta[1].sum() == pytest.approx(tb[1].sum(), rel=1e-6)
+
+
 def test_verdi_fp32_chi2():
     """VERDI FP32 on the GPU against the FP64 oracle on independent streams,
     monitors with more than 10 bins of >= 10 entries (the moderator and
