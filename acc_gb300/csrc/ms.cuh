@@ -55,11 +55,11 @@ __device__ __forceinline__ int locate_at(const mcv_component& c,
   return ms_locate<R>(c, n.x + n.vx * t, n.y + n.vy * t, n.z + n.vz * t);
 }
 
-// _is_exiting (propagation.py:24-50)
+// _is_exiting (propagation.py:24-50) of a neutron at location `loc`
+// (ms_locate of its position)
 template <typename R>
-__device__ __noinline__ bool ms_is_exiting(const mcv_component& c,
-                                              const Neutron<R>& n) {
-  const int loc = ms_locate<R>(c, n.x, n.y, n.z);
+__device__ __noinline__ bool ms_is_exiting_at(const mcv_component& c,
+                                              const Neutron<R>& n, int loc) {
   if (loc == kInside) return false;
   const Hits<R> h = forward_hits(c, n);
   if (h.n == 0) return true;
@@ -71,6 +71,12 @@ __device__ __noinline__ bool ms_is_exiting(const mcv_component& c,
     previous = now;
   }
   return true;
+}
+
+template <typename R>
+__device__ __forceinline__ bool ms_is_exiting(const mcv_component& c,
+                                              const Neutron<R>& n) {
+  return ms_is_exiting_at(c, n, ms_locate<R>(c, n.x, n.y, n.z));
 }
 
 // _propagate_out (propagation.py:52-59)
@@ -209,18 +215,44 @@ __device__ __forceinline__ void ms_exit_attenuated(const mcv_component& c,
   n.p *= transmission_prob;
 }
 
+// The same for a neutron inside the shape: _tof_before_first_exit and
+// _propagate_to_next_exiting_surface both take the first forward hit of
+// the same ray, found once here.
+template <typename R>
+__device__ __forceinline__ void ms_exit_attenuated_inside(
+    const mcv_component& c, Neutron<R>& n) {
+  const Hits<R> h = forward_hits(c, n);
+  const R tof = h.n == 0 ? R(0) : h.t0;
+  const R v = m_sqrt(n.vx * n.vx + n.vy * n.vy + n.vz * n.vz);
+  const R distance = tof * v;
+  const R atten = ms_atten_coeff(n, c);
+  const R transmission_prob = m_exp(-atten * distance);
+  prop_dt(n, h.t0);
+  n.p *= transmission_prob;
+}
+
 // _interactM1 (:86-121): the transmitted and the scattered neutron.  The
 // absorbed copy (:106-110) is overwritten by the scattered one and the
 // kernels' absorb is a no-op (kernels/__init__.py:164-166), so it is not
 // formed.  A point left outside the shape (the reference raises) gives no
-// output.
+// output.  For a neutron inside the shape the time to the first exit and
+// the transmitted neutron's move come from one forward hit (the two
+// reference functions find the same one).
 template <typename R, typename Rng>
 __device__ __noinline__ int ms_interact_m1(const mcv_component& c,
                                               Rng& rng, Neutron<R>* out,
                                               Neutron<R>& n) {
   const R vx = n.vx, vy = n.vy, vz = n.vz;
-  if (ms_locate<R>(c, n.x, n.y, n.z) != kInside) ms_to_incident(c, n);
-  const R tof = ms_tof_before_first_exit(c, n);
+  R tof, t_exit;
+  if (ms_locate<R>(c, n.x, n.y, n.z) != kInside) {
+    ms_to_incident(c, n);
+    tof = ms_tof_before_first_exit(c, n);
+    t_exit = R(-1);
+  } else {
+    const Hits<R> h = forward_hits(c, n);
+    tof = h.n == 0 ? R(0) : h.t0;
+    t_exit = h.t0;
+  }
   if (!(tof > R(0))) return 0;
   const R v = m_sqrt(vx * vx + vy * vy + vz * vz);
   const R distance = tof * v;
@@ -228,7 +260,8 @@ __device__ __noinline__ int ms_interact_m1(const mcv_component& c,
   const R mu = hss_mu<R>(n, c);
   const R transmission_prob = m_exp(-(mu + sigma) * distance);
   out[0] = n;
-  ms_to_exiting(c, out[0]);
+  if (t_exit >= R(0)) prop_dt(out[0], t_exit);
+  else ms_to_exiting(c, out[0]);
   out[0].p *= transmission_prob;
   const R rand = rng.next();
   const R x = distance * rand;
