@@ -380,12 +380,16 @@ void launch_ms(mcv_ctx* ctx, const mcv_chain* chain, uint64_t ncount,
                uint64_t first, uint64_t seed, const mcv_launch* launch,
                cudaStream_t s) {
   int blocks, threads;
+  // block-synchronous passes for a convex (primitive) shape
+  int k = 0;
+  while (chain->comp[k].opcode != MCV_OP_HMS) ++k;
+  const bool block = chain->comp[k].ip[0] == MCV_CSG_PRIMITIVE;
   // one warp handles a run of incident neutrons: the grid's warps each
   // take at least 32
   launch_shape(
-      ctx, [](int t) { return Launchers<R>::occupancy_ms(t); },
+      ctx, [block](int t) { return Launchers<R>::occupancy_ms(t, block); },
       (ncount + 31) / 32 * 32, launch, &blocks, &threads);
-  Launchers<R>::ms(blocks, threads, s, *chain, ncount, first, seed,
+  Launchers<R>::ms(blocks, threads, block, s, *chain, ncount, first, seed,
                    ctx->d_status);
 }
 

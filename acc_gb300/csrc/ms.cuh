@@ -239,7 +239,7 @@ __device__ __forceinline__ void ms_exit_attenuated_inside(
 // the transmitted neutron's move come from one forward hit (the two
 // reference functions find the same one).
 template <typename R, typename Rng>
-__device__ __noinline__ int ms_interact_m1(const mcv_component& c,
+__device__ __forceinline__ int ms_interact_m1(const mcv_component& c,
                                               Rng& rng, Neutron<R>* out,
                                               Neutron<R>& n) {
   const R vx = n.vx, vy = n.vy, vz = n.vz;
