@@ -302,6 +302,30 @@ __global__ void __launch_bounds__(kMaxThreads, kDense ? 4 : 0)
   flush_counters(k, st);
 }
 
+// The stream the components after the multiple scatterer see in the tree
+// kernel: none of them draws (chains whose later components draw run in the
+// thread kernel), and the neutron-storage components read the incident
+// neutron's index.  Holding no state, it leaves the lane's Philox stream in
+// registers across the out-of-line call below.
+struct IndexOnlyStream {
+  uint64_t idx;
+  __device__ __forceinline__ float next() { return 0.5f; }
+  __device__ __forceinline__ void skip(int) {}
+  __device__ __forceinline__ int overrun() const { return 0; }
+  __device__ __forceinline__ uint64_t index() const { return idx; }
+};
+
+// ms_downstream for the tree kernel: the counts to add (x: guide bounce
+// overflows, y: non-finite weights) come back by value.
+template <typename R>
+__device__ __noinline__ uint2 ms_downstream_out(Neutron<R> m, uint64_t index,
+                                                const mcv_chain& ch, int c) {
+  IndexOnlyStream rng{index};
+  Counters k{0, 0, 0, 0};
+  ms_downstream<R, true>(m, rng, ch, c, k);
+  return make_uint2(k.overflow, k.nonfinite);
+}
+
 // ---------------------------------------------------------------------------
 // Chains with a multiple scatterer: a warp-synchronous form of the
 // scattering tree.
@@ -476,33 +500,54 @@ __device__ __forceinline__ bool ms_advance(const mcv_component& c, MsLane<R>& S,
   }
 }
 
-// File the outputs `sc` of the lane's _interactM1 call (:147-162)
+// File the outputs of the lane's _interactM1 call (:147-162): `t0` the
+// transmitted neutron, the scattered one written in place at the next
+// list's free entry (S.ptbs[S.pb ^ 1][S.ps2]), which appending it takes.
 template <typename R, typename Emit>
 __device__ __forceinline__ void ms_file(const mcv_component& c, MsLane<R>& S,
-                                        const Neutron<R>* sc, int ns,
+                                        const Neutron<R>& t0, int ns,
                                         R min_prob, Emit& emit) {
   const int max_sc = c.ip[6];
-#pragma unroll
-  for (int j = 0; j < 2; ++j) {
-    if (j >= ns) break;
-    const Neutron<R>& s1 = sc[j];
-    if (s1.p < min_prob) continue;
-    const int loc = ms_locate<R>(c, s1.x, s1.y, s1.z);
-    if (loc != kInside) {
-      ms_take<R>(c, S, s1, min_prob, max_sc, emit, loc);
-      // the rest of the tree of a neutron that has all its outputs is not
-      // drawn: nothing after it reads the incident neutron's stream
-      if (++S.pout >= max_sc || S.done) {
-        S.pphase = 2;
+  if (ns > 0) {
+    if (!(t0.p < min_prob)) {
+      const int loc = ms_locate<R>(c, t0.x, t0.y, t0.z);
+      if (loc != kInside) {
+        ms_take<R>(c, S, t0, min_prob, max_sc, emit, loc);
+        // the rest of the tree of a neutron that has all its outputs is
+        // not drawn: nothing after it reads the incident neutron's stream
+        if (++S.pout >= max_sc || S.done) {
+          S.pphase = 2;
+          return;
+        }
+      } else {
+        // a transmitted neutron left inside (it is on the exit surface up
+        // to rounding) is appended first, the scattered one after it
+        Neutron<R>* nx = S.ptbs[S.pb ^ 1];
+        const Neutron<R> s1 = nx[S.ps2];
+        nx[S.ps2++] = t0;
+        if (S.ps2 >= max_sc) {
+          S.pi = S.pntbs;
+          return;
+        }
+        nx[S.ps2] = s1;
+      }
+    }
+    const Neutron<R>& s1 = S.ptbs[S.pb ^ 1][S.ps2];
+    if (!(s1.p < min_prob)) {
+      const int loc = ms_locate<R>(c, s1.x, s1.y, s1.z);
+      if (loc != kInside) {
+        ms_take<R>(c, S, s1, min_prob, max_sc, emit, loc);
+        if (++S.pout >= max_sc || S.done) {
+          S.pphase = 2;
+          return;
+        }
+      } else if (++S.ps2 >= max_sc) {
+        S.pi = S.pntbs;
         return;
       }
-      continue;
     }
-    S.ptbs[S.pb ^ 1][S.ps2++] = s1;
-    if (S.ps2 >= max_sc) break;
   }
-  if (S.ps2 >= max_sc) S.pi = S.pntbs;
-  else ++S.pi;
+  ++S.pi;
 }
 
 // kBlock: the warps of a block run each pass's phases (refill and
@@ -534,7 +579,9 @@ __global__ void __launch_bounds__(kMaxThreads, 4)
   PhiloxStream rng(seed, 0, 0u);
   int state = 0;  // 0 idle, 1 in a tree, 2 no neutrons left
   auto emit = [&](const Neutron<R>& o) {
-    ms_downstream<R, true>(o, rng, ch, hms, k);
+    const uint2 r = ms_downstream_out<R>(o, rng.index(), ch, hms);
+    k.overflow += r.x;
+    k.nonfinite += r.y;
   };
   for (;;) {
     // lanes take new neutrons together, once every tree of the warp has
@@ -587,11 +634,15 @@ __global__ void __launch_bounds__(kMaxThreads, 4)
       if (!call) state = 0;
     }
     if constexpr (kBlock) __syncthreads();
-    Neutron<R> sc[2];
+    // a call comes with S.ps2 < max_scattered_neutrons: the scattered
+    // neutron's entry exists
+    Neutron<R> t0;
     int ns = 0;
-    if (call) ns = ms_interact_m1(c, rng, sc, S.ptbs[S.pb][S.pi]);
+    if (call)
+      ns = ms_interact_m1(c, rng, t0, S.ptbs[S.pb ^ 1][S.ps2],
+                          S.ptbs[S.pb][S.pi]);
     if constexpr (kBlock) __syncthreads();
-    if (call) ms_file<R>(c, S, sc, ns, min_prob, emit);
+    if (call) ms_file<R>(c, S, t0, ns, min_prob, emit);
   }
   flush_counters(k, st);
 }

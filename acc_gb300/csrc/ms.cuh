@@ -237,10 +237,12 @@ __device__ __forceinline__ void ms_exit_attenuated_inside(
 // formed.  A point left outside the shape (the reference raises) gives no
 // output.  For a neutron inside the shape the time to the first exit and
 // the transmitted neutron's move come from one forward hit (the two
-// reference functions find the same one).
+// reference functions find the same one).  The outputs go to `out0`
+// (transmitted) and `out1` (scattered), neither of them `n`.
 template <typename R, typename Rng>
 __device__ __forceinline__ int ms_interact_m1(const mcv_component& c,
-                                              Rng& rng, Neutron<R>* out,
+                                              Rng& rng, Neutron<R>& out0,
+                                              Neutron<R>& out1,
                                               Neutron<R>& n) {
   const R vx = n.vx, vy = n.vy, vz = n.vz;
   R tof, t_exit;
@@ -259,18 +261,18 @@ __device__ __forceinline__ int ms_interact_m1(const mcv_component& c,
   const R sigma = hss_sigma<R, true>(n, c);
   const R mu = hss_mu<R>(n, c);
   const R transmission_prob = m_exp(-(mu + sigma) * distance);
-  out[0] = n;
-  if (t_exit >= R(0)) prop_dt(out[0], t_exit);
-  else ms_to_exiting(c, out[0]);
-  out[0].p *= transmission_prob;
+  out0 = n;
+  if (t_exit >= R(0)) prop_dt(out0, t_exit);
+  else ms_to_exiting(c, out0);
+  out0.p *= transmission_prob;
   const R rand = rng.next();
   const R x = distance * rand;
   const R prob = distance * m_exp(-(mu + sigma) * x);
-  out[1] = n;
-  out[1].p *= prob;
-  prop_dt(out[1], x / v);
+  out1 = n;
+  out1.p *= prob;
+  prop_dt(out1, x / v);
   NoTrack trk;
-  hss_kernel<R, true>(out[1], rng, c, trk);
+  hss_kernel<R, true>(out1, rng, c, trk);
   return 2;
 }
 
@@ -293,7 +295,7 @@ __device__ __noinline__ void ms_path1(const mcv_component& c, Rng& rng,
     int s2 = 0;
     for (int i = 0; i < ntbs; ++i) {
       Neutron<R> sc[2];
-      const int ns = ms_interact_m1(c, rng, sc, tbs[i]);
+      const int ns = ms_interact_m1(c, rng, sc[0], sc[1], tbs[i]);
       for (int j = 0; j < ns; ++j) {
         const Neutron<R>& s1 = sc[j];
         if (s1.p < min_prob) continue;
