@@ -16,6 +16,10 @@ int mcv_fp64_fma_occupancy(int x, int threads);
 void mcv_fp64_fma_chain(int x, int blocks, int threads, cudaStream_t s,
                         const mcv_chain& ch, uint64_t n, uint64_t first,
                         uint64_t seed, void* status);
+int mcv_fp64_fma_ms_occupancy(bool block, int threads);
+void mcv_fp64_fma_ms(bool block, int blocks, int threads, cudaStream_t s,
+                     const mcv_chain& ch, uint64_t n, uint64_t first,
+                     uint64_t seed, void* status);
 
 // =================================================================== host
 using namespace mcv;
@@ -375,10 +379,11 @@ bool use_ms_kernel(const mcv_chain* ch, const mcv_launch* launch) {
   return true;
 }
 
+// fma: the FP64 kernel with contracted multiply-adds (launch_fp64_fma.cu)
 template <typename R>
 void launch_ms(mcv_ctx* ctx, const mcv_chain* chain, uint64_t ncount,
                uint64_t first, uint64_t seed, const mcv_launch* launch,
-               cudaStream_t s) {
+               cudaStream_t s, bool fma = false) {
   int blocks, threads;
   // block-synchronous passes for a convex (primitive) shape
   int k = 0;
@@ -387,10 +392,18 @@ void launch_ms(mcv_ctx* ctx, const mcv_chain* chain, uint64_t ncount,
   // one warp handles a run of incident neutrons: the grid's warps each
   // take at least 32
   launch_shape(
-      ctx, [block](int t) { return Launchers<R>::occupancy_ms(t, block); },
+      ctx,
+      [block, fma](int t) {
+        return fma ? mcv_fp64_fma_ms_occupancy(block, t)
+                   : Launchers<R>::occupancy_ms(t, block);
+      },
       (ncount + 31) / 32 * 32, launch, &blocks, &threads);
-  Launchers<R>::ms(blocks, threads, block, s, *chain, ncount, first, seed,
-                   ctx->d_status);
+  if (fma)
+    mcv_fp64_fma_ms(block, blocks, threads, s, *chain, ncount, first, seed,
+                    ctx->d_status);
+  else
+    Launchers<R>::ms(blocks, threads, block, s, *chain, ncount, first, seed,
+                     ctx->d_status);
 }
 
 // The rarer components run in their own kernel instantiations (kX): the
@@ -724,12 +737,12 @@ int mcv_run_chain(mcv_ctx* ctx, const mcv_chain* chain, uint64_t ncount,
   if (ncount == 0) return st ? mcv_ctx_status(ctx, stream, 0, st) : MCV_OK;
   DeviceGuard g(ctx->device);
   cudaStream_t s = (cudaStream_t)stream;
-  if (use_ms_kernel(chain, launch) &&
-      !(launch && launch->variant == MCV_VARIANT_FP64_FMA)) {
+  if (use_ms_kernel(chain, launch)) {
     if (precision == MCV_FP32)
       launch_ms<float>(ctx, chain, ncount, first, seed, launch, s);
     else
-      launch_ms<double>(ctx, chain, ncount, first, seed, launch, s);
+      launch_ms<double>(ctx, chain, ncount, first, seed, launch, s,
+                        launch && launch->variant == MCV_VARIANT_FP64_FMA);
   } else if (precision == MCV_FP32) {
     if (use_regen(chain, launch)) {
       int blocks, threads;

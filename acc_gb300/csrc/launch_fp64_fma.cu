@@ -7,7 +7,7 @@
 // (mcv_launch.variant == MCV_VARIANT_FP64_FMA in mcv_run_chain) the same
 // kernel with contracted multiply-adds.  It is compiled with -Dmcv=mcv_fma,
 // so that its kernels, device functions and launchers are symbols of their
-// own; only the two entry points below are seen by engine.cu.
+// own; only the entry points below are seen by engine.cu.
 #include "kernels.cuh"
 
 int mcv_fp64_fma_occupancy(int x, int threads) {
@@ -26,4 +26,24 @@ void mcv_fp64_fma_chain(int x, int blocks, int threads, cudaStream_t s,
   else
     mcv::chain_kernel<double, 0, false><<<blocks, threads, 0, s>>>(
         ch, n, first, seed, nullptr, 0, nullptr, nullptr, st);
+}
+
+// the multiple-scattering tree kernel (block: its block-synchronous form)
+int mcv_fp64_fma_ms_occupancy(bool block, int threads) {
+  return block ? mcv::occupancy_of(mcv::ms_chain_kernel<double, true>,
+                                   threads, 0)
+               : mcv::occupancy_of(mcv::ms_chain_kernel<double, false>,
+                                   threads, 0);
+}
+
+void mcv_fp64_fma_ms(bool block, int blocks, int threads, cudaStream_t s,
+                     const mcv_chain& ch, uint64_t n, uint64_t first,
+                     uint64_t seed, void* status) {
+  auto* st = static_cast<mcv::DevStatus*>(status);
+  if (block)
+    mcv::ms_chain_kernel<double, true><<<blocks, threads, 0, s>>>(
+        ch, n, first, seed, st);
+  else
+    mcv::ms_chain_kernel<double, false><<<blocks, threads, 0, s>>>(
+        ch, n, first, seed, st);
 }

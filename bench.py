@@ -101,7 +101,22 @@ KERNEL_COUNTS = {
                     "warp_inst_per_neutron": 35.23,
                     "thread_inst_per_neutron": 823.2,
                     "dram_bytes_per_launch": 135936,
-                    "captured_neutrons": 10_000_000},
+                    "captured_neutrons": 10_000_000,
+                    "kernel": "mcv::regen_kernel<float>",
+                    "traffic_note": "the tally bins, independent of the "
+                                    "neutron count"},
+    # the multiple-scattering tree kernel (block-synchronous instantiation,
+    # 608 blocks x 256 threads on a 1e6-neutron launch); its DRAM traffic is
+    # the local-memory working set (tree lists and spills of 1024 lanes an
+    # SM) leaving L2, and grows with the neutron count
+    "un_ms": {"warp_inst_per_neutron": 923.7,
+              "thread_inst_per_neutron": 923.7 * 15.33,
+              "dram_bytes_per_neutron": 1422.3,
+              "captured_neutrons": 1_000_000,
+              "kernel": "mcv::ms_chain_kernel<float, true>",
+              "traffic_note": "local memory (tree lists, spills) evicted "
+                              "from L2, 1.42 KB per incident neutron; 76 B "
+                              "at 2 blocks an SM, 16% slower"},
 }
 
 
@@ -621,20 +636,23 @@ def ours_arm(a, rank, world, local_rank):
     mhz = (clk or {}).get("sm_mhz") or 2070.0
     peak_issue = sms * 4 * mhz * 1e6
     got = wpn * ncount / mean_s if wpn else None
+    traffic = counts.get("dram_bytes_per_launch")
+    if traffic is None and counts.get("dram_bytes_per_neutron"):
+        traffic = counts["dram_bytes_per_neutron"] * ncount
     roofline = {
         "bound": "issue",
         "achieved": got, "peak": peak_issue, "unit": "warp-inst/s",
         "frac": got / peak_issue if got else None,
-        "traffic": counts.get("dram_bytes_per_launch"),
-        "kernel": "mcv::regen_kernel<float>",
+        "traffic": traffic,
+        "kernel": counts.get("kernel"),
         "per_unit": f"{wpn} warp instructions per neutron (ncu count), "
                     f"{counts.get('thread_inst_per_neutron')} thread "
                     "instructions",
         "peak_source": "SMs x 4 issue slots x median SM clock sampled "
                        "during the timed region",
-        "traffic_note": "DRAM bytes of one launch from ncu on a "
-                        f"{counts.get('captured_neutrons')}-neutron launch: "
-                        "the tally bins, independent of the neutron count",
+        "traffic_note": "DRAM bytes from ncu on a "
+                        f"{counts.get('captured_neutrons')}-neutron launch, "
+                        f"per launch of this run: {counts.get('traffic_note')}",
         "fp32_pipe": fp32_pipe,
     }
     cpu = None
@@ -678,7 +696,9 @@ def ours_arm(a, rank, world, local_rank):
         "fp32_one_neutron_per_thread": {
             "value": world * ncount * a.steps / t_thread, "unit": UNIT,
             "ms_per_step": 1e3 * t_thread / a.steps,
-            "note": "same FP32 kernel body without path regeneration"},
+            "note": "launch variant 1: one neutron per thread to the end "
+                    "of the chain (no path regeneration, no multiple-"
+                    "scattering tree state machine)"},
         "chi2_fp32_vs_fp64": chi2,
         "bwd_over_fwd": grads,
         "powder_banked_forward": powder,

@@ -516,7 +516,8 @@ def test_un_multiple_scattering_fp32_chi2():
 
 
 @pytest.mark.parametrize("name", ["guide_chain", "sphere_theta_tof",
-                                  "powder_direct"])
+                                  "powder_direct", "un_ms",
+                                  "ms_hollow_cylinder"])
 def test_fp64_fma_variant_histograms(name):
     """MCV_VARIANT_FP64_FMA (the FP64 chain kernel with contracted
     multiply-adds) against the oracle on the same stream: contraction moves
@@ -524,12 +525,13 @@ def test_fp64_fma_variant_histograms(name):
     edge may change bins (at most 1e-5 of the entries) and bin sums agree
     within 1e-9 relative where the counts agree."""
     n, seed = 200000, 5
-    ins = BUILDERS[name]()
+    build = {**BUILDERS, **MS_CHAINS}[name]
+    ins = build()
     st = engine.run_instrument(ins, n, seed=seed, floattype="float64",
                                variant="fp64_fma")
     assert st.processed == n
     gt = gpu_tallies(ins)
-    ot, _, _, _ = oracle_run(BUILDERS[name](), n, seed=seed)
+    ot, _, _, _ = oracle_run(build(), n, seed=seed)
     for (gc, g), (oc, o) in zip(gt.items(), ot.items()):
         moved = np.abs(g[0] - o[0]).sum() / 2
         assert moved <= max(2, 1e-5 * o[0].sum()), (gc.name, moved)
