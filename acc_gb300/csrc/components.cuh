@@ -575,8 +575,10 @@ __device__ __forceinline__ int guide(Neutron<R>& n, const mcv_component& c,
 
 // guide_tapering.Guide.propagate (acc/components/optics/guide_tapering.py
 // :140-291): nseg equal segments, each a tapered channel, read from the
-// component's table (rows w1 w2 h1 h2 ww hh whalf hhalf lwhalf lhhalf).
-// Returns 1 when a bounce loop ran out of MCV_MAX_BOUNCES iterations.
+// component's table (rows w1 w2 h1 h2 ww hh whalf hhalf lwhalf lhhalf;
+// then, when ip[1] > 0, the narrowest width and height of each block of
+// ip[1] segments).  Returns 1 when a bounce loop ran out of
+// MCV_MAX_BOUNCES iterations.
 template <typename R>
 __device__ __forceinline__ const R* taper_table(const mcv_component& c) {
   if constexpr (sizeof(R) == 4)
@@ -606,7 +608,37 @@ __device__ __forceinline__ int guide_tapering(Neutron<R>& n,
   z = R(0);
   t.add(dt);
   int overflow = 0;
+  const int blk = c.ip[1];
+  const int nblk = blk > 0 ? (nseg + blk - 1) / blk : 0;
+  const R* bminw = d + 10 * nseg;
+  const R* bminh = bminw + nblk;
   for (int seg = 0; seg < nseg; ++seg) {
+    if (blk > 0 && vz > R(0) && seg % blk == 0) {
+      // Quiet blocks: a forward flight that stays inside the block's
+      // narrowest opening at the block's entrance and exit planes stays
+      // inside every segment's channel in between (|x(z)| is convex along
+      // the ray, the walls are planar): each segment of the block would
+      // pass its entrance check and its quiet test.  The neutron goes to
+      // the entrance of the block's last segment, where those segments
+      // would have left it.  The margin keeps flights within rounding of
+      // a wall on the per-segment path.
+      const int b = seg / blk;
+      const int send = seg + blk < nseg ? seg + blk : nseg;
+      const R ta = (seg * l_seg - z) / vz, tb = (send * l_seg - z) / vz;
+      const R keep = sizeof(R) == 4 ? R(0.5 - 0.5e-4) : R(0.5 - 0.5e-9);
+      const R hw = keep * __ldg(&bminw[b]), hh2 = keep * __ldg(&bminh[b]);
+      const R xa = x + vx * ta, xb = x + vx * tb;
+      const R ya = y + vy * ta, yb = y + vy * tb;
+      if (m_fabs(xa) < hw && m_fabs(xb) < hw && m_fabs(ya) < hh2 &&
+          m_fabs(yb) < hh2) {
+        dt = ((send - 1) * l_seg - z) / vz;
+        x += vx * dt;
+        y += vy * dt;
+        z += vz * dt;
+        seg = send - 1;
+        continue;
+      }
+    }
     const R zr = seg * l_seg;
     const R w1s = __ldg(&w1[seg]), hhalfs = __ldg(&hhalf[seg]);
     const R wws = __ldg(&ww[seg]), hhs = __ldg(&hh[seg]),

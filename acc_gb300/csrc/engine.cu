@@ -249,15 +249,19 @@ int validate_component(const mcv_component& c, int k, mcv_status* st) {
       }
       break;
     }
-    case MCV_OP_GUIDE_TAPERING:
-      if (c.ip[0] < 1 || !c.table || !c.ftable ||
-          c.table_len < (uint64_t)10 * c.ip[0] || !(c.dp[0] > 0)) {
+    case MCV_OP_GUIDE_TAPERING: {
+      const uint64_t nblk =
+          c.ip[1] > 0 ? ((uint64_t)c.ip[0] + c.ip[1] - 1) / c.ip[1] : 0;
+      if (c.ip[0] < 1 || !c.table || !c.ftable || c.ip[1] < 0 ||
+          c.table_len < (uint64_t)10 * c.ip[0] + 2 * nblk ||
+          !(c.dp[0] > 0)) {
         set_msg(st, MCV_EINVAL,
                 "component %s%lld: tapered guide needs >= 1 segment, its "
-                "10 x nseg table and a positive segment length", "",
-                (long long)k);
+                "10 x nseg table (and 2 x nblocks block rows when ip[1] > "
+                "0) and a positive segment length", "", (long long)k);
         return MCV_EINVAL;
       }
+    }
       break;
     case MCV_OP_HSS:
     case MCV_OP_HMS: {

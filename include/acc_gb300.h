@@ -214,10 +214,12 @@ enum {
  *   fused thread kernel and the batched launch run it (mcv_process_buffer,
  *   mcv_backward and the regeneration kernel reject it).
  * GUIDE_TAPERING (guide_tapering.py:22-291): nseg equal segments
- *   ip[0]=nseg
+ *   ip[0]=nseg  ip[1]=segments per quiet-test block (0: no blocks)
  *   dp: 0 l_seg 1 R0 2 Qcx 3 Qcy 4 alphax 5 alphay 6 mx 7 my 8 W
  *   table: float64 [10][nseg] rows w1 w2 h1 h2 ww hh whalf hhalf lwhalf
- *          lhhalf (the reference's data block, prep_inputs_kernel :122-138);
+ *          lhhalf (the reference's data block, prep_inputs_kernel :122-138),
+ *          then, when ip[1] > 0, [2][nblocks] rows: each block's smallest
+ *          w1 or w2, and smallest h1 or h2 (nblocks = ceil(nseg / ip[1]));
  *          ftable: its float32 copy
  * SNS_SOURCE (SNS_source.py:20-207, _SNS_source_utils.py:187-223)
  *   ip: 0 square 1 nE 2 nt 3 Eidx_start 4 Eidx_stop 5 tidx_start

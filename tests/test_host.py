@@ -235,6 +235,52 @@ def test_chain_keeps_its_tables_alive():
     assert ch.comp[1].table != 0
 
 
+def test_tapered_guide_quiet_blocks():
+    """A guide of QUIET_MIN_SEGMENTS segments or more packs ip[1] = 16 and,
+    after the 10 x nseg rows, each block's narrowest width and height; a
+    shorter one packs neither.  The engine rejects a table missing the
+    block rows."""
+    import ctypes
+    from acc_gb300.components.optics.guide_tapering import Guide
+    n = 300
+    z = np.linspace(0.0, 1.0, n)
+    w1 = 0.03 + 0.01 * np.sin(3 * z)
+    w2 = np.roll(w1, -1)
+    h1 = 0.04 - 0.01 * z
+    h2 = h1 - 0.0001
+    g = Guide("g", l=10.0, segments=(h1, h2, w1, w2))
+    ch = build_chain([g], binder=HostBinder())
+    c = ch.comp[0]
+    assert (c.ip[0], c.ip[1]) == (n, 16)
+    nblk = -(-n // 16)
+    assert c.table_len == 10 * n + 2 * nblk
+    flat = np.ctypeslib.as_array(ctypes.cast(c.table, ctypes.POINTER(
+        ctypes.c_double)), shape=(c.table_len,))
+    rows = flat[10 * n:].reshape(2, nblk)
+    for b in range(nblk):
+        s = slice(16 * b, min(16 * b + 16, n))
+        assert rows[0, b] == min(w1[s].min(), w2[s].min())
+        assert rows[1, b] == min(h1[s].min(), h2[s].min())
+    short = Guide("s", l=1.0, segments=(h1[:100], h2[:100], w1[:100],
+                                         w2[:100]))
+    c2 = build_chain([short], binder=HostBinder()).comp[0]
+    assert c2.ip[1] == 0 and c2.table_len == 1000
+    # mcv_run_chain validates the chain before it looks at the context
+    import ctypes as C
+    L = nat.lib()
+    st = nat.mcv_status()
+    c.table_len = 10 * n
+    rc = L.mcv_run_chain(None, C.byref(ch), 1, 0, 0, 32, None, None,
+                         C.byref(st))
+    with pytest.raises(nat.EngineError, match="block rows"):
+        nat.check(rc, st)
+    c.table_len = 10 * n + 2 * nblk
+    rc = L.mcv_run_chain(None, C.byref(ch), 1, 0, 0, 32, None, None,
+                         C.byref(st))
+    with pytest.raises(nat.EngineError, match="context is NULL"):
+        nat.check(rc, st)
+
+
 def test_isotropic_box():
     """IsotropicBox (isotropic_box.py) is the single scatterer on a box with
     the isotropic kernel."""
