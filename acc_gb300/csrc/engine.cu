@@ -516,13 +516,18 @@ bool host_is_monitor(const mcv_component& c) {
 
 // The FP32 fused run uses path regeneration when asked to, or by default
 // when the chain has a guide (whose bounce count varies from neutron to
-// neutron); chains without one have near-uniform paths.
+// neutron) or a long segmented guide (one taking quiet blocks, ip[1] > 0:
+// a neutron may die in its first segment or fly through all of them; VERDI
+// 5.68e8 n/s against 5.32e8); chains without one have near-uniform paths.
 bool use_regen(const mcv_chain* ch, const mcv_launch* launch) {
   if (has_hms(ch)) return false;  // the fan-out runs in the thread kernel
   if (launch && launch->variant == 1) return false;
   if (launch && (launch->variant == 2 || launch->variant == 3)) return true;
-  for (int k = 0; k < ch->ncomp; ++k)
-    if (ch->comp[k].opcode == MCV_OP_GUIDE) return true;
+  for (int k = 0; k < ch->ncomp; ++k) {
+    const mcv_component& c = ch->comp[k];
+    if (c.opcode == MCV_OP_GUIDE) return true;
+    if (c.opcode == MCV_OP_GUIDE_TAPERING && c.ip[1] > 0) return true;
+  }
   return false;
 }
 

@@ -180,6 +180,30 @@ __device__ __noinline__ int ms_downstream(Neutron<R> m, Rng& rng,
   return last;
 }
 
+// The multiple scatterer's fan-out in the thread kernel: the rest of the
+// chain for every output neutron, on the same stream (run_script.py:66-92,
+// 245-260); outputs run it as they become final unless a later component
+// draws random numbers (ms_downstream_draws), when they wait in `outs` for
+// the whole tree as in the reference.  Out of line, so that the tree's
+// lists and registers do not weigh on the chains without a multiple
+// scatterer that share the kernel.  Returns the last component reached.
+template <typename R, typename Rng>
+__device__ __noinline__ int ms_fan_out(const Neutron<R>& n, Rng& rng,
+                                       const mcv_chain& ch, int c,
+                                       Counters& k) {
+  const bool hold = ms_downstream_draws(ch, c);
+  Neutron<R> outs[MCV_MS_MAX_SCATTERED];
+  int nout = 0, last = c;
+  auto emit = [&](const Neutron<R>& o) {
+    if (hold) outs[nout++] = o;
+    else last = ms_downstream<R, true>(o, rng, ch, c, k);
+  };
+  ms_scatter<R>(ch.comp[c], rng, n, weight_up<R>(ch), emit);
+  for (int j = 0; j < nout; ++j)
+    last = ms_downstream<R, true>(outs[j], rng, ch, c, k);
+  return last;
+}
+
 // Whole chain on one neutron (the body of the generated
 // process_kernel_no_buffer, acc/run_script.py:182-196).  A neutron leaves
 // the chain after a component that leaves its weight not positive.
@@ -201,21 +225,7 @@ __device__ __forceinline__ int run_chain_one(Neutron<R>& n, Rng& rng,
     trk.begin_component(ch, c);
     if constexpr (kX && !std::decay_t<Trk>::kActive) {
       if (ch.comp[c].opcode == MCV_OP_HMS) {
-        // fan-out: the rest of the chain for every output neutron, on the
-        // same stream (run_script.py:66-92, 245-260); outputs run it as
-        // they become final unless a later component draws random numbers
-        // (ms_downstream_draws), when they wait in `outs` for the whole
-        // tree as in the reference
-        const bool hold = ms_downstream_draws(ch, c);
-        Neutron<R> outs[MCV_MS_MAX_SCATTERED];
-        int nout = 0;
-        auto emit = [&](const Neutron<R>& o) {
-          if (hold) outs[nout++] = o;
-          else last = ms_downstream<R, kX>(o, rng, ch, c, k);
-        };
-        ms_scatter<R>(ch.comp[c], rng, n, weight_up<R>(ch), emit);
-        for (int j = 0; j < nout; ++j)
-          last = ms_downstream<R, kX>(outs[j], rng, ch, c, k);
+        last = ms_fan_out<R>(n, rng, ch, c, k);
         alive = false;
         continue;
       }
@@ -272,8 +282,12 @@ constexpr int kMaxThreads = 256;
 // registers, some spills), which pays for chains whose time goes into
 // sample kernels and the multiple scatterer (latency-bound at 3 blocks)
 // and loses for the long guide loops; the host picks (dense_kx_chain).
+// The other FP32 kX instantiation is held to 3 blocks (85 registers):
+// left free, the compiler takes 128 and 2 blocks, and the segmented, mesh
+// and SNS-source chains ran 2-12% slower.
 template <typename R, int MODE, bool kX = false, bool kDense = false>
-__global__ void __launch_bounds__(kMaxThreads, kDense ? 4 : 0)
+__global__ void __launch_bounds__(
+    kMaxThreads, kDense ? 4 : ((kX && sizeof(R) == 4) ? 3 : 0))
     chain_kernel(const __grid_constant__ mcv_chain ch, uint64_t n,
                  uint64_t first, uint64_t seed, const float* __restrict__ uni,
                  int stride, double* __restrict__ out_n,
