@@ -116,7 +116,8 @@ KERNEL_COUNTS = {
               "kernel": "mcv::ms_chain_kernel<float, true>",
               "traffic_note": "local memory (tree lists, spills) evicted "
                               "from L2, 1.42 KB per incident neutron; 76 B "
-                              "at 2 blocks an SM, 16% slower"},
+                              "at 2 blocks an SM (16% slower), 0.69 KB at "
+                              "3 (9% slower)"},
 }
 
 
