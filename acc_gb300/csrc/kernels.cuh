@@ -355,12 +355,13 @@ __device__ __noinline__ uint2 ms_downstream_out(Neutron<R> m, uint64_t index,
 // pass of a warp-uniform loop first advances every lane's bookkeeping to its
 // next _interactM1 call (or to the end of its tree, emitting the outputs on
 // the way), then makes that call on all lanes together and files its two
-// outputs.  When every tree of the warp has ended the lanes take the next
-// incident neutrons.  Every neutron goes through the same operations in
-// the same order, with its own Philox stream, as in the thread kernel, so
-// results agree neutron by neutron.  Used when no component after the
-// scatterer draws random numbers (the outputs then run the rest of the
-// chain as they become final, ms_downstream_draws).
+// outputs.  When every tree of the warp (of the block, for convex shapes)
+// has ended the lanes take the next incident neutrons.  Every neutron goes
+// through the same operations in the same order, with its own Philox
+// stream, as in the thread kernel, so results agree neutron by neutron.
+// Used when no component after the scatterer draws random numbers (the
+// outputs then run the rest of the chain as they become final,
+// ms_downstream_draws).
 template <typename R>
 struct MsLane {
   Neutron<R> tbs[2][MCV_MS_MAX_SCATTERED];   // _scatterM's work lists
@@ -598,15 +599,19 @@ __global__ void __launch_bounds__(kMaxThreads, 4)
     k.nonfinite += r.y;
   };
   for (;;) {
-    // lanes take new neutrons together, once every tree of the warp has
-    // ended: trees started in the same pass stay in the same phase (the
-    // same branches of ms_advance and ms_file) for most of their length,
-    // which on UN pays more than the lanes left idle behind the longest
-    // tree (2.8e8 n/s against 1.7e8 when each lane refills as soon as its
-    // tree ends)
-    const unsigned idle = __any_sync(kFull, state == 1)
-                              ? 0u
-                              : __ballot_sync(kFull, state == 0);
+    // lanes take new neutrons together, once every tree of the warp (of
+    // the block, in the block-synchronous form) has ended: trees started in
+    // the same pass stay in the same phase (the same branches of
+    // ms_advance and ms_file) for most of their length, which on UN pays
+    // more than the lanes left idle behind the longest tree (2.8e8 n/s
+    // against 1.7e8 when each lane refills as soon as its tree ends).  With
+    // warps refilling on their own, the warps of an SM drift apart over a
+    // long launch (UN: 5.2e8 n/s at 3e6 neutrons a launch, 4.3e8 at 1e8);
+    // refilling a block at once keeps them together (6.2e8 at 1e8).
+    bool busy;
+    if constexpr (kBlock) busy = __syncthreads_or(state == 1);
+    else busy = __any_sync(kFull, state == 1);
+    const unsigned idle = busy ? 0u : __ballot_sync(kFull, state == 0);
     if (idle) {
       if (state == 0) {
         const uint64_t idx = next + (uint64_t)__popc(idle & below);

@@ -109,13 +109,13 @@ KERNEL_COUNTS = {
     # 608 blocks x 256 threads on a 1e6-neutron launch); its DRAM traffic is
     # the local-memory working set (tree lists and spills of 1024 lanes an
     # SM) leaving L2, and grows with the neutron count
-    "un_ms": {"warp_inst_per_neutron": 923.7,
-              "thread_inst_per_neutron": 923.7 * 15.33,
-              "dram_bytes_per_neutron": 1422.3,
+    "un_ms": {"warp_inst_per_neutron": 919.4,
+              "thread_inst_per_neutron": 919.4 * 15.35,
+              "dram_bytes_per_neutron": 1438.0,
               "captured_neutrons": 1_000_000,
               "kernel": "mcv::ms_chain_kernel<float, true>",
               "traffic_note": "local memory (tree lists, spills) evicted "
-                              "from L2, 1.42 KB per incident neutron; 76 B "
+                              "from L2, 1.44 KB per incident neutron; 76 B "
                               "at 2 blocks an SM (16% slower), 0.69 KB at "
                               "3 (9% slower)"},
 }
