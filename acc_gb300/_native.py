@@ -186,6 +186,8 @@ _SIGNATURES = {
     "mcv_probe_fma_peak": (ctypes.c_int, [ctypes.c_int, ctypes.c_int,
                                           ctypes.c_int,
                                           ctypes.POINTER(ctypes.c_double)]),
+    "mcv_probe_sfu_rate": (ctypes.c_int, [ctypes.c_int, ctypes.c_int,
+                                          ctypes.POINTER(ctypes.c_double)]),
     "mcv_probe_atomic_rate": (ctypes.c_int, [ctypes.c_int, ctypes.c_uint64,
                                              ctypes.c_int,
                                              ctypes.POINTER(ctypes.c_double)]),

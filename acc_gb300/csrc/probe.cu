@@ -1,5 +1,5 @@
-// probe.cu -- FMA-pipe and L2-atomic throughput probes
-// (include/acc_gb300_probe.h).
+// probe.cu -- FMA-pipe, special-function-unit and L2-atomic throughput
+// probes (include/acc_gb300_probe.h).
 
 #include <cuda_runtime.h>
 
@@ -25,6 +25,25 @@ __global__ void __launch_bounds__(256) fma_kernel(int iters, T seed, T* sink) {
 #pragma unroll
   for (int k = 0; k < kChains; ++k) s += a[k];
   if (s == T(-12345.678)) *sink = s;  // never true; keeps the chains live
+}
+
+// kChains independent chains of one base-2 exponential each (the
+// special-function unit's ex2.approx, flushing denormals): a chain's value
+// saturates within a few steps, which does not change the unit's rate
+__global__ void __launch_bounds__(256) sfu_kernel(int iters, float seed,
+                                                  float* sink) {
+  float a[kChains];
+#pragma unroll
+  for (int k = 0; k < kChains; ++k) a[k] = seed * float(threadIdx.x + k);
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < kChains; ++k)
+      asm volatile("ex2.approx.ftz.f32 %0, %0;" : "+f"(a[k]));
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int k = 0; k < kChains; ++k) s += a[k];
+  if (s == -12345.678f) *sink = s;  // never true; keeps the chains live
 }
 
 __global__ void __launch_bounds__(256)
@@ -84,6 +103,46 @@ extern "C" int mcv_probe_fma_peak(int device, int precision, int repeats,
                              : 1;
   cudaSetDevice(prev);
   return rc;
+}
+
+extern "C" int mcv_probe_sfu_rate(int device, int repeats,
+                                  double* ops_per_s) {
+  if (!ops_per_s || repeats < 1) return 1;
+  int prev = 0;
+  cudaGetDevice(&prev);
+  cudaSetDevice(device);
+  int sms = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sfu_kernel, 256, 0);
+  if (per_sm < 1) per_sm = 1;
+  const int blocks = sms * per_sm, iters = 4000;
+  float* sink = nullptr;
+  if (cudaMalloc(&sink, sizeof(float)) != cudaSuccess) {
+    cudaSetDevice(prev);
+    return 2;
+  }
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  double best = 0;
+  for (int r = 0; r < repeats + 1; ++r) {
+    cudaEventRecord(e0);
+    sfu_kernel<<<blocks, 256>>>(iters, 1e-3f, sink);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    const double ops =
+        (double)kChains * iters * blocks * 256.0 / (ms * 1e-3);
+    if (r > 0 && ops > best) best = ops;  // first launch is warm-up
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(sink);
+  cudaSetDevice(prev);
+  *ops_per_s = best;
+  return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 
 extern "C" int mcv_probe_atomic_rate(int device, uint64_t nbins, int repeats,

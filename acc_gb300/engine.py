@@ -289,6 +289,16 @@ def probe_fma_peak(precision=32, repeats=3, device=None):
     return out.value
 
 
+def probe_sfu_rate(repeats=3, device=None):
+    """Measured special-function-unit rate of the current GPU (FP32
+    base-2 exponentials per second)."""
+    ctx = nat.context(device)
+    out = ctypes.c_double()
+    nat.check(nat.lib().mcv_probe_sfu_rate(ctx.device, int(repeats),
+                                           ctypes.byref(out)))
+    return out.value
+
+
 def probe_atomic_rate(nbins, repeats=3, device=None):
     """Measured FP64 atomicAdd rate (ops/s) into `nbins` doubles."""
     ctx = nat.context(device)

@@ -613,6 +613,7 @@ def ours_arm(a, rank, world, local_rank):
 
     fp32_peak = engine.probe_fma_peak(32)
     fp64_peak = engine.probe_fma_peak(64)
+    sfu_rate = engine.probe_sfu_rate()
     mean_s = statistics.mean(ms32) / 1e3
     counts = KERNEL_COUNTS.get(a.workload, {})
     fpn = counts.get("fp32_flops_per_neutron")
@@ -625,6 +626,9 @@ def ours_arm(a, rank, world, local_rank):
                        "(mcv_probe_fma_peak); the measured peak file has "
                        "HBM and bf16-tensor peaks only",
         "fp64_peak_tflops": fp64_peak,
+        "sfu_peak_ops_per_s": sfu_rate,
+        "sfu_peak_source": "mcv_probe_sfu_rate: FP32 ex2.approx chains on "
+                           "every SM, measured in this run",
     }
     # the binding limit: one warp instruction per cycle per SM sub-partition
     # (4 per SM); divergence (SIMT efficiency) sets how many warp
