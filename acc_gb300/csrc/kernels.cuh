@@ -355,8 +355,8 @@ __device__ __noinline__ uint2 ms_downstream_out(Neutron<R> m, uint64_t index,
 // pass of a warp-uniform loop first advances every lane's bookkeeping to its
 // next _interactM1 call (or to the end of its tree, emitting the outputs on
 // the way), then makes that call on all lanes together and files its two
-// outputs.  When every tree of the warp (of the block, for convex shapes)
-// has ended the lanes take the next incident neutrons.  Every neutron goes
+// outputs.  When every tree of the block has ended the lanes take the next
+// incident neutrons.  Every neutron goes
 // through the same operations in the same order, with its own Philox
 // stream, as in the thread kernel, so results agree neutron by neutron.
 // Used when no component after the scatterer draws random numbers (the
@@ -565,10 +565,11 @@ __device__ __forceinline__ void ms_file(const mcv_component& c, MsLane<R>& S,
   ++S.pi;
 }
 
-// kBlock: the warps of a block run each pass's phases (refill and
-// bookkeeping, the _interactM1 calls, the filing of their outputs) between
-// block barriers, so that they execute the same code at the same time and
-// share the instruction cache.  Chosen for a convex shape (a primitive),
+// Every form refills and ends a block at once (two block barriers a
+// pass).  kBlock: the warps of a block also run each pass's phases (refill
+// and bookkeeping, the _interactM1 calls, the filing of their outputs)
+// between block barriers, so that they execute the same code at the same
+// time and share the instruction cache.  Chosen for a convex shape (a primitive),
 // where every tree has one outer loop and the trees are alike: UN runs at
 // 5.2e8 n/s with it and 4.1e8 without; the hollow cylinder's trees (outputs
 // re-entering through the inner surface) are uneven, and the barriers hold
@@ -599,18 +600,16 @@ __global__ void __launch_bounds__(kMaxThreads, 4)
     k.nonfinite += r.y;
   };
   for (;;) {
-    // lanes take new neutrons together, once every tree of the warp (of
-    // the block, in the block-synchronous form) has ended: trees started in
-    // the same pass stay in the same phase (the same branches of
-    // ms_advance and ms_file) for most of their length, which on UN pays
-    // more than the lanes left idle behind the longest tree (2.8e8 n/s
-    // against 1.7e8 when each lane refills as soon as its tree ends).  With
-    // warps refilling on their own, the warps of an SM drift apart over a
-    // long launch (UN: 5.2e8 n/s at 3e6 neutrons a launch, 4.3e8 at 1e8);
-    // refilling a block at once keeps them together (6.2e8 at 1e8).
-    bool busy;
-    if constexpr (kBlock) busy = __syncthreads_or(state == 1);
-    else busy = __any_sync(kFull, state == 1);
+    // lanes take new neutrons together, once every tree of the block has
+    // ended: trees started in the same pass stay in the same phase (the
+    // same branches of ms_advance and ms_file) for most of their length,
+    // which pays more than the lanes left idle behind the longest tree (UN:
+    // 2.8e8 n/s against 1.7e8 when each lane refills as soon as its tree
+    // ends).  With warps refilling on their own, the warps of an SM drift
+    // apart over a long launch (UN: 5.2e8 n/s at 3e6 neutrons a launch,
+    // 4.3e8 at 1e8); refilling a block at once keeps them together (UN
+    // 6.2e8 at 1e8; the hollow cylinder 8.5e7 against 6.9e7).
+    const bool busy = __syncthreads_or(state == 1);
     const unsigned idle = busy ? 0u : __ballot_sync(kFull, state == 0);
     if (idle) {
       if (state == 0) {
@@ -642,11 +641,7 @@ __global__ void __launch_bounds__(kMaxThreads, 4)
       next += (uint64_t)__popc(idle);
       if (next > end) next = end;
     }
-    if constexpr (kBlock) {
-      if (__syncthreads_and(state == 2)) break;
-    } else {
-      if (__all_sync(kFull, state == 2)) break;
-    }
+    if (__syncthreads_and(state == 2)) break;
     bool call = false;
     if (state == 1) {
       call = ms_advance<R>(c, S, min_prob, emit);
