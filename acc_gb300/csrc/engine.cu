@@ -16,8 +16,8 @@ int mcv_fp64_fma_occupancy(int x, int threads);
 void mcv_fp64_fma_chain(int x, int blocks, int threads, cudaStream_t s,
                         const mcv_chain& ch, uint64_t n, uint64_t first,
                         uint64_t seed, void* status);
-int mcv_fp64_fma_ms_occupancy(bool block, int threads);
-void mcv_fp64_fma_ms(bool block, int blocks, int threads, cudaStream_t s,
+int mcv_fp64_fma_ms_occupancy(int threads);
+void mcv_fp64_fma_ms(int blocks, int threads, cudaStream_t s,
                      const mcv_chain& ch, uint64_t n, uint64_t first,
                      uint64_t seed, void* status);
 
@@ -389,24 +389,20 @@ void launch_ms(mcv_ctx* ctx, const mcv_chain* chain, uint64_t ncount,
                uint64_t first, uint64_t seed, const mcv_launch* launch,
                cudaStream_t s, bool fma = false) {
   int blocks, threads;
-  // block-synchronous passes for a convex (primitive) shape
-  int k = 0;
-  while (chain->comp[k].opcode != MCV_OP_HMS) ++k;
-  const bool block = chain->comp[k].ip[0] == MCV_CSG_PRIMITIVE;
   // one warp handles a run of incident neutrons: the grid's warps each
   // take at least 32
   launch_shape(
       ctx,
-      [block, fma](int t) {
-        return fma ? mcv_fp64_fma_ms_occupancy(block, t)
-                   : Launchers<R>::occupancy_ms(t, block);
+      [fma](int t) {
+        return fma ? mcv_fp64_fma_ms_occupancy(t)
+                   : Launchers<R>::occupancy_ms(t);
       },
       (ncount + 31) / 32 * 32, launch, &blocks, &threads);
   if (fma)
-    mcv_fp64_fma_ms(block, blocks, threads, s, *chain, ncount, first, seed,
+    mcv_fp64_fma_ms(blocks, threads, s, *chain, ncount, first, seed,
                     ctx->d_status);
   else
-    Launchers<R>::ms(blocks, threads, block, s, *chain, ncount, first, seed,
+    Launchers<R>::ms(blocks, threads, s, *chain, ncount, first, seed,
                      ctx->d_status);
 }
 

@@ -355,8 +355,8 @@ __device__ __noinline__ uint2 ms_downstream_out(Neutron<R> m, uint64_t index,
 // pass of a warp-uniform loop first advances every lane's bookkeeping to its
 // next _interactM1 call (or to the end of its tree, emitting the outputs on
 // the way), then makes that call on all lanes together and files its two
-// outputs.  When every tree of the block has ended the lanes take the next
-// incident neutrons.  Every neutron goes
+// outputs.  The warps of a block run each phase together, and when every
+// tree of the block has ended the lanes take the next incident neutrons.  Every neutron goes
 // through the same operations in the same order, with its own Philox
 // stream, as in the thread kernel, so results agree neutron by neutron.
 // Used when no component after the scatterer draws random numbers (the
@@ -565,16 +565,14 @@ __device__ __forceinline__ void ms_file(const mcv_component& c, MsLane<R>& S,
   ++S.pi;
 }
 
-// Every form refills and ends a block at once (two block barriers a
-// pass).  kBlock: the warps of a block also run each pass's phases (refill
-// and bookkeeping, the _interactM1 calls, the filing of their outputs)
-// between block barriers, so that they execute the same code at the same
-// time and share the instruction cache.  Chosen for a convex shape (a primitive),
-// where every tree has one outer loop and the trees are alike: UN runs at
-// 5.2e8 n/s with it and 4.1e8 without; the hollow cylinder's trees (outputs
-// re-entering through the inner surface) are uneven, and the barriers hold
-// its warps (6.3e7 against 7.7e7).
-template <typename R, bool kBlock>
+// The warps of a block run each pass's phases (refill and bookkeeping, the
+// _interactM1 calls, the filing of their outputs) between block barriers,
+// so that they execute the same code at the same time and share the
+// instruction cache, and they refill and end together (UN: 4.1e8 n/s
+// without the phase barriers, 5.2e8 with them and warp refills, 6.2e8
+// with block refills; the hollow cylinder, whose trees are uneven: 8.5e7
+// with block refills alone, 1.09e8 with the phase barriers too).
+template <typename R>
 __global__ void __launch_bounds__(kMaxThreads, 4)
     ms_chain_kernel(const __grid_constant__ mcv_chain ch, uint64_t n,
                     uint64_t first, uint64_t seed, DevStatus* st) {
@@ -647,7 +645,7 @@ __global__ void __launch_bounds__(kMaxThreads, 4)
       call = ms_advance<R>(c, S, min_prob, emit);
       if (!call) state = 0;
     }
-    if constexpr (kBlock) __syncthreads();
+    __syncthreads();
     // a call comes with S.ps2 < max_scattered_neutrons: the scattered
     // neutron's entry exists
     Neutron<R> t0;
@@ -655,7 +653,7 @@ __global__ void __launch_bounds__(kMaxThreads, 4)
     if (call)
       ns = ms_interact_m1(c, rng, t0, S.ptbs[S.pb ^ 1][S.ps2],
                           S.ptbs[S.pb][S.pi]);
-    if constexpr (kBlock) __syncthreads();
+    __syncthreads();
     if (call) ms_file<R>(c, S, t0, ns, min_prob, emit);
   }
   flush_counters(k, st);
@@ -1143,10 +1141,9 @@ struct Launchers {
   static void buffer(int blocks, int threads, bool x, cudaStream_t s,
                      const mcv_chain& ch, void* buf, uint64_t n,
                      uint64_t first, uint64_t seed, DevStatus* st);
-  static int occupancy_ms(int threads, bool block);
-  static void ms(int blocks, int threads, bool block, cudaStream_t s,
-                 const mcv_chain& ch, uint64_t n, uint64_t first,
-                 uint64_t seed, DevStatus* st);
+  static int occupancy_ms(int threads);
+  static void ms(int blocks, int threads, cudaStream_t s, const mcv_chain& ch,
+                 uint64_t n, uint64_t first, uint64_t seed, DevStatus* st);
   static int occupancy_batched(int threads, size_t smem);
   static void batched(int blocks, int threads, size_t smem, cudaStream_t s,
                       const mcv_chain* variants, int nvar,
@@ -1301,21 +1298,15 @@ void Launchers<R>::buffer(int blocks, int threads, bool x, cudaStream_t s,
 }
 
 template <typename R>
-int Launchers<R>::occupancy_ms(int threads, bool block) {
-  return block ? occupancy_of(ms_chain_kernel<R, true>, threads, 0)
-               : occupancy_of(ms_chain_kernel<R, false>, threads, 0);
+int Launchers<R>::occupancy_ms(int threads) {
+  return occupancy_of(ms_chain_kernel<R>, threads, 0);
 }
 
 template <typename R>
-void Launchers<R>::ms(int blocks, int threads, bool block, cudaStream_t s,
+void Launchers<R>::ms(int blocks, int threads, cudaStream_t s,
                       const mcv_chain& ch, uint64_t n, uint64_t first,
                       uint64_t seed, DevStatus* st) {
-  if (block)
-    ms_chain_kernel<R, true><<<blocks, threads, 0, s>>>(ch, n, first, seed,
-                                                        st);
-  else
-    ms_chain_kernel<R, false><<<blocks, threads, 0, s>>>(ch, n, first, seed,
-                                                         st);
+  ms_chain_kernel<R><<<blocks, threads, 0, s>>>(ch, n, first, seed, st);
 }
 
 template <typename R>

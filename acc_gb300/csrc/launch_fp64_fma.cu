@@ -28,22 +28,15 @@ void mcv_fp64_fma_chain(int x, int blocks, int threads, cudaStream_t s,
         ch, n, first, seed, nullptr, 0, nullptr, nullptr, st);
 }
 
-// the multiple-scattering tree kernel (block: its block-synchronous form)
-int mcv_fp64_fma_ms_occupancy(bool block, int threads) {
-  return block ? mcv::occupancy_of(mcv::ms_chain_kernel<double, true>,
-                                   threads, 0)
-               : mcv::occupancy_of(mcv::ms_chain_kernel<double, false>,
-                                   threads, 0);
+// the multiple-scattering tree kernel
+int mcv_fp64_fma_ms_occupancy(int threads) {
+  return mcv::occupancy_of(mcv::ms_chain_kernel<double>, threads, 0);
 }
 
-void mcv_fp64_fma_ms(bool block, int blocks, int threads, cudaStream_t s,
+void mcv_fp64_fma_ms(int blocks, int threads, cudaStream_t s,
                      const mcv_chain& ch, uint64_t n, uint64_t first,
                      uint64_t seed, void* status) {
   auto* st = static_cast<mcv::DevStatus*>(status);
-  if (block)
-    mcv::ms_chain_kernel<double, true><<<blocks, threads, 0, s>>>(
-        ch, n, first, seed, st);
-  else
-    mcv::ms_chain_kernel<double, false><<<blocks, threads, 0, s>>>(
-        ch, n, first, seed, st);
+  mcv::ms_chain_kernel<double><<<blocks, threads, 0, s>>>(ch, n, first, seed,
+                                                          st);
 }

@@ -105,15 +105,15 @@ KERNEL_COUNTS = {
                     "kernel": "mcv::regen_kernel<float>",
                     "traffic_note": "the tally bins, independent of the "
                                     "neutron count"},
-    # the multiple-scattering tree kernel (block-synchronous instantiation,
-    # 608 blocks x 256 threads on a 1e6-neutron launch); its DRAM traffic is
+    # the multiple-scattering tree kernel (608 blocks x 256 threads on a
+    # 1e6-neutron launch); its DRAM traffic is
     # the local-memory working set (tree lists and spills of 1024 lanes an
     # SM) leaving L2, and grows with the neutron count
     "un_ms": {"warp_inst_per_neutron": 919.4,
               "thread_inst_per_neutron": 919.4 * 15.35,
               "dram_bytes_per_neutron": 1438.0,
               "captured_neutrons": 1_000_000,
-              "kernel": "mcv::ms_chain_kernel<float, true>",
+              "kernel": "mcv::ms_chain_kernel<float>",
               "traffic_note": "local memory (tree lists, spills) evicted "
                               "from L2, 1.44 KB per incident neutron; 76 B "
                               "at 2 blocks an SM (16% slower), 0.69 KB at "
