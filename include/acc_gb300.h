@@ -210,9 +210,11 @@ enum {
  *   dp[14]=minimum_neutron_event_probability
  *   One incident neutron gives up to max_scattered_neutrons output
  *   neutrons; the components after it run on each output in turn, drawing
- *   from the incident neutron's stream.  At most one HMS per chain; the
- *   fused thread kernel and the batched launch run it (mcv_process_buffer,
- *   mcv_backward and the regeneration kernel reject it).
+ *   from the incident neutron's stream.  At most one HMS per chain;
+ *   mcv_run_chain runs it (the tree kernel, or the thread kernel when a
+ *   later component draws or launch variant 1 asks for it);
+ *   mcv_replay_uniforms, mcv_process_buffer, mcv_backward and the batched
+ *   launches reject it.
  * GUIDE_TAPERING (guide_tapering.py:22-291): nseg equal segments
  *   ip[0]=nseg  ip[1]=segments per quiet-test block (0: no blocks)
  *   dp: 0 l_seg 1 R0 2 Qcx 3 Qcy 4 alphax 5 alphay 6 mx 7 my 8 W
